@@ -1,0 +1,537 @@
+"""Benchmark: GraphBlox's CSR kernel set on one GB300, RMAT scale 22.
+
+Workload (the full-kernel-set configuration): RMAT scale 22 (4,194,304
+vertices, 2^26 generated edges, a/b/c/d = .57/.19/.19/.05, seed 1), self loops
+and duplicates removed, uint32 CSR. One step runs, on the resident graph:
+  bfs     direction-optimising BFS from 64 seeded non-isolated roots
+  sssp    delta-stepping from 4 of those roots, uint32 weights U[1,255]
+  cc      Afforest on the symmetrised graph
+  tc      triangle count on the symmetrised, degree-ordered graph (DAG)
+  spmv    y = A x, values U(0,1], x U[-1,1] (FP32)
+  pr      pull PageRank, 20 iterations (FP32 ranks, FP64 residual)
+  reorder count-sort degree reordering of the directed edge list
+Metric: GTEPS per kernel and its fraction of the measured HBM roofline; the
+headline `value` is the kernel set's aggregate GTEPS (sum of traversed edges
+over sum of kernel times). Traversed edges follow the Graph500 convention
+(BFS/SSSP: out-degree sum of reached vertices per source), E*iterations for
+PR, E for SpMV/CC/reorder, |E+| (DAG edges) for TC.
+
+`value` times kernels on device-resident inputs with CUDA events on the
+launching stream, L2 flushed (256 MiB write) before every kernel. `e2e` is
+the same metric through the C ABI with pinned host buffers: the CSR upload,
+every kernel and the copy-back of every result inside the timed region.
+
+--impl reference times the CPU oracle port (oracle/gbx_oracle.c, OpenMP on
+all host cores) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+SCALE = 22
+EDGE_FACTOR = 16
+SEED = 1
+N_ROOTS = 64
+N_SSSP_ROOTS = 4
+PR_ITERS = 20
+W_LO, W_HI = 1, 255
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# workload construction (untimed)
+
+
+def build_workload(gbx, scale=SCALE, ef=EDGE_FACTOR, seed=SEED):
+    V = 1 << scale
+    t0 = time.time()
+    src, dst = gbx.generate_rmat(scale, V * ef, seed=seed)
+    w = gbx.generate_values(src.shape[0], 0, W_LO, W_HI, seed=seed + 11)
+    el = gbx.EdgeList(V, src, dst, w)
+    g = gbx.graph_csr_preprocessing(el, sort=1, dedup=True, directed=True, keep_weights=True)
+    # symmetrised, deduplicated graph for CC/TC, and its degree-ordered form
+    sym = gbx.EdgeList(V, np.concatenate([src, dst]), np.concatenate([dst, src]))
+    gs = gbx.graph_csr_preprocessing(sym, sort=1, dedup=True, directed=False, keep_weights=False)
+    elr = gbx.EdgeList(V, gs.src.copy(), gs.dest.copy())
+    gbx.degree_reorder(elr, 1)
+    gsr = gbx.graph_csr_preprocessing(elr, sort=1, directed=False, keep_weights=False)
+    x = gbx.generate_values(V, 2, seed=seed + 21)
+    vals = gbx.generate_values(g.num_edges, 1, seed=seed + 31)
+    rng = np.random.default_rng(seed)
+    nz = np.nonzero(g.out_degree)[0]
+    roots = [int(r) for r in rng.choice(nz, N_ROOTS, replace=False)]
+    log(f"workload built in {time.time() - t0:.1f}s: V={V} E={g.num_edges} Esym={gs.num_edges}")
+    return dict(V=V, g=g, gs=gs, gsr=gsr, x=x, vals=vals, roots=roots, edges_src=g.src, edges_dst=g.dest)
+
+
+def dag_stats(gsr):
+    """|E+| and the TC algorithmic bytes sum over DAG edges of 4(d+u + d+v),
+    with d+(u) = number of neighbours with id <= u (ids are degree order)."""
+    deg = gsr.out_degree.astype(np.int64)
+    src = gsr.src.astype(np.int64)
+    dst = gsr.dest.astype(np.int64)
+    lower = dst <= src
+    dplus = np.bincount(src[lower], minlength=gsr.num_vertices).astype(np.int64)
+    e_plus = int(lower.sum())
+    tc_bytes = 4 * (gsr.num_vertices + 1) + 4 * e_plus + int((4 * (dplus[src[lower]] + dplus[dst[lower]])).sum())
+    return e_plus, tc_bytes
+
+
+# ---------------------------------------------------------------------------
+# clocks
+
+
+class ClockSampler:
+    def __init__(self):
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self, device_index=0):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9 or parts[0] != str(device_index):
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+
+
+def run_gpu(args):
+    import torch
+
+    import graphblox_gb300 as gbx
+    from graphblox_gb300 import _lib
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    _lib.call("gbx_set_device", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    W = build_workload(gbx)
+    g, gs, gsr = W["g"], W["gs"], W["gsr"]
+    V, E = g.num_vertices, g.num_edges
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+    dg = gbx.DeviceGraph.from_graph_csr(g, stream=sp)
+    dgs = gbx.DeviceGraph.from_graph_csr(gs, use_weights=False, stream=sp)
+    dgr = gbx.DeviceGraph.from_graph_csr(gsr, use_weights=False, stream=sp)
+    for h in (dg, dgs, dgr):
+        h.label_array = None  # roots are given in the graph's own ids
+    # device-resident buffers
+    dist_d = torch.empty(V, dtype=torch.int32, device=dev)
+    par_d = torch.empty(V, dtype=torch.int32, device=dev)
+    sssp_d = torch.empty(V, dtype=torch.int32, device=dev)
+    comp_d = torch.empty(V, dtype=torch.int32, device=dev)
+    ranks_d = torch.empty(V, dtype=torch.float32, device=dev)
+    x_d = torch.from_numpy(W["x"]).to(dev)
+    vals_d = torch.from_numpy(W["vals"]).to(dev)
+    y_d = torch.zeros(V, dtype=torch.float32, device=dev)
+    es_d = torch.from_numpy(W["edges_src"].view(np.int32)).to(dev)
+    ed_d = torch.from_numpy(W["edges_dst"].view(np.int32)).to(dev)
+    es_w = torch.empty_like(es_d)
+    ed_w = torch.empty_like(ed_d)
+    lab_d = torch.empty(V, dtype=torch.int32, device=dev)
+    inv_d = torch.empty(V, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    e_plus, tc_bytes = dag_stats(gsr)
+    roots = W["roots"]
+    sssp_roots = roots[:N_SSSP_ROOTS]
+    ident = torch.arange(V, dtype=torch.int32, device=dev)
+
+    def kernels():
+        """(name, fn) -> fn returns (traversed edges, algorithmic bytes)"""
+        def bfs():
+            te = tb = 0
+            for r in roots:
+                st = gbx.breadth_first_search(dg, r, 2, distances=dist_d, parents=par_d, stream=sp)
+                te += st.edges_traversed
+                tb += 4 * (V + 1) + 4 * st.edges_traversed + 8 * V
+            return te, tb
+
+        def sssp():
+            te = tb = 0
+            for r in sssp_roots:
+                st = gbx.sssp(dg, r, 0, distances=sssp_d, stream=sp)
+                te += st.edges_traversed
+                tb += 4 * (V + 1) + 8 * st.edges_traversed + 8 * V
+            return te, tb
+
+        def cc():
+            gbx.connected_components(dgs, 1, components=comp_d, stream=sp)
+            return gs.num_edges, 4 * (V + 1) + 8 * gs.num_edges + 8 * V
+
+        def tc():
+            gbx.triangle_count(dgr, stream=sp)
+            return e_plus, tc_bytes
+
+        def spmv():
+            y_d.zero_()
+            gbx.spmv(dg, x_d, values=vals_d, iterations=1, y=y_d, stream=sp)
+            return E, 12 * E + 8 * V
+
+        def pr():
+            gbx.page_rank(dg, PR_ITERS, 0.0, ranks=ranks_d, stream=sp)
+            return E * PR_ITERS, PR_ITERS * (8 * E + 20 * V)
+
+        def reorder():
+            es_w.copy_(es_d)
+            ed_w.copy_(ed_d)
+            lab_d.copy_(ident)
+            _lib.call("gbx_degree_reorder", V, E, es_w.data_ptr(), ed_w.data_ptr(), 1, lab_d.data_ptr(),
+                      inv_d.data_ptr(), sp)
+            return E, 20 * E + 24 * V
+
+        return [("bfs", bfs), ("sssp", sssp), ("cc", cc), ("tc", tc), ("spmv", spmv), ("pr", pr),
+                ("reorder", reorder)]
+
+    ks = kernels()
+    ev = {n: [] for n, _ in ks}
+    work = {}
+
+    def one_step(record):
+        for n, fn in ks:
+            flush.fill_(1)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            te, tb = fn()
+            b.record(stream)
+            if record:
+                ev[n].append((a, b))
+                work[n] = (te, tb)
+
+    for _ in range(args.warmup):
+        one_step(False)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler()
+    clocks.start()
+    launches0 = _lib.load().gbx_kernel_launches()
+    torch.cuda.synchronize()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for _ in range(args.steps):
+        one_step(True)
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches = _lib.load().gbx_kernel_launches() - launches0
+    clk = clocks.stop(local)
+    wall_ms = t_start.elapsed_time(t_end)
+    per = {}
+    peak, peak_kind = peaks()
+    tot_edges = tot_ms = 0.0
+    for n, _ in ks:
+        ms = float(np.mean([a.elapsed_time(b) for a, b in ev[n]]))
+        te, tb = work[n]
+        per[n] = {"ms": round(ms, 4), "gteps": round(te / (ms * 1e-3) / 1e9, 3),
+                  "achieved_gbs": round(tb / (ms * 1e-3) / 1e9, 1),
+                  "frac": round(tb / (ms * 1e-3) / 1e9 / peak, 3), "edges": int(te), "alg_bytes": int(tb)}
+        tot_edges += te
+        tot_ms += ms
+    ms_step = tot_ms
+    gteps = tot_edges / (tot_ms * 1e-3) / 1e9
+    if dist:
+        t = torch.tensor([ms_step], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+        gteps = world * tot_edges / (ms_step * 1e-3) / 1e9
+    dom = max(per, key=lambda n: per[n]["ms"])
+    roof = {"kernel": dom, "bound": "hbm", "achieved": per[dom]["achieved_gbs"], "peak": peak,
+            "peak_kind": peak_kind, "unit": "GB/s", "frac": per[dom]["frac"],
+            "traffic": args.traffic, "note": "achieved = algorithmic bytes / CUDA-event time"}
+
+    e2e = run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(W, args, roots)
+    dg.close(), dgs.close(), dgr.close()
+    line = {
+        "metric": "GTEPS per kernel (aggregate over the kernel set) & %HBM-peak per kernel",
+        "value": round(gteps, 3), "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32 (ids, levels, distances) + f32 (ranks, SpMV)",
+        "data": "synthetic",
+        "config": {"workload": "rmat22_full_kernel_set", "scale": SCALE, "num_vertices": V,
+                   "edges_generated": V * EDGE_FACTOR, "num_edges": E, "num_edges_symmetric": gs.num_edges,
+                   "dag_edges": e_plus, "bfs_roots": N_ROOTS, "sssp_roots": N_SSSP_ROOTS,
+                   "pr_iterations": PR_ITERS, "l2": "flushed (256 MiB write) before every kernel",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "kernels": per, "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk,
+        "gpu_launches": int(launches), "wall_ms_timed_region": round(wall_ms, 3),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp):
+    """Same kernel set through the C ABI with pinned host buffers: upload of
+    the CSRs and copy-back of every result inside the timed region."""
+    import torch
+
+    g, gs, gsr = W["g"], W["gs"], W["gsr"]
+    V, E = g.num_vertices, g.num_edges
+
+    def pinned(a):
+        t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        return t.numpy()
+
+    hg = gbx.GraphCSR(V, E, pinned(g.out_degree), pinned(g.edges_idx), pinned(g.dest), pinned(g.src),
+                      pinned(g.weight), g.label_array, g.inverse_label_array, pinned(g.inverse_out_degree),
+                      pinned(g.inverse_edges_idx), pinned(g.inverse_dest), pinned(g.inverse_weight))
+    hgs = gbx.GraphCSR(V, gs.num_edges, pinned(gs.out_degree), pinned(gs.edges_idx), pinned(gs.dest),
+                       pinned(gs.src), None, gs.label_array, gs.inverse_label_array)
+    hgr = gbx.GraphCSR(V, gsr.num_edges, pinned(gsr.out_degree), pinned(gsr.edges_idx), pinned(gsr.dest),
+                       pinned(gsr.src), None, gsr.label_array, gsr.inverse_label_array)
+    dist_h = pinned(np.zeros(V, np.uint32))
+    par_h = pinned(np.zeros(V, np.int32))
+    comp_h = pinned(np.zeros(V, np.uint32))
+    ranks_h = pinned(np.zeros(V, np.float32))
+    y_h = pinned(np.zeros(V, np.float32))
+    x_h = pinned(W["x"])
+    vals_h = pinned(W["vals"])
+    h2d = d2h = 0
+
+    def step():
+        nonlocal h2d, d2h
+        edges = 0
+        h2d = d2h = 0
+        dg = gbx.DeviceGraph.from_graph_csr(hg, stream=sp)
+        dg.label_array = None
+        h2d += sum(a.nbytes for a in (hg.out_degree, hg.edges_idx, hg.dest, hg.weight, hg.inverse_out_degree,
+                                      hg.inverse_edges_idx, hg.inverse_dest, hg.inverse_weight))
+        for r in roots:
+            st = gbx.breadth_first_search(dg, r, 2, distances=dist_h, parents=par_h, stream=sp)
+            edges += st.edges_traversed
+            d2h += 8 * V
+        for r in sssp_roots:
+            st = gbx.sssp(dg, r, 0, distances=dist_h, stream=sp)
+            edges += st.edges_traversed
+            d2h += 4 * V
+        y_h[:] = 0
+        gbx.spmv(dg, x_h, values=vals_h, iterations=1, y=y_h, stream=sp)
+        h2d += x_h.nbytes + vals_h.nbytes + y_h.nbytes
+        d2h += y_h.nbytes
+        edges += E
+        gbx.page_rank(dg, PR_ITERS, 0.0, ranks=ranks_h, stream=sp)
+        d2h += 4 * V
+        edges += E * PR_ITERS
+        dg.close()
+        dgs = gbx.DeviceGraph.from_graph_csr(hgs, use_weights=False, stream=sp)
+        h2d += hgs.out_degree.nbytes + hgs.edges_idx.nbytes + hgs.dest.nbytes
+        gbx.connected_components(dgs, 1, components=comp_h, stream=sp)
+        d2h += 4 * V
+        edges += gs.num_edges
+        dgs.close()
+        dgr = gbx.DeviceGraph.from_graph_csr(hgr, use_weights=False, stream=sp)
+        h2d += hgr.out_degree.nbytes + hgr.edges_idx.nbytes + hgr.dest.nbytes
+        gbx.triangle_count(dgr, stream=sp)
+        d2h += 8
+        edges += e_plus
+        dgr.close()
+        el = gbx.EdgeList(V, g.src.copy(), g.dest.copy())
+        gbx.degree_reorder(el, 1, stream=sp)
+        h2d += 8 * E + 8 * V
+        d2h += 8 * E + 8 * V
+        edges += E
+        return edges
+
+    for _ in range(max(1, min(args.warmup, 2))):
+        step()
+    torch.cuda.synchronize()
+    times = []
+    edges = 0
+    for _ in range(max(1, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        edges = step()
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    t = float(np.mean(times))
+    return {"value": round(edges / t / 1e9, 3), "unit": "GTEPS", "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "ms_per_step": round(t * 1e3, 2),
+            "path": "C ABI (gbx_graph_create_csr + per-kernel entry points), pinned host buffers"}
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle port (baseline and reference arm)
+
+
+def cpu_sample(W, roots, n_bfs=4, pr_iters=PR_ITERS, n_sssp=1, with_tc=True, threads=0):
+    from oracle import pyoracle as po
+
+    g, gs, gsr = W["g"], W["gs"], W["gsr"]
+    V = g.num_vertices
+    host = po.HostCSR(V, g.out_degree, g.edges_idx, g.dest, g.weight, g.src)
+    pull = po.HostCSR(V, g.inverse_out_degree, g.inverse_edges_idx, g.inverse_dest, g.inverse_weight)
+    hs = po.HostCSR(V, gs.out_degree, gs.edges_idx, gs.dest)
+    hr = po.HostCSR(V, gsr.out_degree, gsr.edges_idx, gsr.dest)
+    res = {}
+
+    def timed(name, fn, edges):
+        t0 = time.perf_counter()
+        fn()
+        dt = time.perf_counter() - t0
+        res[name] = (edges() if callable(edges) else edges, dt)
+
+    bfs_edges = []
+
+    def bfs():
+        for r in roots[:n_bfs]:
+            d, _, _, _ = po.bfs(host, r, pull, threads)
+            reached = (d > 0)
+            reached[r] = True
+            bfs_edges.append(int(g.out_degree[reached].astype(np.int64).sum()))
+
+    timed("bfs", bfs, lambda: sum(bfs_edges))
+    sssp_edges = []
+
+    def sssp():
+        for r in roots[:n_sssp]:
+            d = po.sssp(host, r, 64, threads)
+            sssp_edges.append(int(g.out_degree[d != 0x7FFFFFFF].astype(np.int64).sum()))
+
+    timed("sssp", sssp, lambda: sum(sssp_edges))
+    timed("cc", lambda: po.cc(hs, 1, None, threads), gs.num_edges)
+    if with_tc:
+        e_plus = int((gsr.dest <= gsr.src).sum())
+        timed("tc", lambda: po.triangle_count(hr, threads), e_plus)
+    timed("spmv", lambda: po.spmv(host, W["x"], W["vals"], pull=pull, threads=threads), g.num_edges)
+    timed("pr", lambda: po.pagerank(host, pr_iters, 0.0, pull, threads), g.num_edges * pr_iters)
+    timed("reorder", lambda: po.degree_reorder(V, g.src, g.dest, 1, threads=threads), g.num_edges)
+    return res
+
+
+def cpu_baseline(W, args, roots):
+    res = cpu_sample(W, roots)
+    edges = sum(e for e, _ in res.values())
+    secs = sum(t for _, t in res.values())
+    return {"value": round(edges / secs / 1e9, 4), "unit": "GTEPS", "cores": os.cpu_count(), "kind": "port",
+            "sample": "RMAT-22 kernel set on the host cores: BFS 4 roots, SSSP 1 root (delta 64), CC Afforest, "
+                      "TC, SpMV, PR 20 iterations, degree reorder (oracle/gbx_oracle.c, OpenMP)",
+            "seconds": round(secs, 2),
+            "per_kernel_gteps": {n: round(e / t / 1e9, 4) for n, (e, t) in res.items()}}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import graphblox_gb300 as gbx
+
+    W = build_workload(gbx)
+    roots = W["roots"]
+    samples = []
+    for i in range(args.warmup + args.steps):
+        res = cpu_sample(W, roots[i % len(roots):] + roots, n_bfs=2, pr_iters=5, n_sssp=1, with_tc=False)
+        if i >= args.warmup:
+            samples.append(res)
+    edges = sum(e for s in samples for e, _ in s.values())
+    secs = sum(t for s in samples for _, t in s.values())
+    value = edges / secs / 1e9
+    line = {
+        "metric": "GTEPS per kernel (aggregate over the kernel set) & %HBM-peak per kernel",
+        "value": round(value, 4), "unit": "GTEPS", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs / len(samples) * 1e3, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32 (ids, levels, distances) + f32 (ranks, SpMV)", "data": "synthetic",
+        "config": {"workload": "rmat22_full_kernel_set", "scale": SCALE, "num_vertices": W["V"],
+                   "num_edges": W["g"].num_edges},
+        "impl": "reference",
+        "cpu_baseline": {"value": round(value, 4), "unit": "GTEPS", "cores": os.cpu_count(), "kind": "port",
+                         "sample": "per step: BFS 2 roots, SSSP 1 root (delta 64), CC, SpMV, PR 5 iterations, "
+                                   "degree reorder on the RMAT-22 graph (oracle/gbx_oracle.c, OpenMP; the "
+                                   "reference tree is not on the GPU host, so its compiled form cannot run)"},
+        "e2e": {"value": round(value, 4), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbx", choices=["gbx", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per launch of the dominant kernel from an ncu capture")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gbx":
+        log("note: fewer than 3 warm-up steps requested")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

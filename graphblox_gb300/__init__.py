@@ -1,0 +1,30 @@
+"""graphblox_gb300 -- GB300 (sm_103a) backend for GraphBlox's CSR graph kernels.
+
+The compute path is libgbx.so (hand-written CUDA kernels behind the C ABI in
+include/gbx.h). This package is the host-side mirror of the reference's
+graph-load and algorithm interfaces; see graph.py.
+"""
+from ._lib import GbxError, load  # noqa: F401
+from .graph import (  # noqa: F401
+    BFSStats,
+    DeviceGraph,
+    EdgeList,
+    GraphCSR,
+    PageRankStats,
+    SSSPStats,
+    breadth_first_search,
+    connected_components,
+    csr_build,
+    degree_reorder,
+    generate_rmat,
+    generate_values,
+    graph_csr_preprocessing,
+    page_rank,
+    read_edge_list_bin,
+    spmv,
+    sssp,
+    triangle_count,
+    write_edge_list_bin,
+)
+
+__version__ = "0.1.0"

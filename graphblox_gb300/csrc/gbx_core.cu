@@ -1,0 +1,346 @@
+// Library core: status strings and thread-local error messages, device
+// queries, pointer classification, and the device-resident graph object
+// (the device copy of the reference's struct GraphCSR, graphCSR.h:14-31).
+#include <atomic>
+#include <cstdarg>
+#include <cstring>
+#include <mutex>
+
+#include "gbx_internal.cuh"
+#include "gbx_gather.cuh"
+
+namespace gbx {
+
+static thread_local char g_err[512] = {0};
+static std::atomic<unsigned long long> g_launches{0};
+
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+void set_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+void clear_error() { g_err[0] = 0; }
+
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
+    const char *base = strrchr(file, '/');
+    set_error("%s:%d: %s failed: %s", base ? base + 1 : file, line, what, cudaGetErrorString(e));
+    if (e == cudaErrorMemoryAllocation) {
+        (void)cudaGetLastError();
+        return GBX_ERR_NOMEM;
+    }
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return GBX_ERR_NO_DEVICE;
+    return GBX_ERR_CUDA;
+}
+
+struct DevProps {
+    int sms = 0;
+    size_t l2 = 0;
+};
+static DevProps g_props[64];
+static std::once_flag g_props_once[64];
+
+int ensure_device() {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        set_error("no usable CUDA device: %s", cudaGetErrorString(e));
+        return GBX_ERR_NO_DEVICE;
+    }
+    int count = 0;
+    e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        (void)cudaGetLastError();
+        set_error("no usable CUDA device: %s", cudaGetErrorString(e));
+        return GBX_ERR_NO_DEVICE;
+    }
+    if (dev < 0 || dev >= 64) return GBX_ERR_NO_DEVICE;
+    std::call_once(g_props_once[dev], [dev]() {
+        cudaDeviceProp p;
+        if (cudaGetDeviceProperties(&p, dev) == cudaSuccess) {
+            g_props[dev].sms = p.multiProcessorCount;
+            g_props[dev].l2 = (size_t)p.l2CacheSize;
+        } else {
+            g_props[dev].sms = 132;
+            g_props[dev].l2 = 50u << 20;
+        }
+    });
+    return GBX_OK;
+}
+
+int num_sms() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return g_props[dev].sms > 0 ? g_props[dev].sms : 148;
+}
+
+size_t l2_bytes() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return g_props[dev].l2;
+}
+
+bool is_device_ptr(const void *p) {
+    if (!p) return false;
+    cudaPointerAttributes a;
+    cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// ---- graph construction kernels ----------------------------------------------
+
+__global__ void mask_ids_kernel(uint32_t *ids, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        ids[i] &= kIdMask;
+}
+
+// degree[v] = offsets[v+1] - offsets[v]
+__global__ void degree_from_offsets_kernel(const uint32_t *off, uint32_t *deg, uint32_t V) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+        deg[v] = off[v + 1] - off[v];
+}
+
+// The reference layout is edges_idx + out_degree over a source-sorted array;
+// it must equal the prefix-sum offsets wherever the degree is non-zero.
+__global__ void check_layout_kernel(const uint32_t *edges_idx, const uint32_t *deg,
+                                    const uint32_t *off, uint32_t V, unsigned *bad) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+        if (deg[v] && edges_idx[v] != off[v]) atomicAdd(bad, 1u);
+}
+
+__global__ void check_offsets_kernel(const uint32_t *off, uint32_t V, uint32_t E, unsigned *bad) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+        if (off[v] > off[v + 1]) atomicAdd(bad, 1u);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (off[0] != 0 || off[V] != E)) atomicAdd(bad, 1u);
+}
+
+__global__ void max_u32_kernel(const uint32_t *a, uint32_t n, uint32_t *out) {
+    uint32_t m = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        m = max(m, a[i]);
+    m = __reduce_max_sync(0xffffffffu, m);
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+static int grid_for(uint64_t n, int threads = 256) {
+    uint64_t b = (n + threads - 1) / threads;
+    uint64_t cap = (uint64_t)num_sms() * 8;
+    if (b > cap) b = cap;
+    return (int)(b ? b : 1);
+}
+
+static int copy_in(void *dst, const void *src, size_t bytes, cudaStream_t s) {
+    if (!bytes) return GBX_OK;
+    cudaMemcpyKind k = is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    GBX_CUDA(cudaMemcpyAsync(dst, src, bytes, k, s));
+    return GBX_OK;
+}
+
+static int dmalloc(void **p, size_t bytes) {
+    *p = nullptr;
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 4);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        set_error("device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+        return GBX_ERR_NOMEM;
+    }
+    return GBX_OK;
+}
+
+// Fill one direction of the graph (forward or inverse) from either layout.
+static int fill_direction(uint32_t V, uint32_t E, const uint32_t *edges_idx, const uint32_t *degree,
+                          const uint32_t *offsets, const uint32_t *ids, const float *w,
+                          uint32_t **d_off, uint32_t **d_ids, float **d_w, uint32_t **d_deg,
+                          uint32_t *max_deg, cudaStream_t s) {
+    GBX_TRY(dmalloc((void **)d_off, (size_t)(V + 1) * 4));
+    GBX_TRY(dmalloc((void **)d_deg, (size_t)V * 4));
+    GBX_TRY(dmalloc((void **)d_ids, (size_t)E * 4));
+    if (w) GBX_TRY(dmalloc((void **)d_w, (size_t)E * 4));
+    DevBuf<unsigned> bad;
+    GBX_TRY(bad.alloc(2, s));
+    GBX_CUDA(cudaMemsetAsync(bad.p, 0, 8, s));
+    if (offsets) {
+        GBX_TRY(copy_in(*d_off, offsets, (size_t)(V + 1) * 4, s));
+        check_offsets_kernel<<<grid_for(V), 256, 0, s>>>(*d_off, V, E, bad.p);
+        GBX_LAUNCH_CHECK();
+        degree_from_offsets_kernel<<<grid_for(V), 256, 0, s>>>(*d_off, *d_deg, V);
+        GBX_LAUNCH_CHECK();
+    } else {
+        GBX_TRY(copy_in(*d_deg, degree, (size_t)V * 4, s));
+        uint32_t *total = nullptr;
+        DevBuf<uint32_t> tot;
+        GBX_TRY(tot.alloc(1, s));
+        total = tot.p;
+        GBX_TRY(exclusive_scan_u32(*d_deg, *d_off, V, s, total));
+        GBX_CUDA(cudaMemcpyAsync(*d_off + V, total, 4, cudaMemcpyDeviceToDevice, s));
+        InArray<uint32_t> eidx;
+        GBX_TRY(eidx.bind(edges_idx, V, s));
+        check_layout_kernel<<<grid_for(V), 256, 0, s>>>(eidx.d, *d_deg, *d_off, V, bad.p);
+        GBX_LAUNCH_CHECK();
+        uint32_t hv = 0;
+        GBX_CUDA(cudaMemcpyAsync(&hv, total, 4, cudaMemcpyDeviceToHost, s));
+        GBX_CUDA(cudaStreamSynchronize(s));
+        GBX_REQUIRE(hv == E, GBX_ERR_INVALID, "sum of degrees (%u) != num_edges (%u)", hv, E);
+    }
+    GBX_TRY(copy_in(*d_ids, ids, (size_t)E * 4, s));
+    if (E) {
+        mask_ids_kernel<<<grid_for(E), 256, 0, s>>>(*d_ids, E);
+        GBX_LAUNCH_CHECK();
+    }
+    if (w) GBX_TRY(copy_in(*d_w, w, (size_t)E * 4, s));
+    max_u32_kernel<<<grid_for(V), 256, 0, s>>>(*d_deg, V, bad.p + 1);
+    GBX_LAUNCH_CHECK();
+    unsigned hb[2] = {0, 0};
+    GBX_CUDA(cudaMemcpyAsync(hb, bad.p, 8, cudaMemcpyDeviceToHost, s));
+    GBX_CUDA(cudaStreamSynchronize(s));
+    GBX_REQUIRE(hb[0] == 0, GBX_ERR_UNSUPPORTED,
+                "CSR layout rejected: %u vertices whose edges_idx is not the prefix sum of the "
+                "degrees (edges must be a source-sorted contiguous array)",
+                hb[0]);
+    *max_deg = hb[1];
+    return GBX_OK;
+}
+
+static int create_common(gbx_graph **out, uint32_t V, uint32_t E, const uint32_t *edges_idx,
+                         const uint32_t *deg, const uint32_t *off, const uint32_t *dest,
+                         const float *w, const uint32_t *in_idx, const uint32_t *in_deg,
+                         const uint32_t *in_off, const uint32_t *in_src, const float *in_w,
+                         void *stream) {
+    clear_error();
+    GBX_REQUIRE(out != nullptr, GBX_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    GBX_REQUIRE(V > 0, GBX_ERR_INVALID, "num_vertices must be > 0");
+    GBX_REQUIRE(V <= kIdMask + 1u, GBX_ERR_INVALID, "num_vertices exceeds 2^30");
+    GBX_REQUIRE((off != nullptr) || (edges_idx != nullptr && deg != nullptr), GBX_ERR_INVALID,
+                "forward CSR arrays missing");
+    GBX_REQUIRE(E == 0 || dest != nullptr, GBX_ERR_INVALID, "dest is NULL");
+    GBX_TRY(ensure_device());
+    cudaStream_t s = (cudaStream_t)stream;
+    gbx_graph *g = new gbx_graph();
+    cudaGetDevice(&g->device);
+    g->V = V;
+    g->E = E;
+    int st = fill_direction(V, E, edges_idx, deg, off, dest, w, &g->offsets, &g->dest, &g->weight,
+                            &g->out_degree, &g->max_out_degree, s);
+    bool want_inv = (in_off != nullptr) || (in_idx != nullptr && in_deg != nullptr);
+    if (st == GBX_OK && want_inv) {
+        if (E && !in_src) {
+            set_error("in_src is NULL");
+            st = GBX_ERR_INVALID;
+        } else {
+            st = fill_direction(V, E, in_idx, in_deg, in_off, in_src, in_w, &g->in_offsets,
+                                &g->in_src, &g->in_weight, &g->in_degree, &g->max_in_degree, s);
+        }
+    }
+    if (st != GBX_OK) {
+        gbx_graph_destroy(g);
+        return st;
+    }
+    *out = g;
+    return GBX_OK;
+}
+
+}  // namespace gbx
+
+using namespace gbx;
+
+extern "C" {
+
+const char *gbx_status_string(int status) {
+    switch (status) {
+    case GBX_OK: return "ok";
+    case GBX_ERR_INVALID: return "invalid argument";
+    case GBX_ERR_CUDA: return "CUDA error";
+    case GBX_ERR_NOMEM: return "out of device memory";
+    case GBX_ERR_ITER_CAP: return "iteration cap reached";
+    case GBX_ERR_NO_DEVICE: return "no usable CUDA device";
+    case GBX_ERR_UNSUPPORTED: return "unsupported graph layout";
+    case GBX_ERR_DEVICE_TIMEOUT: return "bounded device wait expired";
+    default: return "unknown status";
+    }
+}
+
+const char *gbx_last_error(void) { return g_err; }
+
+const char *gbx_version(void) { return "0.1.0"; }
+
+uint64_t gbx_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int gbx_set_device(int device) {
+    clear_error();
+    GBX_CUDA(cudaSetDevice(device));
+    return ensure_device();
+}
+
+int gbx_graph_create_csr(gbx_graph **out, uint32_t num_vertices, uint32_t num_edges,
+                         const uint32_t *edges_idx, const uint32_t *out_degree,
+                         const uint32_t *dest, const float *weight,
+                         const uint32_t *in_edges_idx, const uint32_t *in_degree,
+                         const uint32_t *in_src, const float *in_weight, void *stream) {
+    GBX_REQUIRE(edges_idx && out_degree, GBX_ERR_INVALID, "edges_idx/out_degree is NULL");
+    return create_common(out, num_vertices, num_edges, edges_idx, out_degree, nullptr, dest, weight,
+                         in_edges_idx, in_degree, nullptr, in_src, in_weight, stream);
+}
+
+int gbx_graph_create_offsets(gbx_graph **out, uint32_t num_vertices, uint32_t num_edges,
+                             const uint32_t *offsets, const uint32_t *dest, const float *weight,
+                             const uint32_t *in_offsets, const uint32_t *in_src,
+                             const float *in_weight, void *stream) {
+    GBX_REQUIRE(offsets, GBX_ERR_INVALID, "offsets is NULL");
+    return create_common(out, num_vertices, num_edges, nullptr, nullptr, offsets, dest, weight,
+                         nullptr, nullptr, in_offsets, in_src, in_weight, stream);
+}
+
+int gbx_graph_destroy(gbx_graph *g) {
+    if (!g) return GBX_OK;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(g->device);
+    cudaDeviceSynchronize();
+    cudaFree(g->offsets);
+    cudaFree(g->dest);
+    cudaFree(g->weight);
+    cudaFree(g->out_degree);
+    cudaFree(g->in_offsets);
+    cudaFree(g->in_src);
+    cudaFree(g->in_weight);
+    cudaFree(g->in_degree);
+    free_plan(g->plan_fwd);
+    free_plan(g->plan_inv);
+    cudaSetDevice(prev);
+    delete g;
+    return GBX_OK;
+}
+
+int gbx_graph_info(const gbx_graph *g, uint32_t *num_vertices, uint32_t *num_edges,
+                   int *has_inverse, int *has_weights) {
+    GBX_REQUIRE(g, GBX_ERR_INVALID, "graph is NULL");
+    if (num_vertices) *num_vertices = g->V;
+    if (num_edges) *num_edges = g->E;
+    if (has_inverse) *has_inverse = g->has_inverse() ? 1 : 0;
+    if (has_weights) *has_weights = g->weight ? 1 : 0;
+    return GBX_OK;
+}
+
+int gbx_graph_device_arrays(const gbx_graph *g, const uint32_t **offsets, const uint32_t **dest,
+                            const float **weight, const uint32_t **in_offsets,
+                            const uint32_t **in_src, const float **in_weight) {
+    GBX_REQUIRE(g, GBX_ERR_INVALID, "graph is NULL");
+    if (offsets) *offsets = g->offsets;
+    if (dest) *dest = g->dest;
+    if (weight) *weight = g->weight;
+    if (in_offsets) *in_offsets = g->in_offsets;
+    if (in_src) *in_src = g->in_src;
+    if (in_weight) *in_weight = g->in_weight;
+    return GBX_OK;
+}
+
+}  // extern "C"

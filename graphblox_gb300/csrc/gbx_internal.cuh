@@ -1,0 +1,223 @@
+// Internal helpers shared by the libgbx translation units: status handling,
+// device queries, stream-ordered buffers, host/device pointer staging, warp
+// and block reductions, and the device-resident graph object.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <cstdio>
+
+#include "gbx.h"
+
+namespace gbx {
+
+constexpr uint32_t kIdMask = 0x3FFFFFFFu;      // EXTRACT_VALUE mask, reorder.h:21-23
+constexpr uint32_t kInfLevel = 0xFFFFFFFFu;    // unvisited BFS level
+constexpr uint32_t kSsspInf = 0xFFFFFFFFu / 2; // UINT_MAX/2, SSSP.c:66-67
+
+// ---- status --------------------------------------------------------------
+void set_error(const char *fmt, ...);
+void clear_error();
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+
+#define GBX_CUDA(call)                                                        \
+    do {                                                                      \
+        cudaError_t gbx_e_ = (call);                                          \
+        if (gbx_e_ != cudaSuccess) return ::gbx::cuda_fail(gbx_e_, #call, __FILE__, __LINE__); \
+    } while (0)
+// counts kernel launches (every launch site is followed by this check)
+void note_launch();
+#define GBX_LAUNCH_CHECK()         \
+    do {                           \
+        ::gbx::note_launch();      \
+        GBX_CUDA(cudaGetLastError()); \
+    } while (0)
+#define GBX_TRY(expr)                                                         \
+    do {                                                                      \
+        int gbx_s_ = (expr);                                                  \
+        if (gbx_s_ != GBX_OK) return gbx_s_;                                  \
+    } while (0)
+#define GBX_REQUIRE(cond, code, ...)                                          \
+    do {                                                                      \
+        if (!(cond)) {                                                        \
+            ::gbx::set_error(__VA_ARGS__);                                    \
+            return (code);                                                    \
+        }                                                                     \
+    } while (0)
+
+// ---- device ----------------------------------------------------------------
+// Make sure a device is usable; caches per-device properties.
+int ensure_device();
+int num_sms();             // SMs of the current device
+size_t l2_bytes();         // L2 size of the current device
+
+// true when p is device (or managed) memory that kernels can read directly
+bool is_device_ptr(const void *p);
+
+inline unsigned ceil_div(uint64_t a, uint64_t b) { return (unsigned)((a + b - 1) / b); }
+
+// ---- stream-ordered device buffer -----------------------------------------
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    cudaStream_t s = nullptr;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    int alloc(size_t count, cudaStream_t stream) {
+        release();
+        s = stream;
+        n = count;
+        if (count == 0) return GBX_OK;
+        cudaError_t e = cudaMallocAsync((void **)&p, count * sizeof(T), stream);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            n = 0;
+            (void)cudaGetLastError();
+            set_error("device allocation of %zu bytes failed: %s", count * sizeof(T),
+                      cudaGetErrorString(e));
+            return GBX_ERR_NOMEM;
+        }
+        return GBX_OK;
+    }
+    void release() {
+        if (p) cudaFreeAsync(p, s);
+        p = nullptr;
+        n = 0;
+    }
+    T *get() const { return p; }
+};
+
+// Input array view: device pointer as is, or a staged device copy of host data.
+template <typename T>
+struct InArray {
+    const T *d = nullptr;
+    DevBuf<T> owned;
+    int bind(const T *src, size_t count, cudaStream_t s) {
+        if (src == nullptr || count == 0) {
+            d = nullptr;
+            return GBX_OK;
+        }
+        if (is_device_ptr(src)) {
+            d = src;
+            return GBX_OK;
+        }
+        GBX_TRY(owned.alloc(count, s));
+        GBX_CUDA(cudaMemcpyAsync(owned.p, src, count * sizeof(T), cudaMemcpyHostToDevice, s));
+        d = owned.p;
+        return GBX_OK;
+    }
+};
+
+// Output array view: write directly into device memory, or into a device
+// buffer copied back to host memory by finish().
+template <typename T>
+struct OutArray {
+    T *d = nullptr;
+    T *host = nullptr;
+    size_t n = 0;
+    DevBuf<T> owned;
+    int bind(T *dst, size_t count, cudaStream_t s) {
+        n = count;
+        host = nullptr;
+        if (dst == nullptr) {
+            d = nullptr;
+            return GBX_OK;
+        }
+        if (is_device_ptr(dst)) {
+            d = dst;
+            return GBX_OK;
+        }
+        host = dst;
+        GBX_TRY(owned.alloc(count ? count : 1, s));
+        d = owned.p;
+        return GBX_OK;
+    }
+    int finish(cudaStream_t s) {
+        if (host && n) GBX_CUDA(cudaMemcpyAsync(host, d, n * sizeof(T), cudaMemcpyDeviceToHost, s));
+        return GBX_OK;
+    }
+    bool to_host() const { return host != nullptr; }
+};
+
+// ---- warp / block reductions -----------------------------------------------
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_min(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        T w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w < v ? w : v;
+    }
+    return v;
+}
+
+// Sum over the block; result valid in thread 0. `sh` holds >= 32 T.
+template <typename T>
+__device__ __forceinline__ T block_sum(T v, T *sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    const int nw = (blockDim.x + 31) >> 5;
+    v = (threadIdx.x < (unsigned)nw) ? sh[threadIdx.x] : T(0);
+    if (wid == 0) v = warp_sum(v);
+    return v;
+}
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+}  // namespace gbx
+
+// ---- device-resident graph ---------------------------------------------------
+struct gbx_gather_plan;  // row classes for the pull engine (gbx_gather.cuh)
+
+struct gbx_graph {
+    int device = 0;
+    uint32_t V = 0;
+    uint32_t E = 0;
+    // forward CSR
+    uint32_t *offsets = nullptr;     // V+1
+    uint32_t *dest = nullptr;        // E
+    float *weight = nullptr;         // E or null
+    uint32_t *out_degree = nullptr;  // V
+    // inverse CSR (in-edges) or null
+    uint32_t *in_offsets = nullptr;  // V+1
+    uint32_t *in_src = nullptr;      // E
+    float *in_weight = nullptr;      // E or null
+    uint32_t *in_degree = nullptr;   // V
+    // lazily built pull plans (forward / inverse)
+    gbx_gather_plan *plan_fwd = nullptr;
+    gbx_gather_plan *plan_inv = nullptr;
+    uint32_t max_out_degree = 0;
+    uint32_t max_in_degree = 0;
+
+    bool has_inverse() const { return in_offsets != nullptr; }
+    // CSR used by pull-direction kernels (reference: inverse when DIRECTED)
+    const uint32_t *pull_offsets() const { return in_offsets ? in_offsets : offsets; }
+    const uint32_t *pull_src() const { return in_offsets ? in_src : dest; }
+    const float *pull_weight() const { return in_offsets ? in_weight : weight; }
+    const uint32_t *pull_degree() const { return in_offsets ? in_degree : out_degree; }
+};
+
+namespace gbx {
+// plan for the pull CSR of g (built on first use, cached on the graph)
+int get_pull_plan(gbx_graph *g, cudaStream_t s, gbx_gather_plan **plan);
+void free_plan(gbx_gather_plan *p);
+// device-wide exclusive scans (gbx_scan.cu); temp storage is internal
+int exclusive_scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, cudaStream_t s,
+                       uint32_t *total_dev /* may be null */);
+int exclusive_scan_u64(const uint32_t *in, uint64_t *out, uint32_t n, cudaStream_t s);
+// stable LSD radix sort of (key, value) pairs on `bits` low key bits (gbx_sort.cu)
+int radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t n, int bits, cudaStream_t s);
+}  // namespace gbx

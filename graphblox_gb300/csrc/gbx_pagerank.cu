@@ -1,0 +1,159 @@
+// Pull PageRank (the reference's pageRankPullGraphCSR, pageRank.c:245-368).
+//
+// One fused kernel per iteration: for every vertex v the pull engine sums
+// contrib[u] over v's in-edges, and the epilogue computes
+//   next = base_pr + damp * sum           (base_pr = 1 - 0.85f, damp = 0.85f)
+//   contrib_next[v] = next / outdeg(v)    (0 for dangling vertices)
+//   |next - prev| -> FP64 error sum, active count (>= epsilon)
+// so the reference's three V-sized passes (contrib, gather, update) become
+// one sweep. Ranks and contributions ping-pong between two buffers.
+//
+// Iterations are launched back to back with no host round trip; iteration
+// `it` returns immediately when iteration it-1 left no active vertex, which
+// reproduces the reference's early exit (stats->iterations = the index of the
+// iteration with no active vertex). A final kernel divides by N (:344-350).
+#include <algorithm>
+
+#include "gbx_gather.cuh"
+
+namespace gbx {
+
+struct PrIterState {
+    double err;
+    unsigned active;
+    unsigned pad;
+};
+
+struct PrTerm {
+    const uint32_t *__restrict__ src;
+    const float *__restrict__ contrib;
+    __device__ __forceinline__ float operator()(uint32_t e) const { return __ldg(contrib + __ldg(src + e)); }
+};
+
+struct PrEpi {
+    const float *__restrict__ r_cur;
+    float *__restrict__ r_next;
+    float *__restrict__ contrib_next;
+    const uint32_t *__restrict__ out_degree;
+    PrIterState *state;  // this iteration's slot
+    double epsilon;
+    double inv_n;
+    double err;
+    unsigned active;
+    __device__ __forceinline__ void operator()(uint32_t v, float sum) {
+        const float damp = 0.85f;
+        const float base = 1.0f - 0.85f;
+        float next = __fadd_rn(base, __fmul_rn(damp, sum));
+        float prev = r_cur[v];
+        r_next[v] = next;
+        uint32_t d = out_degree[v];
+        contrib_next[v] = d ? __fdiv_rn(next, (float)d) : 0.0f;
+        double e = (double)fabsf(__fsub_rn(next, prev));
+        err += e * inv_n;
+        active += (e >= epsilon) ? 1u : 0u;
+    }
+    __device__ __forceinline__ void block_finish() {
+        __shared__ double sd[32];
+        __shared__ unsigned su[32];
+        double te = block_sum(err, sd);
+        unsigned ta = block_sum(active, su);
+        if (threadIdx.x == 0) {
+            if (te != 0.0) atomicAdd(&state->err, te);
+            if (ta) atomicAdd(&state->active, ta);
+        }
+    }
+};
+
+__global__ void pr_init_kernel(float *r, float *contrib, const uint32_t *out_degree, uint32_t V) {
+    const float base = 1.0f - 0.85f;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        r[v] = base;
+        uint32_t d = out_degree[v];
+        contrib[v] = d ? __fdiv_rn(base, (float)d) : 0.0f;
+    }
+}
+
+// Iteration `it`: skip when the previous iteration converged.
+template <class Term, class Epi>
+__global__ void __launch_bounds__(kGatherThreads)
+    pr_iteration_kernel(const uint32_t *__restrict__ off, uint32_t V, gbx_gather_plan plan,
+                        GatherGeometry geo, Term term, Epi epi, const PrIterState *prev) {
+    if (prev && prev->active == 0) return;
+    gather_rows_kernel_body(off, V, plan, geo, term, epi);
+}
+
+// final ranks: pick the buffer holding the last executed iteration
+__global__ void pr_finish_kernel(const float *r0, const float *r1, const PrIterState *st,
+                                 uint32_t max_it, uint32_t V, float *out, uint32_t *iters_out,
+                                 gbx_pr_result *res_dev) {
+    __shared__ uint32_t s_k;
+    if (threadIdx.x == 0) {
+        uint32_t k = max_it;
+        for (uint32_t i = 0; i < max_it; ++i)
+            if (st[i].active == 0) { k = i; break; }
+        s_k = k;
+    }
+    __syncthreads();
+    uint32_t k = s_k;
+    uint32_t executed = k < max_it ? k + 1 : max_it;
+    const float *r = (executed & 1u) ? r1 : r0;
+    const float nf = (float)V;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+        out[v] = __fdiv_rn(r[v], nf);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        res_dev->iterations = k;
+        uint32_t last = executed ? executed - 1 : 0;
+        res_dev->active_last = executed ? st[last].active : 0;
+        res_dev->error_total = executed ? st[last].err : 0.0;
+        if (iters_out) *iters_out = k;
+    }
+}
+
+}  // namespace gbx
+
+using namespace gbx;
+
+extern "C" int gbx_pagerank_pull(gbx_graph *g, uint32_t max_iterations, double epsilon,
+                                 float *ranks, gbx_pr_result *result, void *stream) {
+    clear_error();
+    GBX_REQUIRE(g && ranks, GBX_ERR_INVALID, "graph or ranks is NULL");
+    GBX_REQUIRE(epsilon >= 0.0, GBX_ERR_INVALID, "epsilon must be >= 0");
+    GBX_TRY(ensure_device());
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t V = g->V;
+    gbx_gather_plan *plan = nullptr;
+    GBX_TRY(get_pull_plan(g, s, &plan));
+    OutArray<float> out;
+    GBX_TRY(out.bind(ranks, V, s));
+    DevBuf<float> rbuf, cbuf;
+    DevBuf<PrIterState> st;
+    DevBuf<gbx_pr_result> res;
+    GBX_TRY(rbuf.alloc((size_t)2 * V, s));
+    GBX_TRY(cbuf.alloc((size_t)2 * V, s));
+    GBX_TRY(st.alloc(max_iterations ? max_iterations : 1, s));
+    GBX_TRY(res.alloc(1, s));
+    GBX_CUDA(cudaMemsetAsync(st.p, 0, sizeof(PrIterState) * (max_iterations ? max_iterations : 1), s));
+    float *r[2] = {rbuf.p, rbuf.p + V};
+    float *c[2] = {cbuf.p, cbuf.p + V};
+    int grid = (int)std::min<uint64_t>((V + 255) / 256, (uint64_t)num_sms() * 8);
+    pr_init_kernel<<<grid, 256, 0, s>>>(r[0], c[0], g->out_degree, V);
+    GBX_LAUNCH_CHECK();
+    GatherGeometry geo = gather_geometry(*plan);
+    const double inv_n = 1.0 / (double)V;
+    for (uint32_t it = 0; it < max_iterations; ++it) {
+        int a = it & 1, b = a ^ 1;
+        PrTerm term{g->pull_src(), c[a]};
+        PrEpi epi{r[a], r[b], c[b], g->out_degree, st.p + it, epsilon, inv_n, 0.0, 0u};
+        pr_iteration_kernel<PrTerm, PrEpi><<<geo.total(), kGatherThreads, 0, s>>>(
+            g->pull_offsets(), V, *plan, geo, term, epi, it ? st.p + it - 1 : nullptr);
+        GBX_LAUNCH_CHECK();
+    }
+    pr_finish_kernel<<<grid, 256, 0, s>>>(r[0], r[1], st.p, max_iterations, V, out.d, nullptr, res.p);
+    GBX_LAUNCH_CHECK();
+    GBX_TRY(out.finish(s));
+    gbx_pr_result hres;
+    GBX_CUDA(cudaMemcpyAsync(&hres, res.p, sizeof(hres), cudaMemcpyDeviceToHost, s));
+    GBX_CUDA(cudaStreamSynchronize(s));
+    if (result) *result = hres;
+    return GBX_OK;
+}

@@ -1,0 +1,87 @@
+// Degree classes for the pull engine (gbx_gather.cuh), built once per graph
+// and direction with an ordered compaction (flags -> exclusive scan ->
+// scatter), so the row lists are in ascending vertex order.
+#include <algorithm>
+
+#include "gbx_gather.cuh"
+
+namespace gbx {
+
+// rows above this degree get a whole CTA
+static uint32_t g_heavy_min = 4096;
+
+__global__ void classify_rows_kernel(const uint32_t *off, uint32_t V, uint32_t heavy_min,
+                                     uint32_t *is_med, uint32_t *is_heavy) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        uint32_t d = off[v + 1] - off[v];
+        is_med[v] = (d > kLightMax && d <= heavy_min) ? 1u : 0u;
+        is_heavy[v] = d > heavy_min ? 1u : 0u;
+    }
+}
+
+__global__ void scatter_rows_kernel(const uint32_t *flag, const uint32_t *pos, uint32_t V,
+                                    uint32_t *out) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+        if (flag[v]) out[pos[v]] = v;
+}
+
+static int build_plan(const uint32_t *off, uint32_t V, cudaStream_t s, gbx_gather_plan **out) {
+    gbx_gather_plan *p = new gbx_gather_plan();
+    p->V = V;
+    p->heavy_min = g_heavy_min;
+    DevBuf<uint32_t> fm, fh, pm, ph, tot;
+    int st = GBX_OK;
+    do {
+        if ((st = fm.alloc(V, s)) || (st = fh.alloc(V, s)) || (st = pm.alloc(V, s)) ||
+            (st = ph.alloc(V, s)) || (st = tot.alloc(2, s)))
+            break;
+        int grid = (int)std::min<uint64_t>((V + 255) / 256, (uint64_t)num_sms() * 8);
+        classify_rows_kernel<<<grid, 256, 0, s>>>(off, V, p->heavy_min, fm.p, fh.p);
+        note_launch();
+        if (cudaGetLastError() != cudaSuccess) { st = GBX_ERR_CUDA; break; }
+        if ((st = exclusive_scan_u32(fm.p, pm.p, V, s, tot.p))) break;
+        if ((st = exclusive_scan_u32(fh.p, ph.p, V, s, tot.p + 1))) break;
+        uint32_t h[2];
+        if (cudaMemcpyAsync(h, tot.p, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            st = GBX_ERR_CUDA;
+            break;
+        }
+        p->n_medium = h[0];
+        p->n_heavy = h[1];
+        if (cudaMalloc(&p->medium_rows, (size_t)(h[0] ? h[0] : 1) * 4) != cudaSuccess ||
+            cudaMalloc(&p->heavy_rows, (size_t)(h[1] ? h[1] : 1) * 4) != cudaSuccess) {
+            st = GBX_ERR_NOMEM;
+            break;
+        }
+        scatter_rows_kernel<<<grid, 256, 0, s>>>(fm.p, pm.p, V, p->medium_rows);
+        scatter_rows_kernel<<<grid, 256, 0, s>>>(fh.p, ph.p, V, p->heavy_rows);
+        note_launch();
+        note_launch();
+        if (cudaGetLastError() != cudaSuccess) { st = GBX_ERR_CUDA; break; }
+    } while (0);
+    if (st != GBX_OK) {
+        (void)cudaGetLastError();
+        if (!gbx_last_error()[0]) set_error("building the pull plan failed");
+        free_plan(p);
+        return st;
+    }
+    *out = p;
+    return GBX_OK;
+}
+
+int get_pull_plan(gbx_graph *g, cudaStream_t s, gbx_gather_plan **plan) {
+    gbx_gather_plan **slot = g->has_inverse() ? &g->plan_inv : &g->plan_fwd;
+    if (!*slot) GBX_TRY(build_plan(g->pull_offsets(), g->V, s, slot));
+    *plan = *slot;
+    return GBX_OK;
+}
+
+void free_plan(gbx_gather_plan *p) {
+    if (!p) return;
+    cudaFree(p->medium_rows);
+    cudaFree(p->heavy_rows);
+    delete p;
+}
+
+}  // namespace gbx

@@ -1,0 +1,296 @@
+// Device preprocessing: the CSR build from an edge list and the degree
+// reordering, i.e. the GPU form of graphCSRPreProcessingStep's sort / dedup /
+// map steps (graphCSR.c:243-327) and of reorderGraphProcessDegree
+// (reorder.c:275-380).
+#include <algorithm>
+
+#include "gbx_internal.cuh"
+
+namespace gbx {
+
+static unsigned grid1d(uint64_t n) {
+    uint64_t b = (n + 255) / 256;
+    uint64_t cap = (uint64_t)num_sms() * 8;
+    return (unsigned)std::max<uint64_t>(1, std::min(b, cap));
+}
+
+__global__ void iota_kernel(uint32_t *a, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = i;
+}
+
+// symmetric: second half holds every edge reversed (edgeList.c:559-576)
+__global__ void stage_edges_kernel(const uint32_t *src, const uint32_t *dst, const float *w,
+                                   uint32_t E, int symmetric, uint32_t *s, uint32_t *d, float *wo) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < E; i += gridDim.x * blockDim.x) {
+        uint32_t a = src[i], b = dst[i];
+        s[i] = a;
+        d[i] = b;
+        if (wo) wo[i] = w ? w[i] : 1.0f;
+        if (symmetric) {
+            s[i + E] = b;
+            d[i + E] = a;
+            if (wo) wo[i + E] = w ? w[i] : 1.0f;
+        }
+    }
+}
+
+__global__ void max_id_kernel(const uint32_t *s, const uint32_t *d, uint32_t n, uint32_t *out) {
+    uint32_t m = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        m = max(m, max(s[i], d[i]));
+    m = __reduce_max_sync(0xffffffffu, m);
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+__global__ void gather_u32_kernel(const uint32_t *in, const uint32_t *perm, uint32_t n, uint32_t *out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = in[perm[i]];
+}
+
+__global__ void gather_f32_kernel(const float *in, const uint32_t *perm, uint32_t n, float *out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = in[perm[i]];
+}
+
+// removeDulpicatesSelfLoopEdges on a (src,dst)-sorted list: keep edge i when
+// it is not a self loop and differs from edge i-1 (edgeList.c:255-321)
+__global__ void dedup_flags_kernel(const uint32_t *s, const uint32_t *d, uint32_t n, uint32_t *keep) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t a = s[i], b = d[i];
+        bool k = a != b && (i == 0 || a != s[i - 1] || b != d[i - 1]);
+        keep[i] = k ? 1u : 0u;
+    }
+}
+
+// compaction; kept weights are truncated through uint32 as the reference's
+// uint32_t tempWeight does (edgeList.c:260,273)
+__global__ void compact_edges_kernel(const uint32_t *s, const uint32_t *d, const float *w,
+                                     const uint32_t *keep, const uint32_t *pos, uint32_t n,
+                                     uint32_t *so, uint32_t *dout, float *wo) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!keep[i]) continue;
+        uint32_t p = pos[i];
+        so[p] = s[i];
+        dout[p] = d[i];
+        if (wo) wo[p] = (float)(uint32_t)w[i];
+    }
+}
+
+// mapVerticesWithInOutDegree_base (vertex.c:204-328)
+__global__ void map_vertices_kernel(const uint32_t *s, uint32_t n, uint32_t *deg, uint32_t *idx) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t v = s[i] & kIdMask;
+        atomicAdd(deg + v, 1u);
+        if (i == 0 || s[i] != s[i - 1]) idx[v] = i;
+    }
+}
+
+__global__ void degree_count_kernel(const uint32_t *s, const uint32_t *d, uint32_t n, int lmode,
+                                    uint32_t *deg) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (lmode == 2) atomicAdd(deg + d[i], 1u);
+        else if (lmode == 3) { atomicAdd(deg + d[i], 1u); atomicAdd(deg + s[i], 1u); }
+        else atomicAdd(deg + s[i], 1u);
+    }
+}
+
+__global__ void new_labels_kernel(const uint32_t *sorted_ids, uint32_t V, uint32_t *newlab) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < V; i += gridDim.x * blockDim.x)
+        newlab[sorted_ids[i]] = V - 1 - i;
+}
+
+__global__ void relabel_edges_kernel(uint32_t *s, uint32_t *d, uint32_t n, const uint32_t *newlab) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        s[i] = newlab[s[i]];
+        d[i] = newlab[d[i]];
+    }
+}
+
+// label_array[v] = labels[label_array[v]]; inverse[label_array[v]] = v  (reorder.c:368-373)
+__global__ void compose_labels_kernel(uint32_t *labels, uint32_t *inv, uint32_t V, const uint32_t *newlab) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        uint32_t l = newlab[labels[v]];
+        labels[v] = l;
+        inv[l] = v;
+    }
+}
+
+static int bits_for(uint32_t maxv) {
+    int b = 0;
+    while (b < 32 && (maxv >> b)) ++b;
+    return b;
+}
+
+}  // namespace gbx
+
+using namespace gbx;
+
+extern "C" int gbx_csr_build(uint32_t num_edges, const uint32_t *src, const uint32_t *dst,
+                             const float *w, int symmetric, int dedup, int sort_mode,
+                             uint32_t num_vertices, uint32_t *out_degree, uint32_t *edges_idx,
+                             uint32_t *src_out, uint32_t *dst_out, float *w_out,
+                             uint32_t *num_edges_out, void *stream) {
+    clear_error();
+    GBX_REQUIRE(num_edges == 0 || (src && dst), GBX_ERR_INVALID, "src/dst is NULL");
+    GBX_REQUIRE(out_degree && edges_idx && num_edges_out, GBX_ERR_INVALID, "output is NULL");
+    GBX_REQUIRE(num_vertices > 0, GBX_ERR_INVALID, "num_vertices must be > 0");
+    GBX_REQUIRE(!dedup || sort_mode == 1 || sort_mode == 3, GBX_ERR_INVALID,
+                "dedup needs a (source,destination) sort (sort_mode 1)");
+    GBX_REQUIRE(!symmetric || num_edges <= 0x7FFFFFFFu, GBX_ERR_INVALID, "too many edges");
+    GBX_TRY(ensure_device());
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t E = num_edges, E2 = symmetric ? 2 * num_edges : num_edges, V = num_vertices;
+    InArray<uint32_t> isrc, idst;
+    InArray<float> iw;
+    GBX_TRY(isrc.bind(src, E, s));
+    GBX_TRY(idst.bind(dst, E, s));
+    GBX_TRY(iw.bind(w, E, s));
+    const bool want_w = w_out != nullptr;
+    DevBuf<uint32_t> es, ed, perm, keys, maxid;
+    DevBuf<float> ew;
+    GBX_TRY(es.alloc(E2, s));
+    GBX_TRY(ed.alloc(E2, s));
+    GBX_TRY(perm.alloc(E2, s));
+    GBX_TRY(keys.alloc(E2, s));
+    GBX_TRY(maxid.alloc(1, s));
+    if (want_w) GBX_TRY(ew.alloc(E2, s));
+    if (E) {
+        stage_edges_kernel<<<grid1d(E), 256, 0, s>>>(isrc.d, idst.d, iw.d, E, symmetric, es.p, ed.p,
+                                                     want_w ? ew.p : nullptr);
+        GBX_LAUNCH_CHECK();
+    }
+    GBX_CUDA(cudaMemsetAsync(maxid.p, 0, 4, s));
+    if (E2) {
+        max_id_kernel<<<grid1d(E2), 256, 0, s>>>(es.p, ed.p, E2, maxid.p);
+        GBX_LAUNCH_CHECK();
+    }
+    uint32_t hmax = 0;
+    GBX_CUDA(cudaMemcpyAsync(&hmax, maxid.p, 4, cudaMemcpyDeviceToHost, s));
+    GBX_CUDA(cudaStreamSynchronize(s));
+    GBX_REQUIRE(E2 == 0 || hmax < V, GBX_ERR_INVALID, "vertex id %u >= num_vertices %u", hmax, V);
+    const int bits = bits_for(hmax);
+    // stable sort: destination pass(es) first, then source (LSD on the pair)
+    iota_kernel<<<grid1d(E2), 256, 0, s>>>(perm.p, E2);
+    GBX_LAUNCH_CHECK();
+    if (sort_mode == 1 || sort_mode == 3) {
+        GBX_CUDA(cudaMemcpyAsync(keys.p, ed.p, (size_t)E2 * 4, cudaMemcpyDeviceToDevice, s));
+        GBX_TRY(radix_sort_pairs(keys.p, perm.p, E2, bits, s));
+    }
+    gather_u32_kernel<<<grid1d(E2), 256, 0, s>>>(es.p, perm.p, E2, keys.p);
+    GBX_LAUNCH_CHECK();
+    GBX_TRY(radix_sort_pairs(keys.p, perm.p, E2, bits, s));
+    // apply the permutation
+    DevBuf<uint32_t> ss, sd, keep, pos, tot;
+    DevBuf<float> sw;
+    GBX_TRY(ss.alloc(E2, s));
+    GBX_TRY(sd.alloc(E2, s));
+    if (want_w) GBX_TRY(sw.alloc(E2, s));
+    GBX_CUDA(cudaMemcpyAsync(ss.p, keys.p, (size_t)E2 * 4, cudaMemcpyDeviceToDevice, s));
+    gather_u32_kernel<<<grid1d(E2), 256, 0, s>>>(ed.p, perm.p, E2, sd.p);
+    if (want_w) gather_f32_kernel<<<grid1d(E2), 256, 0, s>>>(ew.p, perm.p, E2, sw.p);
+    GBX_LAUNCH_CHECK();
+    uint32_t Eout = E2;
+    OutArray<uint32_t> os, od, odeg, oidx;
+    OutArray<float> ow;
+    const uint32_t *fs = ss.p, *fd = sd.p;
+    const float *fw = sw.p;
+    if (dedup && E2) {
+        GBX_TRY(keep.alloc(E2, s));
+        GBX_TRY(pos.alloc(E2, s));
+        GBX_TRY(tot.alloc(1, s));
+        dedup_flags_kernel<<<grid1d(E2), 256, 0, s>>>(ss.p, sd.p, E2, keep.p);
+        GBX_LAUNCH_CHECK();
+        GBX_TRY(exclusive_scan_u32(keep.p, pos.p, E2, s, tot.p));
+        GBX_CUDA(cudaMemcpyAsync(&Eout, tot.p, 4, cudaMemcpyDeviceToHost, s));
+        GBX_CUDA(cudaStreamSynchronize(s));
+        // compact into es/ed/ew (free now)
+        compact_edges_kernel<<<grid1d(E2), 256, 0, s>>>(ss.p, sd.p, sw.p, keep.p, pos.p, E2, es.p,
+                                                        ed.p, want_w ? ew.p : nullptr);
+        GBX_LAUNCH_CHECK();
+        fs = es.p;
+        fd = ed.p;
+        fw = ew.p;
+    }
+    GBX_TRY(odeg.bind(out_degree, V, s));
+    GBX_TRY(oidx.bind(edges_idx, V, s));
+    GBX_CUDA(cudaMemsetAsync(odeg.d, 0, (size_t)V * 4, s));
+    GBX_CUDA(cudaMemsetAsync(oidx.d, 0, (size_t)V * 4, s));
+    if (Eout) {
+        map_vertices_kernel<<<grid1d(Eout), 256, 0, s>>>(fs, Eout, odeg.d, oidx.d);
+        GBX_LAUNCH_CHECK();
+    }
+    GBX_TRY(odeg.finish(s));
+    GBX_TRY(oidx.finish(s));
+    if (src_out) {
+        GBX_TRY(os.bind(src_out, Eout, s));
+        GBX_CUDA(cudaMemcpyAsync(os.d, fs, (size_t)Eout * 4, cudaMemcpyDeviceToDevice, s));
+        GBX_TRY(os.finish(s));
+    }
+    if (dst_out) {
+        GBX_TRY(od.bind(dst_out, Eout, s));
+        GBX_CUDA(cudaMemcpyAsync(od.d, fd, (size_t)Eout * 4, cudaMemcpyDeviceToDevice, s));
+        GBX_TRY(od.finish(s));
+    }
+    if (want_w) {
+        GBX_TRY(ow.bind(w_out, Eout, s));
+        GBX_CUDA(cudaMemcpyAsync(ow.d, fw, (size_t)Eout * 4, cudaMemcpyDeviceToDevice, s));
+        GBX_TRY(ow.finish(s));
+    }
+    GBX_CUDA(cudaStreamSynchronize(s));
+    *num_edges_out = Eout;
+    return GBX_OK;
+}
+
+extern "C" int gbx_degree_reorder(uint32_t num_vertices, uint32_t num_edges, uint32_t *src,
+                                  uint32_t *dst, int lmode, uint32_t *labels,
+                                  uint32_t *inverse_labels, void *stream) {
+    clear_error();
+    GBX_REQUIRE(num_vertices > 0, GBX_ERR_INVALID, "num_vertices must be > 0");
+    GBX_REQUIRE(num_edges == 0 || (src && dst), GBX_ERR_INVALID, "src/dst is NULL");
+    GBX_REQUIRE(labels && inverse_labels, GBX_ERR_INVALID, "labels is NULL");
+    GBX_REQUIRE(lmode >= 1 && lmode <= 3, GBX_ERR_INVALID, "lmode must be 1, 2 or 3");
+    GBX_TRY(ensure_device());
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t V = num_vertices, E = num_edges;
+    OutArray<uint32_t> os, od, ol, oi;
+    GBX_TRY(os.bind(src, E, s));
+    GBX_TRY(od.bind(dst, E, s));
+    GBX_TRY(ol.bind(labels, V, s));
+    GBX_TRY(oi.bind(inverse_labels, V, s));
+    if (os.to_host() && E) GBX_CUDA(cudaMemcpyAsync(os.d, src, (size_t)E * 4, cudaMemcpyHostToDevice, s));
+    if (od.to_host() && E) GBX_CUDA(cudaMemcpyAsync(od.d, dst, (size_t)E * 4, cudaMemcpyHostToDevice, s));
+    if (ol.to_host()) GBX_CUDA(cudaMemcpyAsync(ol.d, labels, (size_t)V * 4, cudaMemcpyHostToDevice, s));
+    DevBuf<uint32_t> deg, ids, newlab, mx;
+    GBX_TRY(deg.alloc(V, s));
+    GBX_TRY(ids.alloc(V, s));
+    GBX_TRY(newlab.alloc(V, s));
+    GBX_TRY(mx.alloc(1, s));
+    GBX_CUDA(cudaMemsetAsync(deg.p, 0, (size_t)V * 4, s));
+    if (E) {
+        degree_count_kernel<<<grid1d(E), 256, 0, s>>>(os.d, od.d, E, lmode, deg.p);
+        GBX_LAUNCH_CHECK();
+    }
+    GBX_CUDA(cudaMemsetAsync(mx.p, 0, 4, s));
+    max_id_kernel<<<grid1d(V), 256, 0, s>>>(deg.p, deg.p, V, mx.p);
+    GBX_LAUNCH_CHECK();
+    uint32_t hmax = 0;
+    GBX_CUDA(cudaMemcpyAsync(&hmax, mx.p, 4, cudaMemcpyDeviceToHost, s));
+    GBX_CUDA(cudaStreamSynchronize(s));
+    iota_kernel<<<grid1d(V), 256, 0, s>>>(ids.p, V);
+    GBX_LAUNCH_CHECK();
+    GBX_TRY(radix_sort_pairs(deg.p, ids.p, V, bits_for(hmax), s));
+    new_labels_kernel<<<grid1d(V), 256, 0, s>>>(ids.p, V, newlab.p);
+    GBX_LAUNCH_CHECK();
+    if (E) {
+        relabel_edges_kernel<<<grid1d(E), 256, 0, s>>>(os.d, od.d, E, newlab.p);
+        GBX_LAUNCH_CHECK();
+    }
+    compose_labels_kernel<<<grid1d(V), 256, 0, s>>>(ol.d, oi.d, V, newlab.p);
+    GBX_LAUNCH_CHECK();
+    GBX_TRY(os.finish(s));
+    GBX_TRY(od.finish(s));
+    GBX_TRY(ol.finish(s));
+    GBX_TRY(oi.finish(s));
+    GBX_CUDA(cudaStreamSynchronize(s));
+    return GBX_OK;
+}

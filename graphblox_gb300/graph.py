@@ -1,0 +1,366 @@
+"""Host-side mirror of the reference's graph-load and algorithm interfaces.
+
+Names and argument meanings follow the GraphBlox host:
+  EdgeList / read_edge_list_bin   -> struct EdgeList, readEdgeListsbin (edgeList.c:450-706)
+  GraphCSR / graph_csr_preprocessing -> struct GraphCSR, graphCSRPreProcessingStep (graphCSR.c:243-327)
+  DeviceGraph                     -> the device copy of a GraphCSR (gbx_graph_create_csr)
+  breadth_first_search, page_rank, sssp, connected_components, triangle_count, spmv
+                                  -> breadthFirstSearchGraphCSR, pageRankGraphCSR, SSSPGraphCSR,
+                                     connectedComponentsGraphCSR, triangleCountGraphCSR, SPMVGraphCSR
+Every compute step runs in libgbx.so on the GPU; this module only moves
+arrays and keeps the reference's bookkeeping (label remapping of sources,
+inverse CSR for directed graphs).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import BfsResult, PrResult, SsspResult, call
+
+ID_MASK = np.uint32(0x3FFFFFFF)  # EXTRACT_VALUE, reorder.h:23
+
+
+def _ptr(a) -> Optional[int]:
+    """Address of a numpy array (host) or a torch tensor (host or device)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("arrays must be C-contiguous")
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        if not a.is_contiguous():
+            raise ValueError("tensors must be contiguous")
+        return a.data_ptr()
+    raise TypeError(f"unsupported array type {type(a)!r}")
+
+
+def _u32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def _f32(a) -> Optional[np.ndarray]:
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float32)
+
+
+# ---------------------------------------------------------------------------
+# edge lists
+
+
+@dataclass
+class EdgeList:
+    """struct EdgeList (edgeList.h:12-23), host arrays."""
+    num_vertices: int
+    src: np.ndarray
+    dst: np.ndarray
+    weight: Optional[np.ndarray] = None
+    label_array: Optional[np.ndarray] = None
+    inverse_label_array: Optional[np.ndarray] = None
+
+    @property
+    def num_edges(self) -> int:
+        return int(self.src.shape[0])
+
+
+def read_edge_list_bin(path: str, symmetric: bool = False, weighted: bool = False) -> EdgeList:
+    """readEdgeListsbin: `.bin` is (uint32 src, uint32 dst) records, `.wbin`
+    adds a float32 weight. symmetric appends every edge reversed; the vertex
+    count is the largest id + 1; labels start as the identity."""
+    raw = np.fromfile(path, dtype=np.uint32)
+    width = 3 if weighted else 2
+    n = raw.shape[0] // width
+    rec = raw[: n * width].reshape(n, width)
+    src = rec[:, 0].copy()
+    dst = rec[:, 1].copy()
+    w = rec[:, 2].copy().view(np.float32) if weighted else np.ones(n, dtype=np.float32)
+    if symmetric:
+        src, dst = np.concatenate([src, dst]), np.concatenate([dst, src])
+        w = np.concatenate([w, w])
+    nv = int(max(src.max(initial=0), dst.max(initial=0))) + 1 if n else 1
+    ident = np.arange(nv, dtype=np.uint32)
+    return EdgeList(nv, src, dst, w, ident.copy(), ident.copy())
+
+
+def write_edge_list_bin(path: str, src, dst, weight=None) -> None:
+    """Write the reference's binary edge-list format (.bin or .wbin with weights)."""
+    src = _u32(src)
+    dst = _u32(dst)
+    if weight is None:
+        rec = np.stack([src, dst], axis=1)
+    else:
+        rec = np.stack([src, dst, _f32(weight).view(np.uint32)], axis=1)
+    np.ascontiguousarray(rec).tofile(path)
+
+
+# ---------------------------------------------------------------------------
+# CSR on the host (result of the GPU preprocessing step)
+
+
+@dataclass
+class GraphCSR:
+    """struct GraphCSR (graphCSR.h:14-31) with host arrays. `inverse_*` hold
+    the in-edge CSR (the reference's DIRECTED build) or None."""
+    num_vertices: int
+    num_edges: int
+    out_degree: np.ndarray
+    edges_idx: np.ndarray
+    dest: np.ndarray
+    src: np.ndarray
+    weight: Optional[np.ndarray]
+    label_array: np.ndarray
+    inverse_label_array: np.ndarray
+    inverse_out_degree: Optional[np.ndarray] = None
+    inverse_edges_idx: Optional[np.ndarray] = None
+    inverse_dest: Optional[np.ndarray] = None
+    inverse_weight: Optional[np.ndarray] = None
+
+    @property
+    def avg_degree(self) -> int:
+        return self.num_edges // self.num_vertices if self.num_vertices else 0
+
+    @property
+    def directed(self) -> bool:
+        return self.inverse_dest is not None
+
+
+def csr_build(src, dst, weight=None, *, num_vertices: int, symmetric: bool = False,
+              dedup: bool = False, sort: int = 1, stream=None):
+    """gbx_csr_build: stable sort (+ optional symmetrisation and dedup) and
+    the per-vertex degree / first-edge arrays. Returns host arrays
+    (out_degree, edges_idx, src, dst, weight)."""
+    src = _u32(src)
+    dst = _u32(dst)
+    w = _f32(weight)
+    e = src.shape[0]
+    cap = 2 * e if symmetric else e
+    V = int(num_vertices)
+    out_degree = np.zeros(V, np.uint32)
+    edges_idx = np.zeros(V, np.uint32)
+    so = np.zeros(max(cap, 1), np.uint32)
+    do = np.zeros(max(cap, 1), np.uint32)
+    wo = np.zeros(max(cap, 1), np.float32) if w is not None else None
+    n_out = _lib.u32(0)
+    call("gbx_csr_build", e, _ptr(src), _ptr(dst), _ptr(w), int(symmetric), int(dedup), int(sort), V,
+         _ptr(out_degree), _ptr(edges_idx), _ptr(so), _ptr(do), _ptr(wo), C.byref(n_out), stream)
+    n = n_out.value
+    return out_degree, edges_idx, so[:n].copy(), do[:n].copy(), (wo[:n].copy() if wo is not None else None)
+
+
+def degree_reorder(el: EdgeList, lmode: int = 1, stream=None) -> EdgeList:
+    """reorderGraphProcessDegree on the GPU: relabels el.src/el.dst in place
+    and composes el.label_array / el.inverse_label_array."""
+    V = el.num_vertices
+    if el.label_array is None:
+        el.label_array = np.arange(V, dtype=np.uint32)
+    if el.inverse_label_array is None:
+        el.inverse_label_array = np.arange(V, dtype=np.uint32)
+    el.src = _u32(el.src)
+    el.dst = _u32(el.dst)
+    call("gbx_degree_reorder", V, el.num_edges, _ptr(el.src), _ptr(el.dst), int(lmode),
+         _ptr(el.label_array), _ptr(el.inverse_label_array), stream)
+    return el
+
+
+def graph_csr_preprocessing(el: EdgeList, *, sort: int = 0, dedup: bool = False, lmode: int = 0,
+                            directed: bool = True, keep_weights: bool = True, stream=None) -> GraphCSR:
+    """graphCSRPreProcessingStep (graphCSR.c:243-327) on the GPU: sort, dedup
+    (-k forces sort 1, GraphBlox.c:355-356), degree reorder + re-sort, CSR
+    map, and for directed graphs the inverse CSR built from the swapped
+    edges with the same sort."""
+    if dedup:
+        sort = 1
+    V = el.num_vertices
+    w = el.weight if keep_weights else None
+    deg, idx, s, d, ww = csr_build(el.src, el.dst, w, num_vertices=V, dedup=dedup, sort=sort, stream=stream)
+    labels = el.label_array if el.label_array is not None else np.arange(V, dtype=np.uint32)
+    inv_labels = el.inverse_label_array if el.inverse_label_array is not None else np.arange(V, dtype=np.uint32)
+    if lmode:
+        tmp = EdgeList(V, s, d, ww, labels.copy(), inv_labels.copy())
+        degree_reorder(tmp, lmode, stream)
+        labels, inv_labels = tmp.label_array, tmp.inverse_label_array
+        deg, idx, s, d, ww = csr_build(tmp.src, tmp.dst, ww, num_vertices=V, sort=sort, stream=stream)
+    g = GraphCSR(V, int(s.shape[0]), deg, idx, d, s, ww, labels, inv_labels)
+    if directed:
+        ideg, iidx, isrc, idst, iw = csr_build(d, s, ww, num_vertices=V, sort=sort, stream=stream)
+        g.inverse_out_degree, g.inverse_edges_idx, g.inverse_dest, g.inverse_weight = ideg, iidx, idst, iw
+    return g
+
+
+# ---------------------------------------------------------------------------
+# device graph
+
+
+class DeviceGraph:
+    """A GraphCSR resident on the GPU (gbx_graph)."""
+
+    def __init__(self, handle: int, num_vertices: int, num_edges: int, label_array=None):
+        self._h = C.c_void_p(handle)
+        self.num_vertices = num_vertices
+        self.num_edges = num_edges
+        self.label_array = label_array
+
+    @classmethod
+    def from_graph_csr(cls, g: GraphCSR, stream=None, use_weights: bool = True) -> "DeviceGraph":
+        h = C.c_void_p()
+        w = g.weight if use_weights else None
+        iw = g.inverse_weight if use_weights else None
+        call("gbx_graph_create_csr", C.byref(h), g.num_vertices, g.num_edges,
+             _ptr(_u32(g.edges_idx)), _ptr(_u32(g.out_degree)), _ptr(_u32(g.dest)), _ptr(_f32(w)),
+             _ptr(None if g.inverse_edges_idx is None else _u32(g.inverse_edges_idx)),
+             _ptr(None if g.inverse_out_degree is None else _u32(g.inverse_out_degree)),
+             _ptr(None if g.inverse_dest is None else _u32(g.inverse_dest)), _ptr(_f32(iw)), stream)
+        return cls(h.value, g.num_vertices, g.num_edges, g.label_array)
+
+    @classmethod
+    def from_offsets(cls, num_vertices, offsets, dest, weight=None, in_offsets=None, in_src=None,
+                     in_weight=None, stream=None) -> "DeviceGraph":
+        h = C.c_void_p()
+        call("gbx_graph_create_offsets", C.byref(h), int(num_vertices), int(len(dest)), _ptr(offsets),
+             _ptr(dest), _ptr(weight), _ptr(in_offsets), _ptr(in_src), _ptr(in_weight), stream)
+        return cls(h.value, int(num_vertices), int(len(dest)))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            _lib.load().gbx_graph_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def _map_source(dg: DeviceGraph, source: int) -> int:
+    # BFS.c:153 / SSSP.c:493: the source is given in original ids
+    if dg.label_array is not None:
+        return int(dg.label_array[source])
+    return int(source)
+
+
+@dataclass
+class BFSStats:
+    distances: object
+    parents: object
+    processed_nodes: int
+    iteration: int
+    depth: int
+    edges_traversed: int
+    source: int
+
+
+def breadth_first_search(dg: DeviceGraph, source: int, pushpull: int = 2, distances=None,
+                         parents=None, stream=None, map_source: bool = True) -> BFSStats:
+    """breadthFirstSearchGraphCSR: pushpull 0 pull, 1 push, 2 direction-optimising."""
+    V = dg.num_vertices
+    src = _map_source(dg, source) if map_source else int(source)
+    if distances is None:
+        distances = np.zeros(V, np.uint32)
+    if parents is None:
+        parents = np.zeros(V, np.int32)
+    mode = {0: 0, 1: 1}.get(int(pushpull), 2)
+    r = BfsResult()
+    call("gbx_bfs", dg.handle, src, mode, _ptr(distances), _ptr(parents), C.byref(r), stream)
+    return BFSStats(distances, parents, r.processed_nodes, r.iteration, r.depth, r.edges_traversed, src)
+
+
+@dataclass
+class PageRankStats:
+    pageRanks: object
+    iterations: int
+    error_total: float
+    active_last: int
+
+
+def page_rank(dg: DeviceGraph, iterations: int = 20, epsilon: float = 1e-4, ranks=None,
+              stream=None) -> PageRankStats:
+    """pageRankPullGraphCSR (pushpull 0)."""
+    if ranks is None:
+        ranks = np.zeros(dg.num_vertices, np.float32)
+    r = PrResult()
+    call("gbx_pagerank_pull", dg.handle, int(iterations), float(epsilon), _ptr(ranks), C.byref(r), stream)
+    return PageRankStats(ranks, r.iterations, r.error_total, r.active_last)
+
+
+@dataclass
+class SSSPStats:
+    distances: object
+    reached: int
+    rounds: int
+    edges_relaxed: int
+    edges_traversed: int
+    source: int
+
+
+def sssp(dg: DeviceGraph, source: int, delta: int = 0, distances=None, stream=None,
+         map_source: bool = True) -> SSSPStats:
+    """SSSPGraphCSR (delta-stepping). Unreached vertices report UINT32_MAX/2."""
+    src = _map_source(dg, source) if map_source else int(source)
+    if distances is None:
+        distances = np.zeros(dg.num_vertices, np.uint32)
+    r = SsspResult()
+    call("gbx_sssp", dg.handle, src, int(delta), _ptr(distances), C.byref(r), stream)
+    return SSSPStats(distances, r.reached, r.rounds, r.edges_relaxed, r.edges_traversed, src)
+
+
+def connected_components(dg: DeviceGraph, variant: int = 1, components=None, stream=None):
+    """connectedComponentsGraphCSR: 0 Shiloach-Vishkin, 1 Afforest, 2 label propagation."""
+    if components is None:
+        components = np.zeros(dg.num_vertices, np.uint32)
+    it = _lib.u32(0)
+    call("gbx_cc", dg.handle, int(variant), _ptr(components), C.byref(it), stream)
+    return components, it.value
+
+
+def triangle_count(dg: DeviceGraph, stream=None) -> int:
+    """triangleCountGraphCSR (pull semantics)."""
+    t = _lib.u64(0)
+    call("gbx_tc", dg.handle, C.byref(t), stream)
+    return int(t.value)
+
+
+def spmv(dg: DeviceGraph, x, values=None, default_value: float = 0.0001, iterations: int = 1, y=None,
+         stream=None):
+    """SPMVGraphCSR pull: y += A x, `iterations` times (y defaults to zeros)."""
+    if isinstance(x, np.ndarray):
+        x = _f32(x)
+    if isinstance(values, np.ndarray):
+        values = _f32(values)
+    if y is None:
+        y = np.zeros(dg.num_vertices, np.float32)
+    call("gbx_spmv", dg.handle, _ptr(values), float(default_value), _ptr(x), _ptr(y), int(iterations), stream)
+    return y
+
+
+# ---------------------------------------------------------------------------
+# synthetic inputs
+
+
+def generate_rmat(scale: int, num_edges: int, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+                  seed: int = 1):
+    src = np.empty(num_edges, np.uint32)
+    dst = np.empty(num_edges, np.uint32)
+    call("gbx_generate_rmat", int(scale), int(num_edges), a, b, c, int(seed), _ptr(src), _ptr(dst))
+    return src, dst
+
+
+def generate_values(count: int, kind: int, lo: int = 0, hi: int = 0, seed: int = 1) -> np.ndarray:
+    """kind 0 int U[lo,hi] as float, 1 U(0,1], 2 U[-1,1), 3 lognormal(0,1)."""
+    out = np.empty(count, np.float32)
+    call("gbx_generate_values", int(count), int(kind), int(lo), int(hi), int(seed), _ptr(out))
+    return out

@@ -1,0 +1,214 @@
+/*
+ * gbx.h -- C ABI of libgbx.so, the GB300 (sm_103a) backend for GraphBlox's
+ * vertex-centric CSR kernels.
+ *
+ * Two layers sit on this ABI:
+ *   - the drop-in "cuda" integration (graphblox_gb300/integration/*.c,
+ *     headers in include/algorithms/cuda/), which exports the same symbols
+ *     and Stats structs as the reference's 01_host/include/algorithms/openmp
+ *     headers so that 01_host/src/utils_graph/graphRun.c links unchanged;
+ *   - the Python host mirror (graphblox_gb300/), which binds it with ctypes.
+ *
+ * Conventions
+ *   - Plain pointers and sizes only. Every array argument may be host memory
+ *     (pageable or pinned) or device memory of the current device; the
+ *     library detects which and copies as needed.
+ *   - Every function returns an int status: GBX_OK (0) or a negative
+ *     GBX_ERR_* code. gbx_last_error() gives a message for the calling thread.
+ *   - `stream` is a cudaStream_t (NULL = the legacy default stream). Entry
+ *     points that return results into host memory synchronize that stream
+ *     before returning; results into device memory are stream-ordered.
+ *   - Vertex ids are uint32 (the reference's limit is 2^30, EXTRACT_VALUE in
+ *     01_host/include/preprocess/reorder.h:23). Edge counts are uint32 in the
+ *     reference-compatible entry points, as in struct GraphCSR.
+ *   - No entry point falls back to the CPU: without a usable GPU every
+ *     compute call fails with GBX_ERR_NO_DEVICE.
+ *
+ * Reference interfaces replaced (paths within the GraphBlox project):
+ *   gbx_graph_create_csr      -> the device copy of struct GraphCSR
+ *                                (01_host/include/structures/graphCSR.h:14-31)
+ *   gbx_bfs                   -> breadthFirstSearchGraphCSR (01_host/src/algorithms/openmp/BFS.c:103-127)
+ *   gbx_pagerank_pull         -> pageRankPullGraphCSR (01_host/src/algorithms/openmp/pageRank.c:245-368)
+ *   gbx_sssp                  -> SSSPGraphCSR (01_host/src/algorithms/openmp/SSSP.c:489-653)
+ *   gbx_cc                    -> connectedComponentsGraphCSR (01_host/src/algorithms/openmp/connectedComponents.c:268-629)
+ *   gbx_tc                    -> triangleCountGraphCSR (01_host/src/algorithms/openmp/triangleCount.c:158-334)
+ *   gbx_spmv                  -> SPMVGraphCSR (01_host/src/algorithms/openmp/SPMV.c:89-215)
+ *   gbx_csr_build             -> graphCSRPreProcessingStep's sort/dedup/map
+ *                                (01_host/src/structures/graphCSR.c:243-327,
+ *                                 radixsort.c:231-339, edgeList.c:255-321, vertex.c:204-328)
+ *   gbx_degree_reorder        -> reorderGraphProcessDegree (01_host/src/preprocess/reorder.c:275-380,1483-1552,1618-1637)
+ * Extension entry points (batched, multi-source, personalised PageRank and
+ * its adjoint, generators) have no reference counterpart.
+ */
+#ifndef GBX_H
+#define GBX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status ---------------------------------------------------------- */
+#define GBX_OK 0
+#define GBX_ERR_INVALID (-1)     /* bad argument (NULL, size, source out of range) */
+#define GBX_ERR_CUDA (-2)        /* a CUDA runtime call failed */
+#define GBX_ERR_NOMEM (-3)       /* device allocation failed */
+#define GBX_ERR_ITER_CAP (-4)    /* an iteration cap was reached before convergence */
+#define GBX_ERR_NO_DEVICE (-5)   /* no usable CUDA device */
+#define GBX_ERR_UNSUPPORTED (-6) /* graph layout not supported by this entry point */
+#define GBX_ERR_DEVICE_TIMEOUT (-7) /* a bounded device-side wait gave up */
+
+const char *gbx_status_string(int status);
+/* Message for the last failing call on this host thread ("" if none). */
+const char *gbx_last_error(void);
+/* Library version as "major.minor.patch". */
+const char *gbx_version(void);
+/* Select the device for subsequent calls on this thread (cudaSetDevice). */
+int gbx_set_device(int device);
+/* Number of kernels this process has launched through the library. */
+uint64_t gbx_kernel_launches(void);
+
+/* ---- device-resident graph ------------------------------------------- */
+typedef struct gbx_graph gbx_graph;
+
+/* Copy a CSR in the reference's layout to the device.
+ *   edges_idx[v], out_degree[v]: first edge position and degree of v (the
+ *     reference's struct Vertex, vertex.h:17-23; edges_idx is 0 for
+ *     degree-0 vertices). The edges of v must be the contiguous run
+ *     dest[edges_idx[v] .. +out_degree[v]) of a source-sorted edge array,
+ *     which is what the reference's CSR build produces; other layouts are
+ *     rejected with GBX_ERR_UNSUPPORTED.
+ *   dest[E], weight[E] (weight may be NULL).
+ *   in_*: the inverse CSR (in-edges; the reference's DIRECTED 1 build), or
+ *     all NULL. Pull-direction kernels use it when present, else they pull
+ *     over the forward CSR (the reference's DIRECTED 0 behaviour).
+ * The top two bits of ids (the reference's mask bits) are cleared. */
+int gbx_graph_create_csr(gbx_graph **out, uint32_t num_vertices, uint32_t num_edges,
+                         const uint32_t *edges_idx, const uint32_t *out_degree,
+                         const uint32_t *dest, const float *weight,
+                         const uint32_t *in_edges_idx, const uint32_t *in_degree,
+                         const uint32_t *in_src, const float *in_weight, void *stream);
+/* Same, from standard CSR offsets (num_vertices+1 entries). */
+int gbx_graph_create_offsets(gbx_graph **out, uint32_t num_vertices, uint32_t num_edges,
+                             const uint32_t *offsets, const uint32_t *dest, const float *weight,
+                             const uint32_t *in_offsets, const uint32_t *in_src,
+                             const float *in_weight, void *stream);
+int gbx_graph_destroy(gbx_graph *g);
+int gbx_graph_info(const gbx_graph *g, uint32_t *num_vertices, uint32_t *num_edges,
+                   int *has_inverse, int *has_weights);
+/* Device pointers of the resident arrays (for zero-copy use by callers). */
+int gbx_graph_device_arrays(const gbx_graph *g, const uint32_t **offsets, const uint32_t **dest,
+                            const float **weight, const uint32_t **in_offsets,
+                            const uint32_t **in_src, const float **in_weight);
+
+/* ---- BFS --------------------------------------------------------------- */
+typedef struct gbx_bfs_result {
+    uint32_t processed_nodes; /* vertices reached, source included (BFSStats.processed_nodes) */
+    uint32_t iteration;       /* steps counted like BFSStats.iteration */
+    uint32_t depth;           /* largest level */
+    uint32_t top_down_steps;
+    uint32_t bottom_up_steps;
+    uint32_t reserved;
+    uint64_t edges_traversed; /* sum of out-degrees of reached vertices (GTEPS numerator) */
+} gbx_bfs_result;
+
+/* Direction-optimising BFS (alpha 15, beta 18 as in BFS.c:374-375).
+ * distances[v] = level (0 for the source and for unreached vertices, as the
+ * reference reports), parents[v] = BFS parent, the source for itself, and
+ * -out_degree[v] (or -1) for unreached vertices. parents may be NULL.
+ * mode: 0 pull-only (bottom-up), 1 push-only (top-down), 2 direction-optimising. */
+int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distances, int32_t *parents,
+            gbx_bfs_result *result, void *stream);
+
+/* ---- PageRank ----------------------------------------------------------- */
+typedef struct gbx_pr_result {
+    uint32_t iterations;  /* counted like PageRankStats.iterations */
+    uint32_t active_last; /* vertices that still moved by >= epsilon */
+    double error_total;   /* mean |delta| of the last iteration (FP64 reduction) */
+} gbx_pr_result;
+
+/* Pull PageRank with the reference's recurrence (damping 0.85f, ranks start
+ * at 1-d, dangling mass dropped, stop when no vertex moves by >= epsilon,
+ * final ranks divided by N). epsilon = 0 runs exactly max_iterations. FP32
+ * ranks; high-degree pull sums use compensated (Kahan) accumulation;
+ * the convergence residual is reduced in FP64. */
+int gbx_pagerank_pull(gbx_graph *g, uint32_t max_iterations, double epsilon, float *ranks,
+                      gbx_pr_result *result, void *stream);
+
+/* ---- SSSP --------------------------------------------------------------- */
+typedef struct gbx_sssp_result {
+    uint32_t reached;        /* vertices with a finite distance */
+    uint32_t rounds;         /* relaxation rounds */
+    uint64_t edges_relaxed;  /* total edge relaxations performed */
+    uint64_t edges_traversed;/* sum of out-degrees of reached vertices */
+} gbx_sssp_result;
+
+/* Single-source shortest paths with the reference's arithmetic
+ * newDistance = (uint32)((float)d + w) (SSSP.c:204,262), weight 1 when the
+ * graph has no weights. distances[v] = UINT32_MAX/2 when unreached.
+ * delta: bucket width of the near/far schedule (0 = autotuned). */
+int gbx_sssp(gbx_graph *g, uint32_t source, uint32_t delta, uint32_t *distances,
+             gbx_sssp_result *result, void *stream);
+
+/* ---- connected components ---------------------------------------------- */
+/* components[v] = smallest vertex id in v's component. variant 0 SV-style
+ * hooking sweeps, 1 Afforest (default), 2 label propagation. All variants
+ * give identical labels. iterations may be NULL. */
+int gbx_cc(gbx_graph *g, int variant, uint32_t *components, uint32_t *iterations, void *stream);
+
+/* ---- triangle count ----------------------------------------------------- */
+/* Count with the reference's pull semantics on a (src,dst)-sorted CSR:
+ * sum over edges u->v with v <= u, over w in N(v) with w <= v, of
+ * [w in N(u)]; on a symmetric, self-loop-free, deduplicated graph this is
+ * the number of triangles. Run after gbx_degree_reorder it is the
+ * degree-ordered DAG count. */
+int gbx_tc(gbx_graph *g, uint64_t *total, void *stream);
+
+/* ---- SpMV ----------------------------------------------------------------- */
+/* y[v] += sum over pull edges (u->v) of w_uv * x[u], `iterations` times.
+ * values: per-edge values in pull-CSR order; NULL uses the graph's weights
+ * in that order, or default_value when the graph has none. */
+int gbx_spmv(gbx_graph *g, const float *values, float default_value, const float *x, float *y,
+             uint32_t iterations, void *stream);
+
+/* ---- preprocessing -------------------------------------------------------- */
+/* CSR build on the device from an edge list (the GraphCSR preprocessing
+ * step): optional symmetrisation (appends every edge reversed), stable sort
+ * by source (sort_mode 0) or by (source,destination) (sort_mode 1), then
+ * optional removal of self loops and adjacent duplicates (dedup; requires
+ * sort_mode 1, keeps the first weight truncated through uint32 as the
+ * reference does). num_vertices = max id + 1 over the input.
+ * Outputs (caller-allocated; capacity = 2*num_edges when symmetric):
+ * out_degree[V], edges_idx[V], src_out[E'], dst_out[E'], w_out[E'] (may be
+ * NULL), *num_edges_out = E'. */
+int gbx_csr_build(uint32_t num_edges, const uint32_t *src, const uint32_t *dst, const float *w,
+                  int symmetric, int dedup, int sort_mode, uint32_t num_vertices,
+                  uint32_t *out_degree, uint32_t *edges_idx, uint32_t *src_out, uint32_t *dst_out,
+                  float *w_out, uint32_t *num_edges_out, void *stream);
+
+/* Degree reordering (lmode 1 out, 2 in, 3 in+out): stable ascending sort
+ * of (degree, id), new label of the i-th = N-1-i; composes labels[] and
+ * inverse_labels[] in place (identity on a fresh graph) and relabels
+ * src/dst in place. The caller re-sorts with gbx_csr_build, as the
+ * reference re-runs sortRunAlgorithms. */
+int gbx_degree_reorder(uint32_t num_vertices, uint32_t num_edges, uint32_t *src, uint32_t *dst,
+                       int lmode, uint32_t *labels, uint32_t *inverse_labels, void *stream);
+
+/* ---- synthetic inputs (no reference counterpart) ------------------------ */
+/* R-MAT edge list: 2^scale vertices, num_edges edges, quadrant
+ * probabilities a, b, c (d = 1-a-b-c), counter-based RNG keyed by seed, so
+ * the same seed gives the same edges on any host or thread count. Host
+ * pointers only. */
+int gbx_generate_rmat(uint32_t scale, uint64_t num_edges, double a, double b, double c,
+                      uint64_t seed, uint32_t *src, uint32_t *dst);
+/* Per-edge value streams keyed by (seed, edge index):
+ * kind 0: integer weights uniform in [lo, hi] stored as float;
+ * kind 1: uniform in (0, 1]; kind 2: uniform in [-1, 1]; kind 3: lognormal(0,1). */
+int gbx_generate_values(uint64_t count, int kind, uint32_t lo, uint32_t hi, uint64_t seed, float *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,722 @@
+/*
+ * gbx_oracle.c -- CPU restatement of the GraphBlox OpenMP host algorithms.
+ *
+ * TEST INFRASTRUCTURE, NOT PRODUCT CODE: the checker for the CUDA path and
+ * the timed CPU baseline ("port"). Built with -ffp-contract=off so that the
+ * FP32 results do not depend on whether the host ISA has FMA (the reference
+ * itself is compiled for x86-64, which has none in its base ISA).
+ *
+ * Each function cites the reference function whose behaviour it restates;
+ * the declarations in gbx_oracle.h document the conventions.
+ */
+#include "gbx_oracle.h"
+
+#include <limits.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <omp.h>
+
+#define ORC_INF (UINT_MAX / 2u)
+
+static void set_threads(int n) {
+    if (n > 0) omp_set_num_threads(n);
+}
+
+static void *xmalloc(size_t n) {
+    void *p = malloc(n ? n : 1);
+    if (!p) abort();
+    return p;
+}
+
+/* ------------------------------------------------------------------------ */
+/* edge list -> CSR                                                         */
+/* ------------------------------------------------------------------------ */
+
+/* One stable counting-sort pass keyed by key[] (values < nkeys). */
+static void counting_pass(uint32_t n, const uint32_t *key, uint32_t nkeys,
+                          const uint32_t *perm_in, uint32_t *perm_out) {
+    uint32_t *cnt = (uint32_t *)calloc((size_t)nkeys + 1, sizeof(uint32_t));
+    if (!cnt) abort();
+    for (uint32_t i = 0; i < n; ++i) cnt[key[perm_in[i]] + 1]++;
+    for (uint32_t k = 0; k < nkeys; ++k) cnt[k + 1] += cnt[k];
+    for (uint32_t i = 0; i < n; ++i) perm_out[cnt[key[perm_in[i]]]++] = perm_in[i];
+    free(cnt);
+}
+
+/* radixSortEdgesBySource / ...BySourceAndDestination (radixsort.c:231-339):
+ * LSD order -- destination pass first, then a stable source pass. */
+void orc_sort_edges(uint32_t num_edges, uint32_t *src, uint32_t *dst, float *w,
+                    int sort_mode, int num_threads) {
+    (void)num_threads;
+    if (num_edges == 0) return;
+    uint32_t maxid = 0;
+    for (uint32_t i = 0; i < num_edges; ++i) {
+        if (src[i] > maxid) maxid = src[i];
+        if (dst[i] > maxid) maxid = dst[i];
+    }
+    uint32_t nkeys = maxid + 1;
+    uint32_t *p0 = (uint32_t *)xmalloc((size_t)num_edges * 4);
+    uint32_t *p1 = (uint32_t *)xmalloc((size_t)num_edges * 4);
+    for (uint32_t i = 0; i < num_edges; ++i) p0[i] = i;
+    uint32_t *cur = p0, *nxt = p1;
+    if (sort_mode == 1 || sort_mode == 3) {
+        counting_pass(num_edges, dst, nkeys, cur, nxt);
+        uint32_t *t = cur; cur = nxt; nxt = t;
+    }
+    counting_pass(num_edges, src, nkeys, cur, nxt);
+    cur = nxt;
+    uint32_t *ts = (uint32_t *)xmalloc((size_t)num_edges * 4);
+    for (uint32_t i = 0; i < num_edges; ++i) ts[i] = src[cur[i]];
+    memcpy(src, ts, (size_t)num_edges * 4);
+    for (uint32_t i = 0; i < num_edges; ++i) ts[i] = dst[cur[i]];
+    memcpy(dst, ts, (size_t)num_edges * 4);
+    if (w) {
+        float *tw = (float *)ts;
+        for (uint32_t i = 0; i < num_edges; ++i) tw[i] = w[cur[i]];
+        memcpy(w, tw, (size_t)num_edges * 4);
+    }
+    free(ts);
+    free(p0);
+    free(p1);
+}
+
+/* removeDulpicatesSelfLoopEdges (edgeList.c:255-321). The reference keeps
+ * the weight in a uint32_t temporary, so kept weights are truncated to
+ * integers; the leading run of self loops is skipped before the first kept
+ * edge. An input made only of self loops yields zero edges here (the
+ * reference reads past the end of its arrays in that case). */
+uint32_t orc_dedup_edges(uint32_t num_edges, uint32_t *src, uint32_t *dst, float *w) {
+    uint32_t i = 0, j = 0;
+    while (i < num_edges && src[i] == dst[i]) ++i;
+    if (i == num_edges) return 0;
+    src[0] = src[i];
+    dst[0] = dst[i];
+    if (w) w[0] = (float)(uint32_t)w[i];
+    j = 1;
+    for (++i; i < num_edges; ++i) {
+        if (src[i] == dst[i]) continue;
+        if (src[j - 1] != src[i] || dst[j - 1] != dst[i]) {
+            src[j] = src[i];
+            dst[j] = dst[i];
+            if (w) w[j] = (float)(uint32_t)w[i];
+            ++j;
+        }
+    }
+    return j;
+}
+
+void orc_map_vertices(uint32_t num_vertices, uint32_t num_edges, const uint32_t *src,
+                      uint32_t *out_degree, uint32_t *edges_idx) {
+    memset(out_degree, 0, (size_t)num_vertices * 4);
+    memset(edges_idx, 0, (size_t)num_vertices * 4);
+    for (uint32_t i = 0; i < num_edges; ++i) {
+        uint32_t v = src[i] & 0x3FFFFFFFu; /* VERTEX_CACHE_MASK_U32, reorder.h */
+        out_degree[v]++;
+        if (i == 0 || src[i] != src[i - 1]) edges_idx[v] = i;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* degree reordering                                                        */
+/* ------------------------------------------------------------------------ */
+
+/* reorderGraphGenerateInOutDegrees + reorderGraphListDegree: stable
+ * ascending sort of (degree, id), label of the i-th smallest = N-1-i, so the
+ * largest degree gets label 0 and, within a degree, the larger old id gets
+ * the smaller new label (reorder.c:342-348). Then label composition
+ * (reorder.c:368-373) and relabelEdgeList (reorder.c:1618-1637). */
+void orc_degree_reorder(uint32_t num_vertices, uint32_t num_edges, uint32_t *src, uint32_t *dst,
+                        int lmode, uint32_t *labels, uint32_t *inverse_labels, int num_threads) {
+    set_threads(num_threads);
+    uint32_t n = num_vertices;
+    uint32_t *deg = (uint32_t *)calloc((size_t)n + 1, 4);
+    if (!deg) abort();
+    for (uint32_t i = 0; i < num_edges; ++i) {
+        if (lmode == 2) deg[dst[i]]++;
+        else if (lmode == 3) { deg[dst[i]]++; deg[src[i]]++; }
+        else deg[src[i]]++;
+    }
+    uint32_t maxdeg = 0;
+    for (uint32_t v = 0; v < n; ++v) if (deg[v] > maxdeg) maxdeg = deg[v];
+    uint32_t *ids = (uint32_t *)calloc((size_t)n + 1, 4);
+    if (!ids) abort();
+    uint32_t *sorted = (uint32_t *)xmalloc((size_t)n * 4 + 4);
+    for (uint32_t v = 0; v < n; ++v) ids[v] = v;
+    counting_pass(n, deg, maxdeg + 1, ids, sorted);
+    uint32_t *newlab = (uint32_t *)xmalloc((size_t)n * 4 + 4);
+    for (uint32_t i = 0; i < n; ++i) newlab[sorted[i]] = n - 1 - i;
+    #pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)num_edges; ++i) {
+        src[i] = newlab[src[i]];
+        dst[i] = newlab[dst[i]];
+    }
+    for (uint32_t v = 0; v < n; ++v) {
+        labels[v] = newlab[labels[v]];
+        inverse_labels[labels[v]] = v;
+    }
+    free(newlab);
+    free(sorted);
+    free(ids);
+    free(deg);
+}
+
+/* ------------------------------------------------------------------------ */
+/* BFS                                                                      */
+/* ------------------------------------------------------------------------ */
+
+/* Frontier of the top-down step: newly discovered vertices are claimed
+ * with a compare-and-swap on parents[] (BFS.c:518-540) and collected in
+ * per-thread buffers that are concatenated (the reference's local queues
+ * flushed to the shared queue, arrayQueue.c:257-270). Returns mf, the sum
+ * of -parent_old over claimed vertices (out-degree, or 1 for degree 0). */
+static uint32_t bfs_top_down(const uint32_t *out_degree, const uint32_t *edges_idx,
+                             const uint32_t *dest, uint32_t *distances, int32_t *parents,
+                             const uint32_t *queue, uint32_t qlen, uint32_t *next,
+                             uint32_t *next_len, uint32_t *scratch, uint32_t n) {
+    uint32_t mf = 0;
+    uint32_t total = 0;
+    int nt = omp_get_max_threads();
+    uint32_t *counts = (uint32_t *)calloc((size_t)nt + 1, 4);
+    if (!counts) abort();
+    #pragma omp parallel reduction(+ : mf)
+    {
+        int t = omp_get_thread_num();
+        int T = omp_get_num_threads();
+        /* each thread owns a slice of scratch of size n/T+1 worst case is
+         * not guaranteed, so threads write to a private heap buffer */
+        uint32_t cap = 1024, len = 0;
+        uint32_t *local = (uint32_t *)xmalloc((size_t)cap * 4);
+        #pragma omp for schedule(dynamic, 64)
+        for (uint32_t i = 0; i < qlen; ++i) {
+            uint32_t v = queue[i];
+            uint32_t b = edges_idx[v], e = b + out_degree[v];
+            for (uint32_t j = b; j < e; ++j) {
+                uint32_t u = dest[j] & 0x3FFFFFFFu;
+                int32_t pu = __atomic_load_n(&parents[u], __ATOMIC_RELAXED);
+                if (pu < 0) {
+                    if (__atomic_compare_exchange_n(&parents[u], &pu, (int32_t)v, 0,
+                                                    __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
+                        distances[u] = distances[v] + 1;
+                        mf += (uint32_t)(-pu);
+                        if (len == cap) {
+                            cap *= 2;
+                            local = (uint32_t *)realloc(local, (size_t)cap * 4);
+                            if (!local) abort();
+                        }
+                        local[len++] = u;
+                    }
+                }
+            }
+        }
+        counts[t + 1] = len;
+        #pragma omp barrier
+        #pragma omp single
+        {
+            for (int k = 0; k < T; ++k) counts[k + 1] += counts[k];
+            total = counts[T];
+        }
+        memcpy(next + counts[t], local, (size_t)len * 4);
+        free(local);
+    }
+    (void)scratch;
+    (void)n;
+    free(counts);
+    *next_len = total;
+    return mf;
+}
+
+/* bottomUpStepGraphCSR (BFS.c:562-613): every unvisited vertex scans its
+ * pull neighbours for one in the current frontier bitmap. */
+static uint32_t bfs_bottom_up(uint32_t n, const uint32_t *pull_degree, const uint32_t *pull_idx,
+                              const uint32_t *pull_src, uint32_t *distances, int32_t *parents,
+                              const uint8_t *curr, uint8_t *next) {
+    uint32_t nf = 0;
+    #pragma omp parallel for schedule(dynamic, 1024) reduction(+ : nf)
+    for (uint32_t v = 0; v < n; ++v) {
+        if (parents[v] < 0) {
+            uint32_t b = pull_idx[v], e = b + pull_degree[v];
+            for (uint32_t j = b; j < e; ++j) {
+                uint32_t u = pull_src[j] & 0x3FFFFFFFu;
+                if (curr[u]) {
+                    parents[v] = (int32_t)u;
+                    distances[v] = distances[u] + 1;
+                    next[v] = 1;
+                    nf++;
+                    break;
+                }
+            }
+        }
+    }
+    return nf;
+}
+
+/* breadthFirstSearchDirectionOptimizedGraphCSR (BFS.c:335-485), with the
+ * stats initialisation of newBFSStatsGraphCSR (BFS.c:42-78). */
+void orc_bfs(uint32_t num_vertices, uint32_t num_edges,
+             const uint32_t *out_degree, const uint32_t *edges_idx, const uint32_t *dest,
+             const uint32_t *pull_degree, const uint32_t *pull_idx, const uint32_t *pull_src,
+             uint32_t source, uint32_t *distances, int32_t *parents,
+             uint32_t *processed_nodes, uint32_t *iterations, int num_threads) {
+    set_threads(num_threads);
+    uint32_t n = num_vertices;
+    #pragma omp parallel for schedule(static)
+    for (uint32_t v = 0; v < n; ++v) {
+        distances[v] = 0;
+        parents[v] = out_degree[v] ? -(int32_t)out_degree[v] : -1;
+    }
+    *processed_nodes = 0;
+    *iterations = 0;
+    if (source >= n) return;
+    uint32_t *queue = (uint32_t *)xmalloc((size_t)n * 4 + 4);
+    uint32_t *next = (uint32_t *)xmalloc((size_t)n * 4 + 4);
+    uint8_t *bcur = (uint8_t *)calloc((size_t)n + 1, 1);
+    uint8_t *bnext = (uint8_t *)calloc((size_t)n + 1, 1);
+    if (!bcur || !bnext) abort();
+    uint32_t qlen = 1;
+    queue[0] = source;
+    parents[source] = (int32_t)source;
+    uint32_t processed = 1, iter = 1;
+    uint32_t mu = num_edges, mf = out_degree[source];
+    const uint32_t alpha = 15, beta = 18;
+    while (qlen) {
+        if (mf > mu / alpha) {
+            memset(bcur, 0, n);
+            for (uint32_t i = 0; i < qlen; ++i) bcur[queue[i]] = 1;
+            uint32_t nf = qlen, nf_prev;
+            do {
+                nf_prev = nf;
+                nf = bfs_bottom_up(n, pull_degree, pull_idx, pull_src, distances, parents, bcur, bnext);
+                uint8_t *t = bcur; bcur = bnext; bnext = t;
+                memset(bnext, 0, n);
+                processed += nf;
+                iter++;
+            } while (nf > nf_prev || nf > n / beta);
+            qlen = 0;
+            for (uint32_t v = 0; v < n; ++v)
+                if (bcur[v]) queue[qlen++] = v;
+            mf = 1;
+        } else {
+            mu -= mf;
+            uint32_t nlen = 0;
+            mf = bfs_top_down(out_degree, edges_idx, dest, distances, parents, queue, qlen, next,
+                              &nlen, NULL, n);
+            uint32_t *t = queue; queue = next; next = t;
+            qlen = nlen;
+            processed += qlen;
+            iter++;
+        }
+    }
+    *processed_nodes = processed;
+    *iterations = iter;
+    free(queue);
+    free(next);
+    free(bcur);
+    free(bnext);
+}
+
+/* ------------------------------------------------------------------------ */
+/* PageRank                                                                 */
+/* ------------------------------------------------------------------------ */
+
+/* pageRankPullGraphCSR (pageRank.c:245-368) with the stats defaults of
+ * newPageRankStatsGraphCSR (pageRank.c:47-75): damp 0.85f, ranks start at
+ * base_pr = 1-damp, contributions r/outdeg (0 for dangling vertices), stop
+ * when no vertex moved by >= epsilon, finally r /= N. */
+void orc_pagerank_pull(uint32_t num_vertices, const uint32_t *out_degree,
+                       const uint32_t *pull_degree, const uint32_t *pull_idx, const uint32_t *pull_src,
+                       uint32_t max_iterations, double epsilon, float *ranks,
+                       uint32_t *iterations, double *error_total, int num_threads) {
+    set_threads(num_threads);
+    const uint32_t n = num_vertices;
+    const float damp = 0.85f;
+    const float base_pr = 1.0f - damp;
+    float *contrib = (float *)xmalloc((size_t)n * 4 + 4);
+    float *sums = (float *)xmalloc((size_t)n * 4 + 4);
+    for (uint32_t v = 0; v < n; ++v) ranks[v] = base_pr;
+    double err = 0.0;
+    uint32_t it;
+    for (it = 0; it < max_iterations; ++it) {
+        err = 0.0;
+        uint32_t active = 0;
+        #pragma omp parallel for schedule(static)
+        for (uint32_t v = 0; v < n; ++v)
+            contrib[v] = out_degree[v] ? ranks[v] / (float)out_degree[v] : 0.0f;
+        #pragma omp parallel for schedule(dynamic, 1024)
+        for (uint32_t v = 0; v < n; ++v) {
+            float s = 0.0f;
+            uint32_t b = pull_idx[v], e = b + pull_degree[v];
+            for (uint32_t j = b; j < e; ++j) s += contrib[pull_src[j] & 0x3FFFFFFFu];
+            sums[v] = s;
+        }
+        #pragma omp parallel for schedule(static) reduction(+ : err, active)
+        for (uint32_t v = 0; v < n; ++v) {
+            float prev = ranks[v];
+            float next = base_pr + damp * sums[v];
+            ranks[v] = next;
+            double e = fabs((double)(next - prev));
+            err += e / n;
+            if (e >= epsilon) active++;
+        }
+        if (active == 0) break;
+    }
+    for (uint32_t v = 0; v < n; ++v) ranks[v] = ranks[v] / (float)n;
+    *iterations = it;
+    *error_total = err;
+    free(contrib);
+    free(sums);
+}
+
+void orc_pagerank_pull_f64(uint32_t num_vertices, const uint32_t *out_degree,
+                           const uint32_t *pull_degree, const uint32_t *pull_idx, const uint32_t *pull_src,
+                           uint32_t max_iterations, double epsilon, double *ranks,
+                           uint32_t *iterations, int num_threads) {
+    set_threads(num_threads);
+    const uint32_t n = num_vertices;
+    /* the FP32 constants, held exactly in FP64, so that the comparison
+     * measures arithmetic rounding only */
+    const double damp = (double)0.85f;
+    const double base_pr = (double)(1.0f - 0.85f);
+    double *contrib = (double *)xmalloc((size_t)n * 8 + 8);
+    double *sums = (double *)xmalloc((size_t)n * 8 + 8);
+    for (uint32_t v = 0; v < n; ++v) ranks[v] = base_pr;
+    uint32_t it;
+    for (it = 0; it < max_iterations; ++it) {
+        uint32_t active = 0;
+        #pragma omp parallel for schedule(static)
+        for (uint32_t v = 0; v < n; ++v)
+            contrib[v] = out_degree[v] ? ranks[v] / (double)out_degree[v] : 0.0;
+        #pragma omp parallel for schedule(dynamic, 1024)
+        for (uint32_t v = 0; v < n; ++v) {
+            double s = 0.0;
+            uint32_t b = pull_idx[v], e = b + pull_degree[v];
+            for (uint32_t j = b; j < e; ++j) s += contrib[pull_src[j] & 0x3FFFFFFFu];
+            sums[v] = s;
+        }
+        #pragma omp parallel for schedule(static) reduction(+ : active)
+        for (uint32_t v = 0; v < n; ++v) {
+            double next = base_pr + damp * sums[v];
+            if (fabs(next - ranks[v]) >= epsilon) active++;
+            ranks[v] = next;
+        }
+        if (active == 0) break;
+    }
+    for (uint32_t v = 0; v < n; ++v) ranks[v] = ranks[v] / (double)n;
+    *iterations = it;
+    free(contrib);
+    free(sums);
+}
+
+/* ------------------------------------------------------------------------ */
+/* SSSP                                                                     */
+/* ------------------------------------------------------------------------ */
+
+static inline uint32_t sssp_add(uint32_t d, float w) {
+    /* SSSP.c:204,262: uint32 + float evaluated in float, stored to uint32 */
+    return (uint32_t)((float)d + w);
+}
+
+static inline int atomic_min_u32(uint32_t *p, uint32_t v) {
+    uint32_t old = __atomic_load_n(p, __ATOMIC_ACQUIRE);
+    while (old > v) {
+        if (__atomic_compare_exchange_n(p, &old, v, 1, __ATOMIC_ACQ_REL, __ATOMIC_ACQUIRE))
+            return 1;
+    }
+    return 0;
+}
+
+/* SSSPDataDrivenPushGraphCSR (SSSP.c:514-653): each vertex sits in at most
+ * one bucket (buckets_map[v] = dist/delta); bucket `cur` is drained
+ * repeatedly by full sweeps over V until it stays empty. The relaxation
+ * takes the minimum with an atomic, and a vertex whose distance drops is
+ * re-filed under min(old bucket, new bucket), so a drop that races with
+ * the vertex being drained is never lost; the fixed point is the unique
+ * shortest-distance vector under the reference's arithmetic. Empty buckets
+ * are skipped by jumping to the smallest occupied one. */
+void orc_sssp(uint32_t num_vertices, const uint32_t *out_degree, const uint32_t *edges_idx,
+              const uint32_t *dest, const float *weights, uint32_t source, uint32_t delta,
+              uint32_t *distances, uint32_t *processed_nodes, int num_threads) {
+    set_threads(num_threads);
+    const uint32_t n = num_vertices;
+    if (delta == 0) delta = 1;
+    uint32_t *bucket = (uint32_t *)xmalloc((size_t)n * 4 + 4);
+    #pragma omp parallel for schedule(static)
+    for (uint32_t v = 0; v < n; ++v) {
+        distances[v] = ORC_INF;
+        bucket[v] = ORC_INF;
+    }
+    uint32_t processed = 0;
+    if (source < n) {
+        distances[source] = 0;
+        bucket[source] = 0;
+        uint32_t cur = 0;
+        for (;;) {
+            int changed = 1;
+            while (changed) {
+                changed = 0;
+                #pragma omp parallel for schedule(dynamic, 1024) reduction(| : changed) reduction(+ : processed)
+                for (uint32_t v = 0; v < n; ++v) {
+                    if (__atomic_load_n(&bucket[v], __ATOMIC_RELAXED) != cur) continue;
+                    uint32_t expect = cur;
+                    if (!__atomic_compare_exchange_n(&bucket[v], &expect, ORC_INF, 0,
+                                                     __ATOMIC_ACQ_REL, __ATOMIC_RELAXED))
+                        continue;
+                    processed++;
+                    uint32_t d = __atomic_load_n(&distances[v], __ATOMIC_ACQUIRE);
+                    uint32_t b = edges_idx[v], e = b + out_degree[v];
+                    for (uint32_t j = b; j < e; ++j) {
+                        uint32_t u = dest[j] & 0x3FFFFFFFu;
+                        float w = weights ? weights[j] : 1.0f;
+                        uint32_t nd = sssp_add(d, w);
+                        if (atomic_min_u32(&distances[u], nd)) {
+                            uint32_t nb = nd / delta;
+                            atomic_min_u32(&bucket[u], nb);
+                            if (nb == cur) changed = 1;
+                        }
+                    }
+                }
+            }
+            uint32_t nextb = ORC_INF;
+            #pragma omp parallel for schedule(static) reduction(min : nextb)
+            for (uint32_t v = 0; v < n; ++v)
+                if (bucket[v] < nextb) nextb = bucket[v];
+            if (nextb == ORC_INF) break;
+            cur = nextb;
+        }
+    }
+    if (processed_nodes) *processed_nodes = processed;
+    free(bucket);
+}
+
+/* ------------------------------------------------------------------------ */
+/* connected components                                                     */
+/* ------------------------------------------------------------------------ */
+
+/* linkNodes (connectedComponents.c:177-196): hook the higher root under
+ * the lower one with a compare-and-swap, re-reading on failure. */
+static void cc_link(uint32_t u, uint32_t v, uint32_t *comp) {
+    uint32_t p1 = __atomic_load_n(&comp[u], __ATOMIC_RELAXED);
+    uint32_t p2 = __atomic_load_n(&comp[v], __ATOMIC_RELAXED);
+    while (p1 != p2) {
+        uint32_t high = p1 > p2 ? p1 : p2;
+        uint32_t low = p1 + (p2 - high);
+        uint32_t phigh = __atomic_load_n(&comp[high], __ATOMIC_RELAXED);
+        if (phigh == low) break;
+        if (phigh == high) {
+            uint32_t expect = high;
+            if (__atomic_compare_exchange_n(&comp[high], &expect, low, 0, __ATOMIC_RELAXED,
+                                            __ATOMIC_RELAXED))
+                break;
+        }
+        p1 = __atomic_load_n(&comp[__atomic_load_n(&comp[high], __ATOMIC_RELAXED)], __ATOMIC_RELAXED);
+        p2 = __atomic_load_n(&comp[low], __ATOMIC_RELAXED);
+    }
+}
+
+/* compressNodes (connectedComponents.c:199-210) */
+static void cc_compress(uint32_t n, uint32_t *comp) {
+    #pragma omp parallel for schedule(dynamic, 2048)
+    for (uint32_t v = 0; v < n; ++v) {
+        while (comp[v] != comp[comp[v]]) comp[v] = comp[comp[v]];
+    }
+}
+
+void orc_cc(uint32_t num_vertices, const uint32_t *out_degree, const uint32_t *edges_idx,
+            const uint32_t *dest, const uint32_t *pull_degree, const uint32_t *pull_idx,
+            const uint32_t *pull_src, int variant, uint32_t *components,
+            uint32_t *iterations, int num_threads) {
+    set_threads(num_threads);
+    const uint32_t n = num_vertices;
+    uint32_t *comp = components;
+    for (uint32_t v = 0; v < n; ++v) comp[v] = v;
+    uint32_t iters = 0;
+    if (variant == 0) {
+        /* Shiloach-Vishkin (connectedComponents.c:293-377) */
+        int change = 1;
+        while (change) {
+            change = 0;
+            iters++;
+            #pragma omp parallel for schedule(dynamic, 512) reduction(| : change)
+            for (uint32_t v = 0; v < n; ++v) {
+                uint32_t b = edges_idx[v], e = b + out_degree[v];
+                for (uint32_t j = b; j < e; ++j) {
+                    uint32_t u = dest[j] & 0x3FFFFFFFu;
+                    uint32_t cs = __atomic_load_n(&comp[v], __ATOMIC_RELAXED);
+                    uint32_t cd = __atomic_load_n(&comp[u], __ATOMIC_RELAXED);
+                    if (cs == cd) continue;
+                    uint32_t high = cs > cd ? cs : cd, low = cs + (cd - high);
+                    if (__atomic_load_n(&comp[high], __ATOMIC_RELAXED) == high) {
+                        /* the reference's plain store races benignly; a CAS keeps
+                         * hooks on roots only */
+                        uint32_t expect = high;
+                        __atomic_compare_exchange_n(&comp[high], &expect, low, 0, __ATOMIC_RELAXED,
+                                                    __ATOMIC_RELAXED);
+                        change = 1;
+                    }
+                }
+                if (pull_degree) {
+                    uint32_t pb = pull_idx[v], pe = pb + pull_degree[v];
+                    for (uint32_t j = pb; j < pe; ++j) {
+                        uint32_t u = pull_src[j] & 0x3FFFFFFFu;
+                        uint32_t cs = __atomic_load_n(&comp[v], __ATOMIC_RELAXED);
+                        uint32_t cd = __atomic_load_n(&comp[u], __ATOMIC_RELAXED);
+                        if (cs == cd) continue;
+                        uint32_t high = cs > cd ? cs : cd, low = cs + (cd - high);
+                        if (__atomic_load_n(&comp[high], __ATOMIC_RELAXED) == high) {
+                            uint32_t expect = high;
+                            __atomic_compare_exchange_n(&comp[high], &expect, low, 0,
+                                                        __ATOMIC_RELAXED, __ATOMIC_RELAXED);
+                            change = 1;
+                        }
+                    }
+                }
+            }
+            cc_compress(n, comp);
+        }
+    } else if (variant == 2) {
+        /* weakly connected label propagation (connectedComponents.c:537-629) */
+        int change = 1;
+        while (change) {
+            change = 0;
+            iters++;
+            #pragma omp parallel for schedule(dynamic, 512) reduction(| : change)
+            for (uint32_t v = 0; v < n; ++v) {
+                uint32_t b = edges_idx[v], e = b + out_degree[v];
+                for (uint32_t j = b; j < e; ++j) {
+                    uint32_t u = dest[j] & 0x3FFFFFFFu;
+                    if (atomic_min_u32(&comp[u], __atomic_load_n(&comp[v], __ATOMIC_RELAXED))) change = 1;
+                    if (atomic_min_u32(&comp[v], __atomic_load_n(&comp[u], __ATOMIC_RELAXED))) change = 1;
+                }
+            }
+        }
+    } else {
+        /* Afforest (connectedComponents.c:379-535): two neighbour rounds,
+         * sample the most frequent component, final link skipping it. */
+        const uint32_t rounds = 2;
+        for (uint32_t r = 0; r < rounds; ++r) {
+            #pragma omp parallel for schedule(dynamic, 2048)
+            for (uint32_t u = 0; u < n; ++u) {
+                if (r < out_degree[u]) cc_link(u, dest[edges_idx[u] + r] & 0x3FFFFFFFu, comp);
+            }
+            cc_compress(n, comp);
+        }
+        /* most frequent component among 1024 sampled vertices (first max in
+         * key order, as the Judy scan does); which one is chosen does not
+         * change the final labels */
+        uint32_t skip = 0;
+        if (n > 0) {
+            uint32_t ns = n < 1024 ? n / 2 : 1024;
+            uint32_t *samp = (uint32_t *)xmalloc((size_t)ns * 4 + 4);
+            uint64_t x = 0x9E3779B97F4A7C15ull;
+            for (uint32_t i = 0; i < ns; ++i) {
+                x ^= x >> 12; x ^= x << 25; x ^= x >> 27;
+                samp[i] = comp[(uint32_t)((x * 2685821657736338717ull) >> 32) % n];
+            }
+            /* insertion-free mode: sort then scan */
+            for (uint32_t i = 1; i < ns; ++i) {
+                uint32_t key = samp[i];
+                int64_t k = (int64_t)i - 1;
+                while (k >= 0 && samp[k] > key) { samp[k + 1] = samp[k]; --k; }
+                samp[k + 1] = key;
+            }
+            uint32_t best = 0, bestc = 0;
+            for (uint32_t i = 0; i < ns;) {
+                uint32_t k = i;
+                while (k < ns && samp[k] == samp[i]) ++k;
+                if (k - i > bestc) { bestc = k - i; best = samp[i]; }
+                i = k;
+            }
+            skip = best;
+            free(samp);
+        }
+        #pragma omp parallel for schedule(dynamic, 2048)
+        for (uint32_t u = 0; u < n; ++u) {
+            if (comp[u] == skip) continue;
+            uint32_t b = edges_idx[u], e = b + out_degree[u];
+            for (uint32_t j = b + rounds; j < e; ++j) cc_link(u, dest[j] & 0x3FFFFFFFu, comp);
+            if (pull_degree) {
+                uint32_t pb = pull_idx[u], pe = pb + pull_degree[u];
+                for (uint32_t j = pb; j < pe; ++j) cc_link(u, pull_src[j] & 0x3FFFFFFFu, comp);
+            }
+        }
+        cc_compress(n, comp);
+        iters = rounds;
+    }
+    if (iterations) *iterations = iters;
+}
+
+/* ------------------------------------------------------------------------ */
+/* triangle count                                                           */
+/* ------------------------------------------------------------------------ */
+
+/* triangleCountPullGraphCSR (triangleCount.c:254-334). The innermost scan
+ * of N(u) for the first element >= w is a membership test on a sorted
+ * list, done here with a binary search; the count is the same. */
+uint64_t orc_triangle_count(uint32_t num_vertices, const uint32_t *out_degree,
+                            const uint32_t *edges_idx, const uint32_t *dest, int num_threads) {
+    set_threads(num_threads);
+    uint64_t count = 0;
+    #pragma omp parallel for schedule(dynamic, 128) reduction(+ : count)
+    for (uint32_t u = 0; u < num_vertices; ++u) {
+        const uint32_t *nu = dest + edges_idx[u];
+        uint32_t du = out_degree[u];
+        for (uint32_t a = 0; a < du; ++a) {
+            uint32_t v = nu[a] & 0x3FFFFFFFu;
+            if (v > u) break;
+            const uint32_t *nv = dest + edges_idx[v];
+            uint32_t dv = out_degree[v];
+            for (uint32_t c = 0; c < dv; ++c) {
+                uint32_t w = nv[c] & 0x3FFFFFFFu;
+                if (w > v) break;
+                /* first element of N(u) that is >= w */
+                uint32_t lo = 0, hi = du;
+                while (lo < hi) {
+                    uint32_t mid = (lo + hi) >> 1;
+                    if ((nu[mid] & 0x3FFFFFFFu) < w) lo = mid + 1; else hi = mid;
+                }
+                if (lo < du && (nu[lo] & 0x3FFFFFFFu) == w) count++;
+            }
+        }
+    }
+    return count;
+}
+
+/* ------------------------------------------------------------------------ */
+/* SpMV                                                                     */
+/* ------------------------------------------------------------------------ */
+
+void orc_spmv_pull(uint32_t num_vertices, const uint32_t *pull_degree, const uint32_t *pull_idx,
+                   const uint32_t *pull_src, const float *weights, float default_weight,
+                   const float *x, float *y, uint32_t iterations, int num_threads) {
+    set_threads(num_threads);
+    for (uint32_t it = 0; it < iterations; ++it) {
+        #pragma omp parallel for schedule(dynamic, 1024)
+        for (uint32_t v = 0; v < num_vertices; ++v) {
+            uint32_t b = pull_idx[v], e = b + pull_degree[v];
+            float acc = y[v];
+            for (uint32_t j = b; j < e; ++j) {
+                float w = weights ? weights[j] : default_weight;
+                acc += w * x[pull_src[j] & 0x3FFFFFFFu];
+            }
+            y[v] = acc;
+        }
+    }
+}
+
+void orc_spmv_pull_f64(uint32_t num_vertices, const uint32_t *pull_degree, const uint32_t *pull_idx,
+                       const uint32_t *pull_src, const float *weights, float default_weight,
+                       const float *x, double *y, uint32_t iterations, int num_threads) {
+    set_threads(num_threads);
+    for (uint32_t it = 0; it < iterations; ++it) {
+        #pragma omp parallel for schedule(dynamic, 1024)
+        for (uint32_t v = 0; v < num_vertices; ++v) {
+            uint32_t b = pull_idx[v], e = b + pull_degree[v];
+            double acc = y[v];
+            for (uint32_t j = b; j < e; ++j) {
+                double w = weights ? (double)weights[j] : (double)default_weight;
+                acc += w * (double)x[pull_src[j] & 0x3FFFFFFFu];
+            }
+            y[v] = acc;
+        }
+    }
+}

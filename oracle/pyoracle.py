@@ -1,0 +1,213 @@
+"""ctypes binding of liboracle.so -- the CPU restatement in gbx_oracle.c.
+
+TEST INFRASTRUCTURE, NOT PRODUCT CODE. Imported only by tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg, as the checker or
+the timed CPU baseline. It also offers `ref_run`, which executes the
+reference host built by build_ref.sh (present only where the reference
+sources are, i.e. not on the GPU host).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import tempfile
+from pathlib import Path
+from typing import Optional
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+REF_DIR = HERE / "_ref"
+
+u32 = C.c_uint32
+u64 = C.c_uint64
+vp = C.c_void_p
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+        lib = C.CDLL(str(LIB))
+        sig = {
+            "orc_sort_edges": (None, [u32, vp, vp, vp, C.c_int, C.c_int]),
+            "orc_dedup_edges": (u32, [u32, vp, vp, vp]),
+            "orc_map_vertices": (None, [u32, u32, vp, vp, vp]),
+            "orc_degree_reorder": (None, [u32, u32, vp, vp, C.c_int, vp, vp, C.c_int]),
+            "orc_bfs": (None, [u32, u32, vp, vp, vp, vp, vp, vp, u32, vp, vp, vp, vp, C.c_int]),
+            "orc_pagerank_pull": (None, [u32, vp, vp, vp, vp, u32, C.c_double, vp, vp, vp, C.c_int]),
+            "orc_pagerank_pull_f64": (None, [u32, vp, vp, vp, vp, u32, C.c_double, vp, vp, C.c_int]),
+            "orc_sssp": (None, [u32, vp, vp, vp, vp, u32, u32, vp, vp, C.c_int]),
+            "orc_cc": (None, [u32, vp, vp, vp, vp, vp, vp, C.c_int, vp, vp, C.c_int]),
+            "orc_triangle_count": (u64, [u32, vp, vp, vp, C.c_int]),
+            "orc_spmv_pull": (None, [u32, vp, vp, vp, vp, C.c_float, vp, vp, u32, C.c_int]),
+            "orc_spmv_pull_f64": (None, [u32, vp, vp, vp, vp, C.c_float, vp, vp, u32, C.c_int]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def _u32(a):
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+class HostCSR:
+    """Reference-layout CSR in numpy (out_degree, edges_idx, dest[, weight])."""
+
+    def __init__(self, num_vertices, out_degree, edges_idx, dest, weight=None, src=None):
+        self.num_vertices = int(num_vertices)
+        self.out_degree = _u32(out_degree)
+        self.edges_idx = _u32(edges_idx)
+        self.dest = _u32(dest)
+        self.weight = None if weight is None else np.ascontiguousarray(weight, np.float32)
+        self.src = None if src is None else _u32(src)
+
+    @property
+    def num_edges(self):
+        return int(self.dest.shape[0])
+
+
+def build_csr(num_vertices, src, dst, weight=None, sort_mode=1, dedup=False, threads=0):
+    """Sort (+dedup) and map, like the reference's preprocessing. Returns
+    (HostCSR, src_sorted)."""
+    s = _u32(src).copy()
+    d = _u32(dst).copy()
+    w = None if weight is None else np.ascontiguousarray(weight, np.float32).copy()
+    lib = load()
+    lib.orc_sort_edges(s.shape[0], _p(s), _p(d), _p(w), sort_mode, threads)
+    n = s.shape[0]
+    if dedup:
+        n = lib.orc_dedup_edges(n, _p(s), _p(d), _p(w))
+        s, d = s[:n].copy(), d[:n].copy()
+        if w is not None:
+            w = w[:n].copy()
+    deg = np.zeros(num_vertices, np.uint32)
+    idx = np.zeros(num_vertices, np.uint32)
+    lib.orc_map_vertices(num_vertices, n, _p(s), _p(deg), _p(idx))
+    return HostCSR(num_vertices, deg, idx, d, w, s)
+
+
+def degree_reorder(num_vertices, src, dst, lmode=1, labels=None, inverse_labels=None, threads=0):
+    s = _u32(src).copy()
+    d = _u32(dst).copy()
+    lab = np.arange(num_vertices, dtype=np.uint32) if labels is None else _u32(labels).copy()
+    inv = np.arange(num_vertices, dtype=np.uint32) if inverse_labels is None else _u32(inverse_labels).copy()
+    load().orc_degree_reorder(num_vertices, s.shape[0], _p(s), _p(d), lmode, _p(lab), _p(inv), threads)
+    return s, d, lab, inv
+
+
+def bfs(g: HostCSR, source, pull: Optional[HostCSR] = None, threads=0):
+    pull = pull or g
+    V = g.num_vertices
+    dist = np.zeros(V, np.uint32)
+    par = np.zeros(V, np.int32)
+    proc = u32(0)
+    it = u32(0)
+    load().orc_bfs(V, g.num_edges, _p(g.out_degree), _p(g.edges_idx), _p(g.dest), _p(pull.out_degree),
+                   _p(pull.edges_idx), _p(pull.dest), int(source), _p(dist), _p(par), C.byref(proc),
+                   C.byref(it), threads)
+    return dist, par, proc.value, it.value
+
+
+def pagerank(g: HostCSR, iterations=20, epsilon=0.0, pull: Optional[HostCSR] = None, threads=0, fp64=False):
+    pull = pull or g
+    V = g.num_vertices
+    it = u32(0)
+    if fp64:
+        r = np.zeros(V, np.float64)
+        load().orc_pagerank_pull_f64(V, _p(g.out_degree), _p(pull.out_degree), _p(pull.edges_idx),
+                                     _p(pull.dest), int(iterations), float(epsilon), _p(r), C.byref(it), threads)
+        return r, it.value, None
+    r = np.zeros(V, np.float32)
+    err = C.c_double(0)
+    load().orc_pagerank_pull(V, _p(g.out_degree), _p(pull.out_degree), _p(pull.edges_idx), _p(pull.dest),
+                             int(iterations), float(epsilon), _p(r), C.byref(it), C.byref(err), threads)
+    return r, it.value, err.value
+
+
+def sssp(g: HostCSR, source, delta=1, threads=0, use_weights=True):
+    V = g.num_vertices
+    dist = np.zeros(V, np.uint32)
+    proc = u32(0)
+    w = g.weight if use_weights else None
+    load().orc_sssp(V, _p(g.out_degree), _p(g.edges_idx), _p(g.dest), _p(w), int(source), int(delta),
+                    _p(dist), C.byref(proc), threads)
+    return dist
+
+
+def cc(g: HostCSR, variant=1, pull: Optional[HostCSR] = None, threads=0):
+    V = g.num_vertices
+    comp = np.zeros(V, np.uint32)
+    it = u32(0)
+    load().orc_cc(V, _p(g.out_degree), _p(g.edges_idx), _p(g.dest),
+                  _p(pull.out_degree) if pull else None, _p(pull.edges_idx) if pull else None,
+                  _p(pull.dest) if pull else None, variant, _p(comp), C.byref(it), threads)
+    return comp
+
+
+def triangle_count(g: HostCSR, threads=0):
+    return int(load().orc_triangle_count(g.num_vertices, _p(g.out_degree), _p(g.edges_idx), _p(g.dest), threads))
+
+
+def spmv(g: HostCSR, x, values=None, default_value=0.0001, iterations=1, y=None, pull: Optional[HostCSR] = None,
+         threads=0, fp64=False):
+    pull = pull or g
+    V = g.num_vertices
+    x = np.ascontiguousarray(x, np.float32)
+    vals = None if values is None else np.ascontiguousarray(values, np.float32)
+    if fp64:
+        yy = np.zeros(V, np.float64) if y is None else np.ascontiguousarray(y, np.float64).copy()
+        load().orc_spmv_pull_f64(V, _p(pull.out_degree), _p(pull.edges_idx), _p(pull.dest), _p(vals),
+                                 float(default_value), _p(x), _p(yy), int(iterations), threads)
+        return yy
+    yy = np.zeros(V, np.float32) if y is None else np.ascontiguousarray(y, np.float32).copy()
+    load().orc_spmv_pull(V, _p(pull.out_degree), _p(pull.edges_idx), _p(pull.dest), _p(vals),
+                         float(default_value), _p(x), _p(yy), int(iterations), threads)
+    return yy
+
+
+def rel_l1(a, ref) -> float:
+    a = np.asarray(a, np.float64)
+    ref = np.asarray(ref, np.float64)
+    den = np.abs(ref).sum()
+    return float(np.abs(a - ref).sum() / den) if den else float(np.abs(a - ref).sum())
+
+
+# ---- the reference host itself (only where its sources were compiled) -----
+
+def ref_available(variant="dw") -> bool:
+    return (REF_DIR / f"gbx_ref_{variant}").exists()
+
+
+def ref_run(graph_file, variant="dw", algorithm=-1, flags=(), threads=4):
+    """Run oracle/_ref/gbx_ref_<variant> and load its dumps as numpy arrays."""
+    exe = REF_DIR / f"gbx_ref_{variant}"
+    with tempfile.TemporaryDirectory() as td:
+        cmd = [str(exe), str(graph_file), td, "-a", str(algorithm), "-n", str(threads), *map(str, flags)]
+        res = subprocess.run(cmd, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True,
+                             env={**os.environ, "OMP_NUM_THREADS": str(threads)})
+        if res.returncode != 0:
+            raise RuntimeError(f"reference run failed: {' '.join(cmd)}\n{res.stderr}")
+        out = {}
+        for f in Path(td).iterdir():
+            if f.name == "scalars.txt":
+                for line in f.read_text().splitlines():
+                    k, v = line.split()
+                    out[k] = float(v) if ("." in v or "e" in v) else int(v)
+            else:
+                stem, ext = f.name.rsplit(".", 1)
+                dt = {"u32": np.uint32, "i32": np.int32, "f32": np.float32}[ext]
+                out[stem] = np.fromfile(f, dtype=dt)
+        return out

@@ -1,0 +1,109 @@
+"""Generate the golden fixtures in tests/golden/*.npz.
+
+Run in a container that has the reference tree (default /root/reference) and
+its build (oracle/build_ref.sh). For every test graph the reference ships in
+03_data/TEST, the fixture stores:
+  - the input edge list (graph.bin / graph.wbin records),
+  - the reference's own CSR text dumps (03_data/TEST/<g>/graph.*bin.*),
+  - outputs of the reference host (oracle/_ref) for each algorithm on that
+    graph, per build variant ("u": as shipped, run on the symmetrised,
+    deduplicated graph; "dw": DIRECTED 1 / WEIGHTED 1, run on the directed
+    graph as is).
+The GPU host has no reference tree, so the parity tests read only these
+fixtures there.
+
+Usage: python tests/golden/make_golden.py [REFERENCE_ROOT]
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from oracle import pyoracle as po  # noqa: E402
+
+GRAPHS = ["v51_e1021", "v300_e2730", "v500_e500", "v529_e3500", "v1000_e10000", "v1024_e4096",
+          "v8192_e32768", "graphbrew", "test"]
+ROOTS = [0, 1, 7, 100]
+
+
+def load_text(p: Path) -> np.ndarray:
+    return np.loadtxt(p, dtype=np.int64, ndmin=1)
+
+
+def main(ref_root: str) -> None:
+    test_dir = Path(ref_root) / "03_data" / "TEST"
+    out_dir = Path(__file__).resolve().parent
+    for name in GRAPHS:
+        gdir = test_dir / name
+        weighted = (gdir / "graph.wbin").exists() and not (gdir / "graph.bin").exists()
+        f = gdir / ("graph.wbin" if weighted else "graph.bin")
+        raw = np.fromfile(f, dtype=np.uint32)
+        width = 3 if weighted else 2
+        rec = raw[: (raw.shape[0] // width) * width].reshape(-1, width)
+        fx: dict[str, np.ndarray] = {
+            "src": rec[:, 0].copy(),
+            "dst": rec[:, 1].copy(),
+            "weighted": np.array(int(weighted)),
+        }
+        if weighted:
+            fx["weight"] = rec[:, 2].copy().view(np.float32)
+        prefix = gdir / f.name
+        if (gdir / (f.name + ".out_degree")).exists():
+            od = load_text(Path(str(prefix) + ".out_degree"))
+            fx["dump_num_vertices"] = np.array(od[0])
+            fx["dump_out_degree"] = od[1:].astype(np.uint32)
+            fx["dump_edges_idx"] = load_text(Path(str(prefix) + ".edges_idx")).astype(np.uint32)
+            fx["dump_dest"] = load_text(Path(str(prefix) + ".edges_array_dest")).astype(np.uint32)
+            fx["dump_src"] = load_text(Path(str(prefix) + ".edges_array_src"))[1:].astype(np.uint32)
+        wflag = ["-w"] if weighted else []
+        for variant, flags in (("u", ["-s", "-k"]), ("dw", []), ("dwk", ["-k"])):
+            exe = "u" if variant == "u" else "dw"
+            fl = ["-o", "1", *wflag, *flags]
+            csr = po.ref_run(f, exe, -1, fl)
+            for k in ("out_degree", "edges_idx", "dest", "src"):
+                fx[f"{variant}_{k}"] = csr[k]
+            if "weight" in csr:
+                fx[f"{variant}_weight"] = csr["weight"]
+            V = int(csr["num_vertices"])
+            fx[f"{variant}_num_vertices"] = np.array(V)
+            bfs_d, bfs_p, bfs_it = [], [], []
+            for r in ROOTS:
+                if r >= V:
+                    continue
+                out = po.ref_run(f, exe, 0, [*fl, "-p", "2", "-r", str(r)])
+                bfs_d.append(out["bfs_distances"])
+                bfs_p.append([r, out["source"], out["processed_nodes"], out["iteration"]])
+            fx[f"{variant}_bfs_distances"] = np.stack(bfs_d)
+            fx[f"{variant}_bfs_meta"] = np.array(bfs_p, dtype=np.int64)
+            out = po.ref_run(f, exe, 1, [*fl, "-i", "20", "-e", "0"])
+            fx[f"{variant}_pr20"] = out["pr_ranks"]
+            out = po.ref_run(f, exe, 1, [*fl, "-i", "100", "-e", "1e-4"])
+            fx[f"{variant}_pr_eps"] = out["pr_ranks"]
+            fx[f"{variant}_pr_eps_iterations"] = np.array(out["iterations"])
+            out = po.ref_run(f, exe, 2, [*fl, "-r", "1", "-b", "1"], threads=1)
+            fx[f"{variant}_sssp"] = out["sssp_distances"]
+            fx[f"{variant}_sssp_source"] = np.array(out["source"])
+            out = po.ref_run(f, exe, 6, [*fl, "-p", "1"])
+            fx[f"{variant}_cc"] = out["cc_components"]
+            out = po.ref_run(f, exe, 5, [*fl, "-i", "2"])
+            fx[f"{variant}_spmv_x"] = out["spmv_x"]
+            fx[f"{variant}_spmv_y"] = out["spmv_y"]
+            if variant == "u":
+                out = po.ref_run(f, exe, 8, [*fl, "-p", "1"])
+                fx["u_tc"] = np.array(out["total_counts"], dtype=np.uint64)
+            # degree reordering (out-degree) of the same input
+            out = po.ref_run(f, exe, -1, [*fl, "-l", "1"])
+            fx[f"{variant}_reorder_label"] = out["label"]
+            fx[f"{variant}_reorder_dest"] = out["dest"]
+            fx[f"{variant}_reorder_out_degree"] = out["out_degree"]
+        np.savez_compressed(out_dir / f"{name}.npz", **fx)
+        print(f"wrote {name}.npz")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,243 @@
+"""GPU parity: every kernel through the C ABI against the reference's golden
+outputs (tests/golden) and the CPU oracle on the same seeded inputs.
+
+Integer results (CSR, reordering, BFS levels and stats, SSSP distances, CC
+labels, TC counts) must be bit-exact. PageRank and SpMV must be within 1e-6
+relative L1 of the FP64 restatement (the tolerance the spec states).
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_GRAPHS, load_golden
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+REL_L1_TOL = 1e-6
+VARIANTS = [("u", True, True), ("dw", False, False), ("dwk", False, True)]
+
+
+def _inputs(fx, variant, symmetric):
+    src, dst = fx["src"], fx["dst"]
+    w = fx.get("weight")
+    if variant == "u":
+        w = None
+    elif w is None:
+        w = np.ones(src.shape[0], np.float32)
+    V = int(max(src.max(), dst.max())) + 1
+    return V, src, dst, w
+
+
+def gpu_graph(gbx, fx, variant, symmetric, dedup):
+    V, src, dst, w = _inputs(fx, variant, symmetric)
+    deg, idx, s, d, ww = gbx.csr_build(src, dst, w, num_vertices=V, symmetric=symmetric, dedup=dedup, sort=1)
+    g = gbx.GraphCSR(V, int(s.shape[0]), deg, idx, d, s, ww, np.arange(V, dtype=np.uint32),
+                     np.arange(V, dtype=np.uint32))
+    if variant != "u":
+        ideg, iidx, _, idst, iw = gbx.csr_build(d, s, ww, num_vertices=V, sort=1)
+        g.inverse_out_degree, g.inverse_edges_idx, g.inverse_dest, g.inverse_weight = ideg, iidx, idst, iw
+    return g
+
+
+def host_views(g):
+    host = po.HostCSR(g.num_vertices, g.out_degree, g.edges_idx, g.dest, g.weight, g.src)
+    pull = None
+    if g.inverse_dest is not None:
+        pull = po.HostCSR(g.num_vertices, g.inverse_out_degree, g.inverse_edges_idx, g.inverse_dest,
+                          g.inverse_weight)
+    return host, pull
+
+
+@pytest.mark.parametrize("name", GOLDEN_GRAPHS)
+@pytest.mark.parametrize("variant,symmetric,dedup", VARIANTS)
+def test_csr_build_golden(gbx, cuda_device, name, variant, symmetric, dedup):
+    fx = load_golden(name)
+    g = gpu_graph(gbx, fx, variant, symmetric, dedup)
+    assert g.num_vertices == int(fx[f"{variant}_num_vertices"])
+    np.testing.assert_array_equal(g.out_degree, fx[f"{variant}_out_degree"])
+    np.testing.assert_array_equal(g.edges_idx, fx[f"{variant}_edges_idx"])
+    np.testing.assert_array_equal(g.dest, fx[f"{variant}_dest"])
+    np.testing.assert_array_equal(g.src, fx[f"{variant}_src"])
+    if f"{variant}_weight" in fx:
+        np.testing.assert_array_equal(g.weight, fx[f"{variant}_weight"])
+
+
+@pytest.mark.parametrize("name", GOLDEN_GRAPHS)
+@pytest.mark.parametrize("variant,symmetric,dedup", VARIANTS)
+def test_degree_reorder_golden(gbx, cuda_device, name, variant, symmetric, dedup):
+    fx = load_golden(name)
+    g = gpu_graph(gbx, fx, variant, symmetric, dedup)
+    el = gbx.EdgeList(g.num_vertices, g.src.copy(), g.dest.copy())
+    gbx.degree_reorder(el, 1)
+    np.testing.assert_array_equal(el.label_array, fx[f"{variant}_reorder_label"])
+    np.testing.assert_array_equal(el.inverse_label_array[el.label_array],
+                                  np.arange(g.num_vertices, dtype=np.uint32))
+    deg, _, _, d, _ = gbx.csr_build(el.src, el.dst, num_vertices=g.num_vertices, sort=1)
+    np.testing.assert_array_equal(d, fx[f"{variant}_reorder_dest"])
+    np.testing.assert_array_equal(deg, fx[f"{variant}_reorder_out_degree"])
+
+
+@pytest.mark.parametrize("name", GOLDEN_GRAPHS)
+@pytest.mark.parametrize("variant,symmetric,dedup", VARIANTS)
+def test_algorithms_golden(gbx, cuda_device, name, variant, symmetric, dedup):
+    fx = load_golden(name)
+    g = gpu_graph(gbx, fx, variant, symmetric, dedup)
+    host, pull = host_views(g)
+    with gbx.DeviceGraph.from_graph_csr(g, use_weights=(variant != "u")) as dg:
+        for dist, meta in zip(fx[f"{variant}_bfs_distances"], fx[f"{variant}_bfs_meta"]):
+            st = gbx.breadth_first_search(dg, int(meta[0]), pushpull=2)
+            np.testing.assert_array_equal(st.distances, dist)
+            assert (st.processed_nodes, st.iteration) == (int(meta[2]), int(meta[3]))
+            for mode in (0, 1):
+                st = gbx.breadth_first_search(dg, int(meta[0]), pushpull=mode)
+                np.testing.assert_array_equal(st.distances, dist)
+        pr = gbx.page_rank(dg, 20, 0.0)
+        ref64, _, _ = po.pagerank(host, 20, 0.0, pull, fp64=True)
+        assert po.rel_l1(pr.pageRanks, ref64) <= REL_L1_TOL
+        assert po.rel_l1(pr.pageRanks, fx[f"{variant}_pr20"]) <= REL_L1_TOL
+        assert pr.iterations == 20
+        st = gbx.sssp(dg, int(fx[f"{variant}_sssp_source"]), delta=1, map_source=False)
+        np.testing.assert_array_equal(st.distances, fx[f"{variant}_sssp"])
+        st = gbx.sssp(dg, int(fx[f"{variant}_sssp_source"]), delta=0, map_source=False)
+        np.testing.assert_array_equal(st.distances, fx[f"{variant}_sssp"])
+        for cv in (0, 1, 2):
+            comp, _ = gbx.connected_components(dg, cv)
+            np.testing.assert_array_equal(comp, fx[f"{variant}_cc"])
+        x = fx[f"{variant}_spmv_x"]
+        y = gbx.spmv(dg, x, iterations=2)
+        y64 = po.spmv(host, x, None if variant == "u" else pull.weight, 0.0001, 2, pull=pull, fp64=True)
+        assert po.rel_l1(y, y64) <= REL_L1_TOL
+        assert po.rel_l1(y, fx[f"{variant}_spmv_y"]) <= REL_L1_TOL
+        if variant == "u":
+            assert gbx.triangle_count(dg) == int(fx["u_tc"])
+
+
+def _rmat_graph(gbx, scale, ef, seed, symmetric=False, weights=None):
+    V = 1 << scale
+    src, dst = gbx.generate_rmat(scale, V * ef, seed=seed)
+    w = None
+    if weights == "int":
+        w = gbx.generate_values(src.shape[0], 0, 1, 255, seed=seed + 11)
+    el = gbx.EdgeList(V, src, dst, w)
+    if symmetric:
+        el = gbx.EdgeList(V, np.concatenate([src, dst]), np.concatenate([dst, src]),
+                          None if w is None else np.concatenate([w, w]))
+    return gbx.graph_csr_preprocessing(el, sort=1, dedup=True, directed=not symmetric,
+                                       keep_weights=w is not None)
+
+
+@pytest.mark.parametrize("scale,ef,seed", [(14, 16, 1), (16, 16, 2)])
+def test_rmat_directed(gbx, cuda_device, scale, ef, seed):
+    g = _rmat_graph(gbx, scale, ef, seed, weights="int")
+    host, pull = host_views(g)
+    # CSR build against the oracle's sort/dedup of the same edge list
+    src, dst = gbx.generate_rmat(scale, (1 << scale) * ef, seed=seed)
+    w = gbx.generate_values(src.shape[0], 0, 1, 255, seed=seed + 11)
+    ref = po.build_csr(1 << scale, src, dst, w, sort_mode=1, dedup=True)
+    np.testing.assert_array_equal(g.dest, ref.dest)
+    np.testing.assert_array_equal(g.edges_idx, ref.edges_idx)
+    np.testing.assert_array_equal(g.weight, ref.weight)
+    rng = np.random.default_rng(seed)
+    roots = [0] + [int(r) for r in rng.choice(np.nonzero(g.out_degree)[0], 5)]
+    with gbx.DeviceGraph.from_graph_csr(g) as dg:
+        for r in roots:
+            st = gbx.breadth_first_search(dg, r)
+            d, _, proc, it = po.bfs(host, r, pull)
+            np.testing.assert_array_equal(st.distances, d)
+            assert (st.processed_nodes, st.iteration) == (proc, it)
+            # parents form a BFS tree
+            par = np.asarray(st.parents)
+            reached = np.nonzero((d > 0))[0]
+            assert np.all(d[par[reached]] == d[reached] - 1)
+        for r in roots[:3]:
+            st = gbx.sssp(dg, r)
+            np.testing.assert_array_equal(st.distances, po.sssp(host, r, 64))
+        pr = gbx.page_rank(dg, 20, 0.0)
+        ref64, _, _ = po.pagerank(host, 20, 0.0, pull, fp64=True)
+        assert po.rel_l1(pr.pageRanks, ref64) <= REL_L1_TOL
+        x = gbx.generate_values(g.num_vertices, 2, seed=5)
+        vals = gbx.generate_values(g.num_edges, 1, seed=6)
+        y = gbx.spmv(dg, x, values=vals)
+        y64 = po.spmv(host, x, vals, pull=pull, fp64=True)
+        assert po.rel_l1(y, y64) <= REL_L1_TOL
+
+
+@pytest.mark.parametrize("scale,ef,seed", [(14, 8, 3), (16, 16, 4)])
+def test_rmat_symmetric(gbx, cuda_device, scale, ef, seed):
+    g = _rmat_graph(gbx, scale, ef, seed, symmetric=True)
+    host, _ = host_views(g)
+    with gbx.DeviceGraph.from_graph_csr(g) as dg:
+        ref = po.cc(host, 1)
+        for cv in (0, 1, 2):
+            comp, _ = gbx.connected_components(dg, cv)
+            np.testing.assert_array_equal(comp, ref)
+        assert gbx.triangle_count(dg) == po.triangle_count(host)
+    # degree-ordered DAG: TC after degree reordering gives the same count
+    el = gbx.EdgeList(g.num_vertices, g.src.copy(), g.dest.copy())
+    gbx.degree_reorder(el, 1)
+    g2 = gbx.graph_csr_preprocessing(el, sort=1, directed=False, keep_weights=False)
+    with gbx.DeviceGraph.from_graph_csr(g2) as dg2:
+        assert gbx.triangle_count(dg2) == po.triangle_count(host)
+
+
+def test_edge_cases(gbx, cuda_device):
+    # single vertex, no edges
+    g = gbx.GraphCSR(1, 0, np.zeros(1, np.uint32), np.zeros(1, np.uint32), np.zeros(0, np.uint32),
+                     np.zeros(0, np.uint32), None, np.zeros(1, np.uint32), np.zeros(1, np.uint32))
+    with gbx.DeviceGraph.from_graph_csr(g) as dg:
+        st = gbx.breadth_first_search(dg, 0)
+        assert st.processed_nodes == 1 and st.distances[0] == 0
+        pr = gbx.page_rank(dg, 5, 0.0)
+        assert np.isclose(pr.pageRanks[0], np.float32(1.0) - np.float32(0.85))
+        assert gbx.triangle_count(dg) == 0
+        comp, _ = gbx.connected_components(dg, 1)
+        assert comp[0] == 0
+        with pytest.raises(gbx.GbxError):
+            gbx.breadth_first_search(dg, 1, map_source=False)  # source out of range
+    # isolated vertices, a degree-0 source, self loops and duplicates kept
+    src = np.array([0, 0, 1, 1, 2, 2, 5, 5, 5], np.uint32)
+    dst = np.array([1, 1, 2, 2, 0, 2, 5, 0, 1], np.uint32)
+    V = 8
+    deg, idx, s, d, _ = gbx.csr_build(src, dst, num_vertices=V, sort=1)
+    ref = po.build_csr(V, src, dst, sort_mode=1)
+    np.testing.assert_array_equal(d, ref.dest)
+    g = gbx.GraphCSR(V, int(s.shape[0]), deg, idx, d, s, None, np.arange(V, dtype=np.uint32),
+                     np.arange(V, dtype=np.uint32))
+    host = po.HostCSR(V, deg, idx, d)
+    with gbx.DeviceGraph.from_graph_csr(g) as dg:
+        for r in range(V):
+            st = gbx.breadth_first_search(dg, r)
+            dd, par, proc, it = po.bfs(host, r)
+            np.testing.assert_array_equal(st.distances, dd)
+            assert (st.processed_nodes, st.iteration) == (proc, it)
+            unreached = (dd == 0) & (np.arange(V) != r)
+            np.testing.assert_array_equal(np.asarray(st.parents)[unreached], par[unreached])
+        assert gbx.triangle_count(dg) == po.triangle_count(host)  # multiplicities and loops
+        comp, _ = gbx.connected_components(dg, 2)
+        np.testing.assert_array_equal(comp, po.cc(host, 2))
+
+
+def test_layout_rejected(gbx, cuda_device):
+    # edges_idx that is not the prefix sum of the degrees
+    g = gbx.GraphCSR(3, 2, np.array([1, 1, 0], np.uint32), np.array([1, 0, 0], np.uint32),
+                     np.array([1, 2], np.uint32), np.array([0, 1], np.uint32), None,
+                     np.arange(3, dtype=np.uint32), np.arange(3, dtype=np.uint32))
+    with pytest.raises(gbx.GbxError) as e:
+        gbx.DeviceGraph.from_graph_csr(g)
+    assert e.value.status == -6
+
+
+def test_device_resident_outputs(gbx, cuda_device):
+    import torch
+
+    g = _rmat_graph(gbx, 12, 8, 9)
+    host, pull = host_views(g)
+    with gbx.DeviceGraph.from_graph_csr(g) as dg:
+        dist = torch.empty(g.num_vertices, dtype=torch.int32, device=cuda_device)
+        st = gbx.breadth_first_search(dg, 0, distances=dist, parents=None)
+        d, _, _, _ = po.bfs(host, 0, pull)
+        np.testing.assert_array_equal(dist.cpu().numpy().view(np.uint32), d)
+        ranks = torch.empty(g.num_vertices, dtype=torch.float32, device=cuda_device)
+        gbx.page_rank(dg, 20, 0.0, ranks=ranks)
+        ref64, _, _ = po.pagerank(host, 20, 0.0, pull, fp64=True)
+        assert po.rel_l1(ranks.cpu().numpy(), ref64) <= REL_L1_TOL
