@@ -170,7 +170,7 @@ def run_gpu(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    W = build_workload(gbx)
+    W = build_workload(gbx, scale=args.scale)
     g, gs, gsr = W["g"], W["gs"], W["gsr"]
     V, E = g.num_vertices, g.num_edges
     dev = torch.device("cuda", local)
@@ -248,7 +248,7 @@ def run_gpu(args):
         return [("bfs", bfs), ("sssp", sssp), ("cc", cc), ("tc", tc), ("spmv", spmv), ("pr", pr),
                 ("reorder", reorder)]
 
-    ks = kernels()
+    ks = [(n, f) for n, f in kernels() if not args.only or n in args.only.split(",")]
     ev = {n: [] for n, _ in ks}
     work = {}
 
@@ -308,7 +308,7 @@ def run_gpu(args):
             "peak_kind": peak_kind, "unit": "GB/s", "frac": per[dom]["frac"],
             "traffic": args.traffic, "note": "achieved = algorithmic bytes / CUDA-event time"}
 
-    e2e = run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp)
+    e2e = None if args.no_e2e else run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(W, args, roots)
@@ -319,7 +319,7 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32 (ids, levels, distances) + f32 (ranks, SpMV)",
         "data": "synthetic",
-        "config": {"workload": "rmat22_full_kernel_set", "scale": SCALE, "num_vertices": V,
+        "config": {"workload": f"rmat{args.scale}_full_kernel_set", "scale": args.scale, "num_vertices": V,
                    "edges_generated": V * EDGE_FACTOR, "num_edges": E, "num_edges_symmetric": gs.num_edges,
                    "dag_edges": e_plus, "bfs_roots": N_ROOTS, "sssp_roots": N_SSSP_ROOTS,
                    "pr_iterations": PR_ITERS, "l2": "flushed (256 MiB write) before every kernel",
@@ -487,7 +487,7 @@ def run_reference(args):
         return
     import graphblox_gb300 as gbx
 
-    W = build_workload(gbx)
+    W = build_workload(gbx, scale=args.scale)
     roots = W["roots"]
     samples = []
     for i in range(args.warmup + args.steps):
@@ -503,7 +503,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs / len(samples) * 1e3, 2),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32 (ids, levels, distances) + f32 (ranks, SpMV)", "data": "synthetic",
-        "config": {"workload": "rmat22_full_kernel_set", "scale": SCALE, "num_vertices": W["V"],
+        "config": {"workload": f"rmat{args.scale}_full_kernel_set", "scale": args.scale, "num_vertices": W["V"],
                    "num_edges": W["g"].num_edges},
         "impl": "reference",
         "cpu_baseline": {"value": round(value, 4), "unit": "GTEPS", "cores": os.cpu_count(), "kind": "port",
@@ -522,6 +522,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbx", choices=["gbx", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--scale", type=int, default=SCALE, help="RMAT scale (22 is the benchmark workload)")
+    ap.add_argument("--only", default="", help="comma-separated kernel subset (profiling runs)")
+    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the dominant kernel from an ncu capture")
     args = ap.parse_args()

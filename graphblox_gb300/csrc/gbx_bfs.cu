@@ -1,45 +1,412 @@
 // Direction-optimising BFS (the reference's
 // breadthFirstSearchDirectionOptimizedGraphCSR, BFS.c:335-485, with the
-// top-down step :498-546 and the bottom-up step :562-613).
+// top-down step :498-546 and the bottom-up step :562-613), as ONE persistent
+// cooperative kernel: the whole traversal, including the direction
+// decisions, runs on the device with one grid barrier per step.
 //
 // State in HBM: level[V] (0xFFFFFFFF = unvisited), parent[V], a visited
-// bitmap and two frontier bitmaps (V/8 bytes each: 512 KiB at 4M vertices,
-// resident in L2), and two vertex queues.
+// bitmap and two frontier bitmaps (V/8 bytes each, L2-resident), and two
+// generations of frontier lists: a queue of vertices with out-degree in
+// (0, kHubDeg] and a hub list for larger ones.
 //
-//  top-down  : the frontier queue's degrees are prefix-summed; a persistent
-//              grid walks the flattened edge list in tiles of 1024 edges
-//              (consecutive threads on consecutive edges, so dest[] loads are
-//              coalesced), finds each edge's frontier vertex by a binary
-//              search bounded to the tile's range, claims unvisited
-//              neighbours with atomicOr on the visited bitmap, and appends
-//              them to the next queue with one atomic per warp (ballot +
-//              popc ranks).
-//  bottom-up : one warp per 32 consecutive vertices = one bitmap word; each
-//              unvisited lane scans its pull neighbours until one is in the
-//              current frontier bitmap; the warp ballot is the next-frontier
-//              word and is or-ed into the visited word by a single writer.
+//  top-down  : warps take work units from an atomic cursor. A unit is either
+//              kHubChunk edges of one hub (hubs are cut so no warp serialises
+//              a hub's row) or 32 queued vertices whose edges the warp
+//              flattens (warp scan of degrees, consecutive lanes on
+//              consecutive edges, 4 loads in flight per lane). Unvisited
+//              neighbours are claimed with atomicOr on the visited bitmap and
+//              appended with one atomic per warp (ballot + popc ranks); a hub
+//              is appended with a single 64-bit atomic that returns both its
+//              list slot and the first of its edge chunks, so the hub list is
+//              born sorted by chunk.
+//  bottom-up : one warp per bitmap word (32 vertices); each unvisited lane
+//              scans its pull neighbours until one is in the current frontier
+//              bitmap; the ballot is the next-frontier word.
 //
-// The direction heuristic is the reference's (alpha 15, beta 18, mu/mf/nf
-// bookkeeping in uint32 arithmetic), evaluated on the host after each step
-// from a 24-byte counter block, so processed_nodes and iteration match the
-// reference's stats.
+// The direction heuristic is the reference's (alpha 15, beta 18, mu/mf/nf in
+// uint32 arithmetic). Every CTA evaluates it redundantly from the previous
+// step's counters (triple-buffered, so CTA 0 can clear the next slot while
+// others still read the last one), which is what lets one barrier per step
+// suffice. processed_nodes and iteration therefore match the reference.
 #include <algorithm>
 
-#include "gbx_internal.cuh"
+#include "gbx_coop.cuh"
 
 namespace gbx {
 
-struct BfsCounters {
-    uint32_t qlen;  // vertices appended to the next queue (degree > 0)
-    uint32_t nf;    // vertices claimed in this step
-    uint32_t mf;    // sum over claimed of max(out_degree, 1) (BFS.c:537)
-    uint32_t pad;
-    unsigned long long edges;  // sum of out_degree over claimed
+constexpr uint32_t kHubDeg = 1024;    // out-degree above which a vertex is a hub
+constexpr uint32_t kHubChunk = 1024;  // edges per hub work unit
+constexpr int kBfsThreads = 256;
+constexpr int kBfsWarps = kBfsThreads / 32;
+
+struct BfsStep {
+    unsigned cursor;          // work-unit cursor
+    unsigned nf;              // vertices claimed
+    unsigned mf;              // sum over claimed of max(out_degree, 1) (BFS.c:537)
+    unsigned qlen;            // next queue length
+    unsigned long long hub;   // next hub list: (count << 32) | chunks
+    unsigned long long edges; // sum of out_degree over claimed
 };
 
-constexpr int kTdThreads = 256;
-constexpr int kTdItems = 4;
-constexpr uint32_t kTdTile = kTdThreads * kTdItems;
+struct BfsState {
+    GridSync gs;
+    BfsStep step[3];
+    BfsStep conv;  // lists rebuilt from a bitmap when leaving bottom-up
+    unsigned processed, iteration, td_steps, bu_steps, depth, status;
+    unsigned long long edges_total;
+};
+
+struct BfsArgs {
+    const uint32_t *off, *dest, *poff, *psrc, *outdeg;
+    uint32_t V, words, E, mode, source;
+    uint32_t *level;
+    int32_t *parent;
+    uint32_t *visited;
+    uint32_t *bm[2];
+    uint32_t *q[2];
+    uint32_t *hv[2];
+    uint32_t *hc[2];
+    BfsState *st;
+};
+
+__device__ __forceinline__ uint32_t hub_chunks(uint32_t d) { return (d + kHubChunk - 1) / kHubChunk; }
+
+// Claim u (reached from v) at level lnext; all lanes call together.
+struct Claimer {
+    const BfsArgs &a;
+    uint32_t lnext;
+    uint32_t *qout, *hvout, *hcout;
+    BfsStep *cnt;
+    unsigned nf = 0, mf = 0;
+    unsigned long long edges = 0;
+    __device__ __forceinline__ Claimer(const BfsArgs &a_, uint32_t l, uint32_t *q, uint32_t *hv, uint32_t *hc,
+                                       BfsStep *c)
+        : a(a_), lnext(l), qout(q), hvout(hv), hcout(hc), cnt(c) {}
+    __device__ __forceinline__ void operator()(uint32_t v, uint32_t u, bool active) {
+        bool push = false;
+        uint32_t du = 0;
+        if (active) {
+            const uint32_t bit = 1u << (u & 31);
+            uint32_t *word = a.visited + (u >> 5);
+            if (!(__ldcg(word) & bit) && !(atomicOr(word, bit) & bit)) {
+                a.level[u] = lnext;
+                a.parent[u] = (int32_t)v;
+                du = __ldg(a.outdeg + u);
+                nf += 1;
+                mf += du ? du : 1u;
+                edges += du;
+                if (du > kHubDeg) {
+                    unsigned long long old = atomicAdd(&cnt->hub, (1ull << 32) | hub_chunks(du));
+                    uint32_t slot = (uint32_t)(old >> 32);
+                    hvout[slot] = u;
+                    hcout[slot] = (uint32_t)old;
+                } else {
+                    push = du > 0;
+                }
+            }
+        }
+        const uint32_t lane = threadIdx.x & 31;
+        unsigned m = __ballot_sync(0xffffffffu, push);
+        if (m) {
+            uint32_t leader = __ffs(m) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(&cnt->qlen, (unsigned)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (push) qout[base + __popc(m & ((1u << lane) - 1u))] = u;
+        }
+    }
+    __device__ __forceinline__ void flush() {
+        unsigned n = warp_sum(nf), f = warp_sum(mf);
+        unsigned long long e = warp_sum(edges);
+        if ((threadIdx.x & 31) == 0 && n) {
+            atomicAdd(&cnt->nf, n);
+            atomicAdd(&cnt->mf, f);
+            atomicAdd(&cnt->edges, e);
+        }
+    }
+};
+
+// last h in [0, n) with hc[h] <= c
+__device__ __forceinline__ uint32_t hub_of_chunk(const uint32_t *hc, uint32_t n, uint32_t c) {
+    uint32_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi + 1) >> 1;
+        if (__ldcg(hc + mid) <= c) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ void top_down_phase(const BfsArgs &a, const uint32_t *qin, uint32_t qn, const uint32_t *hvin,
+                               const uint32_t *hcin, uint32_t nh, uint32_t nc, BfsStep *cur, uint32_t *qout,
+                               uint32_t *hvout, uint32_t *hcout, uint32_t lnext, uint32_t *s_pre,
+                               uint32_t *s_base, uint32_t *s_v) {
+    const uint32_t lane = threadIdx.x & 31;
+    Claimer claim(a, lnext, qout, hvout, hcout, cur);
+    const uint32_t units = nc + (qn + 31) / 32;
+    for (;;) {
+        uint32_t unit = 0;
+        if (lane == 0) unit = atomicAdd(&cur->cursor, 1u);
+        unit = __shfl_sync(0xffffffffu, unit, 0);
+        if (unit >= units) break;
+        if (unit < nc) {
+            // kHubChunk edges of one hub
+            const uint32_t h = hub_of_chunk(hcin, nh, unit);
+            const uint32_t v = __ldcg(hvin + h);
+            const uint32_t rb = __ldg(a.off + v), re = __ldg(a.off + v + 1);
+            const uint32_t cb = rb + (unit - __ldcg(hcin + h)) * kHubChunk;
+            const uint32_t ce = min(cb + kHubChunk, re);
+            for (uint32_t j0 = cb; j0 < ce; j0 += 128) {
+                uint32_t u[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    uint32_t j = j0 + q * 32 + lane;
+                    u[q] = j < ce ? __ldg(a.dest + j) : 0u;
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) claim(v, u[q], j0 + q * 32 + lane < ce);
+            }
+        } else {
+            // 32 queued vertices, edges flattened over the warp
+            const uint32_t qi = (unit - nc) * 32 + lane;
+            uint32_t v = 0, b = 0, d = 0;
+            if (qi < qn) {
+                v = __ldcg(qin + qi);
+                b = __ldg(a.off + v);
+                d = __ldg(a.off + v + 1) - b;
+            }
+            uint32_t incl = d;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= (uint32_t)o) incl += t;
+            }
+            s_pre[lane] = incl - d;
+            s_base[lane] = b;
+            s_v[lane] = v;
+            if (lane == 31) s_pre[32] = incl;
+            __syncwarp();
+            const uint32_t tot = s_pre[32];
+            uint32_t k = 0;
+            for (uint32_t i0 = 0; i0 < tot; i0 += 128) {
+                uint32_t u[4], src[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    uint32_t i = i0 + q * 32 + lane;
+                    u[q] = 0;
+                    src[q] = 0;
+                    if (i < tot) {
+                        while (s_pre[k + 1] <= i) ++k;
+                        src[q] = s_v[k];
+                        u[q] = __ldg(a.dest + s_base[k] + (i - s_pre[k]));
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) claim(src[q], u[q], i0 + q * 32 + lane < tot);
+            }
+            __syncwarp();
+        }
+    }
+    claim.flush();
+}
+
+__device__ void bottom_up_phase(const BfsArgs &a, const uint32_t *cur_bm, uint32_t *next_bm, uint32_t lnext,
+                                BfsStep *cnt) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    unsigned nf = 0;
+    unsigned long long edges = 0;
+    for (uint32_t w = gw; w < a.words; w += nw) {
+        const uint32_t vis = __ldcg(a.visited + w);
+        if (vis == 0xFFFFFFFFu) {
+            if (lane == 0) next_bm[w] = 0;
+            continue;
+        }
+        const uint32_t v = w * 32 + lane;
+        bool found = false;
+        if (v < a.V && !((vis >> lane) & 1u)) {
+            const uint32_t b = __ldg(a.poff + v), e = __ldg(a.poff + v + 1);
+            for (uint32_t j = b; j < e; ++j) {
+                const uint32_t u = __ldg(a.psrc + j);
+                if ((__ldcg(cur_bm + (u >> 5)) >> (u & 31)) & 1u) {
+                    a.level[v] = lnext;
+                    a.parent[v] = (int32_t)u;
+                    found = true;
+                    break;
+                }
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, found);
+        if (found) edges += __ldg(a.outdeg + v);
+        if (lane == 0) {
+            next_bm[w] = m;
+            if (m) a.visited[w] = vis | m;
+            nf += __popc(m);
+        }
+    }
+    edges = warp_sum(edges);
+    if (lane == 0 && (nf || edges)) {
+        atomicAdd(&cnt->nf, nf);
+        atomicAdd(&cnt->edges, edges);
+    }
+}
+
+__device__ void level_to_bitmap_phase(const BfsArgs &a, uint32_t l, uint32_t *bm) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t w = gw; w < a.words; w += nw) {
+        const uint32_t v = w * 32 + lane;
+        const unsigned m = __ballot_sync(0xffffffffu, v < a.V && __ldcg(a.level + v) == l);
+        if (lane == 0) bm[w] = m;
+    }
+}
+
+// bitmapToArrayQueue (arrayQueue.c:310-337): a frontier bitmap -> queue + hubs
+__device__ void bitmap_to_lists_phase(const BfsArgs &a, const uint32_t *bm, uint32_t *qout, uint32_t *hvout,
+                                      uint32_t *hcout, BfsStep *cnt) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t w = gw; w < a.words; w += nw) {
+        const uint32_t word = __ldcg(bm + w);
+        if (!word) continue;
+        const uint32_t v = w * 32 + lane;
+        bool push = false;
+        if (((word >> lane) & 1u) && v < a.V) {
+            const uint32_t d = __ldg(a.outdeg + v);
+            if (d > kHubDeg) {
+                unsigned long long old = atomicAdd(&cnt->hub, (1ull << 32) | hub_chunks(d));
+                uint32_t slot = (uint32_t)(old >> 32);
+                hvout[slot] = v;
+                hcout[slot] = (uint32_t)old;
+            } else {
+                push = d > 0;
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, push);
+        if (m) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(&cnt->qlen, (unsigned)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (push) qout[base + __popc(m & ((1u << lane) - 1u))] = v;
+        }
+    }
+}
+
+__device__ __forceinline__ void zero_step(BfsStep *s) {
+    s->cursor = 0;
+    s->nf = 0;
+    s->mf = 0;
+    s->qlen = 0;
+    s->hub = 0;
+    s->edges = 0;
+}
+
+__global__ void __launch_bounds__(kBfsThreads) bfs_persistent_kernel(BfsArgs a) {
+    __shared__ uint32_t s_pre[kBfsWarps][33];
+    __shared__ uint32_t s_base[kBfsWarps][32];
+    __shared__ uint32_t s_v[kBfsWarps][32];
+    const uint32_t wid = threadIdx.x >> 5;
+    BfsState *st = a.st;
+    const uint32_t alpha = 15, beta = 18;
+    // DO bookkeeping, evaluated identically by every CTA
+    uint32_t mu = a.E, mf = __ldg(a.outdeg + a.source), qsize = 1, nf_prev = 0, L = 0;
+    uint32_t processed = 1, iteration = 1, td = 0, bu = 0;
+    unsigned long long edges_total = __ldg(a.outdeg + a.source);
+    bool in_bu = false, last_was_bu = false, done = false, failed = false;
+    const uint32_t max_steps = 2 * a.V + 16;
+    // lists for step 0: prepared by the host in generation 0
+    uint32_t qn = __ldcg(&st->conv.qlen);
+    unsigned long long hub0 = __ldcg(&st->conv.hub);
+    uint32_t nh = (uint32_t)(hub0 >> 32), nc = (uint32_t)hub0;
+    for (uint32_t s = 0; !done; ++s) {
+        if (s >= max_steps) {
+            failed = true;
+            break;
+        }
+        BfsStep *cur = &st->step[s % 3];
+        if (blockIdx.x == 0 && threadIdx.x == 0) zero_step(&st->step[(s + 1) % 3]);
+        const uint32_t ib = s & 1, ob = ib ^ 1;
+        bool use_bu;
+        if (a.mode == 0) {
+            use_bu = true;
+        } else if (a.mode == 1) {
+            use_bu = false;
+        } else if (in_bu) {
+            use_bu = true;  // still inside the reference's do { } while loop
+        } else {
+            use_bu = mf > mu / alpha;
+        }
+        if (use_bu) {
+            if (!in_bu) {
+                // arrayQueueToBitmap: frontier bitmap of the current level
+                level_to_bitmap_phase(a, L, a.bm[ib]);
+                if (!grid_barrier(&st->gs)) { failed = true; break; }
+                nf_prev = qsize;
+                in_bu = true;
+            }
+            bottom_up_phase(a, a.bm[ib], a.bm[ob], L + 1, cur);
+            if (!grid_barrier(&st->gs)) { failed = true; break; }
+            const uint32_t nf = __ldcg(&cur->nf);
+            processed += nf;
+            iteration++;
+            bu++;
+            edges_total += __ldcg(&cur->edges);
+            if (nf) L++;
+            bool again = a.mode == 0 ? nf > 0 : (nf > nf_prev || nf > a.V / beta);
+            nf_prev = nf;
+            if (!again) {
+                in_bu = false;
+                qsize = nf;
+                if (nf == 0 || a.mode == 0) {
+                    done = true;
+                } else {
+                    // bitmapToArrayQueue into the list generation step s+1 reads
+                    if (blockIdx.x == 0 && threadIdx.x == 0) zero_step(&st->conv);
+                    if (!grid_barrier(&st->gs)) { failed = true; break; }
+                    bitmap_to_lists_phase(a, a.bm[ob], a.q[ob], a.hv[ob], a.hc[ob], &st->conv);
+                    if (!grid_barrier(&st->gs)) { failed = true; break; }
+                    qn = __ldcg(&st->conv.qlen);
+                    unsigned long long hb = __ldcg(&st->conv.hub);
+                    nh = (uint32_t)(hb >> 32);
+                    nc = (uint32_t)hb;
+                    mf = 1;
+                }
+            }
+            last_was_bu = true;
+        } else {
+            mu -= mf;
+            top_down_phase(a, a.q[ib], qn, a.hv[ib], a.hc[ib], nh, nc, cur, a.q[ob], a.hv[ob], a.hc[ob], L + 1,
+                           s_pre[wid], s_base[wid], s_v[wid]);
+            if (!grid_barrier(&st->gs)) { failed = true; break; }
+            const uint32_t nf = __ldcg(&cur->nf);
+            mf = __ldcg(&cur->mf);
+            qsize = nf;
+            processed += nf;
+            iteration++;
+            td++;
+            edges_total += __ldcg(&cur->edges);
+            qn = __ldcg(&cur->qlen);
+            unsigned long long hb = __ldcg(&cur->hub);
+            nh = (uint32_t)(hb >> 32);
+            nc = (uint32_t)hb;
+            if (nf) L++;
+            if (qsize == 0) done = true;
+            last_was_bu = false;
+        }
+    }
+    (void)last_was_bu;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->processed = processed;
+        st->iteration = iteration;
+        st->td_steps = td;
+        st->bu_steps = bu;
+        st->depth = L;
+        st->edges_total = edges_total;
+        st->status = failed ? 1u : 0u;
+    }
+}
 
 __global__ void bfs_init_kernel(uint32_t *level, int32_t *parent, uint32_t *visited, uint32_t V,
                                 uint32_t words, uint32_t source) {
@@ -51,173 +418,24 @@ __global__ void bfs_init_kernel(uint32_t *level, int32_t *parent, uint32_t *visi
         visited[w] = (w == (source >> 5)) ? (1u << (source & 31)) : 0u;
 }
 
-__global__ void gather_degrees_kernel(const uint32_t *q, uint32_t qlen, const uint32_t *deg,
-                                      uint32_t *out) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < qlen; i += gridDim.x * blockDim.x)
-        out[i] = deg[q[i]];
-}
-
-// largest f in [lo, hi] with pre[f] <= i
-__device__ __forceinline__ uint32_t frontier_search(const uint32_t *pre, uint32_t lo, uint32_t hi,
-                                                    uint32_t i) {
-    while (lo < hi) {
-        uint32_t mid = (lo + hi + 1) >> 1;
-        if (__ldg(pre + mid) <= i) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
-
-__global__ void __launch_bounds__(kTdThreads)
-    bfs_top_down_kernel(const uint32_t *__restrict__ q, const uint32_t *__restrict__ pre, uint32_t qlen,
-                        const uint32_t *__restrict__ total_edges, const uint32_t *__restrict__ off,
-                        const uint32_t *__restrict__ dest, const uint32_t *__restrict__ outdeg,
-                        uint32_t *visited, uint32_t *level, int32_t *parent, uint32_t lnext,
-                        uint32_t *qnext, BfsCounters *cnt) {
-    __shared__ uint32_t s_range[2];
-    const uint32_t M = *total_edges;
-    const uint32_t lane = threadIdx.x & 31;
-    uint32_t nf = 0, mf = 0;
-    unsigned long long edges = 0;
-    for (uint64_t base = (uint64_t)blockIdx.x * kTdTile; base < M; base += (uint64_t)gridDim.x * kTdTile) {
-        uint64_t tile_end = base + kTdTile < M ? base + kTdTile : (uint64_t)M;
-        uint32_t last = (uint32_t)tile_end - 1;
-        if (threadIdx.x < 2) {
-            uint32_t target = threadIdx.x == 0 ? (uint32_t)base : last;
-            s_range[threadIdx.x] = frontier_search(pre, 0, qlen - 1, target);
-        }
-        __syncthreads();
-        const uint32_t flo = s_range[0], fhi = s_range[1];
-#pragma unroll
-        for (int k = 0; k < kTdItems; ++k) {
-            uint64_t i = base + (uint64_t)k * kTdThreads + threadIdx.x;
-            bool claimed = false;
-            uint32_t u = 0, du = 0;
-            if (i < M) {
-                uint32_t f = frontier_search(pre, flo, fhi, (uint32_t)i);
-                uint32_t v = __ldg(q + f);
-                uint32_t e = __ldg(off + v) + ((uint32_t)i - __ldg(pre + f));
-                u = __ldg(dest + e);
-                uint32_t bit = 1u << (u & 31);
-                uint32_t *word = visited + (u >> 5);
-                if (!(__ldcg(word) & bit)) {
-                    uint32_t old = atomicOr(word, bit);
-                    if (!(old & bit)) {
-                        claimed = true;
-                        level[u] = lnext;
-                        parent[u] = (int32_t)v;
-                        du = __ldg(outdeg + u);
-                        nf += 1;
-                        mf += du ? du : 1u;
-                        edges += du;
-                    }
-                }
-            }
-            bool push = claimed && du > 0;
-            unsigned m = __ballot_sync(0xffffffffu, push);
-            if (m) {
-                uint32_t leader = __ffs(m) - 1;
-                uint32_t basepos = 0;
-                if (lane == leader) basepos = atomicAdd(&cnt->qlen, (uint32_t)__popc(m));
-                basepos = __shfl_sync(0xffffffffu, basepos, leader);
-                if (push) qnext[basepos + __popc(m & ((1u << lane) - 1u))] = u;
-            }
-        }
-        __syncthreads();
-    }
-    // per-warp counter flush
-    nf = warp_sum(nf);
-    mf = warp_sum(mf);
-    edges = warp_sum(edges);
-    if (lane == 0 && nf) {
-        atomicAdd(&cnt->nf, nf);
-        atomicAdd(&cnt->mf, mf);
-        atomicAdd(&cnt->edges, edges);
+// generation-0 lists: the source alone (as a hub when its degree is large)
+__global__ void bfs_seed_kernel(const uint32_t *outdeg, uint32_t source, uint32_t *q0, uint32_t *hv0,
+                                uint32_t *hc0, BfsState *st) {
+    const uint32_t d = outdeg[source];
+    st->conv.qlen = 0;
+    st->conv.hub = 0;
+    if (d > kHubDeg) {
+        hv0[0] = source;
+        hc0[0] = 0;
+        st->conv.hub = (1ull << 32) | hub_chunks(d);
+    } else if (d > 0) {
+        q0[0] = source;
+        st->conv.qlen = 1;
     }
 }
 
-// frontier bitmap of the vertices at level `l` (entering bottom-up)
-__global__ void level_to_bitmap_kernel(const uint32_t *level, uint32_t V, uint32_t l, uint32_t *bm,
-                                       uint32_t words) {
-    const uint32_t lane = threadIdx.x & 31;
-    uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t w = gw; w < words; w += nw) {
-        uint32_t v = w * 32 + lane;
-        unsigned m = __ballot_sync(0xffffffffu, v < V && level[v] == l);
-        if (lane == 0) bm[w] = m;
-    }
-}
-
-__global__ void __launch_bounds__(256)
-    bfs_bottom_up_kernel(const uint32_t *__restrict__ poff, const uint32_t *__restrict__ psrc,
-                         const uint32_t *__restrict__ cur, uint32_t *__restrict__ next,
-                         uint32_t *visited, uint32_t *level, int32_t *parent,
-                         const uint32_t *__restrict__ outdeg, uint32_t V, uint32_t words,
-                         uint32_t lnext, BfsCounters *cnt) {
-    const uint32_t lane = threadIdx.x & 31;
-    uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    uint32_t nf = 0;
-    unsigned long long edges = 0;
-    for (uint32_t w = gw; w < words; w += nw) {
-        uint32_t vis = visited[w];
-        if (vis == 0xFFFFFFFFu) {
-            if (lane == 0) next[w] = 0;
-            continue;
-        }
-        uint32_t v = w * 32 + lane;
-        bool found = false;
-        if (v < V && !((vis >> lane) & 1u)) {
-            uint32_t b = __ldg(poff + v), e = __ldg(poff + v + 1);
-            for (uint32_t j = b; j < e; ++j) {
-                uint32_t u = __ldg(psrc + j);
-                if ((__ldg(cur + (u >> 5)) >> (u & 31)) & 1u) {
-                    level[v] = lnext;
-                    parent[v] = (int32_t)u;
-                    found = true;
-                    break;
-                }
-            }
-        }
-        unsigned m = __ballot_sync(0xffffffffu, found);
-        if (found) edges += __ldg(outdeg + v);
-        if (lane == 0) {
-            next[w] = m;
-            if (m) visited[w] = vis | m;
-            nf += __popc(m);
-        }
-    }
-    edges = warp_sum(edges);
-    if (lane == 0) {
-        if (nf) atomicAdd(&cnt->nf, nf);
-        if (edges) atomicAdd(&cnt->edges, edges);
-    }
-}
-
-// bitmapToArrayQueue (arrayQueue.c:310-337): frontier bitmap -> queue of its
-// vertices with out-degree > 0 (degree-0 vertices have nothing to expand)
-__global__ void bitmap_to_queue_kernel(const uint32_t *bm, uint32_t words, uint32_t V,
-                                       const uint32_t *outdeg, uint32_t *q, BfsCounters *cnt) {
-    const uint32_t lane = threadIdx.x & 31;
-    uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t w = gw; w < words; w += nw) {
-        uint32_t word = bm[w];
-        if (!word) continue;
-        uint32_t v = w * 32 + lane;
-        bool push = ((word >> lane) & 1u) && v < V && outdeg[v] > 0;
-        unsigned m = __ballot_sync(0xffffffffu, push);
-        if (!m) continue;
-        uint32_t basepos = 0;
-        if (lane == 0) basepos = atomicAdd(&cnt->qlen, (uint32_t)__popc(m));
-        basepos = __shfl_sync(0xffffffffu, basepos, 0);
-        if (push) q[basepos + __popc(m & ((1u << lane) - 1u))] = v;
-    }
-}
-
-__global__ void bfs_finish_kernel(const uint32_t *level, const int32_t *parent,
-                                  const uint32_t *outdeg, uint32_t V, uint32_t *dist,
-                                  int32_t *par_out) {
+__global__ void bfs_finish_kernel(const uint32_t *level, const int32_t *parent, const uint32_t *outdeg,
+                                  uint32_t V, uint32_t *dist, int32_t *par_out) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
         uint32_t l = level[v];
         if (dist) dist[v] = l == kInfLevel ? 0u : l;
@@ -229,9 +447,9 @@ __global__ void bfs_finish_kernel(const uint32_t *level, const int32_t *parent,
 }
 
 struct BfsWork {
-    DevBuf<uint32_t> level, visited, bm0, bm1, q0, q1, degs, pre, total;
+    DevBuf<uint32_t> level, visited, bm0, bm1, q0, q1, hv0, hv1, hc0, hc1;
     DevBuf<int32_t> parent;
-    DevBuf<BfsCounters> cnt;
+    DevBuf<BfsState> st;
     int alloc(uint32_t V, cudaStream_t s) {
         uint32_t words = (V + 31) / 32;
         GBX_TRY(level.alloc(V, s));
@@ -241,52 +459,14 @@ struct BfsWork {
         GBX_TRY(bm1.alloc(words, s));
         GBX_TRY(q0.alloc(V, s));
         GBX_TRY(q1.alloc(V, s));
-        GBX_TRY(degs.alloc(V, s));
-        GBX_TRY(pre.alloc(V, s));
-        GBX_TRY(total.alloc(1, s));
-        GBX_TRY(cnt.alloc(1, s));
+        GBX_TRY(hv0.alloc(V, s));
+        GBX_TRY(hv1.alloc(V, s));
+        GBX_TRY(hc0.alloc(V, s));
+        GBX_TRY(hc1.alloc(V, s));
+        GBX_TRY(st.alloc(1, s));
         return GBX_OK;
     }
 };
-
-static int grid_for(uint64_t n, int threads = 256, int per_sm = 8) {
-    uint64_t b = (n + threads - 1) / threads;
-    uint64_t cap = (uint64_t)num_sms() * per_sm;
-    return (int)std::max<uint64_t>(1, std::min(b, cap));
-}
-
-static int read_counters(BfsCounters *h, BfsCounters *d, cudaStream_t s) {
-    GBX_CUDA(cudaMemcpyAsync(h, d, sizeof(BfsCounters), cudaMemcpyDeviceToHost, s));
-    GBX_CUDA(cudaStreamSynchronize(s));
-    return GBX_OK;
-}
-
-// One top-down step from queue q (qlen entries). Returns counters in *h.
-static int top_down_step(gbx_graph *g, BfsWork &w, const uint32_t *q, uint32_t qlen, uint32_t *qnext,
-                         uint32_t lnext, BfsCounters *h, cudaStream_t s) {
-    GBX_CUDA(cudaMemsetAsync(w.cnt.p, 0, sizeof(BfsCounters), s));
-    if (qlen > 0) {
-        gather_degrees_kernel<<<grid_for(qlen), 256, 0, s>>>(q, qlen, g->out_degree, w.degs.p);
-        GBX_LAUNCH_CHECK();
-        GBX_TRY(exclusive_scan_u32(w.degs.p, w.pre.p, qlen, s, w.total.p));
-        bfs_top_down_kernel<<<num_sms() * 8, kTdThreads, 0, s>>>(
-            q, w.pre.p, qlen, w.total.p, g->offsets, g->dest, g->out_degree, w.visited.p,
-            w.level.p, w.parent.p, lnext, qnext, w.cnt.p);
-        GBX_LAUNCH_CHECK();
-    }
-    return read_counters(h, w.cnt.p, s);
-}
-
-static int bottom_up_step(gbx_graph *g, BfsWork &w, const uint32_t *cur, uint32_t *next,
-                          uint32_t lnext, BfsCounters *h, cudaStream_t s) {
-    uint32_t words = (g->V + 31) / 32;
-    GBX_CUDA(cudaMemsetAsync(w.cnt.p, 0, sizeof(BfsCounters), s));
-    bfs_bottom_up_kernel<<<grid_for((uint64_t)words * 32), 256, 0, s>>>(
-        g->pull_offsets(), g->pull_src(), cur, next, w.visited.p, w.level.p, w.parent.p,
-        g->out_degree, g->V, words, lnext, w.cnt.p);
-    GBX_LAUNCH_CHECK();
-    return read_counters(h, w.cnt.p, s);
-}
 
 }  // namespace gbx
 
@@ -307,86 +487,57 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
     OutArray<int32_t> par;
     GBX_TRY(dist.bind(distances, V, s));
     GBX_TRY(par.bind(parents, V, s));
-
-    bfs_init_kernel<<<grid_for(V), 256, 0, s>>>(w.level.p, w.parent.p, w.visited.p, V, words, source);
+    const unsigned grid1 = std::min<unsigned>(ceil_div(V, 256), (unsigned)num_sms() * 8);
+    bfs_init_kernel<<<grid1, 256, 0, s>>>(w.level.p, w.parent.p, w.visited.p, V, words, source);
     GBX_LAUNCH_CHECK();
-    uint32_t hdeg = 0;
-    GBX_CUDA(cudaMemcpyAsync(&hdeg, g->out_degree + source, 4, cudaMemcpyDeviceToHost, s));
-    GBX_CUDA(cudaMemcpyAsync(w.q0.p, &source, 4, cudaMemcpyHostToDevice, s));
-    GBX_CUDA(cudaStreamSynchronize(s));
-
-    gbx_bfs_result r = {};
-    r.processed_nodes = 1;
-    r.iteration = 1;
-    r.edges_traversed = hdeg;
-    uint32_t *q = w.q0.p, *qn = w.q1.p;
-    uint32_t *bcur = w.bm0.p, *bnext = w.bm1.p;
-    uint32_t qlen = hdeg ? 1u : 0u;  // queue of vertices to expand (degree > 0)
-    uint32_t qsize = 1;              // the reference's queue size (all claimed)
-    uint32_t L = 0;
-    const uint32_t alpha = 15, beta = 18;
-    uint32_t mu = g->E, mf = hdeg;
-    BfsCounters h;
-
-    auto do_bottom_up_phase = [&](uint32_t nf_start, bool until_empty) -> int {
-        level_to_bitmap_kernel<<<grid_for((uint64_t)words * 32), 256, 0, s>>>(w.level.p, V, L, bcur, words);
-        GBX_LAUNCH_CHECK();
-        uint32_t nf = nf_start, nf_prev;
-        do {
-            nf_prev = nf;
-            GBX_TRY(bottom_up_step(g, w, bcur, bnext, L + 1, &h, s));
-            nf = h.nf;
-            std::swap(bcur, bnext);
-            r.processed_nodes += nf;
-            r.iteration++;
-            r.bottom_up_steps++;
-            r.edges_traversed += h.edges;
-            if (nf) L++;
-            if (until_empty && nf == 0) break;
-        } while (until_empty ? true : (nf > nf_prev || nf > V / beta));
-        qsize = nf;
-        // bitmapToArrayQueue: the last step's new vertices become the queue
-        GBX_CUDA(cudaMemsetAsync(w.cnt.p, 0, sizeof(BfsCounters), s));
-        if (nf) {
-            bitmap_to_queue_kernel<<<grid_for((uint64_t)words * 32), 256, 0, s>>>(
-                bcur, words, V, g->out_degree, q, w.cnt.p);
-            GBX_LAUNCH_CHECK();
-        }
-        GBX_TRY(read_counters(&h, w.cnt.p, s));
-        qlen = h.qlen;
-        return GBX_OK;
-    };
-
-    if (mode == 0) {
-        // pull-only BFS (BFS.c:140-213): bottom-up steps until no vertex is added
-        GBX_TRY(do_bottom_up_phase(1, true));
-    } else {
-        while (qsize) {
-            if (mode == 2 && mf > mu / alpha) {
-                GBX_TRY(do_bottom_up_phase(qsize, false));
-                mf = 1;
-            } else {
-                mu -= mf;
-                GBX_TRY(top_down_step(g, w, q, qlen, qn, L + 1, &h, s));
-                mf = h.mf;
-                qsize = h.nf;
-                qlen = h.qlen;
-                std::swap(q, qn);
-                r.processed_nodes += qsize;
-                r.iteration++;
-                r.top_down_steps++;
-                r.edges_traversed += h.edges;
-                if (qsize) L++;
-            }
-        }
-    }
-    r.depth = L;
-    bfs_finish_kernel<<<grid_for(V), 256, 0, s>>>(w.level.p, w.parent.p, g->out_degree, V, dist.d,
-                                                  par.d);
+    GBX_CUDA(cudaMemsetAsync(w.st.p, 0, sizeof(BfsState), s));
+    bfs_seed_kernel<<<1, 1, 0, s>>>(g->out_degree, source, w.q0.p, w.hv0.p, w.hc0.p, w.st.p);
+    GBX_LAUNCH_CHECK();
+    BfsArgs a;
+    a.off = g->offsets;
+    a.dest = g->dest;
+    a.poff = g->pull_offsets();
+    a.psrc = g->pull_src();
+    a.outdeg = g->out_degree;
+    a.V = V;
+    a.words = words;
+    a.E = g->E;
+    a.mode = (uint32_t)mode;
+    a.source = source;
+    a.level = w.level.p;
+    a.parent = w.parent.p;
+    a.visited = w.visited.p;
+    a.bm[0] = w.bm0.p;
+    a.bm[1] = w.bm1.p;
+    a.q[0] = w.q0.p;
+    a.q[1] = w.q1.p;
+    a.hv[0] = w.hv0.p;
+    a.hv[1] = w.hv1.p;
+    a.hc[0] = w.hc0.p;
+    a.hc[1] = w.hc1.p;
+    a.st = w.st.p;
+    int grid = 0;
+    GBX_TRY(coop_grid(bfs_persistent_kernel, kBfsThreads, 0, &grid));
+    void *args[] = {&a};
+    GBX_CUDA(cudaLaunchCooperativeKernel((const void *)bfs_persistent_kernel, grid, kBfsThreads, args, 0, s));
+    GBX_LAUNCH_CHECK();
+    bfs_finish_kernel<<<grid1, 256, 0, s>>>(w.level.p, w.parent.p, g->out_degree, V, dist.d, par.d);
     GBX_LAUNCH_CHECK();
     GBX_TRY(dist.finish(s));
     GBX_TRY(par.finish(s));
+    BfsState hs;
+    GBX_CUDA(cudaMemcpyAsync(&hs, w.st.p, sizeof(hs), cudaMemcpyDeviceToHost, s));
     GBX_CUDA(cudaStreamSynchronize(s));
-    if (result) *result = r;
+    GBX_REQUIRE(hs.gs.error == 0, GBX_ERR_DEVICE_TIMEOUT, "BFS grid barrier wait expired");
+    GBX_REQUIRE(hs.status == 0, GBX_ERR_ITER_CAP, "BFS step cap reached");
+    if (result) {
+        result->processed_nodes = hs.processed;
+        result->iteration = hs.iteration;
+        result->depth = hs.depth;
+        result->top_down_steps = hs.td_steps;
+        result->bottom_up_steps = hs.bu_steps;
+        result->reserved = 0;
+        result->edges_traversed = hs.edges_total;
+    }
     return GBX_OK;
 }

@@ -313,6 +313,7 @@ int gbx_graph_destroy(gbx_graph *g) {
     cudaFree(g->in_src);
     cudaFree(g->in_weight);
     cudaFree(g->in_degree);
+    cudaFree(g->low_count);
     free_plan(g->plan_fwd);
     free_plan(g->plan_inv);
     cudaSetDevice(prev);

@@ -201,6 +201,10 @@ struct gbx_graph {
     gbx_gather_plan *plan_inv = nullptr;
     uint32_t max_out_degree = 0;
     uint32_t max_in_degree = 0;
+    // forward rows hold no repeated neighbour: -1 unknown, 0 no, 1 yes
+    int simple_rows = -1;
+    // per vertex: number of neighbours with id <= its own (built by TC on demand)
+    uint32_t *low_count = nullptr;
 
     bool has_inverse() const { return in_offsets != nullptr; }
     // CSR used by pull-direction kernels (reference: inverse when DIRECTED)

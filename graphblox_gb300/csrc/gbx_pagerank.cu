@@ -27,7 +27,8 @@ struct PrIterState {
 struct PrTerm {
     const uint32_t *__restrict__ src;
     const float *__restrict__ contrib;
-    __device__ __forceinline__ float operator()(uint32_t e) const { return __ldg(contrib + __ldg(src + e)); }
+    __device__ __forceinline__ uint32_t src_of(uint32_t e) const { return __ldg(src + e); }
+    __device__ __forceinline__ float value(uint32_t, uint32_t u) const { return __ldg(contrib + u); }
 };
 
 struct PrEpi {
@@ -40,6 +41,7 @@ struct PrEpi {
     double inv_n;
     double err;
     unsigned active;
+    bool reduce;  // accumulate the residual and the active count this iteration
     __device__ __forceinline__ void operator()(uint32_t v, float sum) {
         const float damp = 0.85f;
         const float base = 1.0f - 0.85f;
@@ -48,11 +50,14 @@ struct PrEpi {
         r_next[v] = next;
         uint32_t d = out_degree[v];
         contrib_next[v] = d ? __fdiv_rn(next, (float)d) : 0.0f;
-        double e = (double)fabsf(__fsub_rn(next, prev));
-        err += e * inv_n;
-        active += (e >= epsilon) ? 1u : 0u;
+        if (reduce) {
+            double e = (double)fabsf(__fsub_rn(next, prev));
+            err += e * inv_n;
+            active += (e >= epsilon) ? 1u : 0u;
+        }
     }
     __device__ __forceinline__ void block_finish() {
+        if (!reduce) return;
         __shared__ double sd[32];
         __shared__ unsigned su[32];
         double te = block_sum(err, sd);
@@ -75,7 +80,7 @@ __global__ void pr_init_kernel(float *r, float *contrib, const uint32_t *out_deg
 
 // Iteration `it`: skip when the previous iteration converged.
 template <class Term, class Epi>
-__global__ void __launch_bounds__(kGatherThreads)
+__global__ void __launch_bounds__(kGatherThreads, kGatherBlocksPerSM)
     pr_iteration_kernel(const uint32_t *__restrict__ off, uint32_t V, gbx_gather_plan plan,
                         GatherGeometry geo, Term term, Epi epi, const PrIterState *prev) {
     if (prev && prev->active == 0) return;
@@ -84,12 +89,12 @@ __global__ void __launch_bounds__(kGatherThreads)
 
 // final ranks: pick the buffer holding the last executed iteration
 __global__ void pr_finish_kernel(const float *r0, const float *r1, const PrIterState *st,
-                                 uint32_t max_it, uint32_t V, float *out, uint32_t *iters_out,
+                                 uint32_t max_it, uint32_t can_stop, uint32_t V, float *out, uint32_t *iters_out,
                                  gbx_pr_result *res_dev) {
     __shared__ uint32_t s_k;
     if (threadIdx.x == 0) {
         uint32_t k = max_it;
-        for (uint32_t i = 0; i < max_it; ++i)
+        for (uint32_t i = 0; can_stop && i < max_it; ++i)
             if (st[i].active == 0) { k = i; break; }
         s_k = k;
     }
@@ -103,7 +108,7 @@ __global__ void pr_finish_kernel(const float *r0, const float *r1, const PrIterS
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         res_dev->iterations = k;
         uint32_t last = executed ? executed - 1 : 0;
-        res_dev->active_last = executed ? st[last].active : 0;
+        res_dev->active_last = executed ? (can_stop ? st[last].active : V) : 0;
         res_dev->error_total = executed ? st[last].err : 0.0;
         if (iters_out) *iters_out = k;
     }
@@ -143,12 +148,16 @@ extern "C" int gbx_pagerank_pull(gbx_graph *g, uint32_t max_iterations, double e
     for (uint32_t it = 0; it < max_iterations; ++it) {
         int a = it & 1, b = a ^ 1;
         PrTerm term{g->pull_src(), c[a]};
-        PrEpi epi{r[a], r[b], c[b], g->out_degree, st.p + it, epsilon, inv_n, 0.0, 0u};
-        pr_iteration_kernel<PrTerm, PrEpi><<<geo.total(), kGatherThreads, 0, s>>>(
-            g->pull_offsets(), V, *plan, geo, term, epi, it ? st.p + it - 1 : nullptr);
+        // with epsilon = 0 every vertex stays active, so only the last
+        // iteration's residual (reported as error_total) is reduced
+        const bool reduce = epsilon > 0.0 || it + 1 == max_iterations;
+        PrEpi epi{r[a], r[b], c[b], g->out_degree, st.p + it, epsilon, inv_n, 0.0, 0u, reduce};
+        pr_iteration_kernel<PrTerm, PrEpi><<<gather_grid(geo), kGatherThreads, 0, s>>>(
+            g->pull_offsets(), V, *plan, geo, term, epi, (it && epsilon > 0.0) ? st.p + it - 1 : nullptr);
         GBX_LAUNCH_CHECK();
     }
-    pr_finish_kernel<<<grid, 256, 0, s>>>(r[0], r[1], st.p, max_iterations, V, out.d, nullptr, res.p);
+    pr_finish_kernel<<<grid, 256, 0, s>>>(r[0], r[1], st.p, max_iterations, epsilon > 0.0 ? 1u : 0u, V, out.d,
+                                          nullptr, res.p);
     GBX_LAUNCH_CHECK();
     GBX_TRY(out.finish(s));
     gbx_pr_result hres;

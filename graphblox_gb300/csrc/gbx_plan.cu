@@ -2,6 +2,7 @@
 // and direction with an ordered compaction (flags -> exclusive scan ->
 // scatter), so the row lists are in ascending vertex order.
 #include <algorithm>
+#include <vector>
 
 #include "gbx_gather.cuh"
 
@@ -59,6 +60,53 @@ static int build_plan(const uint32_t *off, uint32_t V, cudaStream_t s, gbx_gathe
         note_launch();
         note_launch();
         if (cudaGetLastError() != cudaSuccess) { st = GBX_ERR_CUDA; break; }
+        // heavy rows -> chunks of kHeavyChunk edges (host side: the list is short)
+        const uint32_t nh = p->n_heavy;
+        std::vector<uint32_t> hrows(nh), hoff(2 * (size_t)nh), first(nh + 1);
+        if (nh) {
+            if (cudaMemcpyAsync(hrows.data(), p->heavy_rows, (size_t)nh * 4, cudaMemcpyDeviceToHost, s) !=
+                    cudaSuccess ||
+                cudaStreamSynchronize(s) != cudaSuccess) {
+                st = GBX_ERR_CUDA;
+                break;
+            }
+            for (uint32_t i = 0; i < nh; ++i) {
+                if (cudaMemcpyAsync(&hoff[2 * i], off + hrows[i], 8, cudaMemcpyDeviceToHost, s) != cudaSuccess) {
+                    st = GBX_ERR_CUDA;
+                    break;
+                }
+            }
+            if (st != GBX_OK || cudaStreamSynchronize(s) != cudaSuccess) {
+                st = GBX_ERR_CUDA;
+                break;
+            }
+        }
+        first[0] = 0;
+        for (uint32_t i = 0; i < nh; ++i) {
+            uint32_t d = hoff[2 * i + 1] - hoff[2 * i];
+            first[i + 1] = first[i] + (d + kHeavyChunk - 1) / kHeavyChunk;
+        }
+        p->n_chunks = first[nh];
+        std::vector<uint32_t> chunk_heavy(p->n_chunks ? p->n_chunks : 1);
+        for (uint32_t i = 0; i < nh; ++i)
+            for (uint32_t c = first[i]; c < first[i + 1]; ++c) chunk_heavy[c] = i;
+        size_t nc = p->n_chunks ? p->n_chunks : 1;
+        if (cudaMalloc(&p->heavy_first, (size_t)(nh + 1) * 4) != cudaSuccess ||
+            cudaMalloc(&p->chunk_heavy, nc * 4) != cudaSuccess ||
+            cudaMalloc(&p->partials, nc * 4) != cudaSuccess ||
+            cudaMalloc(&p->tickets, (size_t)(nh ? nh : 1) * 4) != cudaSuccess) {
+            st = GBX_ERR_NOMEM;
+            break;
+        }
+        if (cudaMemcpyAsync(p->heavy_first, first.data(), (size_t)(nh + 1) * 4, cudaMemcpyHostToDevice, s) !=
+                cudaSuccess ||
+            cudaMemcpyAsync(p->chunk_heavy, chunk_heavy.data(), nc * 4, cudaMemcpyHostToDevice, s) !=
+                cudaSuccess ||
+            cudaMemsetAsync(p->tickets, 0, (size_t)(nh ? nh : 1) * 4, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            st = GBX_ERR_CUDA;
+            break;
+        }
     } while (0);
     if (st != GBX_OK) {
         (void)cudaGetLastError();
@@ -81,6 +129,10 @@ void free_plan(gbx_gather_plan *p) {
     if (!p) return;
     cudaFree(p->medium_rows);
     cudaFree(p->heavy_rows);
+    cudaFree(p->heavy_first);
+    cudaFree(p->chunk_heavy);
+    cudaFree(p->partials);
+    cudaFree(p->tickets);
     delete p;
 }
 

@@ -1,34 +1,56 @@
 // Single-source shortest paths (the reference's SSSPDataDrivenPushGraphCSR,
-// SSSP.c:514-653, with its relaxation SSSPAtomicRelax, :180-254).
+// SSSP.c:514-653, with its relaxation SSSPAtomicRelax, :180-254), as one
+// persistent cooperative kernel.
 //
 // Near/far delta-stepping: vertices whose tentative distance is below the
-// current threshold form the "near" queue and are relaxed round after round
-// (edge-balanced expansion, atomicMin on dist[]); improvements at or above
-// the threshold go to the "far" pile (each vertex at most once, flagged).
-// When near drains, the threshold jumps past the smallest far distance
-// (empty buckets cost nothing, unlike the reference's full-V bucket scans),
-// and far entries that fall below it move to near. A vertex is re-expanded
-// only if its distance changed since it was last expanded, so the result is
-// the unique fixed point dist[u] = min over (v->u) of (uint32)((float)dist[v] + w),
-// identical to the reference's distances.
+// current threshold form the "near" list and are relaxed round after round
+// (atomicMin on dist[]); improvements at or above the threshold go to the
+// "far" pile (each vertex at most once, flagged). When near drains, the
+// threshold jumps one delta past the smallest pending far distance (empty
+// buckets cost nothing, unlike the reference's full-V bucket sweeps), and far
+// entries below it move to near. Each round first snapshots the distance of
+// every near vertex (settled[v]); edges are relaxed from that snapshot, and a
+// far entry whose distance still equals its snapshot is dropped as already
+// expanded. The result is the unique fixed point
+//   dist[u] = min over (v->u) of (uint32)((float)dist[v] + w),
+// i.e. the reference's distances. Work units and hub splitting are those of
+// the persistent BFS (gbx_bfs.cu): 32 near vertices flattened per warp, or
+// kHubChunk edges of one high-degree vertex.
 #include <algorithm>
 
-#include "gbx_frontier.cuh"
+#include "gbx_coop.cuh"
 
 namespace gbx {
 
-__global__ void gather_queue_degrees_kernel(const uint32_t *q, uint32_t qlen, const uint32_t *deg,
-                                            uint32_t *out) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < qlen; i += gridDim.x * blockDim.x)
-        out[i] = deg[q[i]];
-}
+constexpr uint32_t kSsspHubDeg = 1024;
+constexpr uint32_t kSsspHubChunk = 1024;
+constexpr int kSsspThreads = 256;
+constexpr int kSsspWarps = kSsspThreads / 32;
 
-struct SsspCounters {
-    uint32_t near_len;
-    uint32_t far_len;
-    uint32_t far_min;
-    uint32_t pad;
+struct SsspRound {
+    unsigned cursor;
+    unsigned near_len;          // next near queue (degree in (0, hub])
+    unsigned far_len;           // far pile length (carried across rounds)
+    unsigned far_min;
+    unsigned long long near_hub;  // next near hubs: (count << 32) | chunks
     unsigned long long relaxed;
+};
+
+struct SsspState {
+    GridSync gs;
+    SsspRound r[3];
+    unsigned rounds, status;
+    unsigned long long relaxed;
+};
+
+struct SsspArgs {
+    const uint32_t *off, *dest, *outdeg;
+    const float *w;
+    uint32_t V, delta, source;
+    uint32_t *dist, *settled, *stamp, *in_far;
+    uint32_t *q[2], *hv[2], *hc[2];
+    uint32_t *far[2];
+    SsspState *st;
 };
 
 __device__ __forceinline__ uint32_t sssp_add(uint32_t d, float w) {
@@ -36,101 +58,294 @@ __device__ __forceinline__ uint32_t sssp_add(uint32_t d, float w) {
     return __float2uint_rz(__fadd_rn(__uint2float_rn(d), w));
 }
 
-struct RelaxVisitor {
-    uint32_t *dist;
-    const uint32_t *settled;  // distance each queued vertex was expanded with
-    const float *w;
-    uint32_t threshold;
-    uint32_t round;
-    uint32_t *stamp;
-    uint32_t *in_far;
-    uint32_t *near_next;
-    uint32_t *far;
-    SsspCounters *cnt;
-    unsigned long long relaxed;
-    __device__ __forceinline__ void operator()(uint32_t v, uint32_t e, uint32_t u, bool active) {
+__device__ __forceinline__ uint32_t sssp_chunks(uint32_t d) { return (d + kSsspHubChunk - 1) / kSsspHubChunk; }
+
+// push u into the next near generation (deduplicated per round by stamp)
+__device__ __forceinline__ void near_push(const SsspArgs &a, SsspRound *cnt, uint32_t *qout, uint32_t *hvout,
+                                          uint32_t *hcout, uint32_t u, bool want) {
+    bool push = false;
+    if (want) {
+        const uint32_t du = __ldg(a.outdeg + u);
+        if (du > kSsspHubDeg) {
+            unsigned long long old = atomicAdd(&cnt->near_hub, (1ull << 32) | sssp_chunks(du));
+            uint32_t slot = (uint32_t)(old >> 32);
+            hvout[slot] = u;
+            hcout[slot] = (uint32_t)old;
+        } else {
+            push = du > 0;
+        }
+    }
+    const uint32_t lane = threadIdx.x & 31;
+    const unsigned m = __ballot_sync(0xffffffffu, push);
+    if (m) {
+        uint32_t leader = __ffs(m) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&cnt->near_len, (unsigned)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (push) qout[base + __popc(m & ((1u << lane) - 1u))] = u;
+    }
+}
+
+__device__ __forceinline__ void far_push(const SsspArgs &a, SsspRound *cnt, uint32_t *far, uint32_t u, bool push) {
+    const uint32_t lane = threadIdx.x & 31;
+    const unsigned m = __ballot_sync(0xffffffffu, push);
+    if (m) {
+        uint32_t leader = __ffs(m) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&cnt->far_len, (unsigned)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (push) far[base + __popc(m & ((1u << lane) - 1u))] = u;
+    }
+}
+
+struct Relaxer {
+    const SsspArgs &a;
+    uint32_t threshold, round;
+    SsspRound *cnt;
+    uint32_t *qout, *hvout, *hcout, *far;
+    unsigned long long relaxed = 0;
+    __device__ __forceinline__ Relaxer(const SsspArgs &a_, uint32_t t, uint32_t r, SsspRound *c, uint32_t *q,
+                                       uint32_t *hv, uint32_t *hc, uint32_t *f)
+        : a(a_), threshold(t), round(r), cnt(c), qout(q), hvout(hv), hcout(hc), far(f) {}
+    __device__ __forceinline__ void operator()(uint32_t d, uint32_t e, uint32_t u, bool active) {
         bool to_near = false, to_far = false;
         if (active) {
-            uint32_t d = __ldg(settled + v);
-            float wt = w ? __ldg(w + e) : 1.0f;
-            uint32_t nd = sssp_add(d, wt);
+            const float wt = a.w ? __ldg(a.w + e) : 1.0f;
+            const uint32_t nd = sssp_add(d, wt);
             relaxed++;
-            if (nd < __ldcg(dist + u)) {
-                uint32_t old = atomicMin(dist + u, nd);
+            if (nd < __ldcg(a.dist + u)) {
+                const uint32_t old = atomicMin(a.dist + u, nd);
                 if (nd < old) {
-                    if (nd < threshold) to_near = atomicExch(stamp + u, round) != round;
-                    else to_far = atomicExch(in_far + u, 1u) == 0u;
+                    if (nd < threshold) to_near = atomicExch(a.stamp + u, round) != round;
+                    else to_far = atomicExch(a.in_far + u, 1u) == 0u;
                 }
             }
         }
-        warp_append(near_next, &cnt->near_len, u, to_near);
-        warp_append(far, &cnt->far_len, u, to_far);
+        near_push(a, cnt, qout, hvout, hcout, u, to_near);
+        far_push(a, cnt, far, u, to_far);
     }
-    __device__ __forceinline__ void finish() {
+    __device__ __forceinline__ void flush() {
         unsigned long long r = warp_sum(relaxed);
         if ((threadIdx.x & 31) == 0 && r) atomicAdd(&cnt->relaxed, r);
     }
 };
 
-// degrees of the near queue + snapshot of the distances used to expand it
-__global__ void sssp_prepare_kernel(const uint32_t *q, uint32_t qlen, const uint32_t *deg,
-                                    const uint32_t *dist, uint32_t *settled, uint32_t *degs) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < qlen; i += gridDim.x * blockDim.x) {
-        uint32_t v = q[i];
-        degs[i] = deg[v];
-        settled[v] = dist[v];
+__device__ __forceinline__ uint32_t sssp_hub_of_chunk(const uint32_t *hc, uint32_t n, uint32_t c) {
+    uint32_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi + 1) >> 1;
+        if (__ldcg(hc + mid) <= c) lo = mid; else hi = mid - 1;
     }
+    return lo;
 }
 
-__global__ void far_min_kernel(const uint32_t *far, uint32_t n, const uint32_t *dist,
-                               const uint32_t *settled, SsspCounters *cnt) {
-    uint32_t m = 0xFFFFFFFFu;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t u = far[i];
-        uint32_t d = dist[u];
-        if (settled[u] != d) m = min(m, d);
+__device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn, const uint32_t *hvin,
+                            const uint32_t *hcin, uint32_t nh, uint32_t nc, Relaxer &rx, SsspRound *cur,
+                            uint32_t *s_pre, uint32_t *s_base, uint32_t *s_d) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t units = nc + (qn + 31) / 32;
+    for (;;) {
+        uint32_t unit = 0;
+        if (lane == 0) unit = atomicAdd(&cur->cursor, 1u);
+        unit = __shfl_sync(0xffffffffu, unit, 0);
+        if (unit >= units) break;
+        if (unit < nc) {
+            const uint32_t h = sssp_hub_of_chunk(hcin, nh, unit);
+            const uint32_t v = __ldcg(hvin + h);
+            const uint32_t d = __ldcg(a.settled + v);
+            const uint32_t rb = __ldg(a.off + v), re = __ldg(a.off + v + 1);
+            const uint32_t cb = rb + (unit - __ldcg(hcin + h)) * kSsspHubChunk;
+            const uint32_t ce = min(cb + kSsspHubChunk, re);
+            for (uint32_t j0 = cb; j0 < ce; j0 += 128) {
+                uint32_t u[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    uint32_t j = j0 + q * 32 + lane;
+                    u[q] = j < ce ? __ldg(a.dest + j) : 0u;
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) rx(d, j0 + q * 32 + lane, u[q], j0 + q * 32 + lane < ce);
+            }
+        } else {
+            const uint32_t qi = (unit - nc) * 32 + lane;
+            uint32_t b = 0, deg = 0, d = 0;
+            if (qi < qn) {
+                const uint32_t v = __ldcg(qin + qi);
+                b = __ldg(a.off + v);
+                deg = __ldg(a.off + v + 1) - b;
+                d = __ldcg(a.settled + v);
+            }
+            uint32_t incl = deg;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= (uint32_t)o) incl += t;
+            }
+            s_pre[lane] = incl - deg;
+            s_base[lane] = b;
+            s_d[lane] = d;
+            if (lane == 31) s_pre[32] = incl;
+            __syncwarp();
+            const uint32_t tot = s_pre[32];
+            uint32_t k = 0;
+            for (uint32_t i0 = 0; i0 < tot; i0 += 128) {
+                uint32_t u[4], e[4], dd[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    uint32_t i = i0 + q * 32 + lane;
+                    u[q] = 0;
+                    e[q] = 0;
+                    dd[q] = 0;
+                    if (i < tot) {
+                        while (s_pre[k + 1] <= i) ++k;
+                        e[q] = s_base[k] + (i - s_pre[k]);
+                        dd[q] = s_d[k];
+                        u[q] = __ldg(a.dest + e[q]);
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) rx(dd[q], e[q], u[q], i0 + q * 32 + lane < tot);
+            }
+            __syncwarp();
+        }
     }
-    m = __reduce_min_sync(0xffffffffu, m);
-    if ((threadIdx.x & 31) == 0 && m != 0xFFFFFFFFu) atomicMin(&cnt->far_min, m);
+    rx.flush();
 }
 
-__global__ void far_split_kernel(const uint32_t *far, uint32_t n, const uint32_t *dist,
-                                 const uint32_t *settled, uint32_t threshold, uint32_t round,
-                                 uint32_t *stamp, uint32_t *in_far, uint32_t *near, uint32_t *far2,
-                                 SsspCounters *cnt) {
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        uint32_t i = base + threadIdx.x;
-        bool to_near = false, keep = false;
-        uint32_t u = 0;
-        if (i < n) {
-            u = far[i];
-            uint32_t d = dist[u];
-            if (settled[u] == d) {
-                in_far[u] = 0;  // already expanded at this distance
-            } else if (d < threshold) {
-                in_far[u] = 0;
-                to_near = atomicExch(stamp + u, round) != round;
-            } else {
-                keep = true;
+__device__ __forceinline__ void zero_round(SsspRound *r, uint32_t far_len) {
+    r->cursor = 0;
+    r->near_len = 0;
+    r->far_len = far_len;
+    r->far_min = 0xFFFFFFFFu;
+    r->near_hub = 0;
+    r->relaxed = 0;
+}
+
+__global__ void __launch_bounds__(kSsspThreads) sssp_persistent_kernel(SsspArgs a) {
+    __shared__ uint32_t s_pre[kSsspWarps][33];
+    __shared__ uint32_t s_base[kSsspWarps][32];
+    __shared__ uint32_t s_d[kSsspWarps][32];
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nthreads = gridDim.x * blockDim.x;
+    SsspState *st = a.st;
+    uint32_t qn = 1, nh = 0, nc = 0, far_len = 0;
+    {
+        const uint32_t d0 = __ldg(a.outdeg + a.source);
+        if (d0 > kSsspHubDeg) { qn = 0; nh = 1; nc = sssp_chunks(d0); }
+        else if (d0 == 0) { qn = 0; }
+    }
+    uint64_t threshold = a.delta;
+    uint32_t round = 1, rounds = 0, fb = 0, gen = 0;
+    unsigned long long relaxed = 0;
+    bool failed = false;
+    const uint32_t max_rounds = 4 * a.V + 64;
+    for (uint32_t s = 0;; ++s) {
+        SsspRound *cur = &st->r[s % 3];
+        if (blockIdx.x == 0 && threadIdx.x == 0) zero_round(&st->r[(s + 1) % 3], 0);
+        if (qn + nh > 0) {
+            if (rounds >= max_rounds) { failed = true; break; }
+            // snapshot the distances this round relaxes from
+            const uint32_t ib = gen & 1;
+            for (uint32_t i = gtid; i < qn; i += nthreads) {
+                uint32_t v = __ldcg(a.q[ib] + i);
+                a.settled[v] = __ldcg(a.dist + v);
+            }
+            for (uint32_t i = gtid; i < nh; i += nthreads) {
+                uint32_t v = __ldcg(a.hv[ib] + i);
+                a.settled[v] = __ldcg(a.dist + v);
+            }
+            if (blockIdx.x == 0 && threadIdx.x == 0) cur->far_len = far_len;
+            if (!grid_barrier(&st->gs)) { failed = true; break; }
+            round++;
+            const uint32_t thr = threshold > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)threshold;
+            Relaxer rx(a, thr, round, cur, a.q[ib ^ 1], a.hv[ib ^ 1], a.hc[ib ^ 1], a.far[fb]);
+            relax_phase(a, a.q[ib], qn, a.hv[ib], a.hc[ib], nh, nc, rx, cur, s_pre[wid], s_base[wid], s_d[wid]);
+            if (!grid_barrier(&st->gs)) { failed = true; break; }
+            relaxed += __ldcg(&cur->relaxed);
+            qn = __ldcg(&cur->near_len);
+            unsigned long long hb = __ldcg(&cur->near_hub);
+            nh = (uint32_t)(hb >> 32);
+            nc = (uint32_t)hb;
+            far_len = __ldcg(&cur->far_len);
+            gen++;
+            rounds++;
+            continue;
+        }
+        if (far_len == 0) break;
+        // smallest far distance not yet expanded -> next threshold
+        {
+            uint32_t m = 0xFFFFFFFFu;
+            for (uint32_t i = gtid; i < far_len; i += nthreads) {
+                uint32_t u = __ldcg(a.far[fb] + i);
+                uint32_t d = __ldcg(a.dist + u);
+                if (__ldcg(a.settled + u) != d) m = min(m, d);
+            }
+            m = __reduce_min_sync(0xffffffffu, m);
+            if (lane == 0 && m != 0xFFFFFFFFu) atomicMin(&cur->far_min, m);
+        }
+        if (!grid_barrier(&st->gs)) { failed = true; break; }
+        const uint32_t fmin = __ldcg(&cur->far_min);
+        if (fmin == 0xFFFFFFFFu) break;  // every far entry is already expanded
+        threshold = ((uint64_t)fmin / a.delta + 1) * a.delta;
+        round++;
+        {
+            // split the far pile: below the threshold -> near, the rest stays
+            const uint32_t ib = gen & 1;
+            const uint32_t thr = threshold > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)threshold;
+            for (uint32_t base = blockIdx.x * blockDim.x; base < far_len; base += nthreads) {
+                const uint32_t i = base + threadIdx.x;
+                bool to_near = false, keep = false;
+                uint32_t u = 0;
+                if (i < far_len) {
+                    u = __ldcg(a.far[fb] + i);
+                    const uint32_t d = __ldcg(a.dist + u);
+                    if (__ldcg(a.settled + u) == d) {
+                        a.in_far[u] = 0;
+                    } else if (d < thr) {
+                        a.in_far[u] = 0;
+                        to_near = atomicExch(a.stamp + u, round) != round;
+                    } else {
+                        keep = true;
+                    }
+                }
+                near_push(a, cur, a.q[ib], a.hv[ib], a.hc[ib], u, to_near);
+                far_push(a, cur, a.far[fb ^ 1], u, keep);
             }
         }
-        warp_append(near, &cnt->near_len, u, to_near);
-        warp_append(far2, &cnt->far_len, u, keep);
+        if (!grid_barrier(&st->gs)) { failed = true; break; }
+        qn = __ldcg(&cur->near_len);
+        unsigned long long hb = __ldcg(&cur->near_hub);
+        nh = (uint32_t)(hb >> 32);
+        nc = (uint32_t)hb;
+        far_len = __ldcg(&cur->far_len);
+        fb ^= 1;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->rounds = rounds;
+        st->relaxed = relaxed;
+        st->status = failed ? 1u : 0u;
     }
 }
 
 __global__ void sssp_init_kernel(uint32_t *dist, uint32_t *settled, uint32_t *stamp, uint32_t *in_far,
-                                 uint32_t V, uint32_t source) {
+                                 uint32_t V, uint32_t source, const uint32_t *outdeg, uint32_t *q0,
+                                 uint32_t *hv0, uint32_t *hc0) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
         dist[v] = v == source ? 0u : kSsspInf;
         settled[v] = 0xFFFFFFFFu;
         stamp[v] = v == source ? 1u : 0u;
         in_far[v] = 0;
     }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        q0[0] = source;
+        hv0[0] = source;
+        hc0[0] = 0;
+    }
 }
 
-__global__ void sssp_finish_kernel(const uint32_t *dist, const uint32_t *outdeg, uint32_t V,
-                                   uint32_t *out, unsigned long long *stats /* reached, edges */) {
+__global__ void sssp_finish_kernel(const uint32_t *dist, const uint32_t *outdeg, uint32_t V, uint32_t *out,
+                                   unsigned long long *stats /* reached, edges */) {
     uint32_t reached = 0;
     unsigned long long edges = 0;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
@@ -162,94 +377,61 @@ extern "C" int gbx_sssp(gbx_graph *g, uint32_t source, uint32_t delta, uint32_t 
     cudaStream_t s = (cudaStream_t)stream;
     const uint32_t V = g->V;
     if (delta == 0) delta = g->weight ? 256u : 1u;
-    DevBuf<uint32_t> dist, settled, stamp, in_far, qa, qb, fa, fb, degs, pre, total;
-    DevBuf<SsspCounters> cnt;
+    DevBuf<uint32_t> dist, settled, stamp, in_far, q0, q1, hv0, hv1, hc0, hc1, f0, f1;
+    DevBuf<SsspState> st;
     DevBuf<unsigned long long> fin;
-    GBX_TRY(dist.alloc(V, s));
-    GBX_TRY(settled.alloc(V, s));
-    GBX_TRY(stamp.alloc(V, s));
-    GBX_TRY(in_far.alloc(V, s));
-    GBX_TRY(qa.alloc(V, s));
-    GBX_TRY(qb.alloc(V, s));
-    GBX_TRY(fa.alloc(V, s));
-    GBX_TRY(fb.alloc(V, s));
-    GBX_TRY(degs.alloc(V, s));
-    GBX_TRY(pre.alloc(V, s));
-    GBX_TRY(total.alloc(1, s));
-    GBX_TRY(cnt.alloc(1, s));
+    for (DevBuf<uint32_t> *b : {&dist, &settled, &stamp, &in_far, &q0, &q1, &hv0, &hv1, &hc0, &hc1, &f0, &f1})
+        GBX_TRY(b->alloc(V, s));
+    GBX_TRY(st.alloc(1, s));
     GBX_TRY(fin.alloc(2, s));
     OutArray<uint32_t> out;
     GBX_TRY(out.bind(distances, V, s));
-    const unsigned grid = std::min<unsigned>(ceil_div(V, 256), (unsigned)num_sms() * 8);
-    sssp_init_kernel<<<grid, 256, 0, s>>>(dist.p, settled.p, stamp.p, in_far.p, V, source);
+    const unsigned grid1 = std::min<unsigned>(ceil_div(V, 256), (unsigned)num_sms() * 8);
+    sssp_init_kernel<<<grid1, 256, 0, s>>>(dist.p, settled.p, stamp.p, in_far.p, V, source, g->out_degree,
+                                           q0.p, hv0.p, hc0.p);
     GBX_LAUNCH_CHECK();
-    GBX_CUDA(cudaMemcpyAsync(qa.p, &source, 4, cudaMemcpyHostToDevice, s));
-    uint32_t *nearq = qa.p, *nextq = qb.p, *farq = fa.p, *far2 = fb.p;
-    uint32_t near_len = 1, far_len = 0, round = 1, rounds = 0;
-    uint64_t threshold = delta;
-    unsigned long long relaxed = 0;
-    SsspCounters h;
-    const uint32_t max_rounds = 4u * V + 64u;  // hard cap: every round settles >= 1 vertex
-    for (;;) {
-        while (near_len > 0) {
-            GBX_REQUIRE(rounds < max_rounds, GBX_ERR_ITER_CAP, "SSSP round cap reached");
-            GBX_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(SsspCounters), s));
-            GBX_CUDA(cudaMemcpyAsync(&cnt.p->far_len, &far_len, 4, cudaMemcpyHostToDevice, s));
-            unsigned pg = std::min<unsigned>(ceil_div(near_len, 256), (unsigned)num_sms() * 8);
-            sssp_prepare_kernel<<<pg, 256, 0, s>>>(nearq, near_len, g->out_degree, dist.p, settled.p, degs.p);
-            GBX_LAUNCH_CHECK();
-            GBX_TRY(exclusive_scan_u32(degs.p, pre.p, near_len, s, total.p));
-            round++;
-            uint32_t thr = threshold > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)threshold;
-            RelaxVisitor vis{dist.p, settled.p, g->weight, thr, round, stamp.p, in_far.p,
-                             nextq, farq, cnt.p, 0ull};
-            expand_kernel<RelaxVisitor><<<num_sms() * 8, kExpThreads, 0, s>>>(
-                nearq, pre.p, near_len, total.p, g->offsets, g->dest, vis);
-            GBX_LAUNCH_CHECK();
-            GBX_CUDA(cudaMemcpyAsync(&h, cnt.p, sizeof(h), cudaMemcpyDeviceToHost, s));
-            GBX_CUDA(cudaStreamSynchronize(s));
-            relaxed += h.relaxed;
-            near_len = h.near_len;
-            far_len = h.far_len;
-            std::swap(nearq, nextq);
-            rounds++;
-        }
-        if (far_len == 0) break;
-        // next threshold: one delta past the smallest pending far distance
-        GBX_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(SsspCounters), s));
-        uint32_t big = 0xFFFFFFFFu;
-        GBX_CUDA(cudaMemcpyAsync(&cnt.p->far_min, &big, 4, cudaMemcpyHostToDevice, s));
-        unsigned fg = std::min<unsigned>(ceil_div(far_len, 256), (unsigned)num_sms() * 8);
-        far_min_kernel<<<fg, 256, 0, s>>>(farq, far_len, dist.p, settled.p, cnt.p);
-        GBX_LAUNCH_CHECK();
-        GBX_CUDA(cudaMemcpyAsync(&h, cnt.p, sizeof(h), cudaMemcpyDeviceToHost, s));
-        GBX_CUDA(cudaStreamSynchronize(s));
-        if (h.far_min == 0xFFFFFFFFu) break;  // every far entry is already expanded
-        threshold = ((uint64_t)h.far_min / delta + 1) * delta;
-        round++;
-        GBX_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(SsspCounters), s));
-        uint32_t thr = threshold > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)threshold;
-        far_split_kernel<<<fg, 256, 0, s>>>(farq, far_len, dist.p, settled.p, thr, round, stamp.p,
-                                            in_far.p, nearq, far2, cnt.p);
-        GBX_LAUNCH_CHECK();
-        GBX_CUDA(cudaMemcpyAsync(&h, cnt.p, sizeof(h), cudaMemcpyDeviceToHost, s));
-        GBX_CUDA(cudaStreamSynchronize(s));
-        near_len = h.near_len;
-        far_len = h.far_len;
-        std::swap(farq, far2);
-        // the near queue was filled under `round`; expansion rounds continue from there
-    }
+    GBX_CUDA(cudaMemsetAsync(st.p, 0, sizeof(SsspState), s));
+    SsspArgs a;
+    a.off = g->offsets;
+    a.dest = g->dest;
+    a.outdeg = g->out_degree;
+    a.w = g->weight;
+    a.V = V;
+    a.delta = delta;
+    a.source = source;
+    a.dist = dist.p;
+    a.settled = settled.p;
+    a.stamp = stamp.p;
+    a.in_far = in_far.p;
+    a.q[0] = q0.p;
+    a.q[1] = q1.p;
+    a.hv[0] = hv0.p;
+    a.hv[1] = hv1.p;
+    a.hc[0] = hc0.p;
+    a.hc[1] = hc1.p;
+    a.far[0] = f0.p;
+    a.far[1] = f1.p;
+    a.st = st.p;
+    int grid = 0;
+    GBX_TRY(coop_grid(sssp_persistent_kernel, kSsspThreads, 0, &grid));
+    void *args[] = {&a};
+    GBX_CUDA(cudaLaunchCooperativeKernel((const void *)sssp_persistent_kernel, grid, kSsspThreads, args, 0, s));
+    GBX_LAUNCH_CHECK();
     GBX_CUDA(cudaMemsetAsync(fin.p, 0, 16, s));
-    sssp_finish_kernel<<<grid, 256, 0, s>>>(dist.p, g->out_degree, V, out.d, fin.p);
+    sssp_finish_kernel<<<grid1, 256, 0, s>>>(dist.p, g->out_degree, V, out.d, fin.p);
     GBX_LAUNCH_CHECK();
     GBX_TRY(out.finish(s));
+    SsspState hs;
     unsigned long long hf[2];
+    GBX_CUDA(cudaMemcpyAsync(&hs, st.p, sizeof(hs), cudaMemcpyDeviceToHost, s));
     GBX_CUDA(cudaMemcpyAsync(hf, fin.p, 16, cudaMemcpyDeviceToHost, s));
     GBX_CUDA(cudaStreamSynchronize(s));
+    GBX_REQUIRE(hs.gs.error == 0, GBX_ERR_DEVICE_TIMEOUT, "SSSP grid barrier wait expired");
+    GBX_REQUIRE(hs.status == 0, GBX_ERR_ITER_CAP, "SSSP round cap reached");
     if (result) {
         result->reached = (uint32_t)hf[0];
-        result->rounds = rounds;
-        result->edges_relaxed = relaxed;
+        result->rounds = hs.rounds;
+        result->edges_relaxed = hs.relaxed;
         result->edges_traversed = hf[1];
     }
     return GBX_OK;

@@ -185,6 +185,26 @@ def rel_l1(a, ref) -> float:
     return float(np.abs(a - ref).sum() / den) if den else float(np.abs(a - ref).sum())
 
 
+FLT_MIN = float(np.finfo(np.float32).tiny)
+FLT_SUBNORMAL_ULP = float(np.finfo(np.float32).smallest_subnormal)
+
+
+def fp32_close(a, ref64, tol=1e-6, subnormal_ulps=64):
+    """Relative-L1 check of an FP32 result against an FP64 reference.
+
+    The relative bar applies to entries whose reference magnitude is in the
+    normal FP32 range; subnormal entries carry only a few significant bits in
+    FP32, so there each |a - ref| must stay within `subnormal_ulps` subnormal
+    steps. Returns (ok, rel_l1_normal, worst_subnormal_ulps)."""
+    a = np.asarray(a, np.float64)
+    ref64 = np.asarray(ref64, np.float64)
+    normal = np.abs(ref64) >= FLT_MIN
+    err = rel_l1(a[normal], ref64[normal]) if normal.any() else 0.0
+    sub = ~normal
+    worst = float((np.abs(a[sub] - ref64[sub]) / FLT_SUBNORMAL_ULP).max()) if sub.any() else 0.0
+    return (err <= tol and worst <= subnormal_ulps), err, worst
+
+
 # ---- the reference host itself (only where its sources were compiled) -----
 
 def ref_available(variant="dw") -> bool:

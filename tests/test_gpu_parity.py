@@ -93,8 +93,8 @@ def test_algorithms_golden(gbx, cuda_device, name, variant, symmetric, dedup):
                 np.testing.assert_array_equal(st.distances, dist)
         pr = gbx.page_rank(dg, 20, 0.0)
         ref64, _, _ = po.pagerank(host, 20, 0.0, pull, fp64=True)
-        assert po.rel_l1(pr.pageRanks, ref64) <= REL_L1_TOL
-        assert po.rel_l1(pr.pageRanks, fx[f"{variant}_pr20"]) <= REL_L1_TOL
+        assert po.fp32_close(pr.pageRanks, ref64, REL_L1_TOL)[0]
+        assert po.fp32_close(pr.pageRanks, fx[f"{variant}_pr20"], REL_L1_TOL)[0]
         assert pr.iterations == 20
         st = gbx.sssp(dg, int(fx[f"{variant}_sssp_source"]), delta=1, map_source=False)
         np.testing.assert_array_equal(st.distances, fx[f"{variant}_sssp"])
@@ -106,8 +106,8 @@ def test_algorithms_golden(gbx, cuda_device, name, variant, symmetric, dedup):
         x = fx[f"{variant}_spmv_x"]
         y = gbx.spmv(dg, x, iterations=2)
         y64 = po.spmv(host, x, None if variant == "u" else pull.weight, 0.0001, 2, pull=pull, fp64=True)
-        assert po.rel_l1(y, y64) <= REL_L1_TOL
-        assert po.rel_l1(y, fx[f"{variant}_spmv_y"]) <= REL_L1_TOL
+        assert po.fp32_close(y, y64, REL_L1_TOL)[0]
+        assert po.fp32_close(y, fx[f"{variant}_spmv_y"], REL_L1_TOL)[0]
         if variant == "u":
             assert gbx.triangle_count(dg) == int(fx["u_tc"])
 
@@ -154,12 +154,12 @@ def test_rmat_directed(gbx, cuda_device, scale, ef, seed):
             np.testing.assert_array_equal(st.distances, po.sssp(host, r, 64))
         pr = gbx.page_rank(dg, 20, 0.0)
         ref64, _, _ = po.pagerank(host, 20, 0.0, pull, fp64=True)
-        assert po.rel_l1(pr.pageRanks, ref64) <= REL_L1_TOL
+        assert po.fp32_close(pr.pageRanks, ref64, REL_L1_TOL)[0]
         x = gbx.generate_values(g.num_vertices, 2, seed=5)
         vals = gbx.generate_values(g.num_edges, 1, seed=6)
         y = gbx.spmv(dg, x, values=vals)
         y64 = po.spmv(host, x, vals, pull=pull, fp64=True)
-        assert po.rel_l1(y, y64) <= REL_L1_TOL
+        assert po.fp32_close(y, y64, REL_L1_TOL)[0]
 
 
 @pytest.mark.parametrize("scale,ef,seed", [(14, 8, 3), (16, 16, 4)])
@@ -240,4 +240,4 @@ def test_device_resident_outputs(gbx, cuda_device):
         ranks = torch.empty(g.num_vertices, dtype=torch.float32, device=cuda_device)
         gbx.page_rank(dg, 20, 0.0, ranks=ranks)
         ref64, _, _ = po.pagerank(host, 20, 0.0, pull, fp64=True)
-        assert po.rel_l1(ranks.cpu().numpy(), ref64) <= REL_L1_TOL
+        assert po.fp32_close(ranks.cpu().numpy(), ref64, REL_L1_TOL)[0]
