@@ -47,6 +47,7 @@ SIGNATURES = {
                                           C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]),
     "gbx_bfs": (C.c_int, [vp, u32, C.c_int, vp, vp, C.POINTER(BfsResult), vp]),
     "gbx_pagerank_pull": (C.c_int, [vp, u32, C.c_double, vp, C.POINTER(PrResult), vp]),
+    "gbx_pagerank_pull_noalloc": (C.c_int, [u32, vp, vp, vp, u32, C.c_double, vp, C.POINTER(PrResult), vp]),
     "gbx_sssp": (C.c_int, [vp, u32, u32, vp, C.POINTER(SsspResult), vp]),
     "gbx_cc": (C.c_int, [vp, C.c_int, vp, C.POINTER(u32), vp]),
     "gbx_tc": (C.c_int, [vp, C.POINTER(u64), vp]),
