@@ -45,6 +45,9 @@ SIGNATURES = {
     "gbx_graph_info": (C.c_int, [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "gbx_graph_device_arrays": (C.c_int, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp),
                                           C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]),
+    "gbx_graph_set_tuning": (C.c_int, [vp, C.c_char_p, C.c_double]),
+    "gbx_graph_get_tuning": (C.c_int, [vp, C.c_char_p, C.POINTER(C.c_double)]),
+    "gbx_autotune": (C.c_int, [vp, u32, u32, vp]),
     "gbx_bfs": (C.c_int, [vp, u32, C.c_int, vp, vp, C.POINTER(BfsResult), vp]),
     "gbx_pagerank_pull": (C.c_int, [vp, u32, C.c_double, vp, C.POINTER(PrResult), vp]),
     "gbx_pagerank_pull_noalloc": (C.c_int, [u32, vp, vp, vp, u32, C.c_double, vp, C.POINTER(PrResult), vp]),

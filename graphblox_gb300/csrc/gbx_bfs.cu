@@ -35,7 +35,7 @@
 namespace gbx {
 
 constexpr uint32_t kHubDeg = 1024;    // out-degree above which a vertex is a hub
-constexpr uint32_t kHubChunk = 1024;  // edges per hub work unit
+constexpr uint32_t kHubChunk = 256;   // edges per hub work unit
 constexpr int kBfsThreads = 256;
 constexpr int kBfsWarps = kBfsThreads / 32;
 
@@ -48,17 +48,43 @@ struct BfsStep {
     unsigned long long edges; // sum of out_degree over claimed
 };
 
+// Step trace (printed when GBX_TRACE is set): kind, frontier size, time.
+constexpr unsigned kTraceMax = 96;
+enum : unsigned { kTrStart = 0, kTrTopDown = 1, kTrBottomUp = 2, kTrToBitmap = 3, kTrToLists = 4 };
+struct TraceRec {
+    unsigned kind, value;
+    unsigned long long ns;
+};
+
 struct BfsState {
     GridSync gs;
     BfsStep step[3];
     BfsStep conv;  // lists rebuilt from a bitmap when leaving bottom-up
     unsigned processed, iteration, td_steps, bu_steps, depth, status;
     unsigned long long edges_total;
+    unsigned ntrace, pad2;
+    TraceRec trace[kTraceMax];
 };
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void trace_step(BfsState *st, unsigned kind, unsigned value) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && st->ntrace < kTraceMax) {
+        TraceRec &r = st->trace[st->ntrace++];
+        r.kind = kind;
+        r.value = value;
+        r.ns = global_ns();
+    }
+}
 
 struct BfsArgs {
     const uint32_t *off, *dest, *poff, *psrc, *outdeg;
     uint32_t V, words, E, mode, source;
+    uint32_t alpha, beta;  // direction switch: bottom-up when mf > mu/alpha, stay while nf > V/beta
     uint32_t *level;
     int32_t *parent;
     uint32_t *visited;
@@ -77,45 +103,54 @@ struct Claimer {
     uint32_t lnext;
     uint32_t *qout, *hvout, *hcout;
     BfsStep *cnt;
+    WarpQueue wq;
     unsigned nf = 0, mf = 0;
     unsigned long long edges = 0;
     __device__ __forceinline__ Claimer(const BfsArgs &a_, uint32_t l, uint32_t *q, uint32_t *hv, uint32_t *hc,
-                                       BfsStep *c)
-        : a(a_), lnext(l), qout(q), hvout(hv), hcout(hc), cnt(c) {}
-    __device__ __forceinline__ void operator()(uint32_t v, uint32_t u, bool active) {
-        bool push = false;
-        uint32_t du = 0;
-        if (active) {
-            const uint32_t bit = 1u << (u & 31);
-            uint32_t *word = a.visited + (u >> 5);
-            if (!(__ldcg(word) & bit) && !(atomicOr(word, bit) & bit)) {
-                a.level[u] = lnext;
-                a.parent[u] = (int32_t)v;
-                du = __ldg(a.outdeg + u);
-                nf += 1;
-                mf += du ? du : 1u;
-                edges += du;
-                if (du > kHubDeg) {
-                    unsigned long long old = atomicAdd(&cnt->hub, (1ull << 32) | hub_chunks(du));
-                    uint32_t slot = (uint32_t)(old >> 32);
-                    hvout[slot] = u;
-                    hcout[slot] = (uint32_t)old;
-                } else {
-                    push = du > 0;
-                }
+                                       BfsStep *c, uint32_t *wbuf)
+        : a(a_), lnext(l), qout(q), hvout(hv), hcout(hc), cnt(c), wq(wbuf) {}
+    // Four candidate edges per lane: the visited-word loads, then the
+    // atomicOr claims, are issued back to back so their latencies overlap.
+    __device__ __forceinline__ void claim4(const uint32_t (&v)[4], const uint32_t (&u)[4], const bool (&act)[4]) {
+        uint32_t pre[4], old[4], du[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) pre[q] = act[q] ? __ldcg(a.visited + (u[q] >> 5)) : 0xFFFFFFFFu;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t bit = 1u << (u[q] & 31);
+            old[q] = (act[q] && !(pre[q] & bit)) ? atomicOr(a.visited + (u[q] >> 5), bit) : 0xFFFFFFFFu;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const bool won = !(old[q] & (1u << (u[q] & 31)));
+            du[q] = won ? __ldg(a.outdeg + u[q]) : 0u;
+            if (won) {
+                a.level[u[q]] = lnext;
+                a.parent[u[q]] = (int32_t)v[q];
             }
         }
-        const uint32_t lane = threadIdx.x & 31;
-        unsigned m = __ballot_sync(0xffffffffu, push);
-        if (m) {
-            uint32_t leader = __ffs(m) - 1;
-            uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(&cnt->qlen, (unsigned)__popc(m));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (push) qout[base + __popc(m & ((1u << lane) - 1u))] = u;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const bool won = !(old[q] & (1u << (u[q] & 31)));
+            bool push = false;
+            if (won) {
+                nf += 1;
+                mf += du[q] ? du[q] : 1u;
+                edges += du[q];
+                if (du[q] > kHubDeg) {
+                    unsigned long long h = atomicAdd(&cnt->hub, (1ull << 32) | hub_chunks(du[q]));
+                    uint32_t slot = (uint32_t)(h >> 32);
+                    hvout[slot] = u[q];
+                    hcout[slot] = (uint32_t)h;
+                } else {
+                    push = du[q] > 0;
+                }
+            }
+            wq.push(u[q], push, qout, &cnt->qlen);
         }
     }
     __device__ __forceinline__ void flush() {
+        wq.flush(qout, &cnt->qlen);
         unsigned n = warp_sum(nf), f = warp_sum(mf);
         unsigned long long e = warp_sum(edges);
         if ((threadIdx.x & 31) == 0 && n) {
@@ -139,14 +174,13 @@ __device__ __forceinline__ uint32_t hub_of_chunk(const uint32_t *hc, uint32_t n,
 __device__ void top_down_phase(const BfsArgs &a, const uint32_t *qin, uint32_t qn, const uint32_t *hvin,
                                const uint32_t *hcin, uint32_t nh, uint32_t nc, BfsStep *cur, uint32_t *qout,
                                uint32_t *hvout, uint32_t *hcout, uint32_t lnext, uint32_t *s_pre,
-                               uint32_t *s_base, uint32_t *s_v) {
+                               uint32_t *s_base, uint32_t *s_v, uint32_t *s_wq) {
     const uint32_t lane = threadIdx.x & 31;
-    Claimer claim(a, lnext, qout, hvout, hcout, cur);
+    Claimer claim(a, lnext, qout, hvout, hcout, cur, s_wq);
     const uint32_t units = nc + (qn + 31) / 32;
+    UnitDealer dealer(&cur->cursor);
     for (;;) {
-        uint32_t unit = 0;
-        if (lane == 0) unit = atomicAdd(&cur->cursor, 1u);
-        unit = __shfl_sync(0xffffffffu, unit, 0);
+        const uint32_t unit = dealer.take(units);
         if (unit >= units) break;
         if (unit < nc) {
             // kHubChunk edges of one hub
@@ -162,8 +196,9 @@ __device__ void top_down_phase(const BfsArgs &a, const uint32_t *qin, uint32_t q
                     uint32_t j = j0 + q * 32 + lane;
                     u[q] = j < ce ? __ldg(a.dest + j) : 0u;
                 }
-#pragma unroll
-                for (int q = 0; q < 4; ++q) claim(v, u[q], j0 + q * 32 + lane < ce);
+                const uint32_t vv[4] = {v, v, v, v};
+                const bool act[4] = {j0 + lane < ce, j0 + 32 + lane < ce, j0 + 64 + lane < ce, j0 + 96 + lane < ce};
+                claim.claim4(vv, u, act);
             }
         } else {
             // 32 queued vertices, edges flattened over the warp
@@ -200,8 +235,8 @@ __device__ void top_down_phase(const BfsArgs &a, const uint32_t *qin, uint32_t q
                         u[q] = __ldg(a.dest + s_base[k] + (i - s_pre[k]));
                     }
                 }
-#pragma unroll
-                for (int q = 0; q < 4; ++q) claim(src[q], u[q], i0 + q * 32 + lane < tot);
+                const bool act[4] = {i0 + lane < tot, i0 + 32 + lane < tot, i0 + 64 + lane < tot, i0 + 96 + lane < tot};
+                claim.claim4(src, u, act);
             }
             __syncwarp();
         }
@@ -212,11 +247,13 @@ __device__ void top_down_phase(const BfsArgs &a, const uint32_t *qin, uint32_t q
 __device__ void bottom_up_phase(const BfsArgs &a, const uint32_t *cur_bm, uint32_t *next_bm, uint32_t lnext,
                                 BfsStep *cnt) {
     const uint32_t lane = threadIdx.x & 31;
-    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     unsigned nf = 0;
     unsigned long long edges = 0;
-    for (uint32_t w = gw; w < a.words; w += nw) {
+    constexpr uint32_t kWordsPerUnit = 8;
+    const uint32_t units = (a.words + kWordsPerUnit - 1) / kWordsPerUnit;
+    UnitDealer dealer(&cnt->cursor);
+    for (uint32_t unit = dealer.take(units); unit < units; unit = dealer.take(units))
+    for (uint32_t w = unit * kWordsPerUnit; w < min(a.words, (unit + 1) * kWordsPerUnit); ++w) {
         const uint32_t vis = __ldcg(a.visited + w);
         if (vis == 0xFFFFFFFFu) {
             if (lane == 0) next_bm[w] = 0;
@@ -226,13 +263,21 @@ __device__ void bottom_up_phase(const BfsArgs &a, const uint32_t *cur_bm, uint32
         bool found = false;
         if (v < a.V && !((vis >> lane) & 1u)) {
             const uint32_t b = __ldg(a.poff + v), e = __ldg(a.poff + v + 1);
-            for (uint32_t j = b; j < e; ++j) {
-                const uint32_t u = __ldg(a.psrc + j);
-                if ((__ldcg(cur_bm + (u >> 5)) >> (u & 31)) & 1u) {
-                    a.level[v] = lnext;
-                    a.parent[v] = (int32_t)u;
-                    found = true;
-                    break;
+            // four neighbours per round: their ids, then their frontier words,
+            // are loaded back to back; the first one in the frontier wins
+            for (uint32_t j = b; j < e && !found; j += 4) {
+                uint32_t u[4], fw[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) u[q] = (j + q < e) ? __ldg(a.psrc + j + q) : 0u;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) fw[q] = (j + q < e) ? __ldcg(cur_bm + (u[q] >> 5)) : 0u;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (!found && ((fw[q] >> (u[q] & 31)) & 1u)) {
+                        a.level[v] = lnext;
+                        a.parent[v] = (int32_t)u[q];
+                        found = true;
+                    }
                 }
             }
         }
@@ -264,8 +309,9 @@ __device__ void level_to_bitmap_phase(const BfsArgs &a, uint32_t l, uint32_t *bm
 
 // bitmapToArrayQueue (arrayQueue.c:310-337): a frontier bitmap -> queue + hubs
 __device__ void bitmap_to_lists_phase(const BfsArgs &a, const uint32_t *bm, uint32_t *qout, uint32_t *hvout,
-                                      uint32_t *hcout, BfsStep *cnt) {
+                                      uint32_t *hcout, BfsStep *cnt, uint32_t *s_wq) {
     const uint32_t lane = threadIdx.x & 31;
+    WarpQueue wq(s_wq);
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t w = gw; w < a.words; w += nw) {
@@ -284,14 +330,9 @@ __device__ void bitmap_to_lists_phase(const BfsArgs &a, const uint32_t *bm, uint
                 push = d > 0;
             }
         }
-        const unsigned m = __ballot_sync(0xffffffffu, push);
-        if (m) {
-            uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(&cnt->qlen, (unsigned)__popc(m));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (push) qout[base + __popc(m & ((1u << lane) - 1u))] = v;
-        }
+        wq.push(v, push, qout, &cnt->qlen);
     }
+    wq.flush(qout, &cnt->qlen);
 }
 
 __device__ __forceinline__ void zero_step(BfsStep *s) {
@@ -307,9 +348,10 @@ __global__ void __launch_bounds__(kBfsThreads) bfs_persistent_kernel(BfsArgs a) 
     __shared__ uint32_t s_pre[kBfsWarps][33];
     __shared__ uint32_t s_base[kBfsWarps][32];
     __shared__ uint32_t s_v[kBfsWarps][32];
+    __shared__ uint32_t s_wq[kBfsWarps][kWarpQueueCap];
     const uint32_t wid = threadIdx.x >> 5;
     BfsState *st = a.st;
-    const uint32_t alpha = 15, beta = 18;
+    const uint32_t alpha = a.alpha, beta = a.beta;
     // DO bookkeeping, evaluated identically by every CTA
     uint32_t mu = a.E, mf = __ldg(a.outdeg + a.source), qsize = 1, nf_prev = 0, L = 0;
     uint32_t processed = 1, iteration = 1, td = 0, bu = 0;
@@ -320,6 +362,7 @@ __global__ void __launch_bounds__(kBfsThreads) bfs_persistent_kernel(BfsArgs a) 
     uint32_t qn = __ldcg(&st->conv.qlen);
     unsigned long long hub0 = __ldcg(&st->conv.hub);
     uint32_t nh = (uint32_t)(hub0 >> 32), nc = (uint32_t)hub0;
+    trace_step(st, kTrStart, 1);
     for (uint32_t s = 0; !done; ++s) {
         if (s >= max_steps) {
             failed = true;
@@ -343,12 +386,14 @@ __global__ void __launch_bounds__(kBfsThreads) bfs_persistent_kernel(BfsArgs a) 
                 // arrayQueueToBitmap: frontier bitmap of the current level
                 level_to_bitmap_phase(a, L, a.bm[ib]);
                 if (!grid_barrier(&st->gs)) { failed = true; break; }
+                trace_step(st, kTrToBitmap, qsize);
                 nf_prev = qsize;
                 in_bu = true;
             }
             bottom_up_phase(a, a.bm[ib], a.bm[ob], L + 1, cur);
             if (!grid_barrier(&st->gs)) { failed = true; break; }
             const uint32_t nf = __ldcg(&cur->nf);
+            trace_step(st, kTrBottomUp, nf);
             processed += nf;
             iteration++;
             bu++;
@@ -365,9 +410,10 @@ __global__ void __launch_bounds__(kBfsThreads) bfs_persistent_kernel(BfsArgs a) 
                     // bitmapToArrayQueue into the list generation step s+1 reads
                     if (blockIdx.x == 0 && threadIdx.x == 0) zero_step(&st->conv);
                     if (!grid_barrier(&st->gs)) { failed = true; break; }
-                    bitmap_to_lists_phase(a, a.bm[ob], a.q[ob], a.hv[ob], a.hc[ob], &st->conv);
+                    bitmap_to_lists_phase(a, a.bm[ob], a.q[ob], a.hv[ob], a.hc[ob], &st->conv, s_wq[wid]);
                     if (!grid_barrier(&st->gs)) { failed = true; break; }
                     qn = __ldcg(&st->conv.qlen);
+                    trace_step(st, kTrToLists, qn);
                     unsigned long long hb = __ldcg(&st->conv.hub);
                     nh = (uint32_t)(hb >> 32);
                     nc = (uint32_t)hb;
@@ -378,9 +424,10 @@ __global__ void __launch_bounds__(kBfsThreads) bfs_persistent_kernel(BfsArgs a) 
         } else {
             mu -= mf;
             top_down_phase(a, a.q[ib], qn, a.hv[ib], a.hc[ib], nh, nc, cur, a.q[ob], a.hv[ob], a.hc[ob], L + 1,
-                           s_pre[wid], s_base[wid], s_v[wid]);
+                           s_pre[wid], s_base[wid], s_v[wid], s_wq[wid]);
             if (!grid_barrier(&st->gs)) { failed = true; break; }
             const uint32_t nf = __ldcg(&cur->nf);
+            trace_step(st, kTrTopDown, nf);
             mf = __ldcg(&cur->mf);
             qsize = nf;
             processed += nf;
@@ -504,6 +551,8 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
     a.E = g->E;
     a.mode = (uint32_t)mode;
     a.source = source;
+    a.alpha = g->bfs_alpha;
+    a.beta = g->bfs_beta;
     a.level = w.level.p;
     a.parent = w.parent.p;
     a.visited = w.visited.p;
@@ -530,6 +579,13 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
     GBX_CUDA(cudaStreamSynchronize(s));
     GBX_REQUIRE(hs.gs.error == 0, GBX_ERR_DEVICE_TIMEOUT, "BFS grid barrier wait expired");
     GBX_REQUIRE(hs.status == 0, GBX_ERR_ITER_CAP, "BFS step cap reached");
+    if (trace_enabled()) {
+        static const char *names[] = {"start", "TD", "BU", "->bitmap", "->lists"};
+        fprintf(stderr, "| gbx_bfs source %u: %-9s | %-10s | %-10s |\n", source, "step", "vertices", "us");
+        for (unsigned i = 1; i < hs.ntrace && i < kTraceMax; ++i)
+            fprintf(stderr, "| %-23s | %-10u | %-10.2f |\n", names[hs.trace[i].kind % 5], hs.trace[i].value,
+                    (hs.trace[i].ns - hs.trace[i - 1].ns) * 1e-3);
+    }
     if (result) {
         result->processed_nodes = hs.processed;
         result->iteration = hs.iteration;

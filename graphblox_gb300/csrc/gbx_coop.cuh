@@ -61,6 +61,59 @@ __device__ __forceinline__ bool grid_barrier(GridSync *gs) {
     return s_ok != 0;
 }
 
+// Per-warp staging of queue appends in shared memory: lanes append with
+// ballot ranks into the warp's buffer, and the warp reserves space in the
+// global queue with one atomic per kWarpQueueCap/2..kWarpQueueCap entries
+// instead of one per ballot round (a single global length counter is
+// otherwise hammered by every warp of the grid).
+constexpr uint32_t kWarpQueueCap = 128;
+
+struct WarpQueue {
+    uint32_t *buf;  // kWarpQueueCap entries of shared memory owned by this warp
+    uint32_t n;     // fill, identical in all lanes
+    __device__ __forceinline__ explicit WarpQueue(uint32_t *b) : buf(b), n(0) {}
+    __device__ __forceinline__ void flush(uint32_t *queue, unsigned *len) {
+        if (n == 0) return;
+        __syncwarp();
+        const uint32_t lane = threadIdx.x & 31;
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(len, n);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        for (uint32_t i = lane; i < n; i += 32) queue[base + i] = buf[i];
+        __syncwarp();
+        n = 0;
+    }
+    // all lanes call together
+    __device__ __forceinline__ void push(uint32_t x, bool p, uint32_t *queue, unsigned *len) {
+        const unsigned m = __ballot_sync(0xffffffffu, p);
+        if (!m) return;
+        const uint32_t lane = threadIdx.x & 31;
+        if (p) buf[n + __popc(m & ((1u << lane) - 1u))] = x;
+        n += __popc(m);
+        if (n > kWarpQueueCap - 32) flush(queue, len);
+    }
+};
+
+// Work-unit dealer: a warp's first unit is its global warp index (no atomic),
+// later ones come from the cursor, offset by the number of warps, so steps
+// with little work cost no atomics at all.
+struct UnitDealer {
+    unsigned *cursor;
+    uint32_t next;
+    uint32_t nwarps;
+    __device__ __forceinline__ UnitDealer(unsigned *c)
+        : cursor(c), next((blockIdx.x * blockDim.x + threadIdx.x) >> 5), nwarps((gridDim.x * blockDim.x) >> 5) {}
+    __device__ __forceinline__ uint32_t take(uint32_t units) {
+        const uint32_t u = next;
+        if (u < units) {
+            uint32_t t = 0;
+            if ((threadIdx.x & 31) == 0) t = atomicAdd(cursor, 1u);
+            next = nwarps + __shfl_sync(0xffffffffu, t, 0);
+        }
+        return u;
+    }
+};
+
 // Largest co-resident grid for `kernel` with `threads` per CTA.
 template <class K>
 inline int coop_grid(K kernel, int threads, size_t smem, int *grid) {

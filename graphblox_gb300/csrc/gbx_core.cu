@@ -16,6 +16,14 @@ static std::atomic<unsigned long long> g_launches{0};
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+bool trace_enabled() {
+    static const bool on = [] {
+        const char *e = getenv("GBX_TRACE");
+        return e && *e && strcmp(e, "0") != 0;
+    }();
+    return on;
+}
+
 void set_error(const char *fmt, ...) {
     va_list ap;
     va_start(ap, fmt);
@@ -314,6 +322,7 @@ int gbx_graph_destroy(gbx_graph *g) {
     cudaFree(g->in_weight);
     cudaFree(g->in_degree);
     cudaFree(g->low_count);
+    gbx_free_tc_plan(g->tc_plan);
     free_plan(g->plan_fwd);
     free_plan(g->plan_inv);
     cudaSetDevice(prev);

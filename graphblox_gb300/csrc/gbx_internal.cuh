@@ -46,6 +46,10 @@ void note_launch();
         }                                                                     \
     } while (0)
 
+// per-step tables on stderr when the environment sets GBX_TRACE (the GPU
+// counterpart of the reference's per-iteration printf tables)
+bool trace_enabled();
+
 // ---- device ----------------------------------------------------------------
 // Make sure a device is usable; caches per-device properties.
 int ensure_device();
@@ -205,6 +209,14 @@ struct gbx_graph {
     int simple_rows = -1;
     // per vertex: number of neighbours with id <= its own (built by TC on demand)
     uint32_t *low_count = nullptr;
+    // every edge has its reverse: -1 unknown, 0 no, 1 yes
+    int symmetric = -1;
+    // tuning (gbx_graph_set_tuning / gbx_autotune): BFS direction switch and
+    // SSSP bucket width (0 = default for the graph's weights)
+    uint32_t bfs_alpha = 15, bfs_beta = 18;
+    uint32_t sssp_delta = 0;
+    // triangle-count work decomposition (gbx_tc.cu)
+    struct gbx_tc_plan *tc_plan = nullptr;
 
     bool has_inverse() const { return in_offsets != nullptr; }
     // CSR used by pull-direction kernels (reference: inverse when DIRECTED)
@@ -213,6 +225,8 @@ struct gbx_graph {
     const float *pull_weight() const { return in_offsets ? in_weight : weight; }
     const uint32_t *pull_degree() const { return in_offsets ? in_degree : out_degree; }
 };
+
+void gbx_free_tc_plan(struct gbx_tc_plan *p);
 
 namespace gbx {
 // plan for the pull CSR of g (built on first use, cached on the graph)

@@ -103,10 +103,11 @@ struct Relaxer {
     uint32_t threshold, round;
     SsspRound *cnt;
     uint32_t *qout, *hvout, *hcout, *far;
+    WarpQueue wnear, wfar;
     unsigned long long relaxed = 0;
     __device__ __forceinline__ Relaxer(const SsspArgs &a_, uint32_t t, uint32_t r, SsspRound *c, uint32_t *q,
-                                       uint32_t *hv, uint32_t *hc, uint32_t *f)
-        : a(a_), threshold(t), round(r), cnt(c), qout(q), hvout(hv), hcout(hc), far(f) {}
+                                       uint32_t *hv, uint32_t *hc, uint32_t *f, uint32_t *bn, uint32_t *bf)
+        : a(a_), threshold(t), round(r), cnt(c), qout(q), hvout(hv), hcout(hc), far(f), wnear(bn), wfar(bf) {}
     __device__ __forceinline__ void operator()(uint32_t d, uint32_t e, uint32_t u, bool active) {
         bool to_near = false, to_far = false;
         if (active) {
@@ -121,10 +122,66 @@ struct Relaxer {
                 }
             }
         }
-        near_push(a, cnt, qout, hvout, hcout, u, to_near);
-        far_push(a, cnt, far, u, to_far);
+        // hubs go straight to the hub list; the rest through the warp buffers
+        bool hub = false;
+        if (to_near) {
+            const uint32_t du = __ldg(a.outdeg + u);
+            if (du > kSsspHubDeg) {
+                hub = true;
+                unsigned long long old = atomicAdd(&cnt->near_hub, (1ull << 32) | sssp_chunks(du));
+                uint32_t slot = (uint32_t)(old >> 32);
+                hvout[slot] = u;
+                hcout[slot] = (uint32_t)old;
+            } else if (du == 0) {
+                hub = true;  // nothing to relax from u
+            }
+        }
+        wnear.push(u, to_near && !hub, qout, &cnt->near_len);
+        wfar.push(u, to_far, far, &cnt->far_len);
+    }
+    // Four relaxations per lane with their loads and atomics issued back to
+    // back (independent), then the queue pushes.
+    __device__ __forceinline__ void relax4(const uint32_t (&d)[4], const uint32_t (&e)[4], const uint32_t (&u)[4],
+                                           const bool (&act)[4]) {
+        uint32_t nd[4], cur[4], old[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float wt = (act[q] && a.w) ? __ldg(a.w + e[q]) : 1.0f;
+            nd[q] = sssp_add(d[q], wt);
+            cur[q] = act[q] ? __ldcg(a.dist + u[q]) : 0u;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) old[q] = (act[q] && nd[q] < cur[q]) ? atomicMin(a.dist + u[q], nd[q]) : 0u;
+        bool to_near[4], to_far[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            relaxed += act[q] ? 1u : 0u;
+            const bool imp = act[q] && nd[q] < cur[q] && nd[q] < old[q];
+            to_near[q] = imp && nd[q] < threshold && atomicExch(a.stamp + u[q], round) != round;
+            to_far[q] = imp && nd[q] >= threshold && atomicExch(a.in_far + u[q], 1u) == 0u;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            bool hub = false;
+            if (to_near[q]) {
+                const uint32_t du = __ldg(a.outdeg + u[q]);
+                if (du > kSsspHubDeg) {
+                    hub = true;
+                    unsigned long long h = atomicAdd(&cnt->near_hub, (1ull << 32) | sssp_chunks(du));
+                    uint32_t slot = (uint32_t)(h >> 32);
+                    hvout[slot] = u[q];
+                    hcout[slot] = (uint32_t)h;
+                } else if (du == 0) {
+                    hub = true;
+                }
+            }
+            wnear.push(u[q], to_near[q] && !hub, qout, &cnt->near_len);
+            wfar.push(u[q], to_far[q], far, &cnt->far_len);
+        }
     }
     __device__ __forceinline__ void flush() {
+        wnear.flush(qout, &cnt->near_len);
+        wfar.flush(far, &cnt->far_len);
         unsigned long long r = warp_sum(relaxed);
         if ((threadIdx.x & 31) == 0 && r) atomicAdd(&cnt->relaxed, r);
     }
@@ -144,10 +201,9 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
                             uint32_t *s_pre, uint32_t *s_base, uint32_t *s_d) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t units = nc + (qn + 31) / 32;
+    UnitDealer dealer(&cur->cursor);
     for (;;) {
-        uint32_t unit = 0;
-        if (lane == 0) unit = atomicAdd(&cur->cursor, 1u);
-        unit = __shfl_sync(0xffffffffu, unit, 0);
+        const uint32_t unit = dealer.take(units);
         if (unit >= units) break;
         if (unit < nc) {
             const uint32_t h = sssp_hub_of_chunk(hcin, nh, unit);
@@ -164,7 +220,10 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
                     u[q] = j < ce ? __ldg(a.dest + j) : 0u;
                 }
 #pragma unroll
-                for (int q = 0; q < 4; ++q) rx(d, j0 + q * 32 + lane, u[q], j0 + q * 32 + lane < ce);
+                const uint32_t dq[4] = {d, d, d, d};
+                const uint32_t eq[4] = {j0 + lane, j0 + 32 + lane, j0 + 64 + lane, j0 + 96 + lane};
+                const bool act[4] = {eq[0] < ce, eq[1] < ce, eq[2] < ce, eq[3] < ce};
+                rx.relax4(dq, eq, u, act);
             }
         } else {
             const uint32_t qi = (unit - nc) * 32 + lane;
@@ -204,7 +263,8 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
                     }
                 }
 #pragma unroll
-                for (int q = 0; q < 4; ++q) rx(dd[q], e[q], u[q], i0 + q * 32 + lane < tot);
+                const bool act[4] = {i0 + lane < tot, i0 + 32 + lane < tot, i0 + 64 + lane < tot, i0 + 96 + lane < tot};
+                rx.relax4(dd, e, u, act);
             }
             __syncwarp();
         }
@@ -225,6 +285,8 @@ __global__ void __launch_bounds__(kSsspThreads) sssp_persistent_kernel(SsspArgs 
     __shared__ uint32_t s_pre[kSsspWarps][33];
     __shared__ uint32_t s_base[kSsspWarps][32];
     __shared__ uint32_t s_d[kSsspWarps][32];
+    __shared__ uint32_t s_wn[kSsspWarps][kWarpQueueCap];
+    __shared__ uint32_t s_wf[kSsspWarps][kWarpQueueCap];
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t nthreads = gridDim.x * blockDim.x;
@@ -259,7 +321,7 @@ __global__ void __launch_bounds__(kSsspThreads) sssp_persistent_kernel(SsspArgs 
             if (!grid_barrier(&st->gs)) { failed = true; break; }
             round++;
             const uint32_t thr = threshold > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)threshold;
-            Relaxer rx(a, thr, round, cur, a.q[ib ^ 1], a.hv[ib ^ 1], a.hc[ib ^ 1], a.far[fb]);
+            Relaxer rx(a, thr, round, cur, a.q[ib ^ 1], a.hv[ib ^ 1], a.hc[ib ^ 1], a.far[fb], s_wn[wid], s_wf[wid]);
             relax_phase(a, a.q[ib], qn, a.hv[ib], a.hc[ib], nh, nc, rx, cur, s_pre[wid], s_base[wid], s_d[wid]);
             if (!grid_barrier(&st->gs)) { failed = true; break; }
             relaxed += __ldcg(&cur->relaxed);
@@ -376,7 +438,7 @@ extern "C" int gbx_sssp(gbx_graph *g, uint32_t source, uint32_t delta, uint32_t 
     GBX_TRY(ensure_device());
     cudaStream_t s = (cudaStream_t)stream;
     const uint32_t V = g->V;
-    if (delta == 0) delta = g->weight ? 256u : 1u;
+    if (delta == 0) delta = g->sssp_delta ? g->sssp_delta : (g->weight ? 256u : 1u);
     DevBuf<uint32_t> dist, settled, stamp, in_far, q0, q1, hv0, hv1, hc0, hc1, f0, f1;
     DevBuf<SsspState> st;
     DevBuf<unsigned long long> fin;

@@ -1,0 +1,138 @@
+// Per-graph tuning knobs and the autotuner that sets them.
+//
+// Knobs (stored on the gbx_graph):
+//   bfs_alpha   switch top-down -> bottom-up when the frontier's edges exceed
+//               unexplored edges / alpha (the reference fixes 15, BFS.c:374)
+//   bfs_beta    stay bottom-up while the frontier exceeds V / beta (18)
+//   sssp_delta  bucket width of the near/far schedule
+// None of them changes a result: BFS levels, processed_nodes and iteration
+// (= depth + 2, one step per level) and SSSP distances are the same for every
+// setting; only the time differs. gbx_autotune times candidates on sample
+// sources of the graph itself with CUDA events and keeps the fastest.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "gbx_internal.cuh"
+
+using namespace gbx;
+
+extern "C" int gbx_graph_set_tuning(gbx_graph *g, const char *key, double value) {
+    clear_error();
+    GBX_REQUIRE(g && key, GBX_ERR_INVALID, "graph or key is NULL");
+    GBX_REQUIRE(value >= 0.0 && value < 4294967296.0, GBX_ERR_INVALID, "value out of range");
+    const uint32_t v = (uint32_t)value;
+    if (!strcmp(key, "bfs_alpha")) {
+        GBX_REQUIRE(v >= 1, GBX_ERR_INVALID, "bfs_alpha must be >= 1");
+        g->bfs_alpha = v;
+    } else if (!strcmp(key, "bfs_beta")) {
+        GBX_REQUIRE(v >= 1, GBX_ERR_INVALID, "bfs_beta must be >= 1");
+        g->bfs_beta = v;
+    } else if (!strcmp(key, "sssp_delta")) {
+        g->sssp_delta = v;
+    } else {
+        GBX_REQUIRE(false, GBX_ERR_INVALID, "unknown tuning key '%s'", key);
+    }
+    return GBX_OK;
+}
+
+extern "C" int gbx_graph_get_tuning(const gbx_graph *g, const char *key, double *value) {
+    clear_error();
+    GBX_REQUIRE(g && key && value, GBX_ERR_INVALID, "NULL argument");
+    if (!strcmp(key, "bfs_alpha")) *value = g->bfs_alpha;
+    else if (!strcmp(key, "bfs_beta")) *value = g->bfs_beta;
+    else if (!strcmp(key, "sssp_delta")) *value = g->sssp_delta;
+    else GBX_REQUIRE(false, GBX_ERR_INVALID, "unknown tuning key '%s'", key);
+    return GBX_OK;
+}
+
+namespace {
+
+// sample sources: vertices with out-degree > 0 picked by a fixed hash
+int sample_sources(gbx_graph *g, uint32_t n, cudaStream_t s, std::vector<uint32_t> *out) {
+    std::vector<uint32_t> deg(g->V);
+    GBX_CUDA(cudaMemcpyAsync(deg.data(), g->out_degree, (size_t)g->V * 4, cudaMemcpyDeviceToHost, s));
+    GBX_CUDA(cudaStreamSynchronize(s));
+    uint64_t x = 0x9E3779B97F4A7C15ull;
+    for (uint32_t tries = 0; out->size() < n && tries < 64 * n + 1024; ++tries) {
+        x ^= x >> 12;
+        x ^= x << 25;
+        x ^= x >> 27;
+        uint32_t v = (uint32_t)((x * 2685821657736338717ull) >> 32) % g->V;
+        if (deg[v] > 0) out->push_back(v);
+    }
+    if (out->empty()) out->push_back(0);
+    return GBX_OK;
+}
+
+template <class F>
+int time_ms(F f, cudaStream_t s, float *ms) {
+    cudaEvent_t a, b;
+    GBX_CUDA(cudaEventCreate(&a));
+    GBX_CUDA(cudaEventCreate(&b));
+    GBX_CUDA(cudaEventRecord(a, s));
+    int st = f();
+    GBX_CUDA(cudaEventRecord(b, s));
+    GBX_CUDA(cudaEventSynchronize(b));
+    GBX_CUDA(cudaEventElapsedTime(ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return st;
+}
+
+}  // namespace
+
+extern "C" int gbx_autotune(gbx_graph *g, uint32_t flags, uint32_t num_samples, void *stream) {
+    clear_error();
+    GBX_REQUIRE(g, GBX_ERR_INVALID, "graph is NULL");
+    GBX_TRY(ensure_device());
+    cudaStream_t s = (cudaStream_t)stream;
+    if (num_samples == 0) num_samples = 4;
+    std::vector<uint32_t> src;
+    GBX_TRY(sample_sources(g, num_samples, s, &src));
+    DevBuf<uint32_t> out;
+    GBX_TRY(out.alloc(g->V, s));
+    if (flags & 1u) {
+        const uint32_t cands[] = {4, 15, 64, 256, 1024, 4096};
+        float best = 1e30f;
+        uint32_t best_a = g->bfs_alpha;
+        for (uint32_t c : cands) {
+            g->bfs_alpha = c;
+            GBX_TRY(gbx_bfs(g, src[0], 2, out.p, nullptr, nullptr, stream));  // warm
+            float ms = 0.f;
+            GBX_TRY(time_ms([&]() {
+                for (uint32_t v : src) GBX_TRY(gbx_bfs(g, v, 2, out.p, nullptr, nullptr, stream));
+                return GBX_OK;
+            }, s, &ms));
+            if (trace_enabled()) fprintf(stderr, "| autotune bfs_alpha %-4u | %9.3f ms |\n", c, ms);
+            if (ms < best) {
+                best = ms;
+                best_a = c;
+            }
+        }
+        g->bfs_alpha = best_a;
+    }
+    if (flags & 2u) {
+        const uint32_t cands_w[] = {128, 512, 1024, 2048, 4096, 16384};
+        const uint32_t cands_u[] = {1, 2, 4};
+        const uint32_t *cands = g->weight ? cands_w : cands_u;
+        const int nc = g->weight ? 6 : 3;
+        float best = 1e30f;
+        uint32_t best_d = g->sssp_delta;
+        const uint32_t n = std::min<uint32_t>(2, (uint32_t)src.size());
+        for (int i = 0; i < nc; ++i) {
+            float ms = 0.f;
+            GBX_TRY(time_ms([&]() {
+                for (uint32_t k = 0; k < n; ++k) GBX_TRY(gbx_sssp(g, src[k], cands[i], out.p, nullptr, stream));
+                return GBX_OK;
+            }, s, &ms));
+            if (trace_enabled()) fprintf(stderr, "| autotune sssp_delta %-4u | %9.3f ms |\n", cands[i], ms);
+            if (ms < best) {
+                best = ms;
+                best_d = cands[i];
+            }
+        }
+        g->sssp_delta = best_d;
+    }
+    return GBX_OK;
+}

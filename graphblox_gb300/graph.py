@@ -228,6 +228,19 @@ class DeviceGraph:
     def handle(self):
         return self._h
 
+    def set_tuning(self, key: str, value: float) -> None:
+        call("gbx_graph_set_tuning", self._h, key.encode(), float(value))
+
+    def get_tuning(self, key: str) -> float:
+        v = C.c_double()
+        call("gbx_graph_get_tuning", self._h, key.encode(), C.byref(v))
+        return v.value
+
+    def autotune(self, bfs: bool = True, sssp: bool = True, samples: int = 4, stream=None) -> dict:
+        """gbx_autotune: time candidate knob settings on this graph, keep the fastest."""
+        call("gbx_autotune", self._h, (1 if bfs else 0) | (2 if sssp else 0), int(samples), stream)
+        return {k: self.get_tuning(k) for k in ("bfs_alpha", "bfs_beta", "sssp_delta")}
+
     def close(self) -> None:
         if self._h and self._h.value:
             _lib.load().gbx_graph_destroy(self._h)

@@ -103,6 +103,18 @@ int gbx_graph_device_arrays(const gbx_graph *g, const uint32_t **offsets, const 
                             const float **weight, const uint32_t **in_offsets,
                             const uint32_t **in_src, const float **in_weight);
 
+/* ---- tuning (no reference counterpart) ---------------------------------- */
+/* Per-graph knobs: "bfs_alpha" (switch to bottom-up when the frontier's edges
+ * exceed unexplored edges / alpha; the reference fixes 15), "bfs_beta" (stay
+ * bottom-up while the frontier exceeds V / beta; 18), "sssp_delta" (bucket
+ * width, 0 = default). No knob changes any result, only the time. */
+int gbx_graph_set_tuning(gbx_graph *g, const char *key, double value);
+int gbx_graph_get_tuning(const gbx_graph *g, const char *key, double *value);
+/* Time candidate settings on num_samples sources of this graph (CUDA
+ * events) and keep the fastest: flags bit 0 BFS direction threshold, bit 1
+ * SSSP bucket width. */
+int gbx_autotune(gbx_graph *g, uint32_t flags, uint32_t num_samples, void *stream);
+
 /* ---- BFS --------------------------------------------------------------- */
 typedef struct gbx_bfs_result {
     uint32_t processed_nodes; /* vertices reached, source included (BFSStats.processed_nodes) */
