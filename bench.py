@@ -183,7 +183,16 @@ def run_gpu(args):
         h.label_array = None  # roots are given in the graph's own ids
     # the in-house autotuner picks the BFS direction threshold and the SSSP
     # bucket width on this graph (untimed setup; results do not depend on them)
-    tuning = dg.autotune(bfs=True, sssp=True, samples=4, stream=sp) if not args.no_autotune else {}
+    if args.tuning:
+        # fixed knob values (profiling runs that must not include autotuning launches)
+        for kv in args.tuning.split(","):
+            k, v = kv.split("=")
+            dg.set_tuning(k, float(v))
+        tuning = {k: dg.get_tuning(k) for k in ("bfs_alpha", "bfs_beta", "sssp_delta")}
+    elif not args.no_autotune:
+        tuning = dg.autotune(bfs=True, sssp=True, samples=4, stream=sp)
+    else:
+        tuning = {}
     log(f"autotune: {tuning}")
     # device-resident buffers
     dist_d = torch.empty(V, dtype=torch.int32, device=dev)
@@ -530,6 +539,7 @@ def main():
     ap.add_argument("--only", default="", help="comma-separated kernel subset (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--tuning", default="", help="fixed knobs instead of autotuning, e.g. bfs_alpha=15,sssp_delta=4096")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the dominant kernel from an ncu capture")
     args = ap.parse_args()
