@@ -45,6 +45,10 @@ SEED = 1
 N_ROOTS = 64
 N_SSSP_ROOTS = 4
 PR_ITERS = 20
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each
+# kernel, from one `ncu --set full` capture of this workload on a GB300
+# (tc, spmv: one launch; pr: one iteration; bfs, sssp: one source).
+NCU_TRAFFIC_PER_LAUNCH = {"tc": 16.053e9, "pr": 0.4006e9, "bfs": 0.1941e9, "sssp": 5.334e9, "spmv": 0.6775e9}
 W_LO, W_HI = 1, 255
 
 
@@ -319,7 +323,9 @@ def run_gpu(args):
     dom = max(per, key=lambda n: per[n]["ms"])
     roof = {"kernel": dom, "bound": "hbm", "achieved": per[dom]["achieved_gbs"], "peak": peak,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": per[dom]["frac"],
-            "traffic": args.traffic, "note": "achieved = algorithmic bytes / CUDA-event time"}
+            "traffic": args.traffic if args.traffic is not None else NCU_TRAFFIC_PER_LAUNCH.get(dom),
+            "traffic_unit": "bytes per launch",
+            "note": "achieved = algorithmic bytes / CUDA-event time; traffic = DRAM bytes of one launch from ncu"}
 
     e2e = None if args.no_e2e else run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp)
     cpu = None
