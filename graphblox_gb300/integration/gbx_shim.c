@@ -1,0 +1,130 @@
+/* Graph cache, allocation and timing helpers for the cuda integration. */
+#define _POSIX_C_SOURCE 200809L
+#include "gbx_shim.h"
+
+#include <pthread.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#define GBX_SHIM_CACHE 4
+
+struct shim_entry {
+    struct GraphCSR *graph;
+    const void *key[4];
+    uint32_t V, E;
+    gbx_graph *dev;
+    unsigned long long stamp;
+};
+
+static struct shim_entry g_cache[GBX_SHIM_CACHE];
+static unsigned long long g_stamp = 0;
+static pthread_mutex_t g_lock = PTHREAD_MUTEX_INITIALIZER;
+
+void *gbx_shim_alloc(size_t bytes) {
+    void *p = NULL;
+    if (posix_memalign(&p, 4096, bytes ? bytes : 1) != 0) return NULL;
+    memset(p, 0, bytes);
+    return p;
+}
+
+double gbx_shim_now(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+void *gbx_shim_fail(const char *what, int status) {
+    fprintf(stderr, "| %s failed: %s (%s)\n", what, gbx_status_string(status), gbx_last_error());
+    return NULL;
+}
+
+void gbx_shim_not_available(const char *algorithm) {
+    printf(" -----------------------------------------------------\n");
+    printf("| %-51s | \n", algorithm);
+    printf("| %-51s | \n", "not available in the cuda integration");
+    printf(" -----------------------------------------------------\n");
+}
+
+static void fill_key(struct GraphCSR *g, const void *key[4]) {
+    key[0] = g->vertices ? (const void *)g->vertices->edges_idx : NULL;
+    key[1] = g->sorted_edges_array ? (const void *)g->sorted_edges_array->edges_array_dest : NULL;
+#if DIRECTED
+    key[2] = g->inverse_sorted_edges_array ? (const void *)g->inverse_sorted_edges_array->edges_array_dest : NULL;
+#else
+    key[2] = NULL;
+#endif
+#if WEIGHTED
+    key[3] = g->sorted_edges_array ? (const void *)g->sorted_edges_array->edges_array_weight : NULL;
+#else
+    key[3] = NULL;
+#endif
+}
+
+gbx_graph *gbx_shim_graph(struct GraphCSR *graph) {
+    const void *key[4];
+    fill_key(graph, key);
+    pthread_mutex_lock(&g_lock);
+    for (int i = 0; i < GBX_SHIM_CACHE; ++i) {
+        struct shim_entry *e = &g_cache[i];
+        if (e->dev && e->graph == graph && e->V == graph->num_vertices && e->E == graph->num_edges &&
+            !memcmp(e->key, key, sizeof(key))) {
+            e->stamp = ++g_stamp;
+            pthread_mutex_unlock(&g_lock);
+            return e->dev;
+        }
+    }
+    const float *w = NULL;
+    const uint32_t *iidx = NULL, *ideg = NULL, *isrc = NULL;
+    const float *iw = NULL;
+#if WEIGHTED
+    w = graph->sorted_edges_array->edges_array_weight;
+#endif
+#if DIRECTED
+    if (graph->inverse_vertices && graph->inverse_sorted_edges_array) {
+        iidx = graph->inverse_vertices->edges_idx;
+        ideg = graph->inverse_vertices->out_degree;
+        isrc = graph->inverse_sorted_edges_array->edges_array_dest;
+#if WEIGHTED
+        iw = graph->inverse_sorted_edges_array->edges_array_weight;
+#endif
+    }
+#endif
+    gbx_graph *dev = NULL;
+    int st = gbx_graph_create_csr(&dev, graph->num_vertices, graph->num_edges, graph->vertices->edges_idx,
+                                  graph->vertices->out_degree, graph->sorted_edges_array->edges_array_dest, w,
+                                  iidx, ideg, isrc, iw, NULL);
+    if (st != GBX_OK) {
+        pthread_mutex_unlock(&g_lock);
+        return (gbx_graph *)gbx_shim_fail("gbx_graph_create_csr", st);
+    }
+    int victim = -1;
+    for (int i = 0; i < GBX_SHIM_CACHE && victim < 0; ++i)
+        if (!g_cache[i].dev) victim = i;
+    if (victim < 0) {
+        victim = 0;
+        for (int i = 1; i < GBX_SHIM_CACHE; ++i)
+            if (g_cache[i].stamp < g_cache[victim].stamp) victim = i;
+    }
+    if (g_cache[victim].dev) gbx_graph_destroy(g_cache[victim].dev);
+    g_cache[victim].graph = graph;
+    memcpy(g_cache[victim].key, key, sizeof(key));
+    g_cache[victim].V = graph->num_vertices;
+    g_cache[victim].E = graph->num_edges;
+    g_cache[victim].dev = dev;
+    g_cache[victim].stamp = ++g_stamp;
+    pthread_mutex_unlock(&g_lock);
+    return dev;
+}
+
+void gbx_shim_release(struct GraphCSR *graph) {
+    pthread_mutex_lock(&g_lock);
+    for (int i = 0; i < GBX_SHIM_CACHE; ++i) {
+        if (g_cache[i].dev && g_cache[i].graph == graph) {
+            gbx_graph_destroy(g_cache[i].dev);
+            memset(&g_cache[i], 0, sizeof(g_cache[i]));
+        }
+    }
+    pthread_mutex_unlock(&g_lock);
+}

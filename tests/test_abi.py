@@ -59,3 +59,23 @@ def test_no_cpu_fallback_without_device(gbx):
                                   None, None, None, None, None, None)
     assert st == -5  # GBX_ERR_NO_DEVICE
     assert b"device" in lib.gbx_last_error()
+
+
+def test_integration_libraries_export_reference_symbols(gbx):
+    """The cuda integration shims export the reference's algorithm entry
+    points (01_host/include/algorithms/openmp/*.h) for both GraphCSR layouts."""
+    import subprocess
+
+    from graphblox_gb300 import _build
+
+    libs = _build.build_integration()
+    assert len(libs) == 2
+    want = ["breadthFirstSearchGraphCSR", "newBFSStatsGraphCSR", "freeBFSStats", "pageRankGraphCSR",
+            "freePageRankStats", "SSSPGraphCSR", "freeSSSPStats", "connectedComponentsGraphCSR", "freeCCStats",
+            "triangleCountGraphCSR", "freeTCStats", "SPMVGraphCSR", "freeSPMVStats", "depthFirstSearchGraphCSR",
+            "bellmanFordGraphCSR", "betweennessCentralityGraphCSR", "clusterGraphCSR"]
+    for lib in libs:
+        nm = subprocess.run(["nm", "-D", str(lib)], capture_output=True, text=True).stdout
+        missing = [s for s in want if f" T {s}" not in nm]
+        assert not missing, f"{lib.name} lacks {missing}"
+        C.CDLL(str(lib))  # loads (resolves libgbx.so through its rpath)
