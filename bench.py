@@ -50,6 +50,11 @@ PR_ITERS = 20
 # (tc, spmv: one launch; pr: one iteration; bfs, sssp: one source).
 NCU_TRAFFIC_PER_LAUNCH = {"tc": 16.053e9, "pr": 0.4006e9, "bfs": 0.1941e9, "sssp": 5.334e9, "spmv": 0.6775e9}
 W_LO, W_HI = 1, 255
+# differentiable personalised PageRank: RMAT-20, 2^24 edges as generated,
+# lognormal(0,1) weights, 64 teleport columns of 32 seeds, d 0.85 to 1e-7 L1
+PPR_SCALE, PPR_EDGES, PPR_K, PPR_SEEDS, PPR_TOL, PPR_D = 20, 1 << 24, 64, 32, 1e-7, 0.85
+# batched: 2,048 RMAT graphs, BFS from 0 plus 30 PageRank iterations each
+BATCH_GRAPHS, BATCH_PR_ITERS = 2048, 30
 
 
 def log(*a):
@@ -314,19 +319,25 @@ def run_gpu(args):
         tot_edges += te
         tot_ms += ms
     ms_step = tot_ms
-    gteps = tot_edges / (tot_ms * 1e-3) / 1e9
+    gteps = tot_edges / (tot_ms * 1e-3) / 1e9 if tot_ms else 0.0
     if dist:
         t = torch.tensor([ms_step], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms_step = float(t.item())
         gteps = world * tot_edges / (ms_step * 1e-3) / 1e9
-    dom = max(per, key=lambda n: per[n]["ms"])
-    roof = {"kernel": dom, "bound": "hbm", "achieved": per[dom]["achieved_gbs"], "peak": peak,
+    dom = max(per, key=lambda n: per[n]["ms"]) if per else None
+    roof = None if dom is None else {"kernel": dom, "bound": "hbm", "achieved": per[dom]["achieved_gbs"], "peak": peak,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": per[dom]["frac"],
             "traffic": args.traffic if args.traffic is not None else NCU_TRAFFIC_PER_LAUNCH.get(dom),
             "traffic_unit": "bytes per launch",
             "note": "achieved = algorithmic bytes / CUDA-event time; traffic = DRAM bytes of one launch from ncu"}
 
+    ppr = None
+    if not args.no_ppr and (not args.only or "ppr" in args.only.split(",")):
+        ppr = run_ppr(args, torch, gbx, dev, stream, peak)
+    batched = None
+    if not args.no_batched and (not args.only or "batched" in args.only.split(",")):
+        batched = run_batched(args, torch, gbx, _lib, dev, stream, peak)
     e2e = None if args.no_e2e else run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -343,13 +354,156 @@ def run_gpu(args):
                    "dag_edges": e_plus, "bfs_roots": N_ROOTS, "sssp_roots": N_SSSP_ROOTS,
                    "pr_iterations": PR_ITERS, "l2": "flushed (256 MiB write) before every kernel",
                    "parallelism": "replicas" if world > 1 else "single GPU", "tuning": tuning},
-        "kernels": per, "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk,
+        "kernels": per, "batched": batched, "ppr_adjoint": ppr, "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk,
         "gpu_launches": int(launches), "wall_ms_timed_region": round(wall_ms, 3),
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def run_ppr(args, torch, gbx, dev, stream, peak):
+    """Personalised PageRank forward and adjoint (gbx_ppr_forward /
+    gbx_ppr_adjoint) on device-resident inputs: mean CUDA-event time of each
+    over `steps` calls after one untimed call of each, and (fwd+adj)/fwd.
+    Algorithmic bytes per sweep, K columns: 4(V+1) offsets + 8E (index +
+    weight) + 4K*E (neighbour-row gather) + 8K*V (row read + write)."""
+    V, E, K = 1 << PPR_SCALE, PPR_EDGES, PPR_K
+    s, d = gbx.generate_rmat(PPR_SCALE, E, seed=SEED)
+    order = np.argsort(s, kind="stable")
+    dst = np.ascontiguousarray(d[order])
+    off = np.zeros(V + 1, np.int64)
+    off[1:] = np.cumsum(np.bincount(s, minlength=V))
+    off = off.astype(np.uint32)
+    w = gbx.generate_values(E, 3, seed=SEED + 1)
+    rng = np.random.default_rng(SEED)
+    T = np.zeros((V, K), np.float32)
+    for k in range(K):
+        T[rng.choice(V, PPR_SEEDS, replace=False), k] = 1.0 / PPR_SEEDS
+    Wl = rng.standard_normal((V, K)).astype(np.float32)
+    dg = gbx.DeviceGraph.from_offsets(V, off, dst)
+    sp = stream.cuda_stream
+    w_d, T_d, W_d = (torch.from_numpy(a).to(dev) for a in (w, T, Wl))
+    R_d = torch.empty((V, K), dtype=torch.float32, device=dev)
+    gw_d = torch.empty(E, dtype=torch.float32, device=dev)
+    gt_d = torch.empty((V, K), dtype=torch.float32, device=dev)
+
+    def fwd():
+        return gbx.ppr_forward(dg, w_d, T_d, PPR_D, PPR_TOL, ranks=R_d, stream=sp)
+
+    def adj():
+        return gbx.ppr_adjoint(dg, w_d, R_d, W_d, PPR_D, PPR_TOL, grad_weights=gw_d, grad_teleport=gt_d, stream=sp)
+
+    fwd(), adj()  # builds the graph's in-edge order and chunk tables (untimed)
+    times = {"fwd": [], "adj": []}
+    info = {}
+    for _ in range(max(1, args.steps)):
+        for name, fn in (("fwd", fwd), ("adj", adj)):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            st = fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            times[name].append(a.elapsed_time(b))
+            info[name] = st
+    dg.close()
+    f_ms, a_ms = float(np.mean(times["fwd"])), float(np.mean(times["adj"]))
+    sweep_bytes = 4 * (V + 1) + 8 * E + 4 * K * E + 8 * K * V
+    fi, ai = info["fwd"].iterations, info["adj"].iterations
+    gbs_f = fi * sweep_bytes / (f_ms * 1e-3) / 1e9
+    gbs_a = ai * sweep_bytes / (a_ms * 1e-3) / 1e9
+    return {"workload": f"rmat{PPR_SCALE}_ppr_k{K}", "num_vertices": V, "num_edges": E, "K": K,
+            "damping": PPR_D, "tol_l1": PPR_TOL, "forward_ms": round(f_ms, 3), "adjoint_ms": round(a_ms, 3),
+            "fwd_plus_adjoint_over_fwd": round((f_ms + a_ms) / f_ms, 3),
+            "forward_sweeps": fi, "adjoint_sweeps": ai, "loss": info["adj"].loss,
+            "forward_gbs": round(gbs_f, 1), "adjoint_gbs": round(gbs_a, 1),
+            "forward_frac": round(gbs_f / peak, 3), "adjoint_frac": round(gbs_a / peak, 3),
+            "alg_bytes_per_sweep": int(sweep_bytes),
+            "note": "adjoint_ms includes dL/dw (one more gather pass), dL/dT and the FP64 loss"}
+
+
+def run_batched(args, torch, gbx, _lib, dev, stream, peak):
+    """2,048 RMAT graphs (scale ~U[8,15], V = floor(2^s), edge factor
+    ~U[4,32]) packed back to back: one step = BFS from vertex 0 plus 30
+    PageRank iterations on every graph. Batched: gbx_bfs_batched +
+    gbx_pr_batched (two persistent launches). Per instance: gbx_bfs +
+    gbx_pagerank_pull called once per graph on resident single graphs, the
+    same device output arrays. Both timed with CUDA events, mean of `steps`."""
+    t0 = time.time()
+    gl = gbx.generate_rmat_batch(BATCH_GRAPHS, seed=SEED)
+    packed = gbx.pack_graphs(gl)
+    del gl
+    G = packed.num_graphs
+    vb = packed.vertex_base.astype(np.int64)
+    Vt, Et = int(vb[-1]), int(packed.offsets[-1])
+    log(f"batch built in {time.time() - t0:.1f}s: {G} graphs, V={Vt} E={Et}")
+    sp = stream.cuda_stream
+    batch = gbx.GraphBatch(packed, stream=sp)
+    singles = []
+    for g in range(G):
+        V, off, dest, ioff, isrc = packed.graph(g)
+        singles.append(gbx.DeviceGraph.from_offsets(V, off, dest, in_offsets=ioff, in_src=isrc, stream=sp))
+    src_d = torch.zeros(G, dtype=torch.int32, device=dev)
+    dist_d = torch.empty(Vt, dtype=torch.int32, device=dev)
+    par_d = torch.empty(Vt, dtype=torch.int32, device=dev)
+    ranks_d = torch.empty(Vt, dtype=torch.float32, device=dev)
+    bres = (_lib.BfsResult * G)()
+    pres = (_lib.PrResult * G)()
+
+    def batched():
+        _lib.call("gbx_bfs_batched", batch.handle, src_d.data_ptr(), dist_d.data_ptr(), par_d.data_ptr(), bres, sp)
+        _lib.call("gbx_pr_batched", batch.handle, BATCH_PR_ITERS, 0.0, ranks_d.data_ptr(), pres, sp)
+
+    r1 = _lib.BfsResult()
+    r2 = _lib.PrResult()
+
+    def per_instance():
+        for g, dg in enumerate(singles):
+            o = int(vb[g]) * 4
+            _lib.call("gbx_bfs", dg.handle, 0, 2, dist_d.data_ptr() + o, par_d.data_ptr() + o, _lib.C.byref(r1), sp)
+            _lib.call("gbx_pagerank_pull", dg.handle, BATCH_PR_ITERS, 0.0, ranks_d.data_ptr() + o,
+                      _lib.C.byref(r2), sp)
+
+    def timed(fn, n):
+        out = []
+        for _ in range(n):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            out.append(a.elapsed_time(b))
+        return float(np.mean(out))
+
+    timed(batched, 2)
+    l0 = _lib.load().gbx_kernel_launches()
+    b_ms = timed(batched, max(1, args.steps))
+    b_launches = (_lib.load().gbx_kernel_launches() - l0) // max(1, args.steps)
+    timed(per_instance, 1)  # builds the single graphs' pull plans
+    l0 = _lib.load().gbx_kernel_launches()
+    p_ms = timed(per_instance, max(1, min(args.steps, 2)))
+    p_launches = (_lib.load().gbx_kernel_launches() - l0) // max(1, min(args.steps, 2))
+    m_reach = sum(int(r.edges_traversed) for r in bres)
+    nv = np.diff(vb)
+    edges = m_reach + BATCH_PR_ITERS * Et
+    alg = (4 * (Vt + G) + 4 * m_reach + 8 * Vt) + BATCH_PR_ITERS * (8 * Et + 4 * (Vt + G) + 16 * Vt)
+    for dg in singles:
+        dg.close()
+    batch.close()
+    return {"workload": f"rmat_batch_{G}_graphs", "num_graphs": G, "num_vertices": Vt, "num_edges": Et,
+            "graph_vertices_min_max": [int(nv.min()), int(nv.max())], "pr_iterations": BATCH_PR_ITERS,
+            "batched_ms": round(b_ms, 3), "per_instance_ms": round(p_ms, 3),
+            "speedup_vs_per_instance": round(p_ms / b_ms, 2),
+            "batched_gteps": round(edges / (b_ms * 1e-3) / 1e9, 3),
+            "per_instance_gteps": round(edges / (p_ms * 1e-3) / 1e9, 3),
+            "batched_achieved_gbs": round(alg / (b_ms * 1e-3) / 1e9, 1),
+            "batched_frac": round(alg / (b_ms * 1e-3) / 1e9 / peak, 3),
+            "launches_batched": int(b_launches), "launches_per_instance": int(p_launches),
+            "edges_per_step": int(edges), "alg_bytes_per_step": int(alg)}
 
 
 def run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp):
@@ -544,6 +698,8 @@ def main():
     ap.add_argument("--scale", type=int, default=SCALE, help="RMAT scale (22 is the benchmark workload)")
     ap.add_argument("--only", default="", help="comma-separated kernel subset (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-ppr", action="store_true", help="skip the personalised PageRank forward/adjoint section")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 2,048-graph batched section")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--tuning", default="", help="fixed knobs instead of autotuning, e.g. bfs_alpha=15,sssp_delta=4096")
     ap.add_argument("--traffic", type=float, default=None,

@@ -9,17 +9,25 @@ from .graph import (  # noqa: F401
     BFSStats,
     DeviceGraph,
     EdgeList,
+    GraphBatch,
     GraphCSR,
+    PackedGraphs,
     PageRankStats,
+    PPRAdjointStats,
+    PPRStats,
     SSSPStats,
     breadth_first_search,
     connected_components,
     csr_build,
     degree_reorder,
     generate_rmat,
+    generate_rmat_batch,
     generate_values,
     graph_csr_preprocessing,
+    pack_graphs,
     page_rank,
+    ppr_adjoint,
+    ppr_forward,
     read_edge_list_bin,
     spmv,
     sssp,

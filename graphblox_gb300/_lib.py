@@ -28,6 +28,11 @@ class PrResult(C.Structure):
     _fields_ = [("iterations", u32), ("active_last", u32), ("error_total", C.c_double)]
 
 
+class PprResult(C.Structure):
+    _fields_ = [("iterations", u32), ("adjoint_iterations", u32), ("residual", C.c_double),
+                ("adjoint_residual", C.c_double), ("loss", C.c_double)]
+
+
 class SsspResult(C.Structure):
     _fields_ = [("reached", u32), ("rounds", u32), ("edges_relaxed", u64), ("edges_traversed", u64)]
 
@@ -51,6 +56,14 @@ SIGNATURES = {
     "gbx_bfs": (C.c_int, [vp, u32, C.c_int, vp, vp, C.POINTER(BfsResult), vp]),
     "gbx_pagerank_pull": (C.c_int, [vp, u32, C.c_double, vp, C.POINTER(PrResult), vp]),
     "gbx_pagerank_pull_noalloc": (C.c_int, [u32, vp, vp, vp, u32, C.c_double, vp, C.POINTER(PrResult), vp]),
+    "gbx_batch_create": (C.c_int, [C.POINTER(vp), u32, vp, vp, vp, vp, vp, vp]),
+    "gbx_batch_destroy": (C.c_int, [vp]),
+    "gbx_batch_info": (C.c_int, [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)]),
+    "gbx_bfs_batched": (C.c_int, [vp, vp, vp, vp, vp, vp]),
+    "gbx_pr_batched": (C.c_int, [vp, u32, C.c_double, vp, vp, vp]),
+    "gbx_ppr_forward": (C.c_int, [vp, u32, vp, vp, C.c_double, C.c_double, u32, vp, C.POINTER(PprResult), vp]),
+    "gbx_ppr_adjoint": (C.c_int, [vp, u32, vp, vp, vp, C.c_double, C.c_double, u32, vp, vp,
+                                  C.POINTER(PprResult), vp]),
     "gbx_sssp": (C.c_int, [vp, u32, u32, vp, C.POINTER(SsspResult), vp]),
     "gbx_cc": (C.c_int, [vp, C.c_int, vp, C.POINTER(u32), vp]),
     "gbx_tc": (C.c_int, [vp, C.POINTER(u64), vp]),

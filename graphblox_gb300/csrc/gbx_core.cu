@@ -323,6 +323,7 @@ int gbx_graph_destroy(gbx_graph *g) {
     cudaFree(g->in_degree);
     cudaFree(g->low_count);
     gbx_free_tc_plan(g->tc_plan);
+    gbx_free_ppr_cache(g->ppr);
     free_plan(g->plan_fwd);
     free_plan(g->plan_inv);
     cudaSetDevice(prev);

@@ -217,6 +217,8 @@ struct gbx_graph {
     uint32_t sssp_delta = 0;
     // triangle-count work decomposition (gbx_tc.cu)
     struct gbx_tc_plan *tc_plan = nullptr;
+    // personalised PageRank: in-edge order and chunk tables (gbx_ppr.cu)
+    struct gbx_ppr_cache *ppr = nullptr;
 
     bool has_inverse() const { return in_offsets != nullptr; }
     // CSR used by pull-direction kernels (reference: inverse when DIRECTED)
@@ -227,6 +229,7 @@ struct gbx_graph {
 };
 
 void gbx_free_tc_plan(struct gbx_tc_plan *p);
+void gbx_free_ppr_cache(struct gbx_ppr_cache *c);
 
 namespace gbx {
 // plan for the pull CSR of g (built on first use, cached on the graph)

@@ -311,6 +311,80 @@ def page_rank(dg: DeviceGraph, iterations: int = 20, epsilon: float = 1e-4, rank
 
 
 @dataclass
+class PPRStats:
+    ranks: object
+    iterations: int
+    residual: float
+
+
+@dataclass
+class PPRAdjointStats:
+    grad_weights: object
+    grad_teleport: object
+    loss: float
+    iterations: int
+    residual: float
+
+
+def _block_k(a, num_vertices: int) -> int:
+    shape = tuple(a.shape)
+    if len(shape) != 2 or shape[0] != num_vertices:
+        raise ValueError(f"expected a [{num_vertices}, K] block, got shape {shape}")
+    return int(shape[1])
+
+
+def _like(a, shape):
+    if isinstance(a, np.ndarray):
+        return np.zeros(shape, np.float32)
+    import torch
+
+    return torch.zeros(shape, dtype=torch.float32, device=a.device)
+
+
+def ppr_forward(dg: DeviceGraph, weights, teleport, damping: float = 0.85, tol: float = 1e-7,
+                max_iterations: int = 1000, ranks=None, stream=None) -> PPRStats:
+    """Personalised PageRank R = (1-d) T + d P R for the K columns of
+    `teleport` ([V, K], K in 32/64/128/256); P from the forward-order edge
+    `weights` normalised per source. No reference counterpart."""
+    if isinstance(weights, np.ndarray):
+        weights = _f32(weights)
+    if isinstance(teleport, np.ndarray):
+        teleport = _f32(teleport)
+    K = _block_k(teleport, dg.num_vertices)
+    if ranks is None:
+        ranks = _like(teleport, (dg.num_vertices, K))
+    r = _lib.PprResult()
+    call("gbx_ppr_forward", dg.handle, K, _ptr(weights), _ptr(teleport), float(damping), float(tol),
+         int(max_iterations), _ptr(ranks), C.byref(r), stream)
+    return PPRStats(ranks, r.iterations, r.residual)
+
+
+def ppr_adjoint(dg: DeviceGraph, weights, ranks, loss_weights, damping: float = 0.85, tol: float = 1e-7,
+                max_iterations: int = 1000, grad_weights=None, grad_teleport=None, want_weights: bool = True,
+                want_teleport: bool = True, stream=None) -> PPRAdjointStats:
+    """Adjoint of ppr_forward for L = sum(loss_weights * ranks): solves
+    Lam = W + d P^T Lam at the converged ranks and returns dL/dw (forward
+    edge order) and dL/dT = (1-d) Lam."""
+    if isinstance(weights, np.ndarray):
+        weights = _f32(weights)
+    if isinstance(ranks, np.ndarray):
+        ranks = _f32(ranks)
+    if isinstance(loss_weights, np.ndarray):
+        loss_weights = _f32(loss_weights)
+    K = _block_k(ranks, dg.num_vertices)
+    if _block_k(loss_weights, dg.num_vertices) != K:
+        raise ValueError("ranks and loss_weights differ in K")
+    if grad_weights is None and want_weights:
+        grad_weights = _like(ranks, (dg.num_edges,))
+    if grad_teleport is None and want_teleport:
+        grad_teleport = _like(ranks, (dg.num_vertices, K))
+    r = _lib.PprResult()
+    call("gbx_ppr_adjoint", dg.handle, K, _ptr(weights), _ptr(ranks), _ptr(loss_weights), float(damping),
+         float(tol), int(max_iterations), _ptr(grad_weights), _ptr(grad_teleport), C.byref(r), stream)
+    return PPRAdjointStats(grad_weights, grad_teleport, r.loss, r.adjoint_iterations, r.adjoint_residual)
+
+
+@dataclass
 class SSSPStats:
     distances: object
     reached: int
@@ -376,4 +450,143 @@ def generate_values(count: int, kind: int, lo: int = 0, hi: int = 0, seed: int =
     """kind 0 int U[lo,hi] as float, 1 U(0,1], 2 U[-1,1), 3 lognormal(0,1)."""
     out = np.empty(count, np.float32)
     call("gbx_generate_values", int(count), int(kind), int(lo), int(hi), int(seed), _ptr(out))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# batches of graphs (gbx_batch): one persistent launch per algorithm
+
+
+def _results_dict(arr, fields):
+    return {f: np.array([getattr(r, f) for r in arr]) for f in fields}
+
+
+@dataclass
+class PackedGraphs:
+    """Back-to-back CSR of several graphs (the gbx_batch_create layout):
+    graph g owns packed vertices vertex_base[g]..vertex_base[g+1]-1, offsets
+    are global edge positions, dest / in_src hold graph-local ids."""
+    vertex_base: np.ndarray
+    offsets: np.ndarray
+    dest: np.ndarray
+    in_offsets: Optional[np.ndarray] = None
+    in_src: Optional[np.ndarray] = None
+
+    @property
+    def num_graphs(self) -> int:
+        return len(self.vertex_base) - 1
+
+    def graph(self, g: int):
+        """(V, offsets rebased to 0, dest, in_offsets, in_src) of graph g."""
+        b, e = int(self.vertex_base[g]), int(self.vertex_base[g + 1])
+        off = self.offsets[b:e + 1].astype(np.int64)
+        out = [e - b, (off - off[0]).astype(np.uint32), self.dest[off[0]:off[-1]]]
+        if self.in_offsets is not None:
+            ioff = self.in_offsets[b:e + 1].astype(np.int64)
+            out += [(ioff - ioff[0]).astype(np.uint32), self.in_src[ioff[0]:ioff[-1]]]
+        else:
+            out += [None, None]
+        return tuple(out)
+
+
+def pack_graphs(graphs, inverse: bool = True, stream=None) -> PackedGraphs:
+    """Pack [(V, src, dst), ...] edge lists into one back-to-back CSR, rows
+    grouped by source in input order (gbx_csr_build, sort by source, on the
+    GPU), with the in-edge CSR when `inverse`."""
+    nv = np.array([int(v) for v, _, _ in graphs], np.int64)
+    vbase = np.zeros(len(graphs) + 1, np.int64)
+    vbase[1:] = np.cumsum(nv)
+    if vbase[-1] >= 1 << 30:
+        raise ValueError("packed vertex count must stay below 2^30")
+    counts = np.array([len(s) for _, s, _ in graphs], np.int64)
+    shift = np.repeat(vbase[:-1], counts).astype(np.uint32)
+    src = np.concatenate([np.asarray(s, np.uint32) for _, s, _ in graphs]) + shift
+    dst = np.concatenate([np.asarray(d, np.uint32) for _, _, d in graphs]) + shift
+    Vt = int(vbase[-1])
+
+    def csr(a, b):
+        deg, _, so, do, _ = csr_build(a, b, num_vertices=Vt, sort=0, stream=stream)
+        off = np.zeros(Vt + 1, np.int64)
+        off[1:] = np.cumsum(deg[:Vt], dtype=np.int64)
+        base = np.repeat(vbase[:-1], np.diff(off[vbase])).astype(np.uint32)
+        return off.astype(np.uint32), (do - base).astype(np.uint32)
+
+    off, dest = csr(src, dst)
+    ioff = isrc = None
+    if inverse:
+        ioff, isrc = csr(dst, src)
+    return PackedGraphs(vbase.astype(np.uint32), off, dest, ioff, isrc)
+
+
+class GraphBatch:
+    """Many graphs resident on the GPU as one packed CSR (gbx_batch)."""
+
+    def __init__(self, packed: PackedGraphs, stream=None):
+        h = C.c_void_p()
+        p = packed
+        call("gbx_batch_create", C.byref(h), p.num_graphs, _ptr(_u32(p.vertex_base)), _ptr(_u32(p.offsets)),
+             _ptr(_u32(p.dest)), _ptr(None if p.in_offsets is None else _u32(p.in_offsets)),
+             _ptr(None if p.in_src is None else _u32(p.in_src)), stream)
+        self._h = h
+        self.num_graphs = p.num_graphs
+        self.num_vertices = int(p.vertex_base[-1])
+        self.num_edges = int(p.offsets[-1])
+
+    @property
+    def handle(self):
+        return self._h
+
+    def bfs(self, sources, distances=None, parents=None, stream=None):
+        """gbx_bfs_batched: (distances, parents, per-graph results dict)."""
+        if isinstance(sources, np.ndarray) or isinstance(sources, (list, tuple)):
+            sources = _u32(sources)
+        if distances is None:
+            distances = np.zeros(self.num_vertices, np.uint32)
+        res = (BfsResult * self.num_graphs)()
+        call("gbx_bfs_batched", self._h, _ptr(sources), _ptr(distances), _ptr(parents), res, stream)
+        return distances, parents, _results_dict(res, ("processed_nodes", "iteration", "depth", "top_down_steps",
+                                                       "bottom_up_steps", "edges_traversed"))
+
+    def page_rank(self, iterations: int = 20, epsilon: float = 1e-4, ranks=None, stream=None):
+        """gbx_pr_batched: (ranks, per-graph results dict)."""
+        if ranks is None:
+            ranks = np.zeros(self.num_vertices, np.float32)
+        res = (PrResult * self.num_graphs)()
+        call("gbx_pr_batched", self._h, int(iterations), float(epsilon), _ptr(ranks), res, stream)
+        return ranks, _results_dict(res, ("iterations", "active_last", "error_total"))
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            _lib.load().gbx_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def generate_rmat_batch(num_graphs: int = 2048, seed: int = 1, scale_lo: float = 8.0, scale_hi: float = 15.0,
+                        ef_lo: float = 4.0, ef_hi: float = 32.0):
+    """Edge lists of `num_graphs` RMAT graphs (a/b/c = .57/.19/.19): scale
+    s ~ U[scale_lo, scale_hi], V = floor(2^s), edge factor ~ U[ef_lo, ef_hi];
+    each graph draws round(ef*V) edges at scale ceil(s) and keeps those with
+    both ends below V. Returns [(V, src, dst), ...]."""
+    rng = np.random.default_rng(seed)
+    s = rng.uniform(scale_lo, scale_hi, num_graphs)
+    ef = rng.uniform(ef_lo, ef_hi, num_graphs)
+    out = []
+    for g in range(num_graphs):
+        V = int(np.floor(2.0 ** s[g]))
+        sc = max(1, int(np.ceil(np.log2(V))))
+        src, dst = generate_rmat(sc, int(round(ef[g] * V)), seed=seed * 1_000_003 + g)
+        keep = (src < V) & (dst < V)
+        out.append((V, src[keep], dst[keep]))
     return out

@@ -165,6 +165,72 @@ int gbx_pagerank_pull_noalloc(uint32_t num_vertices, const uint32_t *pull_offset
                               uint32_t max_iterations, double epsilon, float *ranks,
                               gbx_pr_result *result, void *stream);
 
+/* ---- batches of graphs -----------------------------------------------------
+ * No counterpart in the reference as a batch: every graph of a batch gets
+ * the results gbx_bfs (mode 2) / gbx_pagerank_pull give it alone, i.e. the
+ * reference's breadthFirstSearchGraphCSR (BFS.c:103-127) and
+ * pageRankPullGraphCSR (pageRank.c:245-368) per graph, from one persistent
+ * launch over a device work queue of whole graphs.
+ * Packed back-to-back CSR of num_graphs graphs: graph g owns packed vertices
+ * vertex_base[g] .. vertex_base[g+1]-1 (vertex_base[0] = 0, every graph has
+ * at least one vertex); offsets (total V + 1) are global edge positions
+ * (offsets[0] = 0); dest holds graph-local ids. in_offsets / in_src give the
+ * in-edge CSR in the same packing (NULL: the forward CSR is its own
+ * transpose, as for symmetric graphs). Inputs may be host or device memory;
+ * they are copied and checked (GBX_ERR_INVALID for a decreasing offset or a
+ * local id at or above its graph's vertex count). */
+typedef struct gbx_batch gbx_batch;
+int gbx_batch_create(gbx_batch **out, uint32_t num_graphs, const uint32_t *vertex_base,
+                     const uint32_t *offsets, const uint32_t *dest, const uint32_t *in_offsets,
+                     const uint32_t *in_src, void *stream);
+int gbx_batch_destroy(gbx_batch *b);
+int gbx_batch_info(const gbx_batch *b, uint32_t *num_graphs, uint32_t *num_vertices,
+                   uint32_t *num_edges);
+/* BFS of every graph from its graph-local sources[g]. distances and parents
+ * (may be NULL) are packed like the vertices; results (may be NULL) has one
+ * entry per graph. */
+int gbx_bfs_batched(gbx_batch *b, const uint32_t *sources, uint32_t *distances, int32_t *parents,
+                    gbx_bfs_result *results, void *stream);
+/* Pull PageRank of every graph (ranks packed like the vertices, each graph's
+ * ranks divided by its own vertex count); results (may be NULL) per graph. */
+int gbx_pr_batched(gbx_batch *b, uint32_t max_iterations, double epsilon, float *ranks,
+                   gbx_pr_result *results, void *stream);
+
+/* ---- personalised PageRank and its adjoint -------------------------------
+ * No counterpart in the reference (its PageRank, pageRank.c:245-368, is the
+ * un-personalised pull recurrence). K teleport vectors at once:
+ *   P[v,u] = w_e / s_u for forward edge e = (u -> v), s_u = sum of u's
+ *            out-weights (a source with s_u = 0 drops its mass)
+ *   R = (1-d) T + d P R          forward fixed point
+ *   L = sum W .* R               loss (FP64 dot)
+ *   Lam = W + d P^T Lam          adjoint fixed point at the converged R
+ *   dL/dT = (1-d) Lam,  dL/dw_e = (d <Lam[v],R[u]> - sum_{e' of u} d <Lam[v'],R[u]> P_e') / s_u
+ * T, R, W, Lam and dL/dT are [V][K] row-major FP32 blocks (K = 32, 64, 128
+ * or 256); weights and dL/dw are in forward-CSR edge order. Both solves stop
+ * when, over all columns, the largest L1 change of an iteration divided by
+ * the L1 norm of the column's source term (T forward, W adjoint; norm 1 for
+ * a zero column) is below tol, reduced in FP64. For teleport columns that
+ * sum to 1 this is the plain L1 residual. GBX_ERR_ITER_CAP when
+ * max_iterations is reached first (the outputs then hold the last iterate).
+ * Arrays may be host or device memory; the first call on a graph builds and
+ * caches its in-edge order. */
+typedef struct gbx_ppr_result {
+    uint32_t iterations;          /* forward sweeps */
+    uint32_t adjoint_iterations;  /* adjoint sweeps */
+    double residual;              /* forward: last relative max-column L1 change */
+    double adjoint_residual;      /* adjoint: last relative max-column L1 change */
+    double loss;                  /* adjoint: sum W .* R in FP64 */
+} gbx_ppr_result;
+
+int gbx_ppr_forward(gbx_graph *g, uint32_t K, const float *weights, const float *teleport,
+                    double damping, double tol, uint32_t max_iterations, float *ranks,
+                    gbx_ppr_result *result, void *stream);
+/* grad_weights (E) and grad_teleport (V*K) may each be NULL to skip them. */
+int gbx_ppr_adjoint(gbx_graph *g, uint32_t K, const float *weights, const float *ranks,
+                    const float *loss_weights, double damping, double tol,
+                    uint32_t max_iterations, float *grad_weights, float *grad_teleport,
+                    gbx_ppr_result *result, void *stream);
+
 /* ---- SSSP --------------------------------------------------------------- */
 typedef struct gbx_sssp_result {
     uint32_t reached;        /* vertices with a finite distance */
