@@ -55,6 +55,7 @@ W_LO, W_HI = 1, 255
 PPR_SCALE, PPR_EDGES, PPR_K, PPR_SEEDS, PPR_TOL, PPR_D = 20, 1 << 24, 64, 32, 1e-7, 0.85
 # batched: 2,048 RMAT graphs, BFS from 0 plus 30 PageRank iterations each
 BATCH_GRAPHS, BATCH_PR_ITERS = 2048, 30
+MS_SOURCES = 256  # multi-source bitmask BFS on the RMAT-22 graph
 
 
 def log(*a):
@@ -157,6 +158,25 @@ class ClockSampler:
             return None
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# replicas: one full workload per rank, no data-path collective
+
+
+def reduce_over_ranks(dist, local_ms, local_edges, device=None):
+    """(ms, GTEPS) of the whole job: the slowest rank's step time, and every
+    rank's traversed edges over it. Every replica runs the same workload
+    (weak scaling), so the job's edges are world * local_edges."""
+    if not dist or not dist.is_initialized() or dist.get_world_size() == 1:
+        return local_ms, (local_edges / (local_ms * 1e-3) / 1e9 if local_ms else 0.0)
+    import torch
+
+    t = torch.tensor([float(local_ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    world = dist.get_world_size()
+    return ms, (world * local_edges / (ms * 1e-3) / 1e9 if ms else 0.0)
 
 
 # ---------------------------------------------------------------------------
@@ -318,13 +338,7 @@ def run_gpu(args):
                   "frac": round(tb / (ms * 1e-3) / 1e9 / peak, 3), "edges": int(te), "alg_bytes": int(tb)}
         tot_edges += te
         tot_ms += ms
-    ms_step = tot_ms
-    gteps = tot_edges / (tot_ms * 1e-3) / 1e9 if tot_ms else 0.0
-    if dist:
-        t = torch.tensor([ms_step], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-        gteps = world * tot_edges / (ms_step * 1e-3) / 1e9
+    ms_step, gteps = reduce_over_ranks(dist, tot_ms, tot_edges, torch.device("cuda", local) if dist else None)
     dom = max(per, key=lambda n: per[n]["ms"]) if per else None
     roof = None if dom is None else {"kernel": dom, "bound": "hbm", "achieved": per[dom]["achieved_gbs"], "peak": peak,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": per[dom]["frac"],
@@ -338,6 +352,7 @@ def run_gpu(args):
     batched = None
     if not args.no_batched and (not args.only or "batched" in args.only.split(",")):
         batched = run_batched(args, torch, gbx, _lib, dev, stream, peak)
+        batched["multisource"] = run_multisource(args, torch, gbx, _lib, dg, W, dev, stream, peak)
     e2e = None if args.no_e2e else run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -504,6 +519,58 @@ def run_batched(args, torch, gbx, _lib, dev, stream, peak):
             "batched_frac": round(alg / (b_ms * 1e-3) / 1e9 / peak, 3),
             "launches_batched": int(b_launches), "launches_per_instance": int(p_launches),
             "edges_per_step": int(edges), "alg_bytes_per_step": int(alg)}
+
+
+def run_multisource(args, torch, gbx, _lib, dg, W, dev, stream, peak):
+    """256-source BFS on the RMAT-22 graph: one gbx_bfs_multisource call
+    (bitmask sweep) against 256 gbx_bfs calls, same sources (seeded,
+    non-isolated), device outputs. Mean CUDA-event time of `steps` calls."""
+    V = W["V"]
+    g = W["g"]
+    rng = np.random.default_rng(SEED + 5)
+    nz = np.nonzero(g.out_degree)[0]
+    src = rng.choice(nz, MS_SOURCES, replace=False).astype(np.uint32)
+    sp = stream.cuda_stream
+    src_d = torch.from_numpy(src.view(np.int32)).to(dev)
+    dist_d = torch.empty((V, MS_SOURCES), dtype=torch.int32, device=dev)
+    d1 = torch.empty(V, dtype=torch.int32, device=dev)
+    res = (_lib.BfsResult * MS_SOURCES)()
+    r1 = _lib.BfsResult()
+
+    def multi():
+        _lib.call("gbx_bfs_multisource", dg.handle, MS_SOURCES, src_d.data_ptr(), dist_d.data_ptr(), res, sp)
+
+    def singles():
+        for s in src:
+            _lib.call("gbx_bfs", dg.handle, int(s), 2, d1.data_ptr(), None, _lib.C.byref(r1), sp)
+
+    def timed(fn, n):
+        out = []
+        for _ in range(n):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            out.append(a.elapsed_time(b))
+        return float(np.mean(out))
+
+    timed(multi, 1)
+    m_ms = timed(multi, max(1, args.steps))
+    timed(singles, 1)
+    s_ms = timed(singles, max(1, min(args.steps, 2)))
+    edges = sum(int(r.edges_traversed) for r in res)
+    levels = int(res[0].top_down_steps + res[0].bottom_up_steps)
+    del dist_d
+    return {"workload": f"rmat{args.scale}_bfs_{MS_SOURCES}_sources", "sources": MS_SOURCES,
+            "multisource_ms": round(m_ms, 3), "per_source_ms": round(s_ms, 3),
+            "speedup_vs_per_source": round(s_ms / m_ms, 2),
+            "multisource_gteps": round(edges / (m_ms * 1e-3) / 1e9, 3),
+            "per_source_gteps": round(edges / (s_ms * 1e-3) / 1e9, 3),
+            "levels": levels, "push_levels": int(res[0].top_down_steps), "pull_levels": int(res[0].bottom_up_steps),
+            "edges_traversed": edges}
 
 
 def run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp):

@@ -16,6 +16,7 @@ from .graph import (  # noqa: F401
     PPRAdjointStats,
     PPRStats,
     SSSPStats,
+    bfs_multisource,
     breadth_first_search,
     connected_components,
     csr_build,

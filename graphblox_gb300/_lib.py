@@ -56,6 +56,7 @@ SIGNATURES = {
     "gbx_bfs": (C.c_int, [vp, u32, C.c_int, vp, vp, C.POINTER(BfsResult), vp]),
     "gbx_pagerank_pull": (C.c_int, [vp, u32, C.c_double, vp, C.POINTER(PrResult), vp]),
     "gbx_pagerank_pull_noalloc": (C.c_int, [u32, vp, vp, vp, u32, C.c_double, vp, C.POINTER(PrResult), vp]),
+    "gbx_bfs_multisource": (C.c_int, [vp, u32, vp, vp, vp, vp]),
     "gbx_batch_create": (C.c_int, [C.POINTER(vp), u32, vp, vp, vp, vp, vp, vp]),
     "gbx_batch_destroy": (C.c_int, [vp]),
     "gbx_batch_info": (C.c_int, [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)]),

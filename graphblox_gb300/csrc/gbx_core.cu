@@ -324,6 +324,8 @@ int gbx_graph_destroy(gbx_graph *g) {
     cudaFree(g->low_count);
     gbx_free_tc_plan(g->tc_plan);
     gbx_free_ppr_cache(g->ppr);
+    gbx_free_ms_plan(g->ms_plan);
+    gbx_free_pr_cache(g->pr_cache);
     free_plan(g->plan_fwd);
     free_plan(g->plan_inv);
     cudaSetDevice(prev);

@@ -219,6 +219,10 @@ struct gbx_graph {
     struct gbx_tc_plan *tc_plan = nullptr;
     // personalised PageRank: in-edge order and chunk tables (gbx_ppr.cu)
     struct gbx_ppr_cache *ppr = nullptr;
+    // multi-source BFS: heavy pull-row chunks (gbx_msbfs.cu)
+    struct gbx_ms_plan *ms_plan = nullptr;
+    // PageRank working memory and captured iteration loop (gbx_pagerank.cu)
+    struct gbx_pr_cache *pr_cache = nullptr;
 
     bool has_inverse() const { return in_offsets != nullptr; }
     // CSR used by pull-direction kernels (reference: inverse when DIRECTED)
@@ -230,6 +234,8 @@ struct gbx_graph {
 
 void gbx_free_tc_plan(struct gbx_tc_plan *p);
 void gbx_free_ppr_cache(struct gbx_ppr_cache *c);
+void gbx_free_ms_plan(struct gbx_ms_plan *p);
+void gbx_free_pr_cache(struct gbx_pr_cache *c);
 
 namespace gbx {
 // plan for the pull CSR of g (built on first use, cached on the graph)

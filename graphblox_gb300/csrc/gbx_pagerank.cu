@@ -12,6 +12,10 @@
 // `it` returns immediately when iteration it-1 left no active vertex, which
 // reproduces the reference's early exit (stats->iterations = the index of the
 // iteration with no active vertex). A final kernel divides by N (:344-350).
+// The loop (state reset, initial ranks, the iterations) is captured once per
+// graph and (max_iterations, epsilon) as a CUDA graph on working memory kept
+// with the graph, and replayed by every later call: one graph launch and the
+// finishing kernel per call.
 #include <algorithm>
 
 #include "gbx_gather.cuh"
@@ -114,9 +118,111 @@ __global__ void pr_finish_kernel(const float *r0, const float *r1, const PrIterS
     }
 }
 
+// Enqueue the iteration loop: state reset, initial ranks, max_it iterations.
+static int pr_enqueue_loop(gbx_graph *g, const gbx_gather_plan &plan, uint32_t max_it, double epsilon, float *rbuf,
+                           float *cbuf, PrIterState *st, cudaStream_t s, uint32_t *kernels) {
+    const uint32_t V = g->V;
+    float *r[2] = {rbuf, rbuf + V};
+    float *c[2] = {cbuf, cbuf + V};
+    GBX_CUDA(cudaMemsetAsync(st, 0, sizeof(PrIterState) * (max_it ? max_it : 1), s));
+    const int grid = (int)std::min<uint64_t>((V + 255) / 256, (uint64_t)num_sms() * 8);
+    pr_init_kernel<<<grid, 256, 0, s>>>(r[0], c[0], g->out_degree, V);
+    GBX_LAUNCH_CHECK();
+    const GatherGeometry geo = gather_geometry(plan);
+    const double inv_n = 1.0 / (double)V;
+    for (uint32_t it = 0; it < max_it; ++it) {
+        const int a = it & 1, b = a ^ 1;
+        PrTerm term{g->pull_src(), c[a]};
+        // with epsilon = 0 every vertex stays active, so only the last
+        // iteration's residual (reported as error_total) is reduced
+        const bool reduce = epsilon > 0.0 || it + 1 == max_it;
+        PrEpi epi{r[a], r[b], c[b], g->out_degree, st + it, epsilon, inv_n, 0.0, 0u, reduce};
+        pr_iteration_kernel<PrTerm, PrEpi><<<gather_grid(geo), kGatherThreads, 0, s>>>(
+            g->pull_offsets(), V, plan, geo, term, epi, (it && epsilon > 0.0) ? st + it - 1 : nullptr);
+        GBX_LAUNCH_CHECK();
+    }
+    *kernels = 1 + max_it;
+    return GBX_OK;
+}
+
 }  // namespace gbx
 
+// Per-graph PageRank working memory and the iteration loop captured as a CUDA
+// graph (re-captured when max_iterations or epsilon change). Calls on one
+// graph object are serialised by the caller, as for every other entry point.
+struct gbx_pr_cache {
+    float *rbuf = nullptr, *cbuf = nullptr;  // 2V each: ping-pong ranks / contributions
+    gbx::PrIterState *st = nullptr;
+    gbx_pr_result *res = nullptr;
+    uint32_t cap = 0;  // slots in st
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint32_t key_it = 0, kernels = 0;
+    double key_eps = -1.0;
+};
+
+void gbx_free_pr_cache(gbx_pr_cache *c) {
+    if (!c) return;
+    if (c->exec) cudaGraphExecDestroy(c->exec);
+    if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
+    cudaFree(c->rbuf);
+    cudaFree(c->cbuf);
+    cudaFree(c->st);
+    cudaFree(c->res);
+    delete c;
+}
+
 using namespace gbx;
+
+namespace {
+
+int pr_cache(gbx_graph *g, uint32_t max_it, gbx_pr_cache **out) {
+    gbx_pr_cache *c = g->pr_cache;
+    if (!c) {
+        c = new gbx_pr_cache();
+        g->pr_cache = c;
+        GBX_CUDA(cudaMalloc(&c->rbuf, sizeof(float) * 2 * (size_t)g->V));
+        GBX_CUDA(cudaMalloc(&c->cbuf, sizeof(float) * 2 * (size_t)g->V));
+        GBX_CUDA(cudaMalloc(&c->res, sizeof(gbx_pr_result)));
+        GBX_CUDA(cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking));
+    }
+    if (c->cap < std::max(max_it, 1u)) {
+        if (c->exec) cudaGraphExecDestroy(c->exec);
+        c->exec = nullptr;
+        cudaFree(c->st);
+        c->st = nullptr;
+        c->cap = std::max(max_it, 64u);
+        GBX_CUDA(cudaMalloc(&c->st, sizeof(PrIterState) * c->cap));
+    }
+    *out = c;
+    return GBX_OK;
+}
+
+// (Re)capture the loop on the cache's own stream.
+int pr_capture(gbx_graph *g, const gbx_gather_plan &plan, uint32_t max_it, double epsilon, gbx_pr_cache *c) {
+    if (c->exec && c->key_it == max_it && c->key_eps == epsilon) return GBX_OK;
+    if (c->exec) cudaGraphExecDestroy(c->exec);
+    c->exec = nullptr;
+    GBX_CUDA(cudaStreamBeginCapture(c->cap_stream, cudaStreamCaptureModeThreadLocal));
+    uint32_t kernels = 0;
+    const int st = pr_enqueue_loop(g, plan, max_it, epsilon, c->rbuf, c->cbuf, c->st, c->cap_stream, &kernels);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(c->cap_stream, &graph);
+    if (st != GBX_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return st;
+    }
+    GBX_CUDA(e);
+    const cudaError_t ei = cudaGraphInstantiate(&c->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    GBX_CUDA(ei);
+    c->key_it = max_it;
+    c->key_eps = epsilon;
+    c->kernels = kernels;
+    return GBX_OK;
+}
+
+}  // namespace
 
 extern "C" int gbx_pagerank_pull(gbx_graph *g, uint32_t max_iterations, double epsilon,
                                  float *ranks, gbx_pr_result *result, void *stream) {
@@ -130,38 +236,20 @@ extern "C" int gbx_pagerank_pull(gbx_graph *g, uint32_t max_iterations, double e
     GBX_TRY(get_pull_plan(g, s, &plan));
     OutArray<float> out;
     GBX_TRY(out.bind(ranks, V, s));
-    DevBuf<float> rbuf, cbuf;
-    DevBuf<PrIterState> st;
-    DevBuf<gbx_pr_result> res;
-    GBX_TRY(rbuf.alloc((size_t)2 * V, s));
-    GBX_TRY(cbuf.alloc((size_t)2 * V, s));
-    GBX_TRY(st.alloc(max_iterations ? max_iterations : 1, s));
-    GBX_TRY(res.alloc(1, s));
-    GBX_CUDA(cudaMemsetAsync(st.p, 0, sizeof(PrIterState) * (max_iterations ? max_iterations : 1), s));
-    float *r[2] = {rbuf.p, rbuf.p + V};
-    float *c[2] = {cbuf.p, cbuf.p + V};
-    int grid = (int)std::min<uint64_t>((V + 255) / 256, (uint64_t)num_sms() * 8);
-    pr_init_kernel<<<grid, 256, 0, s>>>(r[0], c[0], g->out_degree, V);
-    GBX_LAUNCH_CHECK();
-    GatherGeometry geo = gather_geometry(*plan);
-    const double inv_n = 1.0 / (double)V;
-    for (uint32_t it = 0; it < max_iterations; ++it) {
-        int a = it & 1, b = a ^ 1;
-        PrTerm term{g->pull_src(), c[a]};
-        // with epsilon = 0 every vertex stays active, so only the last
-        // iteration's residual (reported as error_total) is reduced
-        const bool reduce = epsilon > 0.0 || it + 1 == max_iterations;
-        PrEpi epi{r[a], r[b], c[b], g->out_degree, st.p + it, epsilon, inv_n, 0.0, 0u, reduce};
-        pr_iteration_kernel<PrTerm, PrEpi><<<gather_grid(geo), kGatherThreads, 0, s>>>(
-            g->pull_offsets(), V, *plan, geo, term, epi, (it && epsilon > 0.0) ? st.p + it - 1 : nullptr);
-        GBX_LAUNCH_CHECK();
-    }
-    pr_finish_kernel<<<grid, 256, 0, s>>>(r[0], r[1], st.p, max_iterations, epsilon > 0.0 ? 1u : 0u, V, out.d,
-                                          nullptr, res.p);
+    gbx_pr_cache *c = nullptr;
+    GBX_TRY(pr_cache(g, max_iterations, &c));
+    GBX_TRY(pr_capture(g, *plan, max_iterations, epsilon, c));
+    GBX_CUDA(cudaGraphLaunch(c->exec, s));
+    for (uint32_t k = 0; k < c->kernels; ++k) note_launch();
+    float *r[2] = {c->rbuf, c->rbuf + V};
+    const int grid = (int)std::min<uint64_t>((V + 255) / 256, (uint64_t)num_sms() * 8);
+    gbx_pr_result *res = c->res;
+    pr_finish_kernel<<<grid, 256, 0, s>>>(r[0], r[1], c->st, max_iterations, epsilon > 0.0 ? 1u : 0u, V, out.d,
+                                          nullptr, res);
     GBX_LAUNCH_CHECK();
     GBX_TRY(out.finish(s));
     gbx_pr_result hres;
-    GBX_CUDA(cudaMemcpyAsync(&hres, res.p, sizeof(hres), cudaMemcpyDeviceToHost, s));
+    GBX_CUDA(cudaMemcpyAsync(&hres, res, sizeof(hres), cudaMemcpyDeviceToHost, s));
     GBX_CUDA(cudaStreamSynchronize(s));
     if (result) *result = hres;
     return GBX_OK;

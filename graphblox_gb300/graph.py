@@ -573,6 +573,21 @@ class GraphBatch:
         self.close()
 
 
+def bfs_multisource(dg: DeviceGraph, sources, distances=None, stream=None, map_source: bool = True):
+    """gbx_bfs_multisource: up to 256 BFS runs in one bitmask sweep. Returns
+    (distances [V, S] vertex-major, per-source results dict); sources are
+    mapped through the graph's label array like breadth_first_search."""
+    srcs = [(_map_source(dg, int(s)) if map_source else int(s)) for s in np.asarray(sources).ravel()]
+    S = len(srcs)
+    src = np.asarray(srcs, np.uint32)
+    if distances is None:
+        distances = np.zeros((dg.num_vertices, S), np.uint32)
+    res = (BfsResult * S)()
+    call("gbx_bfs_multisource", dg.handle, S, _ptr(src), _ptr(distances), res, stream)
+    return distances, _results_dict(res, ("processed_nodes", "iteration", "depth", "top_down_steps",
+                                          "bottom_up_steps", "edges_traversed"))
+
+
 def generate_rmat_batch(num_graphs: int = 2048, seed: int = 1, scale_lo: float = 8.0, scale_hi: float = 15.0,
                         ef_lo: float = 4.0, ef_hi: float = 32.0):
     """Edge lists of `num_graphs` RMAT graphs (a/b/c = .57/.19/.19): scale

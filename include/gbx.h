@@ -165,6 +165,17 @@ int gbx_pagerank_pull_noalloc(uint32_t num_vertices, const uint32_t *pull_offset
                               uint32_t max_iterations, double epsilon, float *ranks,
                               gbx_pr_result *result, void *stream);
 
+/* Multi-source BFS: num_sources (1..256) BFS runs on one graph in one
+ * level-synchronous sweep over per-vertex source bitmasks. No counterpart in
+ * the reference as a batch; per source the results equal gbx_bfs from that
+ * source (BFS.c:103-127). distances is vertex-major, num_vertices *
+ * num_sources entries: distances[v * num_sources + i] = level of v from
+ * sources[i] (0 for the source itself and for unreached vertices). results
+ * (may be NULL) has one entry per source; top_down_steps / bottom_up_steps
+ * count the shared push / pull levels. Sources may repeat. */
+int gbx_bfs_multisource(gbx_graph *g, uint32_t num_sources, const uint32_t *sources,
+                        uint32_t *distances, gbx_bfs_result *results, void *stream);
+
 /* ---- batches of graphs -----------------------------------------------------
  * No counterpart in the reference as a batch: every graph of a batch gets
  * the results gbx_bfs (mode 2) / gbx_pagerank_pull give it alone, i.e. the
