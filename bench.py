@@ -384,8 +384,9 @@ def run_ppr(args, torch, gbx, dev, stream, peak):
     over `steps` calls after one untimed call of each, and (fwd+adj)/fwd.
     Algorithmic bytes per sweep, K columns: 4(V+1) offsets + 8E (index +
     weight) + 4K*E (neighbour-row gather) + 8K*V (row read + write)."""
-    V, E, K = 1 << PPR_SCALE, PPR_EDGES, PPR_K
-    s, d = gbx.generate_rmat(PPR_SCALE, E, seed=SEED)
+    scale = args.ppr_scale
+    V, E, K = 1 << scale, PPR_EDGES >> (PPR_SCALE - scale), PPR_K
+    s, d = gbx.generate_rmat(scale, E, seed=SEED)
     order = np.argsort(s, kind="stable")
     dst = np.ascontiguousarray(d[order])
     off = np.zeros(V + 1, np.int64)
@@ -429,7 +430,7 @@ def run_ppr(args, torch, gbx, dev, stream, peak):
     fi, ai = info["fwd"].iterations, info["adj"].iterations
     gbs_f = fi * sweep_bytes / (f_ms * 1e-3) / 1e9
     gbs_a = ai * sweep_bytes / (a_ms * 1e-3) / 1e9
-    return {"workload": f"rmat{PPR_SCALE}_ppr_k{K}", "num_vertices": V, "num_edges": E, "K": K,
+    return {"workload": f"rmat{scale}_ppr_k{K}", "num_vertices": V, "num_edges": E, "K": K,
             "damping": PPR_D, "tol_l1": PPR_TOL, "forward_ms": round(f_ms, 3), "adjoint_ms": round(a_ms, 3),
             "fwd_plus_adjoint_over_fwd": round((f_ms + a_ms) / f_ms, 3),
             "forward_sweeps": fi, "adjoint_sweeps": ai, "loss": info["adj"].loss,
@@ -447,7 +448,7 @@ def run_batched(args, torch, gbx, _lib, dev, stream, peak):
     gbx_pagerank_pull called once per graph on resident single graphs, the
     same device output arrays. Both timed with CUDA events, mean of `steps`."""
     t0 = time.time()
-    gl = gbx.generate_rmat_batch(BATCH_GRAPHS, seed=SEED)
+    gl = gbx.generate_rmat_batch(args.batch_graphs, seed=SEED)
     packed = gbx.pack_graphs(gl)
     del gl
     G = packed.num_graphs
@@ -767,6 +768,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-ppr", action="store_true", help="skip the personalised PageRank forward/adjoint section")
     ap.add_argument("--no-batched", action="store_true", help="skip the 2,048-graph batched section")
+    ap.add_argument("--ppr-scale", type=int, default=PPR_SCALE, help="RMAT scale of the PPR section (20 is the workload)")
+    ap.add_argument("--batch-graphs", type=int, default=BATCH_GRAPHS, help="graphs in the batched section (2048)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--tuning", default="", help="fixed knobs instead of autotuning, e.g. bfs_alpha=15,sssp_delta=4096")
     ap.add_argument("--traffic", type=float, default=None,

@@ -50,7 +50,7 @@ constexpr int kBbWarps = kBbThreads / 32;
 constexpr uint32_t kBbWordsCap = 4096;  // bitmap words in shared memory: V <= 131072
 constexpr int kBpThreads = 1024;
 constexpr int kBpWarps = kBpThreads / 32;
-constexpr uint32_t kBpSmemV = 53248;  // contributions in shared memory: V <= 53248 (208 KiB)
+constexpr uint32_t kBpSmemV = 49152;  // contributions in shared memory: V <= 49152 (192 KiB)
 
 __device__ __forceinline__ uint32_t bb_next_graph(uint32_t *cursor, uint32_t G, const uint32_t *order,
                                                   uint32_t *s_slot) {
@@ -278,11 +278,68 @@ struct BpArgs {
     gbx_pr_result *res;
 };
 
-__global__ void __launch_bounds__(kBpThreads, 1) pr_batched_kernel(BpArgs a) {
-    extern __shared__ float s_contrib[];
-    __shared__ uint32_t s_slot, s_active;
-    __shared__ double s_err;
+// Shared memory of one PageRank CTA (dynamic): contributions, then the
+// partial sums of heavy-row pieces, then the heavy-row table.
+constexpr uint32_t kBpHeavyMax = 1024;                // heavy rows per graph
+constexpr uint32_t kBpSlots = 4096 + kBpHeavyMax;     // piece partials
+constexpr uint32_t kBpHeavyMin = 512;                 // in-degree above which a row is split
+constexpr size_t kBpSmemBytes = (size_t)kBpSmemV * 4 + (size_t)kBpSlots * 4 + (size_t)(2 * kBpHeavyMax + 1) * 4;
+
+__device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
+    const float y = __fsub_rn(x, comp);
+    const float t = __fadd_rn(sum, y);
+    comp = __fsub_rn(__fsub_rn(t, sum), y);
+    sum = t;
+}
+
+// Exclusive scan of one value per thread over the block (blockDim.x = kBpThreads);
+// returns the thread's prefix, *total the sum. Uses s_tmp[32].
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t x, uint32_t *s_tmp, uint32_t *total) {
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= (uint32_t)o) incl += t;
+    }
+    __syncthreads();
+    if (lane == 31) s_tmp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < kBpWarps ? s_tmp[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            if (lane >= (uint32_t)o) w += t;
+        }
+        s_tmp[lane] = w;  // inclusive warp totals
+    }
+    __syncthreads();
+    const uint32_t before = warp ? s_tmp[warp - 1] : 0u;
+    *total = s_tmp[kBpWarps - 1];
+    return before + incl - x;
+}
+
+// Rows of one graph, per iteration, as tasks dealt to warps by a
+// shared-memory counter (so a slow task does not hold a fixed share):
+//   pieces  kBpHeavyMin..-edge slices of the heavy rows (in-degree > T); a
+//           warp sums one with per-lane Kahan and a warp reduction, and the
+//           partial goes to its slot;
+//   units   32 consecutive rows: light rows (<= 32 in-edges) one lane each,
+//           four index loads in flight, medium rows by the whole warp with
+//           per-lane Kahan; heavy rows are skipped here.
+// After the barrier one thread per heavy row adds its pieces' partials in
+// piece order. Every sum has a fixed order, so ranks are deterministic.
+__global__ void __launch_bounds__(kBpThreads, 1) pr_batched_kernel(BpArgs a) {
+    extern __shared__ float s_mem[];
+    float *s_contrib = s_mem;
+    float *s_part = s_mem + kBpSmemV;
+    uint32_t *s_hrow = reinterpret_cast<uint32_t *>(s_part + kBpSlots);
+    uint32_t *s_hfirst = s_hrow + kBpHeavyMax;
+    __shared__ uint32_t s_slot, s_active, s_task, s_cnt, s_tmp[32];
+    __shared__ unsigned long long s_hedges;
+    __shared__ double s_err;
+    const uint32_t lane = threadIdx.x & 31;
     const float damp = 0.85f;
     const float base = 1.0f - 0.85f;
     const bool can_stop = a.epsilon > 0.0;
@@ -295,6 +352,54 @@ __global__ void __launch_bounds__(kBpThreads, 1) pr_batched_kernel(BpArgs a) {
         const uint32_t *poff = a.poff + vb;
         float *rc = a.ranks + vb, *rn = a.rother + vb;
         const double inv_n = 1.0 / (double)Vg;
+        // heavy rows: the smallest threshold T >= kBpHeavyMin with at most
+        // kBpHeavyMax rows above it
+        uint32_t T = kBpHeavyMin;
+        for (;;) {
+            if (threadIdx.x == 0) {
+                s_cnt = 0;
+                s_hedges = 0;
+            }
+            __syncthreads();
+            uint32_t c = 0;
+            unsigned long long he = 0;
+            for (uint32_t v = threadIdx.x; v < Vg; v += blockDim.x) {
+                const uint32_t d = poff[v + 1] - poff[v];
+                if (d > T) {
+                    ++c;
+                    he += d;
+                }
+            }
+            c = warp_sum(c);
+            he = warp_sum(he);
+            if (lane == 0 && c) {
+                atomicAdd(&s_cnt, c);
+                atomicAdd(&s_hedges, he);
+            }
+            __syncthreads();
+            if (s_cnt <= kBpHeavyMax) break;
+            T *= 2;
+            __syncthreads();
+        }
+        const uint32_t nh = s_cnt;
+        // piece length: a multiple of 32 that keeps the pieces within the slots
+        const unsigned long long want = (s_hedges + (kBpSlots - kBpHeavyMax) - 1) / (kBpSlots - kBpHeavyMax);
+        const uint32_t P = (uint32_t)max(512ull, (want + 31) / 32 * 32);
+        __syncthreads();
+        if (threadIdx.x == 0) s_cnt = 0;
+        __syncthreads();
+        for (uint32_t v = threadIdx.x; v < Vg; v += blockDim.x)
+            if (poff[v + 1] - poff[v] > T) s_hrow[atomicAdd(&s_cnt, 1u)] = v;
+        __syncthreads();
+        uint32_t np = 0;
+        if (threadIdx.x < nh) {
+            const uint32_t h = s_hrow[threadIdx.x];
+            np = (poff[h + 1] - poff[h] + P - 1) / P;
+        }
+        uint32_t n_pieces = 0;
+        const uint32_t first = block_exclusive_scan(np, s_tmp, &n_pieces);
+        if (threadIdx.x < nh) s_hfirst[threadIdx.x] = first;
+        if (threadIdx.x == 0) s_hfirst[nh] = n_pieces;
         for (uint32_t v = threadIdx.x; v < Vg; v += blockDim.x) {
             rc[v] = base;
             const uint32_t d = off[v + 1] - off[v];
@@ -303,48 +408,86 @@ __global__ void __launch_bounds__(kBpThreads, 1) pr_batched_kernel(BpArgs a) {
         if (threadIdx.x == 0) {
             s_active = 0;
             s_err = 0.0;
+            s_task = 0;
         }
         __syncthreads();
+        const uint32_t units = (Vg + 31) / 32;
+        const uint32_t n_tasks = n_pieces + units;
         uint32_t k = a.max_it, executed = 0, active_last = 0;
         double err_last = 0.0;
         for (uint32_t it = 0; it < a.max_it; ++it) {
             const bool reduce = can_stop || it + 1 == a.max_it;
             double err = 0.0;
             uint32_t active = 0;
-            const uint32_t units = (Vg + 31) / 32;
-            for (uint32_t un = warp; un < units; un += kBpWarps) {
-                const uint32_t v = un * 32 + lane;
+            for (;;) {
+                uint32_t t = 0;
+                if (lane == 0) t = atomicAdd(&s_task, 1u);
+                t = __shfl_sync(0xFFFFFFFFu, t, 0);
+                if (t >= n_tasks) break;
+                if (t < n_pieces) {
+                    uint32_t lo = 0, hi = nh - 1;  // last heavy row with first piece <= t
+                    while (lo < hi) {
+                        const uint32_t mid = (lo + hi + 1) >> 1;
+                        if (s_hfirst[mid] <= t) lo = mid; else hi = mid - 1;
+                    }
+                    const uint32_t h = s_hrow[lo];
+                    const uint32_t pb = poff[h] + (t - s_hfirst[lo]) * P;
+                    const uint32_t pe = min(pb + P, poff[h + 1]);
+                    float s = 0.f, c = 0.f;
+                    for (uint32_t j = pb + lane; j < pe; j += 32) kahan_add(s, c, contrib[__ldg(a.psrc + j)]);
+                    s = warp_sum(s);
+                    if (lane == 0) s_part[t] = s;
+                    continue;
+                }
+                const uint32_t v = (t - n_pieces) * 32 + lane;
                 const bool ok = v < Vg;
                 const uint32_t b = ok ? poff[v] : 0, e = ok ? poff[v + 1] : 0;
+                const uint32_t d = e - b;
                 float sum = 0.f;
-                const bool heavy = e - b > 32;
-                if (!heavy) {
-                    for (uint32_t j = b; j < e; ++j) sum += contrib[__ldg(a.psrc + j)];
-                }
-                uint32_t hv = __ballot_sync(0xFFFFFFFFu, heavy);
-                while (hv) {
-                    const uint32_t kk = __ffs(hv) - 1;
-                    hv &= hv - 1;
-                    const uint32_t hb = __shfl_sync(0xFFFFFFFFu, b, kk), he = __shfl_sync(0xFFFFFFFFu, e, kk);
-                    float s = 0.f, c = 0.f;
-                    for (uint32_t j = hb + lane; j < he; j += 32) {
-                        const float y = __fsub_rn(contrib[__ldg(a.psrc + j)], c);
-                        const float t = __fadd_rn(s, y);
-                        c = __fsub_rn(__fsub_rn(t, s), y);
-                        s = t;
+                if (d <= 32) {
+                    uint32_t j = b;
+                    for (; j + 4 <= e; j += 4) {
+                        const uint32_t u0 = __ldg(a.psrc + j), u1 = __ldg(a.psrc + j + 1);
+                        const uint32_t u2 = __ldg(a.psrc + j + 2), u3 = __ldg(a.psrc + j + 3);
+                        const float x0 = contrib[u0], x1 = contrib[u1], x2 = contrib[u2], x3 = contrib[u3];
+                        sum = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(sum, x0), x1), x2), x3);
                     }
+                    for (; j < e; ++j) sum = __fadd_rn(sum, contrib[__ldg(a.psrc + j)]);
+                }
+                uint32_t mv = __ballot_sync(0xFFFFFFFFu, d > 32 && d <= T);
+                while (mv) {
+                    const uint32_t kk = __ffs(mv) - 1;
+                    mv &= mv - 1;
+                    const uint32_t hb = __shfl_sync(0xFFFFFFFFu, b, kk), hd = __shfl_sync(0xFFFFFFFFu, e, kk);
+                    float s = 0.f, c = 0.f;
+                    for (uint32_t j = hb + lane; j < hd; j += 32) kahan_add(s, c, contrib[__ldg(a.psrc + j)]);
                     s = warp_sum(s);
                     if (lane == kk) sum = s;
                 }
-                if (ok) {
+                if (ok && d <= T) {
                     const float next = __fadd_rn(base, __fmul_rn(damp, sum));
                     const float prev = rc[v];
                     rn[v] = next;
                     if (reduce) {
-                        const double d = (double)fabsf(__fsub_rn(next, prev));
-                        err += d * inv_n;
-                        active += d >= a.epsilon ? 1u : 0u;
+                        const double dd = (double)fabsf(__fsub_rn(next, prev));
+                        err += dd * inv_n;
+                        active += dd >= a.epsilon ? 1u : 0u;
                     }
+                }
+            }
+            __syncthreads();
+            // heavy rows: pieces in order
+            if (threadIdx.x < nh) {
+                const uint32_t h = s_hrow[threadIdx.x];
+                float s = 0.f, c = 0.f;
+                for (uint32_t p = s_hfirst[threadIdx.x]; p < s_hfirst[threadIdx.x + 1]; ++p) kahan_add(s, c, s_part[p]);
+                const float next = __fadd_rn(base, __fmul_rn(damp, s));
+                const float prev = rc[h];
+                rn[h] = next;
+                if (reduce) {
+                    const double dd = (double)fabsf(__fsub_rn(next, prev));
+                    err += dd * inv_n;
+                    active += dd >= a.epsilon ? 1u : 0u;
                 }
             }
             if (reduce) {
@@ -363,6 +506,7 @@ __global__ void __launch_bounds__(kBpThreads, 1) pr_batched_kernel(BpArgs a) {
             }
             const uint32_t act = s_active;
             const double er = s_err;
+            if (threadIdx.x == 0) s_task = 0;
             __syncthreads();
             if (threadIdx.x == 0) {
                 s_active = 0;
@@ -620,7 +764,7 @@ extern "C" int gbx_pr_batched(gbx_batch *b, uint32_t max_iterations, double epsi
     GBX_TRY(other.alloc(b->V, s));
     GBX_TRY(cursor.alloc(1, s));
     GBX_CUDA(cudaMemsetAsync(cursor.p, 0, 4, s));
-    const size_t smem = (size_t)kBpSmemV * sizeof(float);
+    const size_t smem = kBpSmemBytes;
     GBX_CUDA(cudaFuncSetAttribute(pr_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0;
     GBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pr_batched_kernel, kBpThreads, smem));

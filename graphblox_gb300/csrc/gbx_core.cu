@@ -170,7 +170,9 @@ static int fill_direction(uint32_t V, uint32_t E, const uint32_t *edges_idx, con
                           uint32_t *max_deg, cudaStream_t s) {
     GBX_TRY(dmalloc((void **)d_off, (size_t)(V + 1) * 4));
     GBX_TRY(dmalloc((void **)d_deg, (size_t)V * 4));
-    GBX_TRY(dmalloc((void **)d_ids, (size_t)E * 4));
+    // four ids of zeroed padding: kernels read rows as aligned 16-byte quads
+    GBX_TRY(dmalloc((void **)d_ids, ((size_t)E + 4) * 4));
+    GBX_CUDA(cudaMemsetAsync(*d_ids + E, 0, 16, s));
     if (w) GBX_TRY(dmalloc((void **)d_w, (size_t)E * 4));
     DevBuf<unsigned> bad;
     GBX_TRY(bad.alloc(2, s));

@@ -158,6 +158,64 @@ __device__ __forceinline__ unsigned long long count_flat(const uint32_t *__restr
     return count;
 }
 
+// Same count with 16-byte loads: each lane's list [base, base+len) is read as
+// the aligned quads that cover it (the neighbour array is 16-byte aligned and
+// padded by four ids), two quads per lane per step, and the elements of a
+// quad outside the list are masked. Four times fewer load instructions and
+// twice the bytes in flight of count_flat.
+template <class Member>
+__device__ __forceinline__ unsigned long long count_flat4(const uint32_t *__restrict__ dest, uint32_t base,
+                                                         uint32_t len, uint32_t *s_pre, uint32_t *s_base,
+                                                         uint32_t *s_end, const Member &member) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t q0 = base >> 2;
+    const uint32_t nq = len ? ((base + len + 3) >> 2) - q0 : 0u;
+    uint32_t incl = nq;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += t;
+    }
+    s_pre[lane] = incl - nq;
+    s_base[lane] = base;
+    s_end[lane] = base + len;
+    if (lane == 31) s_pre[32] = incl;
+    __syncwarp();
+    const uint32_t tot = s_pre[32];
+    const uint4 *d4 = reinterpret_cast<const uint4 *>(dest);
+    unsigned long long count = 0;
+    uint32_t k = 0;  // owner lane of this lane's current quad, advanced monotonically
+    for (uint32_t i0 = 0; i0 < tot; i0 += 64) {
+        uint4 w[2];
+        uint32_t e0[2], lo[2], hi[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const uint32_t i = i0 + q * 32 + lane;
+            lo[q] = hi[q] = e0[q] = 0;
+            w[q] = make_uint4(0u, 0u, 0u, 0u);
+            if (i < tot) {
+                while (s_pre[k + 1] <= i) ++k;
+                const uint32_t qa = (s_base[k] >> 2) + (i - s_pre[k]);
+                w[q] = __ldg(d4 + qa);
+                e0[q] = qa * 4;
+                lo[q] = s_base[k];
+                hi[q] = s_end[k];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const uint32_t x[4] = {w[q].x, w[q].y, w[q].z, w[q].w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const uint32_t e = e0[q] + j;
+                if (e >= lo[q] && e < hi[q] && member(x[j])) count++;
+            }
+        }
+    }
+    __syncwarp();
+    return count;
+}
+
 struct HashMember {
     const uint32_t *table;
     uint32_t mask;
@@ -175,7 +233,7 @@ struct SortedMember {
 __device__ __forceinline__ unsigned long long v_unit(const uint32_t *__restrict__ off,
                                                     const uint32_t *__restrict__ dest, uint32_t v, uint32_t pv,
                                                     uint32_t ub, uint32_t ue, uint32_t *table, uint32_t *s_pre,
-                                                    uint32_t *s_base) {
+                                                    uint32_t *s_base, uint32_t *s_end) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t *nv = dest + __ldg(off + v);
     unsigned long long count = 0;
@@ -193,7 +251,7 @@ __device__ __forceinline__ unsigned long long v_unit(const uint32_t *__restrict_
                 base = __ldg(off + u);
                 len = count_le(dest + base, __ldg(off + u + 1) - base, v);
             }
-            count += count_flat(dest, base, len, s_pre, s_base, m);
+            count += count_flat4(dest, base, len, s_pre, s_base, s_end, m);
         }
         __syncwarp();
     } else {
@@ -205,7 +263,7 @@ __device__ __forceinline__ unsigned long long v_unit(const uint32_t *__restrict_
                 base = __ldg(off + u);
                 len = count_le(dest + base, __ldg(off + u + 1) - base, v);
             }
-            count += count_flat(dest, base, len, s_pre, s_base, m);
+            count += count_flat4(dest, base, len, s_pre, s_base, s_end, m);
         }
     }
     return count;
@@ -223,6 +281,7 @@ __global__ void __launch_bounds__(kTcThreads)
     __shared__ uint32_t tables[kTcWarps][kTcWarpSlots];
     __shared__ uint32_t s_pre[kTcWarps][33];
     __shared__ uint32_t s_base[kTcWarps][32];
+    __shared__ uint32_t s_end[kTcWarps][32];
     __shared__ unsigned long long sred[32];
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     unsigned long long count = 0;
@@ -240,7 +299,8 @@ __global__ void __launch_bounds__(kTcThreads)
         const TcBig bg = big[lo];
         const uint32_t ub = bg.ub + (unit - bg.first_unit) * kUpperChunk;
         const uint32_t ue = min(ub + kUpperChunk, bg.ue);
-        count += v_unit(off, dest, bg.v, __ldg(low + bg.v), ub, ue, tables[wid], s_pre[wid], s_base[wid]);
+        count += v_unit(off, dest, bg.v, __ldg(low + bg.v), ub, ue, tables[wid], s_pre[wid], s_base[wid],
+                        s_end[wid]);
     }
     // the other v's: one warp each
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -252,7 +312,7 @@ __global__ void __launch_bounds__(kTcThreads)
         const uint32_t b = __ldg(off + v), d = __ldg(off + v + 1) - b;
         const uint32_t ub = count_lt(dest + b, d, v);
         if (ub >= d) continue;
-        count += v_unit(off, dest, v, pv, ub, d, tables[wid], s_pre[wid], s_base[wid]);
+        count += v_unit(off, dest, v, pv, ub, d, tables[wid], s_pre[wid], s_base[wid], s_end[wid]);
     }
     count = block_sum(count, sred);
     if (threadIdx.x == 0 && count) atomicAdd(total, count);
