@@ -56,6 +56,7 @@ PPR_SCALE, PPR_EDGES, PPR_K, PPR_SEEDS, PPR_TOL, PPR_D = 20, 1 << 24, 64, 32, 1e
 # batched: 2,048 RMAT graphs, BFS from 0 plus 30 PageRank iterations each
 BATCH_GRAPHS, BATCH_PR_ITERS = 2048, 30
 MS_SOURCES = 256  # multi-source bitmask BFS on the RMAT-22 graph
+C5_V, C5_MEAN = 40_000_000, 30  # scale-up: Chung-Lu 4e7 vertices, 1.2e9 edges (opt-in, --c5)
 
 
 def log(*a):
@@ -353,6 +354,14 @@ def run_gpu(args):
     if not args.no_batched and (not args.only or "batched" in args.only.split(",")):
         batched = run_batched(args, torch, gbx, _lib, dev, stream, peak)
         batched["multisource"] = run_multisource(args, torch, gbx, _lib, dg, W, dev, stream, peak)
+    c5 = None
+    if args.c5:
+        dg.close(), dgs.close(), dgr.close()
+        torch.cuda.empty_cache()
+        c5 = run_c5(args, torch, gbx, _lib, dev, stream, peak)
+        dg = gbx.DeviceGraph.from_graph_csr(g, stream=sp)
+        dgs = gbx.DeviceGraph.from_graph_csr(gs, use_weights=False, stream=sp)
+        dgr = gbx.DeviceGraph.from_graph_csr(gsr, use_weights=False, stream=sp)
     e2e = None if args.no_e2e else run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp, tuning)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -369,7 +378,7 @@ def run_gpu(args):
                    "dag_edges": e_plus, "bfs_roots": N_ROOTS, "sssp_roots": N_SSSP_ROOTS,
                    "pr_iterations": PR_ITERS, "l2": "flushed (256 MiB write) before every kernel",
                    "parallelism": "replicas" if world > 1 else "single GPU", "tuning": tuning},
-        "kernels": per, "batched": batched, "ppr_adjoint": ppr, "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk,
+        "kernels": per, "batched": batched, "ppr_adjoint": ppr, "c5": c5, "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk,
         "gpu_launches": int(launches), "wall_ms_timed_region": round(wall_ms, 3),
     }
     if rank == 0:
@@ -572,6 +581,104 @@ def run_multisource(args, torch, gbx, _lib, dg, W, dev, stream, peak):
             "per_source_gteps": round(edges / (s_ms * 1e-3) / 1e9, 3),
             "levels": levels, "push_levels": int(res[0].top_down_steps), "pull_levels": int(res[0].bottom_up_steps),
             "edges_traversed": edges}
+
+
+def run_c5(args, torch, gbx, _lib, dev, stream, peak):
+    """The scale-up configuration (opt-in, --c5): a Chung-Lu graph of 4e7
+    vertices, mean out-degree 30 (1.2e9 edges, kept as generated), out-degree
+    power-law exponent 2.1, 70% of edges inside 4,096-id windows, generated
+    and built on the GPU. Timed with CUDA events: BFS from 4 seeded roots,
+    pull PageRank to epsilon 1e-6, Afforest CC on the symmetrised graph
+    (2.4e9 edges), one degree reordering of the edge list."""
+    import ctypes as C
+
+    sp = stream.cuda_stream
+    V, E = C5_V, C5_V * C5_MEAN
+    i32 = dict(dtype=torch.int32, device=dev)
+    t0 = time.time()
+    src = torch.empty(E, **i32)
+    dst = torch.empty(E, **i32)
+    gbx.generate_chung_lu(V, E, 2.1, 4096, 0.7, SEED, src=src, dst=dst, stream=sp)
+
+    def build(a, b, symmetric=False):
+        n = E * (2 if symmetric else 1)
+        deg, idx = torch.empty(V, **i32), torch.empty(V, **i32)
+        so, do = torch.empty(n, **i32), torch.empty(n, **i32)
+        got = _lib.u32(0)
+        _lib.call("gbx_csr_build", E, a.data_ptr(), b.data_ptr(), None, int(symmetric), 0, 0, V, deg.data_ptr(),
+                  idx.data_ptr(), so.data_ptr(), do.data_ptr(), None, C.byref(got), sp)
+        return deg, idx, so, do
+
+    def create(deg, idx, dest, ideg=None, iidx=None, isrc=None, n=E):
+        h = C.c_void_p()
+        p = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+        _lib.call("gbx_graph_create_csr", C.byref(h), V, n, p(idx), p(deg), p(dest), None, p(iidx), p(ideg),
+                  p(isrc), None, sp)
+        return gbx.DeviceGraph(h.value, V, n)
+
+    deg, idx, so, do = build(src, dst)
+    ideg, iidx, _, ido = build(do, so)  # in-edges: sorted by destination, sources in the "dst" slot
+    del so
+    dg = create(deg, idx, do, ideg, iidx, ido)
+    del do, ido, ideg, iidx
+    torch.cuda.empty_cache()
+    degs = deg.cpu().numpy()
+    rng = np.random.default_rng(SEED)
+    roots = [int(r) for r in rng.choice(np.nonzero(degs)[0], 4, replace=False)]
+    log(f"c5 built in {time.time() - t0:.1f}s: V={V} E={E}")
+
+    def ev(fn):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        out = fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b), out
+
+    res = {}
+    dist_d = torch.empty(V, **i32)
+    par_d = torch.empty(V, **i32)
+    gbx.breadth_first_search(dg, roots[0], 2, distances=dist_d, parents=par_d, stream=sp, map_source=False)
+    ms, te = 0.0, 0
+    for r in roots:
+        t, st = ev(lambda: gbx.breadth_first_search(dg, r, 2, distances=dist_d, parents=par_d, stream=sp,
+                                                    map_source=False))
+        ms += t
+        te += st.edges_traversed
+    res["bfs"] = {"ms_per_root": round(ms / len(roots), 3), "gteps": round(te / (ms * 1e-3) / 1e9, 3),
+                  "frac": round((len(roots) * (4 * (V + 1) + 8 * V) + 4 * te) / (ms * 1e-3) / 1e9 / peak, 3)}
+    ranks = torch.empty(V, dtype=torch.float32, device=dev)
+    t, pr = ev(lambda: gbx.page_rank(dg, 1000, 1e-6, ranks=ranks, stream=sp))
+    it = pr.iterations + 1
+    res["pr"] = {"ms": round(t, 3), "iterations": pr.iterations, "gteps": round(E * it / (t * 1e-3) / 1e9, 3),
+                 "frac": round(it * (8 * E + 20 * V) / (t * 1e-3) / 1e9 / peak, 3), "epsilon": 1e-6}
+    dg.close()
+    del dist_d, par_d, ranks
+    # symmetrised graph for CC
+    sdeg, sidx, sso, sdo = build(src, dst, symmetric=True)
+    del sso
+    torch.cuda.empty_cache()
+    dgs = create(sdeg, sidx, sdo, n=2 * E)
+    del sdo
+    comp = torch.empty(V, **i32)
+    gbx.connected_components(dgs, 1, components=comp, stream=sp)
+    t, (c_out, sweeps) = ev(lambda: gbx.connected_components(dgs, 1, components=comp, stream=sp))
+    res["cc"] = {"ms": round(t, 3), "gteps": round(2 * E / (t * 1e-3) / 1e9, 3), "num_edges": 2 * E,
+                 "components": int(torch.unique(comp).numel())}
+    dgs.close()
+    del comp
+    torch.cuda.empty_cache()
+    lab, inv = torch.arange(V, **i32), torch.arange(V, **i32)
+    t, _ = ev(lambda: _lib.call("gbx_degree_reorder", V, E, src.data_ptr(), dst.data_ptr(), 1, lab.data_ptr(),
+                                inv.data_ptr(), sp))
+    res["reorder"] = {"ms": round(t, 3), "gteps": round(E / (t * 1e-3) / 1e9, 3),
+                      "frac": round((20 * E + 24 * V) / (t * 1e-3) / 1e9 / peak, 3)}
+    del src, dst, lab, inv
+    torch.cuda.empty_cache()
+    return {"workload": "chung_lu_40M_1.2B", "num_vertices": V, "num_edges": E, "exponent": 2.1, "window": 4096,
+            "local_fraction": 0.7, "offsets": "uint32 (E < 2^32)", "kernels": res}
 
 
 def run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp, tuning=None):
@@ -778,6 +885,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the 2,048-graph batched section")
     ap.add_argument("--ppr-scale", type=int, default=PPR_SCALE, help="RMAT scale of the PPR section (20 is the workload)")
     ap.add_argument("--batch-graphs", type=int, default=BATCH_GRAPHS, help="graphs in the batched section (2048)")
+    ap.add_argument("--c5", action="store_true",
+                    help="also run the Chung-Lu 4e7-vertex / 1.2e9-edge scale-up (BFS, PR to 1e-6, CC, reorder)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--tuning", default="", help="fixed knobs instead of autotuning, e.g. bfs_alpha=15,sssp_delta=4096")
     ap.add_argument("--traffic", type=float, default=None,

@@ -21,6 +21,7 @@ from .graph import (  # noqa: F401
     connected_components,
     csr_build,
     degree_reorder,
+    generate_chung_lu,
     generate_rmat,
     generate_rmat_batch,
     generate_values,

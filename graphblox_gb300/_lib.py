@@ -74,6 +74,7 @@ SIGNATURES = {
     "gbx_degree_reorder": (C.c_int, [u32, u32, vp, vp, C.c_int, vp, vp, vp]),
     "gbx_generate_rmat": (C.c_int, [u32, u64, C.c_double, C.c_double, C.c_double, u64, vp, vp]),
     "gbx_generate_values": (C.c_int, [u64, C.c_int, u32, u32, u64, vp]),
+    "gbx_generate_chung_lu": (C.c_int, [u32, u64, C.c_double, u32, C.c_double, u64, vp, vp, vp]),
 }
 
 _lib = None

@@ -573,6 +573,20 @@ class GraphBatch:
         self.close()
 
 
+def generate_chung_lu(num_vertices: int, num_edges: int, exponent: float = 2.1, window: int = 4096,
+                      local_fraction: float = 0.7, seed: int = 1, src=None, dst=None, stream=None):
+    """gbx_generate_chung_lu (on the GPU): power-law out-degrees with the given
+    exponent, local_fraction of the edges inside window-aligned id blocks.
+    src/dst may be preallocated torch CUDA tensors (else host numpy arrays)."""
+    if src is None:
+        src = np.empty(num_edges, np.uint32)
+    if dst is None:
+        dst = np.empty(num_edges, np.uint32)
+    call("gbx_generate_chung_lu", int(num_vertices), int(num_edges), float(exponent), int(window),
+         float(local_fraction), int(seed), _ptr(src), _ptr(dst), stream)
+    return src, dst
+
+
 def bfs_multisource(dg: DeviceGraph, sources, distances=None, stream=None, map_source: bool = True):
     """gbx_bfs_multisource: up to 256 BFS runs in one bitmask sweep. Returns
     (distances [V, S] vertex-major, per-source results dict); sources are

@@ -312,6 +312,17 @@ int gbx_generate_rmat(uint32_t scale, uint64_t num_edges, double a, double b, do
  * kind 0: integer weights uniform in [lo, hi] stored as float;
  * kind 1: uniform in (0, 1]; kind 2: uniform in [-1, 1]; kind 3: lognormal(0,1). */
 int gbx_generate_values(uint64_t count, int kind, uint32_t lo, uint32_t hi, uint64_t seed, float *out);
+/* Chung-Lu edge list generated on the GPU: vertex i has weight
+ * (i + i0)^(-1/(exponent-1)) (i0 puts the largest expected degree near
+ * sqrt(num_edges)); each edge's source is drawn by weight, its destination
+ * with probability local_fraction uniformly inside the source's block of
+ * `window` consecutive ids, otherwise by weight. Out-degrees follow a power
+ * law with the given exponent and mean num_edges / num_vertices.
+ * Counter-based streams keyed by (seed, edge index). src/dst may be host or
+ * device memory (num_edges entries each, num_edges < 2^32). */
+int gbx_generate_chung_lu(uint32_t num_vertices, uint64_t num_edges, double exponent, uint32_t window,
+                          double local_fraction, uint64_t seed, uint32_t *src, uint32_t *dst,
+                          void *stream);
 
 #ifdef __cplusplus
 }
