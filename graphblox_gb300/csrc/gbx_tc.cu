@@ -60,6 +60,23 @@ __device__ __forceinline__ uint32_t count_lt(const uint32_t *a, uint32_t n, uint
     return lo;
 }
 
+// count_le by galloping from the front: 2*log2(answer) loads instead of
+// log2(n), for lists whose prefix <= x is short (x a high-degree id)
+__device__ __forceinline__ uint32_t count_le_front(const uint32_t *a, uint32_t n, uint32_t x) {
+    if (n == 0 || __ldg(a) > x) return 0;
+    uint32_t lo = 1, hi = 2;  // a[lo-1] <= x
+    while (hi <= n && __ldg(a + hi - 1) <= x) {
+        lo = hi;
+        hi *= 2;
+    }
+    hi = min(hi - 1, n);  // answer in [lo, hi]
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (__ldg(a + mid - 1) <= x) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
 __device__ __forceinline__ bool sorted_contains(const uint32_t *a, uint32_t n, uint32_t x) {
     uint32_t i = count_lt(a, n, x);
     return i < n && __ldg(a + i) == x;
@@ -103,23 +120,40 @@ __global__ void tc_low_count_kernel(const uint32_t *off, const uint32_t *dest, u
     }
 }
 
-// flags: bit 0 = some row repeats a neighbour, bit 1 = some edge has no reverse
-__global__ void tc_shape_check_kernel(const uint32_t *off, const uint32_t *dest, uint32_t V, unsigned *flags) {
+__device__ __forceinline__ unsigned long long pair_hash(uint32_t a, uint32_t b) {
+    // splitmix64 finaliser (Steele, Lea, Flood 2014) of the packed pair
+    unsigned long long z = ((unsigned long long)a << 32 | b) + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// flags: bit 0 = some row repeats a neighbour. *asym accumulates, over all
+// edges v->u, hash(v,u) - hash(u,v) (mod 2^64): zero when the edge multiset
+// equals its reverse (the CSR is symmetric); a non-symmetric CSR sums to zero
+// only by a 64-bit hash coincidence. One streaming pass instead of a search
+// per edge.
+__global__ void tc_shape_check_kernel(const uint32_t *off, const uint32_t *dest, uint32_t V, unsigned *flags,
+                                      unsigned long long *asym) {
     const uint32_t lane = threadIdx.x & 31;
     uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     unsigned f = 0;
+    unsigned long long h = 0;
     for (uint32_t v = gw; v < V; v += nw) {
         uint32_t b = off[v], e = off[v + 1];
         for (uint32_t j = b + lane; j < e; j += 32) {
             uint32_t u = dest[j];
             if (j > b && u == dest[j - 1]) f |= 1u;
-            uint32_t ub = off[u];
-            if (!sorted_contains(dest + ub, off[u + 1] - ub, v)) f |= 2u;
+            h += pair_hash(v, u) - pair_hash(u, v);
         }
     }
     f = __reduce_or_sync(0xffffffffu, f);
-    if (lane == 0 && f) atomicOr(flags, f);
+    h = warp_sum(h);
+    if (lane == 0) {
+        if (f) atomicOr(flags, f);
+        if (h) atomicAdd(asym, h);
+    }
 }
 
 // Count the elements of the lanes' lists (base_k, len_k), flattened over the
@@ -238,7 +272,7 @@ __device__ __forceinline__ unsigned long long stream_pairs(const uint32_t *__res
                                                           const uint32_t *__restrict__ dest, const uint32_t *nv,
                                                           uint32_t v, uint32_t ub, uint32_t ue, uint32_t *s_pre,
                                                           uint32_t *s_base, uint32_t *s_end, const Member &m,
-                                                          uint32_t step = 32) {
+                                                          uint32_t step = 32, bool front = false) {
     const uint32_t lane = threadIdx.x & 31;
     unsigned long long count = 0;
     for (uint32_t a0 = ub; a0 < ue; a0 += step) {
@@ -246,7 +280,8 @@ __device__ __forceinline__ unsigned long long stream_pairs(const uint32_t *__res
         if (a0 + lane < ue) {
             const uint32_t u = __ldg(nv + a0 + lane);
             base = __ldg(off + u);
-            len = count_le(dest + base, __ldg(off + u + 1) - base, v);
+            const uint32_t du = __ldg(off + u + 1) - base;
+            len = front ? count_le_front(dest + base, du, v) : count_le(dest + base, du, v);
         }
         count += count_flat4(dest, base, len, s_pre, s_base, s_end, m);
     }
@@ -423,7 +458,7 @@ __global__ void __launch_bounds__(kWideThreads, 1)
             }
             __syncthreads();
             count += stream_pairs(off, dest, nv, v, ub + wid * 32, ue, s_pre[wid], s_base[wid], s_end[wid],
-                                  BitmapMember{s_table}, nwarps * 32);
+                                  BitmapMember{s_table}, nwarps * 32, true);
             __syncthreads();
             for (uint32_t i = threadIdx.x; i < pv; i += blockDim.x) s_table[__ldg(nv + i) >> 5] = 0u;
         } else {
@@ -434,7 +469,7 @@ __global__ void __launch_bounds__(kWideThreads, 1)
             for (uint32_t i = threadIdx.x; i < pv; i += blockDim.x) hash_insert(s_table, mask, __ldg(nv + i));
             __syncthreads();
             count += stream_pairs(off, dest, nv, v, ub + wid * 32, ue, s_pre[wid], s_base[wid], s_end[wid],
-                                  HashMember{s_table, mask}, nwarps * 32);
+                                  HashMember{s_table, mask}, nwarps * 32, true);
             __syncthreads();
             for (uint32_t i = threadIdx.x; i <= mask; i += blockDim.x) s_table[i] = 0u;
         }
@@ -505,16 +540,17 @@ static int tc_prepare(gbx_graph *g, cudaStream_t s) {
         g->low_count = low;
     }
     if (g->simple_rows < 0) {
-        DevBuf<unsigned> flags;
-        GBX_TRY(flags.alloc(1, s));
-        GBX_CUDA(cudaMemsetAsync(flags.p, 0, 4, s));
-        tc_shape_check_kernel<<<wgrid, kTcThreads, 0, s>>>(g->offsets, g->dest, V, flags.p);
+        DevBuf<unsigned long long> flags;  // [0] repeat flags, [1] asymmetry hash sum
+        GBX_TRY(flags.alloc(2, s));
+        GBX_CUDA(cudaMemsetAsync(flags.p, 0, 16, s));
+        tc_shape_check_kernel<<<wgrid, kTcThreads, 0, s>>>(g->offsets, g->dest, V,
+                                                           reinterpret_cast<unsigned *>(flags.p), flags.p + 1);
         GBX_LAUNCH_CHECK();
-        unsigned h = 0;
-        GBX_CUDA(cudaMemcpyAsync(&h, flags.p, 4, cudaMemcpyDeviceToHost, s));
+        unsigned long long h[2] = {0, 0};
+        GBX_CUDA(cudaMemcpyAsync(h, flags.p, 16, cudaMemcpyDeviceToHost, s));
         GBX_CUDA(cudaStreamSynchronize(s));
-        g->simple_rows = (h & 1u) ? 0 : 1;
-        g->symmetric = (h & 2u) ? 0 : 1;
+        g->simple_rows = (h[0] & 1u) ? 0 : 1;
+        g->symmetric = h[1] ? 0 : 1;
     }
     if (g->simple_rows == 1 && g->symmetric == 1 && !g->tc_plan) {
         DevBuf<uint32_t> flag, pos, units, unit_pre, ub, tot;

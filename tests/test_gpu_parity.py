@@ -180,6 +180,25 @@ def test_rmat_symmetric(gbx, cuda_device, scale, ef, seed):
         assert gbx.triangle_count(dg2) == po.triangle_count(host)
 
 
+def test_tc_asymmetric_simple_graphs(gbx, cuda_device):
+    """Simple (no repeated neighbour) but not symmetric CSRs take the
+    reference-multiplicity path: a directed RMAT graph, and a symmetric graph
+    with one reverse edge removed."""
+    g = _rmat_graph(gbx, 12, 8, 7)
+    host, _ = host_views(g)
+    with gbx.DeviceGraph.from_graph_csr(g, use_weights=False) as dg:
+        assert gbx.triangle_count(dg) == po.triangle_count(host)
+    gs = _rmat_graph(gbx, 12, 8, 7, symmetric=True)
+    keep = np.ones(gs.num_edges, bool)
+    keep[np.nonzero(gs.src < gs.dest)[0][len(gs.src) // 7]] = False  # drop one direction of one edge
+    src, dst = gs.src[keep], gs.dest[keep]
+    deg, idx, s, d, _ = gbx.csr_build(src, dst, num_vertices=gs.num_vertices, sort=1)
+    g1 = gbx.GraphCSR(gs.num_vertices, int(s.shape[0]), deg, idx, d, s, None,
+                      np.arange(gs.num_vertices, dtype=np.uint32), np.arange(gs.num_vertices, dtype=np.uint32))
+    with gbx.DeviceGraph.from_graph_csr(g1) as dg:
+        assert gbx.triangle_count(dg) == po.triangle_count(po.HostCSR(gs.num_vertices, deg, idx, d))
+
+
 def test_edge_cases(gbx, cuda_device):
     # single vertex, no edges
     g = gbx.GraphCSR(1, 0, np.zeros(1, np.uint32), np.zeros(1, np.uint32), np.zeros(0, np.uint32),
