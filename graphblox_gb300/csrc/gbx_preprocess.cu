@@ -76,21 +76,43 @@ __global__ void compact_edges_kernel(const uint32_t *s, const uint32_t *d, const
     }
 }
 
-// mapVerticesWithInOutDegree_base (vertex.c:204-328)
+// mapVerticesWithInOutDegree_base (vertex.c:204-328) on a source-sorted edge
+// list: each run of equal sources writes its first position (idx) and its end
+// (into deg); degrees_from_runs_kernel turns the end into the run length. No
+// atomics: a hub's run would otherwise take one atomic per edge on one address.
 __global__ void map_vertices_kernel(const uint32_t *s, uint32_t n, uint32_t *deg, uint32_t *idx) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t v = s[i] & kIdMask;
-        atomicAdd(deg + v, 1u);
-        if (i == 0 || s[i] != s[i - 1]) idx[v] = i;
+        const uint32_t v = s[i] & kIdMask;
+        if (i == 0 || v != (s[i - 1] & kIdMask)) idx[v] = i;
+        if (i + 1 == n || v != (s[i + 1] & kIdMask)) deg[v] = i + 1;
+    }
+}
+
+__global__ void degrees_from_runs_kernel(uint32_t *deg, const uint32_t *idx, uint32_t V) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+        if (deg[v]) deg[v] -= idx[v];
+}
+
+// deg[key] += 1 for the active lanes, one atomic per distinct key in the warp
+// (edge lists sorted by source repeat a key along the warp; hubs repeat
+// everywhere, and one address taking every increment serialises the atomics)
+__device__ __forceinline__ void count_keys(uint32_t *deg, uint32_t key, unsigned active) {
+    const uint32_t lane = threadIdx.x & 31;
+    if ((active >> lane) & 1u) {
+        const unsigned peers = __match_any_sync(active, key);
+        if (lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(deg + key, (uint32_t)__popc(peers));
     }
 }
 
 __global__ void degree_count_kernel(const uint32_t *s, const uint32_t *d, uint32_t n, int lmode,
                                     uint32_t *deg) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (lmode == 2) atomicAdd(deg + d[i], 1u);
-        else if (lmode == 3) { atomicAdd(deg + d[i], 1u); atomicAdd(deg + s[i], 1u); }
-        else atomicAdd(deg + s[i], 1u);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * blockDim.x;  // a multiple of 32
+    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += stride) {
+        const uint32_t i = base + lane;
+        const unsigned active = __ballot_sync(0xffffffffu, i < n);
+        if (lmode == 2 || lmode == 3) count_keys(deg, i < n ? d[i] : 0u, active);
+        if (lmode != 2) count_keys(deg, i < n ? s[i] : 0u, active);
     }
 }
 
@@ -217,6 +239,8 @@ extern "C" int gbx_csr_build(uint32_t num_edges, const uint32_t *src, const uint
     GBX_CUDA(cudaMemsetAsync(oidx.d, 0, (size_t)V * 4, s));
     if (Eout) {
         map_vertices_kernel<<<grid1d(Eout), 256, 0, s>>>(fs, Eout, odeg.d, oidx.d);
+        GBX_LAUNCH_CHECK();
+        degrees_from_runs_kernel<<<grid1d(V), 256, 0, s>>>(odeg.d, oidx.d, V);
         GBX_LAUNCH_CHECK();
     }
     GBX_TRY(odeg.finish(s));
