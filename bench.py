@@ -218,9 +218,9 @@ def run_gpu(args):
         for kv in args.tuning.split(","):
             k, v = kv.split("=")
             dg.set_tuning(k, float(v))
-        tuning = {k: dg.get_tuning(k) for k in ("bfs_alpha", "bfs_beta", "sssp_delta")}
+        tuning = {k: dg.get_tuning(k) for k in ("bfs_alpha", "bfs_beta", "sssp_delta", "pull_heavy_min")}
     elif not args.no_autotune:
-        tuning = dg.autotune(bfs=True, sssp=True, samples=4, stream=sp)
+        tuning = dg.autotune(bfs=True, sssp=True, samples=4, stream=sp, pull=True)
     else:
         tuning = {}
     log(f"autotune: {tuning}")
@@ -826,14 +826,32 @@ def cpu_sample(W, roots, n_bfs=4, pr_iters=PR_ITERS, n_sssp=1, with_tc=True, thr
     return res
 
 
+def step_mix(W, res, n_bfs, n_sssp):
+    """Traversed edges of one full kernel-set step (64 BFS roots, 4 SSSP roots,
+    CC, TC, SpMV, 20 PR iterations, reorder), BFS/SSSP from the sampled roots'
+    mean reach."""
+    g, gs, gsr = W["g"], W["gs"], W["gsr"]
+    E = g.num_edges
+    return {"bfs": res["bfs"][0] / n_bfs * N_ROOTS, "sssp": res["sssp"][0] / n_sssp * N_SSSP_ROOTS,
+            "cc": gs.num_edges, "tc": int((gsr.dest <= gsr.src).sum()), "spmv": E, "pr": E * PR_ITERS,
+            "reorder": E}
+
+
+def mix_gteps(res, mix):
+    """Aggregate GTEPS of the full step at the sampled per-kernel rates: the
+    same kernel mix as the GPU `value`."""
+    secs = sum(mix[k] / (e / t) for k, (e, t) in res.items())
+    return sum(mix[k] for k in res) / secs / 1e9, secs
+
+
 def cpu_baseline(W, args, roots):
     res = cpu_sample(W, roots)
-    edges = sum(e for e, _ in res.values())
-    secs = sum(t for _, t in res.values())
-    return {"value": round(edges / secs / 1e9, 4), "unit": "GTEPS", "cores": os.cpu_count(), "kind": "port",
+    value, secs = mix_gteps(res, step_mix(W, res, 4, 1))
+    return {"value": round(value, 4), "unit": "GTEPS", "cores": os.cpu_count(), "kind": "port",
             "sample": "RMAT-22 kernel set on the host cores: BFS 4 roots, SSSP 1 root (delta 64), CC Afforest, "
-                      "TC, SpMV, PR 20 iterations, degree reorder (oracle/gbx_oracle.c, OpenMP)",
-            "seconds": round(secs, 2),
+                      "TC, SpMV, PR 20 iterations, degree reorder (oracle/gbx_oracle.c, OpenMP); value = the "
+                      "full step's edges (64 BFS roots, 4 SSSP roots, ...) at the sampled per-kernel rates",
+            "seconds_sampled": round(sum(t for _, t in res.values()), 2), "seconds_full_step": round(secs, 2),
             "per_kernel_gteps": {n: round(e / t / 1e9, 4) for n, (e, t) in res.items()}}
 
 
@@ -845,27 +863,29 @@ def run_reference(args):
 
     W = build_workload(gbx, scale=args.scale)
     roots = W["roots"]
-    samples = []
+    values, secs = [], []
     for i in range(args.warmup + args.steps):
-        res = cpu_sample(W, roots[i % len(roots):] + roots, n_bfs=2, pr_iters=5, n_sssp=1, with_tc=False)
+        res = cpu_sample(W, roots[i % len(roots):] + roots, n_bfs=2, pr_iters=5, n_sssp=1, with_tc=True)
         if i >= args.warmup:
-            samples.append(res)
-    edges = sum(e for s in samples for e, _ in s.values())
-    secs = sum(t for s in samples for _, t in s.values())
-    value = edges / secs / 1e9
+            v, s = mix_gteps(res, step_mix(W, res, 2, 1))
+            values.append(v)
+            secs.append(s)
+    value = float(np.mean(values))
     line = {
         "metric": "GTEPS per kernel (aggregate over the kernel set) & %HBM-peak per kernel",
         "value": round(value, 4), "unit": "GTEPS", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs / len(samples) * 1e3, 2),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(float(np.mean(secs)) * 1e3, 2),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32 (ids, levels, distances) + f32 (ranks, SpMV)", "data": "synthetic",
         "config": {"workload": f"rmat{args.scale}_full_kernel_set", "scale": args.scale, "num_vertices": W["V"],
                    "num_edges": W["g"].num_edges},
         "impl": "reference",
         "cpu_baseline": {"value": round(value, 4), "unit": "GTEPS", "cores": os.cpu_count(), "kind": "port",
-                         "sample": "per step: BFS 2 roots, SSSP 1 root (delta 64), CC, SpMV, PR 5 iterations, "
-                                   "degree reorder on the RMAT-22 graph (oracle/gbx_oracle.c, OpenMP; the "
-                                   "reference tree is not on the GPU host, so its compiled form cannot run)"},
+                         "sample": "per step: BFS 2 roots, SSSP 1 root (delta 64), CC, TC, SpMV, PR 5 "
+                                   "iterations, degree reorder on the RMAT-22 graph (oracle/gbx_oracle.c, OpenMP; "
+                                   "the reference tree is not on the GPU host, so its compiled form cannot run); "
+                                   "value and ms_per_step = the full step's edges (64 BFS roots, 4 SSSP roots, "
+                                   "20 PR iterations, ...) at the sampled per-kernel rates, the GPU value's mix"},
         "e2e": {"value": round(value, 4), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

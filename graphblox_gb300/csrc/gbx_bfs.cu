@@ -36,6 +36,7 @@ namespace gbx {
 
 constexpr uint32_t kHubDeg = 1024;    // out-degree above which a vertex is a hub
 constexpr uint32_t kHubChunk = 256;   // edges per hub work unit
+constexpr uint32_t kBuProbe = 64;     // bottom-up: in-edges a lane probes alone before the warp helps
 constexpr int kBfsThreads = 256;
 constexpr int kBfsWarps = kBfsThreads / 32;
 
@@ -261,16 +262,18 @@ __device__ void bottom_up_phase(const BfsArgs &a, const uint32_t *cur_bm, uint32
         }
         const uint32_t v = w * 32 + lane;
         bool found = false;
+        uint32_t tb = 0, te = 0;  // in-edges still to probe after the lane's own first kBuProbe
         if (v < a.V && !((vis >> lane) & 1u)) {
             const uint32_t b = __ldg(a.poff + v), e = __ldg(a.poff + v + 1);
+            const uint32_t el = min(e, b + kBuProbe);
             // four neighbours per round: their ids, then their frontier words,
             // are loaded back to back; the first one in the frontier wins
-            for (uint32_t j = b; j < e && !found; j += 4) {
+            for (uint32_t j = b; j < el && !found; j += 4) {
                 uint32_t u[4], fw[4];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) u[q] = (j + q < e) ? __ldg(a.psrc + j + q) : 0u;
+                for (int q = 0; q < 4; ++q) u[q] = (j + q < el) ? __ldg(a.psrc + j + q) : 0u;
 #pragma unroll
-                for (int q = 0; q < 4; ++q) fw[q] = (j + q < e) ? __ldcg(cur_bm + (u[q] >> 5)) : 0u;
+                for (int q = 0; q < 4; ++q) fw[q] = (j + q < el) ? __ldcg(cur_bm + (u[q] >> 5)) : 0u;
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     if (!found && ((fw[q] >> (u[q] & 31)) & 1u)) {
@@ -278,6 +281,40 @@ __device__ void bottom_up_phase(const BfsArgs &a, const uint32_t *cur_bm, uint32
                         a.parent[v] = (int32_t)u[q];
                         found = true;
                     }
+                }
+            }
+            if (!found && el < e) {
+                tb = el;
+                te = e;
+            }
+        }
+        // rows longer than kBuProbe that found nothing in their first part: the
+        // whole warp scans the rest, 128 in-edges per step, one row at a time
+        for (unsigned tv = __ballot_sync(0xffffffffu, tb < te); tv; tv &= tv - 1) {
+            const uint32_t k = __ffs(tv) - 1;
+            const uint32_t hb = __shfl_sync(0xffffffffu, tb, k), he = __shfl_sync(0xffffffffu, te, k);
+            for (uint32_t j0 = hb; j0 < he; j0 += 128) {
+                uint32_t u[4], fw[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const uint32_t j = j0 + q * 32 + lane;
+                    u[q] = j < he ? __ldg(a.psrc + j) : 0u;
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) fw[q] = j0 + q * 32 + lane < he ? __ldcg(cur_bm + (u[q] >> 5)) : 0u;
+                uint32_t pick = 0xFFFFFFFFu;
+#pragma unroll
+                for (int q = 3; q >= 0; --q)
+                    if ((fw[q] >> (u[q] & 31)) & 1u) pick = u[q];
+                const unsigned hm = __ballot_sync(0xffffffffu, pick != 0xFFFFFFFFu);
+                if (hm) {
+                    const uint32_t pu = __shfl_sync(0xffffffffu, pick, __ffs(hm) - 1);
+                    if (lane == k) {
+                        a.level[v] = lnext;
+                        a.parent[v] = (int32_t)pu;
+                        found = true;
+                    }
+                    break;
                 }
             }
         }

@@ -215,6 +215,9 @@ struct gbx_graph {
     // SSSP bucket width (0 = default for the graph's weights)
     uint32_t bfs_alpha = 15, bfs_beta = 18;
     uint32_t sssp_delta = 0;
+    // pull engine (PR, SpMV): in-degree above which a row is cut into
+    // CTA-sized chunks; rows between 32 and it get a warp each
+    uint32_t pull_heavy_min = 4096;
     // triangle-count work decomposition (gbx_tc.cu)
     struct gbx_tc_plan *tc_plan = nullptr;
     // personalised PageRank: in-edge order and chunk tables (gbx_ppr.cu)

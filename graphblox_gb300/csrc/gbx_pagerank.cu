@@ -31,7 +31,9 @@ struct PrIterState {
 struct PrTerm {
     const uint32_t *__restrict__ src;
     const float *__restrict__ contrib;
-    __device__ __forceinline__ uint32_t src_of(uint32_t e) const { return __ldg(src + e); }
+    // the in-edge stream is read once per iteration: evict-first, so it does
+    // not push the gathered contributions out of L2
+    __device__ __forceinline__ uint32_t src_of(uint32_t e) const { return __ldcs(src + e); }
     __device__ __forceinline__ float value(uint32_t, uint32_t u) const { return __ldg(contrib + u); }
 };
 

@@ -8,8 +8,6 @@
 
 namespace gbx {
 
-// rows above this degree get a whole CTA
-static uint32_t g_heavy_min = 4096;
 
 __global__ void classify_rows_kernel(const uint32_t *off, uint32_t V, uint32_t heavy_min,
                                      uint32_t *is_med, uint32_t *is_heavy) {
@@ -34,10 +32,11 @@ __global__ void row_bounds_kernel(const uint32_t *off, const uint32_t *rows, uin
     }
 }
 
-static int build_plan(const uint32_t *off, uint32_t V, cudaStream_t s, gbx_gather_plan **out) {
+// rows above heavy_min edges get whole CTAs (chunks of kHeavyChunk)
+static int build_plan(const uint32_t *off, uint32_t V, uint32_t heavy_min, cudaStream_t s, gbx_gather_plan **out) {
     gbx_gather_plan *p = new gbx_gather_plan();
     p->V = V;
-    p->heavy_min = g_heavy_min;
+    p->heavy_min = heavy_min;
     DevBuf<uint32_t> fm, fh, pm, ph, tot;
     int st = GBX_OK;
     do {
@@ -122,7 +121,7 @@ static int build_plan(const uint32_t *off, uint32_t V, cudaStream_t s, gbx_gathe
 
 int get_pull_plan(gbx_graph *g, cudaStream_t s, gbx_gather_plan **plan) {
     gbx_gather_plan **slot = g->has_inverse() ? &g->plan_inv : &g->plan_fwd;
-    if (!*slot) GBX_TRY(build_plan(g->pull_offsets(), g->V, s, slot));
+    if (!*slot) GBX_TRY(build_plan(g->pull_offsets(), g->V, g->pull_heavy_min, s, slot));
     *plan = *slot;
     return GBX_OK;
 }

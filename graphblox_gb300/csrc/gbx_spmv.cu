@@ -11,9 +11,10 @@ struct SpmvTerm {
     const float *__restrict__ val;  // may be null
     float dflt;
     const float *__restrict__ x;
-    __device__ __forceinline__ uint32_t src_of(uint32_t e) const { return __ldg(src + e); }
+    // index and value streams are read once: evict-first, keeping x in L2
+    __device__ __forceinline__ uint32_t src_of(uint32_t e) const { return __ldcs(src + e); }
     __device__ __forceinline__ float value(uint32_t e, uint32_t u) const {
-        float w = val ? __ldg(val + e) : dflt;
+        float w = val ? __ldcs(val + e) : dflt;
         return __fmul_rn(w, __ldg(x + u));
     }
 };

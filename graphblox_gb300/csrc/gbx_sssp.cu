@@ -15,7 +15,9 @@
 //   dist[u] = min over (v->u) of (uint32)((float)dist[v] + w),
 // i.e. the reference's distances. Work units and hub splitting are those of
 // the persistent BFS (gbx_bfs.cu): 32 near vertices flattened per warp, or
-// kHubChunk edges of one high-degree vertex.
+// kHubChunk edges of one high-degree vertex. Edge ids and weights are read
+// with evict-first loads: they stream from HBM either way, and dist / stamp /
+// in_far (12 bytes per vertex) should keep the L2.
 #include <algorithm>
 
 #include "gbx_coop.cuh"
@@ -111,7 +113,7 @@ struct Relaxer {
     __device__ __forceinline__ void operator()(uint32_t d, uint32_t e, uint32_t u, bool active) {
         bool to_near = false, to_far = false;
         if (active) {
-            const float wt = a.w ? __ldg(a.w + e) : 1.0f;
+            const float wt = a.w ? __ldcs(a.w + e) : 1.0f;
             const uint32_t nd = sssp_add(d, wt);
             relaxed++;
             if (nd < __ldcg(a.dist + u)) {
@@ -146,7 +148,7 @@ struct Relaxer {
         uint32_t nd[4], cur[4], old[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            const float wt = (act[q] && a.w) ? __ldg(a.w + e[q]) : 1.0f;
+            const float wt = (act[q] && a.w) ? __ldcs(a.w + e[q]) : 1.0f;
             nd[q] = sssp_add(d[q], wt);
             cur[q] = act[q] ? __ldcg(a.dist + u[q]) : 0u;
         }
@@ -217,7 +219,7 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     uint32_t j = j0 + q * 32 + lane;
-                    u[q] = j < ce ? __ldg(a.dest + j) : 0u;
+                    u[q] = j < ce ? __ldcs(a.dest + j) : 0u;
                 }
 #pragma unroll
                 const uint32_t dq[4] = {d, d, d, d};
@@ -259,7 +261,7 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
                         while (s_pre[k + 1] <= i) ++k;
                         e[q] = s_base[k] + (i - s_pre[k]);
                         dd[q] = s_d[k];
-                        u[q] = __ldg(a.dest + e[q]);
+                        u[q] = __ldcs(a.dest + e[q]);
                     }
                 }
 #pragma unroll

@@ -5,10 +5,14 @@
 //               unexplored edges / alpha (the reference fixes 15, BFS.c:374)
 //   bfs_beta    stay bottom-up while the frontier exceeds V / beta (18)
 //   sssp_delta  bucket width of the near/far schedule
+//   pull_heavy_min  in-degree above which the pull engine (PR, SpMV) cuts a
+//               row into CTA-sized chunks (rows of 33 up to it get a warp)
 // None of them changes a result: BFS levels, processed_nodes and iteration
 // (= depth + 2, one step per level) and SSSP distances are the same for every
-// setting; only the time differs. gbx_autotune times candidates on sample
-// sources of the graph itself with CUDA events and keeps the fastest.
+// setting, and PR/SpMV sums only change their FP32 summation order (within
+// the 1e-6 relative L1 bound); only the time differs. gbx_autotune times
+// candidates on sample sources of the graph itself with CUDA events and keeps
+// the fastest.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -30,6 +34,18 @@ extern "C" int gbx_graph_set_tuning(gbx_graph *g, const char *key, double value)
         g->bfs_beta = v;
     } else if (!strcmp(key, "sssp_delta")) {
         g->sssp_delta = v;
+    } else if (!strcmp(key, "pull_heavy_min")) {
+        GBX_REQUIRE(v >= 64, GBX_ERR_INVALID, "pull_heavy_min must be >= 64");
+        if (v != g->pull_heavy_min) {
+            // the pull plans and PageRank's captured loop embed the old classes
+            cudaDeviceSynchronize();
+            free_plan(g->plan_fwd);
+            free_plan(g->plan_inv);
+            g->plan_fwd = g->plan_inv = nullptr;
+            gbx_free_pr_cache(g->pr_cache);
+            g->pr_cache = nullptr;
+            g->pull_heavy_min = v;
+        }
     } else {
         GBX_REQUIRE(false, GBX_ERR_INVALID, "unknown tuning key '%s'", key);
     }
@@ -42,6 +58,7 @@ extern "C" int gbx_graph_get_tuning(const gbx_graph *g, const char *key, double 
     if (!strcmp(key, "bfs_alpha")) *value = g->bfs_alpha;
     else if (!strcmp(key, "bfs_beta")) *value = g->bfs_beta;
     else if (!strcmp(key, "sssp_delta")) *value = g->sssp_delta;
+    else if (!strcmp(key, "pull_heavy_min")) *value = g->pull_heavy_min;
     else GBX_REQUIRE(false, GBX_ERR_INVALID, "unknown tuning key '%s'", key);
     return GBX_OK;
 }
@@ -133,6 +150,26 @@ extern "C" int gbx_autotune(gbx_graph *g, uint32_t flags, uint32_t num_samples, 
             }
         }
         g->sssp_delta = best_d;
+    }
+    if (flags & 4u) {
+        // pull-engine row classes, timed on pull PageRank iterations
+        const uint32_t cands[] = {1024, 4096, 16384};
+        DevBuf<float> ranks;
+        GBX_TRY(ranks.alloc(g->V, s));
+        float best = 1e30f;
+        uint32_t best_h = g->pull_heavy_min;
+        for (uint32_t c : cands) {
+            GBX_TRY(gbx_graph_set_tuning(g, "pull_heavy_min", c));
+            GBX_TRY(gbx_pagerank_pull(g, 5, 0.0, ranks.p, nullptr, stream));  // builds the plan, captures
+            float ms = 0.f;
+            GBX_TRY(time_ms([&]() { return gbx_pagerank_pull(g, 5, 0.0, ranks.p, nullptr, stream); }, s, &ms));
+            if (trace_enabled()) fprintf(stderr, "| autotune pull_heavy_min %-5u | %9.3f ms |\n", c, ms);
+            if (ms < best) {
+                best = ms;
+                best_h = c;
+            }
+        }
+        GBX_TRY(gbx_graph_set_tuning(g, "pull_heavy_min", best_h));
     }
     return GBX_OK;
 }

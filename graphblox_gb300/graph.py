@@ -236,10 +236,12 @@ class DeviceGraph:
         call("gbx_graph_get_tuning", self._h, key.encode(), C.byref(v))
         return v.value
 
-    def autotune(self, bfs: bool = True, sssp: bool = True, samples: int = 4, stream=None) -> dict:
+    def autotune(self, bfs: bool = True, sssp: bool = True, samples: int = 4, stream=None,
+                 pull: bool = False) -> dict:
         """gbx_autotune: time candidate knob settings on this graph, keep the fastest."""
-        call("gbx_autotune", self._h, (1 if bfs else 0) | (2 if sssp else 0), int(samples), stream)
-        return {k: self.get_tuning(k) for k in ("bfs_alpha", "bfs_beta", "sssp_delta")}
+        call("gbx_autotune", self._h, (1 if bfs else 0) | (2 if sssp else 0) | (4 if pull else 0), int(samples),
+             stream)
+        return {k: self.get_tuning(k) for k in ("bfs_alpha", "bfs_beta", "sssp_delta", "pull_heavy_min")}
 
     def close(self) -> None:
         if self._h and self._h.value:

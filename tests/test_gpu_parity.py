@@ -260,3 +260,43 @@ def test_device_resident_outputs(gbx, cuda_device):
         gbx.page_rank(dg, 20, 0.0, ranks=ranks)
         ref64, _, _ = po.pagerank(host, 20, 0.0, pull, fp64=True)
         assert po.fp32_close(ranks.cpu().numpy(), ref64, REL_L1_TOL)[0]
+
+
+def test_tuning_knobs_keep_results(gbx, cuda_device):
+    """Every knob setting gives the oracle's integer results; the pull-engine
+    threshold only reorders FP32 sums (PR, SpMV stay within the L1 bound)."""
+    g = _rmat_graph(gbx, 15, 16, 12, weights="int")
+    host, pull = host_views(g)
+    x = gbx.generate_values(g.num_vertices, 2, seed=7)
+    vals = gbx.generate_values(g.num_edges, 1, seed=8)
+    ref_pr, _, _ = po.pagerank(host, 20, 0.0, pull, fp64=True)
+    ref_y = po.spmv(host, x, vals, pull=pull, fp64=True)
+    ref_bfs = po.bfs(host, 0, pull)
+    ref_sssp = po.sssp(host, 0, 64)
+    with gbx.DeviceGraph.from_graph_csr(g) as dg:
+        assert dg.get_tuning("pull_heavy_min") == 4096
+        for heavy in (64, 200, 1024, 4096, 1 << 20):
+            dg.set_tuning("pull_heavy_min", heavy)
+            assert dg.get_tuning("pull_heavy_min") == heavy
+            pr = gbx.page_rank(dg, 20, 0.0)
+            assert po.fp32_close(pr.pageRanks, ref_pr, REL_L1_TOL)[0], heavy
+            y = gbx.spmv(dg, x, values=vals)
+            assert po.fp32_close(y, ref_y, REL_L1_TOL)[0], heavy
+        for alpha, beta in ((1, 1), (4, 18), (4096, 64)):
+            dg.set_tuning("bfs_alpha", alpha)
+            dg.set_tuning("bfs_beta", beta)
+            st = gbx.breadth_first_search(dg, 0)
+            np.testing.assert_array_equal(st.distances, ref_bfs[0])
+            assert (st.processed_nodes, st.iteration) == ref_bfs[2:]
+        for delta in (1, 100, 4096):
+            dg.set_tuning("sssp_delta", delta)
+            np.testing.assert_array_equal(gbx.sssp(dg, 0).distances, ref_sssp)
+        tuned = dg.autotune(bfs=True, sssp=True, samples=2, pull=True)
+        assert tuned["pull_heavy_min"] in (1024, 4096, 16384)
+        assert tuned["bfs_alpha"] >= 1 and tuned["sssp_delta"] >= 1
+        np.testing.assert_array_equal(gbx.breadth_first_search(dg, 0).distances, ref_bfs[0])
+        assert po.fp32_close(gbx.page_rank(dg, 20, 0.0).pageRanks, ref_pr, REL_L1_TOL)[0]
+        for key, bad in (("pull_heavy_min", 8), ("bfs_alpha", 0), ("no_such_knob", 1)):
+            with pytest.raises(gbx.GbxError) as e:
+                dg.set_tuning(key, bad)
+            assert e.value.status == -1
