@@ -21,7 +21,11 @@
 //              born sorted by chunk.
 //  bottom-up : one warp per bitmap word (32 vertices); each unvisited lane
 //              scans its pull neighbours until one is in the current frontier
-//              bitmap; the ballot is the next-frontier word.
+//              bitmap (4, then 16 probes in flight; the warp finishes rows
+//              longer than kBuProbe together); the ballot is the
+//              next-frontier word. Found vertices are also appended to the
+//              next generation's queue / hub list, so leaving bottom-up needs
+//              no bitmap-to-list pass.
 //
 // The direction heuristic is the reference's (alpha 15, beta 18, mu/mf/nf in
 // uint32 arithmetic). Every CTA evaluates it redundantly from the previous
@@ -37,6 +41,7 @@ namespace gbx {
 constexpr uint32_t kHubDeg = 1024;    // out-degree above which a vertex is a hub
 constexpr uint32_t kHubChunk = 256;   // edges per hub work unit
 constexpr uint32_t kBuProbe = 64;     // bottom-up: in-edges a lane probes alone before the warp helps
+constexpr uint32_t kTdMaxSplit = 8;   // top-down: most warps sharing one 32-vertex group's edges
 constexpr int kBfsThreads = 256;
 constexpr int kBfsWarps = kBfsThreads / 32;
 
@@ -86,6 +91,7 @@ struct BfsArgs {
     const uint32_t *off, *dest, *poff, *psrc, *outdeg;
     uint32_t V, words, E, mode, source;
     uint32_t alpha, beta;  // direction switch: bottom-up when mf > mu/alpha, stay while nf > V/beta
+    uint32_t pull_live;    // every pull neighbour has out-degree > 0
     uint32_t *level;
     int32_t *parent;
     uint32_t *visited;
@@ -178,7 +184,12 @@ __device__ void top_down_phase(const BfsArgs &a, const uint32_t *qin, uint32_t q
                                uint32_t *s_base, uint32_t *s_v, uint32_t *s_wq) {
     const uint32_t lane = threadIdx.x & 31;
     Claimer claim(a, lnext, qout, hvout, hcout, cur, s_wq);
-    const uint32_t units = nc + (qn + 31) / 32;
+    // a frontier with fewer 32-vertex groups than warps cuts each group's
+    // edges into `split` interleaved parts of 128-edge batches
+    const uint32_t groups = (qn + 31) / 32;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t split = groups ? max(1u, min(kTdMaxSplit, nwarps / groups)) : 1u;
+    const uint32_t units = nc + groups * split;
     UnitDealer dealer(&cur->cursor);
     for (;;) {
         const uint32_t unit = dealer.take(units);
@@ -202,8 +213,9 @@ __device__ void top_down_phase(const BfsArgs &a, const uint32_t *qin, uint32_t q
                 claim.claim4(vv, u, act);
             }
         } else {
-            // 32 queued vertices, edges flattened over the warp
-            const uint32_t qi = (unit - nc) * 32 + lane;
+            // 32 queued vertices, edges flattened over the warp (one part)
+            const uint32_t group = (unit - nc) / split, part = (unit - nc) % split;
+            const uint32_t qi = group * 32 + lane;
             uint32_t v = 0, b = 0, d = 0;
             if (qi < qn) {
                 v = __ldcg(qin + qi);
@@ -223,7 +235,7 @@ __device__ void top_down_phase(const BfsArgs &a, const uint32_t *qin, uint32_t q
             __syncwarp();
             const uint32_t tot = s_pre[32];
             uint32_t k = 0;
-            for (uint32_t i0 = 0; i0 < tot; i0 += 128) {
+            for (uint32_t i0 = part * 128; i0 < tot; i0 += split * 128) {
                 uint32_t u[4], src[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
@@ -245,17 +257,59 @@ __device__ void top_down_phase(const BfsArgs &a, const uint32_t *qin, uint32_t q
     claim.flush();
 }
 
+// Probe in-edges [j, el) of one vertex, N at a time: the ids, then their
+// frontier words, are loaded back to back; returns the first frontier member
+// or 0xFFFFFFFF. The frontier bitmap is read through L1: it was written in
+// the previous step, and the grid barrier's acquire orders those writes
+// before these loads.
+template <int N>
+__device__ __forceinline__ uint32_t bu_probe(const BfsArgs &a, const uint32_t *cur_bm, uint32_t j, uint32_t el) {
+    uint32_t u[N], fw[N];
+#pragma unroll
+    for (int q = 0; q < N; ++q) u[q] = (j + q < el) ? __ldg(a.psrc + j + q) : 0u;
+#pragma unroll
+    for (int q = 0; q < N; ++q) fw[q] = (j + q < el) ? cur_bm[u[q] >> 5] : 0u;
+    uint32_t pick = 0xFFFFFFFFu;
+#pragma unroll
+    for (int q = N - 1; q >= 0; --q)
+        if ((fw[q] >> (u[q] & 31)) & 1u) pick = u[q];
+    return pick;
+}
+
 __device__ void bottom_up_phase(const BfsArgs &a, const uint32_t *cur_bm, uint32_t *next_bm, uint32_t lnext,
-                                BfsStep *cnt) {
+                                BfsStep *cnt, uint32_t *qout, uint32_t *hvout, uint32_t *hcout, uint32_t *s_wq) {
     const uint32_t lane = threadIdx.x & 31;
     unsigned nf = 0;
     unsigned long long edges = 0;
+    WarpQueue wq(s_wq);
     constexpr uint32_t kWordsPerUnit = 8;
     const uint32_t units = (a.words + kWordsPerUnit - 1) / kWordsPerUnit;
     UnitDealer dealer(&cnt->cursor);
-    for (uint32_t unit = dealer.take(units); unit < units; unit = dealer.take(units))
-    for (uint32_t w = unit * kWordsPerUnit; w < min(a.words, (unit + 1) * kWordsPerUnit); ++w) {
-        const uint32_t vis = __ldcg(a.visited + w);
+    // The unit's visited words come in one load (lane k holds word k; only
+    // this warp writes them during the step), and each lane's row bounds and
+    // out-degree for the next word are fetched while the current word is
+    // probed, so a word's dependent chain starts at the in-edge loads.
+    for (uint32_t unit = dealer.take(units); unit < units; unit = dealer.take(units)) {
+        const uint32_t w0 = unit * kWordsPerUnit;
+        const uint32_t nw = min(a.words - w0, kWordsPerUnit);
+        const uint32_t vis_unit = lane < nw ? __ldcg(a.visited + w0 + lane) : 0xFFFFFFFFu;
+        auto row_of = [&](uint32_t k, uint32_t &rb, uint32_t &re, uint32_t &rd) {
+            const uint32_t vk = __shfl_sync(0xffffffffu, vis_unit, k);
+            const uint32_t vv = (w0 + k) * 32 + lane;
+            rb = re = rd = 0;
+            if (vk != 0xFFFFFFFFu && vv < a.V && !((vk >> lane) & 1u)) {
+                rb = __ldg(a.poff + vv);
+                re = __ldg(a.poff + vv + 1);
+                rd = __ldg(a.outdeg + vv);
+            }
+        };
+        uint32_t nb, ne, nd;
+        row_of(0, nb, ne, nd);
+    for (uint32_t k = 0; k < nw; ++k) {
+        const uint32_t w = w0 + k;
+        const uint32_t vis = __shfl_sync(0xffffffffu, vis_unit, k);
+        const uint32_t b = nb, e = ne, dv_pre = nd;
+        if (k + 1 < nw) row_of(k + 1, nb, ne, nd);
         if (vis == 0xFFFFFFFFu) {
             if (lane == 0) next_bm[w] = 0;
             continue;
@@ -264,26 +318,16 @@ __device__ void bottom_up_phase(const BfsArgs &a, const uint32_t *cur_bm, uint32
         bool found = false;
         uint32_t tb = 0, te = 0;  // in-edges still to probe after the lane's own first kBuProbe
         if (v < a.V && !((vis >> lane) & 1u)) {
-            const uint32_t b = __ldg(a.poff + v), e = __ldg(a.poff + v + 1);
             const uint32_t el = min(e, b + kBuProbe);
-            // four neighbours per round: their ids, then their frontier words,
-            // are loaded back to back; the first one in the frontier wins
-            for (uint32_t j = b; j < el && !found; j += 4) {
-                uint32_t u[4], fw[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) u[q] = (j + q < el) ? __ldg(a.psrc + j + q) : 0u;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) fw[q] = (j + q < el) ? __ldcg(cur_bm + (u[q] >> 5)) : 0u;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    if (!found && ((fw[q] >> (u[q] & 31)) & 1u)) {
-                        a.level[v] = lnext;
-                        a.parent[v] = (int32_t)u[q];
-                        found = true;
-                    }
-                }
-            }
-            if (!found && el < e) {
+            // a short first round (most vertices that have a frontier
+            // in-neighbour meet it among their first few), then wide rounds
+            uint32_t pu = bu_probe<4>(a, cur_bm, b, el);
+            for (uint32_t j = b + 4; pu == 0xFFFFFFFFu && j < el; j += 16) pu = bu_probe<16>(a, cur_bm, j, el);
+            if (pu != 0xFFFFFFFFu) {
+                a.level[v] = lnext;
+                a.parent[v] = (int32_t)pu;
+                found = true;
+            } else if (el < e) {
                 tb = el;
                 te = e;
             }
@@ -301,7 +345,7 @@ __device__ void bottom_up_phase(const BfsArgs &a, const uint32_t *cur_bm, uint32
                     u[q] = j < he ? __ldg(a.psrc + j) : 0u;
                 }
 #pragma unroll
-                for (int q = 0; q < 4; ++q) fw[q] = j0 + q * 32 + lane < he ? __ldcg(cur_bm + (u[q] >> 5)) : 0u;
+                for (int q = 0; q < 4; ++q) fw[q] = j0 + q * 32 + lane < he ? cur_bm[u[q] >> 5] : 0u;
                 uint32_t pick = 0xFFFFFFFFu;
 #pragma unroll
                 for (int q = 3; q >= 0; --q)
@@ -319,13 +363,28 @@ __device__ void bottom_up_phase(const BfsArgs &a, const uint32_t *cur_bm, uint32
             }
         }
         const unsigned m = __ballot_sync(0xffffffffu, found);
-        if (found) edges += __ldg(a.outdeg + v);
+        // the vertices found also form the next step's lists, in case the
+        // traversal returns to top-down after this step (bitmapToArrayQueue)
+        uint32_t dv = 0;
+        if (found) {
+            dv = dv_pre;
+            edges += dv;
+            if (dv > kHubDeg) {
+                const unsigned long long h = atomicAdd(&cnt->hub, (1ull << 32) | hub_chunks(dv));
+                const uint32_t slot = (uint32_t)(h >> 32);
+                hvout[slot] = v;
+                hcout[slot] = (uint32_t)h;
+            }
+        }
+        wq.push(v, found && dv > 0 && dv <= kHubDeg, qout, &cnt->qlen);
         if (lane == 0) {
             next_bm[w] = m;
             if (m) a.visited[w] = vis | m;
             nf += __popc(m);
         }
     }
+    }
+    wq.flush(qout, &cnt->qlen);
     edges = warp_sum(edges);
     if (lane == 0 && (nf || edges)) {
         atomicAdd(&cnt->nf, nf);
@@ -333,43 +392,36 @@ __device__ void bottom_up_phase(const BfsArgs &a, const uint32_t *cur_bm, uint32
     }
 }
 
+// arrayQueueToBitmap (arrayQueue.c:284-308) from the lists themselves, into a
+// bitmap that is still all zero: the queue and hub lists hold every frontier
+// vertex with out-degree > 0, and the caller checks that the others cannot
+// matter (no other frontier vertex, or no pull neighbour of out-degree 0).
+__device__ void lists_to_bitmap_phase(const uint32_t *qin, uint32_t qn, const uint32_t *hvin, uint32_t nh,
+                                      uint32_t *bm) {
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+    for (uint32_t i = tid; i < qn + nh; i += nt) {
+        const uint32_t v = i < qn ? __ldcg(qin + i) : __ldcg(hvin + (i - qn));
+        atomicOr(bm + (v >> 5), 1u << (v & 31));
+    }
+}
+
 __device__ void level_to_bitmap_phase(const BfsArgs &a, uint32_t l, uint32_t *bm) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t w = gw; w < a.words; w += nw) {
-        const uint32_t v = w * 32 + lane;
-        const unsigned m = __ballot_sync(0xffffffffu, v < a.V && __ldcg(a.level + v) == l);
-        if (lane == 0) bm[w] = m;
-    }
-}
-
-// bitmapToArrayQueue (arrayQueue.c:310-337): a frontier bitmap -> queue + hubs
-__device__ void bitmap_to_lists_phase(const BfsArgs &a, const uint32_t *bm, uint32_t *qout, uint32_t *hvout,
-                                      uint32_t *hcout, BfsStep *cnt, uint32_t *s_wq) {
-    const uint32_t lane = threadIdx.x & 31;
-    WarpQueue wq(s_wq);
-    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t w = gw; w < a.words; w += nw) {
-        const uint32_t word = __ldcg(bm + w);
-        if (!word) continue;
-        const uint32_t v = w * 32 + lane;
-        bool push = false;
-        if (((word >> lane) & 1u) && v < a.V) {
-            const uint32_t d = __ldg(a.outdeg + v);
-            if (d > kHubDeg) {
-                unsigned long long old = atomicAdd(&cnt->hub, (1ull << 32) | hub_chunks(d));
-                uint32_t slot = (uint32_t)(old >> 32);
-                hvout[slot] = v;
-                hcout[slot] = (uint32_t)old;
-            } else {
-                push = d > 0;
-            }
+    for (uint32_t w0 = gw; w0 < a.words; w0 += 4 * nw) {
+        uint32_t lv[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t v = (w0 + q * nw) * 32 + lane;
+            lv[q] = (w0 + q * nw < a.words && v < a.V) ? __ldcg(a.level + v) : kInfLevel;
         }
-        wq.push(v, push, qout, &cnt->qlen);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const unsigned m = __ballot_sync(0xffffffffu, lv[q] == l);
+            if (lane == 0 && w0 + q * nw < a.words) bm[w0 + q * nw] = m;
+        }
     }
-    wq.flush(qout, &cnt->qlen);
 }
 
 __device__ __forceinline__ void zero_step(BfsStep *s) {
@@ -388,12 +440,14 @@ __global__ void __launch_bounds__(kBfsThreads) bfs_persistent_kernel(BfsArgs a) 
     __shared__ uint32_t s_wq[kBfsWarps][kWarpQueueCap];
     const uint32_t wid = threadIdx.x >> 5;
     BfsState *st = a.st;
+    grid_barrier_init();
     const uint32_t alpha = a.alpha, beta = a.beta;
     // DO bookkeeping, evaluated identically by every CTA
     uint32_t mu = a.E, mf = __ldg(a.outdeg + a.source), qsize = 1, nf_prev = 0, L = 0;
     uint32_t processed = 1, iteration = 1, td = 0, bu = 0;
     unsigned long long edges_total = __ldg(a.outdeg + a.source);
     bool in_bu = false, last_was_bu = false, done = false, failed = false;
+    bool bm_clean[2] = {true, true};  // frontier bitmaps still all zero (cleared by bfs_init_kernel)
     const uint32_t max_steps = 2 * a.V + 16;
     // lists for step 0: prepared by the host in generation 0
     uint32_t qn = __ldcg(&st->conv.qlen);
@@ -420,14 +474,21 @@ __global__ void __launch_bounds__(kBfsThreads) bfs_persistent_kernel(BfsArgs a) 
         }
         if (use_bu) {
             if (!in_bu) {
-                // arrayQueueToBitmap: frontier bitmap of the current level
-                level_to_bitmap_phase(a, L, a.bm[ib]);
+                // arrayQueueToBitmap: frontier bitmap of the current level,
+                // scattered from the lists when they hold the whole frontier
+                // and the bitmap is still clear, else from level[]
+                if (bm_clean[ib] && (a.pull_live || qsize == qn + nh))
+                    lists_to_bitmap_phase(a.q[ib], qn, a.hv[ib], nh, a.bm[ib]);
+                else
+                    level_to_bitmap_phase(a, L, a.bm[ib]);
+                bm_clean[ib] = false;
                 if (!grid_barrier(&st->gs)) { failed = true; break; }
                 trace_step(st, kTrToBitmap, qsize);
                 nf_prev = qsize;
                 in_bu = true;
             }
-            bottom_up_phase(a, a.bm[ib], a.bm[ob], L + 1, cur);
+            bottom_up_phase(a, a.bm[ib], a.bm[ob], L + 1, cur, a.q[ob], a.hv[ob], a.hc[ob], s_wq[wid]);
+            bm_clean[ob] = false;
             if (!grid_barrier(&st->gs)) { failed = true; break; }
             const uint32_t nf = __ldcg(&cur->nf);
             trace_step(st, kTrBottomUp, nf);
@@ -444,14 +505,10 @@ __global__ void __launch_bounds__(kBfsThreads) bfs_persistent_kernel(BfsArgs a) 
                 if (nf == 0 || a.mode == 0) {
                     done = true;
                 } else {
-                    // bitmapToArrayQueue into the list generation step s+1 reads
-                    if (blockIdx.x == 0 && threadIdx.x == 0) zero_step(&st->conv);
-                    if (!grid_barrier(&st->gs)) { failed = true; break; }
-                    bitmap_to_lists_phase(a, a.bm[ob], a.q[ob], a.hv[ob], a.hc[ob], &st->conv, s_wq[wid]);
-                    if (!grid_barrier(&st->gs)) { failed = true; break; }
-                    qn = __ldcg(&st->conv.qlen);
-                    trace_step(st, kTrToLists, qn);
-                    unsigned long long hb = __ldcg(&st->conv.hub);
+                    // bitmapToArrayQueue: the step itself wrote the lists of
+                    // generation s+1
+                    qn = __ldcg(&cur->qlen);
+                    unsigned long long hb = __ldcg(&cur->hub);
                     nh = (uint32_t)(hb >> 32);
                     nc = (uint32_t)hb;
                     mf = 1;
@@ -492,14 +549,17 @@ __global__ void __launch_bounds__(kBfsThreads) bfs_persistent_kernel(BfsArgs a) 
     }
 }
 
-__global__ void bfs_init_kernel(uint32_t *level, int32_t *parent, uint32_t *visited, uint32_t V,
-                                uint32_t words, uint32_t source) {
+__global__ void bfs_init_kernel(uint32_t *level, int32_t *parent, uint32_t *visited, uint32_t *bm0,
+                                uint32_t *bm1, uint32_t V, uint32_t words, uint32_t source) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
         level[v] = v == source ? 0u : kInfLevel;
         parent[v] = v == source ? (int32_t)source : -1;
     }
-    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < words; w += gridDim.x * blockDim.x)
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < words; w += gridDim.x * blockDim.x) {
         visited[w] = (w == (source >> 5)) ? (1u << (source & 31)) : 0u;
+        bm0[w] = 0;
+        bm1[w] = 0;
+    }
 }
 
 // generation-0 lists: the source alone (as a hub when its degree is large)
@@ -516,6 +576,14 @@ __global__ void bfs_seed_kernel(const uint32_t *outdeg, uint32_t source, uint32_
         q0[0] = source;
         st->conv.qlen = 1;
     }
+}
+
+// sets *bad when some pull neighbour has out-degree 0
+__global__ void pull_live_kernel(const uint32_t *psrc, uint32_t E, const uint32_t *outdeg, uint32_t *bad) {
+    bool dead = false;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < E; j += gridDim.x * blockDim.x)
+        dead |= __ldg(outdeg + __ldcs(psrc + j)) == 0;
+    if (__any_sync(0xffffffffu, dead) && (threadIdx.x & 31) == 0) *bad = 1;
 }
 
 __global__ void bfs_finish_kernel(const uint32_t *level, const int32_t *parent, const uint32_t *outdeg,
@@ -572,7 +640,22 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
     GBX_TRY(dist.bind(distances, V, s));
     GBX_TRY(par.bind(parents, V, s));
     const unsigned grid1 = std::min<unsigned>(ceil_div(V, 256), (unsigned)num_sms() * 8);
-    bfs_init_kernel<<<grid1, 256, 0, s>>>(w.level.p, w.parent.p, w.visited.p, V, words, source);
+    if (g->pull_sources_live < 0) {
+        DevBuf<uint32_t> bad;
+        GBX_TRY(bad.alloc(1, s));
+        GBX_CUDA(cudaMemsetAsync(bad.p, 0, 4, s));
+        if (g->E) {
+            pull_live_kernel<<<std::min<unsigned>(ceil_div(g->E, 256), (unsigned)num_sms() * 8), 256, 0, s>>>(
+                g->pull_src(), g->E, g->out_degree, bad.p);
+            GBX_LAUNCH_CHECK();
+        }
+        uint32_t h = 0;
+        GBX_CUDA(cudaMemcpyAsync(&h, bad.p, 4, cudaMemcpyDeviceToHost, s));
+        GBX_CUDA(cudaStreamSynchronize(s));
+        g->pull_sources_live = h ? 0 : 1;
+    }
+    bfs_init_kernel<<<grid1, 256, 0, s>>>(w.level.p, w.parent.p, w.visited.p, w.bm0.p, w.bm1.p, V, words,
+                                          source);
     GBX_LAUNCH_CHECK();
     GBX_CUDA(cudaMemsetAsync(w.st.p, 0, sizeof(BfsState), s));
     bfs_seed_kernel<<<1, 1, 0, s>>>(g->out_degree, source, w.q0.p, w.hv0.p, w.hc0.p, w.st.p);
@@ -590,6 +673,7 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
     a.source = source;
     a.alpha = g->bfs_alpha;
     a.beta = g->bfs_beta;
+    a.pull_live = g->pull_sources_live == 1 ? 1u : 0u;
     a.level = w.level.p;
     a.parent = w.parent.p;
     a.visited = w.visited.p;

@@ -1,12 +1,16 @@
 // Persistent cooperative kernels: a grid barrier with a bounded wait and the
 // launch helper that sizes the grid to what is co-resident.
 //
-// The barrier is a generation counter: each CTA's thread 0 reads the
-// generation, arrives with an atomicAdd, and the last arrival resets the
-// count and advances the generation; the others spin (with __nanosleep) until
-// it moves. The kernels are launched with cudaLaunchCooperativeKernel, which
-// guarantees that every CTA is resident, so the wait always ends; it is still
-// capped (kBarrierSpinLimit, about two seconds): on expiry the CTA raises the
+// The barrier is one monotonic 64-bit arrival counter: at its n-th barrier
+// each CTA's thread 0 adds 1 with release semantics (no reply awaited) and
+// polls the counter with acquire loads until it reaches n * gridDim.x. The
+// __syncthreads on either side extends the ordering to the whole CTA. Nobody
+// resets or re-arms anything, so a barrier costs one arrival plus one poll
+// round trip (about half the latency of a count-and-generation barrier, whose
+// last arrival must reset the count and then publish the generation). The
+// kernels are launched with cudaLaunchCooperativeKernel, which guarantees
+// that every CTA is resident, so the wait always ends; it is still capped
+// (kBarrierSpinLimit polls, about two seconds): on expiry the CTA raises the
 // error word and every CTA leaves the kernel at its next barrier, so the host
 // sees GBX_ERR_DEVICE_TIMEOUT instead of a hung device.
 #pragma once
@@ -16,13 +20,15 @@
 namespace gbx {
 
 struct GridSync {
-    unsigned count;
-    unsigned gen;
-    unsigned error;  // 1 = a barrier wait expired
+    unsigned long long arrived;  // total arrivals since launch (zeroed by the host)
+    unsigned error;              // 1 = a barrier wait expired
     unsigned pad;
 };
 
-constexpr unsigned kBarrierSpinLimit = 1u << 25;
+constexpr unsigned kBarrierSpinLimit = 1u << 22;
+
+// this CTA's arrival target for its next barrier (set by grid_barrier_init)
+__shared__ unsigned long long s_grid_target;
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
     unsigned v;
@@ -30,30 +36,34 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
     return v;
 }
 
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Once at kernel start, before the first grid_barrier (whose leading
+// __syncthreads orders it).
+__device__ __forceinline__ void grid_barrier_init() {
+    if (threadIdx.x == 0) s_grid_target = 0;
+}
+
 // Returns false when the grid must stop (a wait expired somewhere).
 __device__ __forceinline__ bool grid_barrier(GridSync *gs) {
     __shared__ unsigned s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        unsigned ok = 1;
-        __threadfence();
-        const unsigned my_gen = ld_acquire_u32(&gs->gen);
-        const unsigned arrived = atomicAdd(&gs->count, 1u) + 1u;
-        if (arrived == gridDim.x) {
-            atomicExch(&gs->count, 0u);
-            __threadfence();
-            atomicAdd(&gs->gen, 1u);
-        } else {
-            unsigned spins = 0;
-            while (ld_acquire_u32(&gs->gen) == my_gen) {
-                if (++spins > kBarrierSpinLimit) {
-                    atomicExch(&gs->error, 1u);
-                    break;
-                }
-                __nanosleep(64);
+        const unsigned long long target = s_grid_target + gridDim.x;
+        s_grid_target = target;
+        asm volatile("red.release.gpu.global.add.u64 [%0], 1;" ::"l"(&gs->arrived) : "memory");
+        unsigned ok = 1, spins = 0;
+        while (ld_acquire_u64(&gs->arrived) < target) {
+            if (++spins > kBarrierSpinLimit) {
+                atomicExch(&gs->error, 1u);
+                break;
             }
+            __nanosleep(32);
         }
-        __threadfence();
         if (ld_acquire_u32(&gs->error)) ok = 0;
         s_ok = ok;
     }
@@ -96,20 +106,25 @@ struct WarpQueue {
 
 // Work-unit dealer: a warp's first unit is its global warp index (no atomic),
 // later ones come from the cursor, offset by the number of warps, so steps
-// with little work cost no atomics at all.
+// with little work cost no atomics at all. The cursor increment for the next
+// unit is issued when a unit is handed out and its reply is only read at the
+// next take(), so its latency overlaps the unit's work.
 struct UnitDealer {
     unsigned *cursor;
-    uint32_t next;
+    uint32_t ticket;  // lane 0: reply of the increment in flight
     uint32_t nwarps;
+    bool first;
     __device__ __forceinline__ UnitDealer(unsigned *c)
-        : cursor(c), next((blockIdx.x * blockDim.x + threadIdx.x) >> 5), nwarps((gridDim.x * blockDim.x) >> 5) {}
+        : cursor(c), ticket(0), nwarps((gridDim.x * blockDim.x) >> 5), first(true) {}
     __device__ __forceinline__ uint32_t take(uint32_t units) {
-        const uint32_t u = next;
-        if (u < units) {
-            uint32_t t = 0;
-            if ((threadIdx.x & 31) == 0) t = atomicAdd(cursor, 1u);
-            next = nwarps + __shfl_sync(0xffffffffu, t, 0);
+        uint32_t u;
+        if (first) {
+            u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+            first = false;
+        } else {
+            u = nwarps + __shfl_sync(0xffffffffu, ticket, 0);
         }
+        if (u < units && (threadIdx.x & 31) == 0) ticket = atomicAdd(cursor, 1u);
         return u;
     }
 };

@@ -1,6 +1,7 @@
 // Library core: status strings and thread-local error messages, device
 // queries, pointer classification, and the device-resident graph object
 // (the device copy of the reference's struct GraphCSR, graphCSR.h:14-31).
+#include <algorithm>
 #include <atomic>
 #include <cstdarg>
 #include <cstring>
@@ -72,6 +73,18 @@ int ensure_device() {
         if (cudaGetDeviceProperties(&p, dev) == cudaSuccess) {
             g_props[dev].sms = p.multiProcessorCount;
             g_props[dev].l2 = (size_t)p.l2CacheSize;
+            // Working buffers come from the device's default stream-ordered
+            // pool. With its default release threshold (0) every stream
+            // synchronize hands freed blocks back to the driver, and the next
+            // call maps them again (hundreds of MB per BFS on large graphs);
+            // keep up to a quarter of device memory (at most 64 GB) cached in
+            // this process instead.
+            cudaMemPool_t pool;
+            if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+                uint64_t keep = std::min<uint64_t>((uint64_t)p.totalGlobalMem / 4, 64ull << 30);
+                (void)cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            }
+            (void)cudaGetLastError();
         } else {
             g_props[dev].sms = 132;
             g_props[dev].l2 = 50u << 20;

@@ -211,6 +211,9 @@ struct gbx_graph {
     uint32_t *low_count = nullptr;
     // every edge has its reverse: -1 unknown, 0 no, 1 yes
     int symmetric = -1;
+    // every pull-CSR neighbour has out-degree > 0 (true for an inverse CSR of
+    // the same edges, and for symmetric graphs): -1 unknown, 0 no, 1 yes
+    int pull_sources_live = -1;
     // tuning (gbx_graph_set_tuning / gbx_autotune): BFS direction switch and
     // SSSP bucket width (0 = default for the graph's weights)
     uint32_t bfs_alpha = 15, bfs_beta = 18;

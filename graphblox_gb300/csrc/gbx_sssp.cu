@@ -26,6 +26,7 @@ namespace gbx {
 
 constexpr uint32_t kSsspHubDeg = 1024;
 constexpr uint32_t kSsspHubChunk = 1024;
+constexpr uint32_t kSsspMaxSplit = 8;  // most warps sharing one 32-vertex group's edges
 constexpr int kSsspThreads = 256;
 constexpr int kSsspWarps = kSsspThreads / 32;
 
@@ -202,7 +203,13 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
                             const uint32_t *hcin, uint32_t nh, uint32_t nc, Relaxer &rx, SsspRound *cur,
                             uint32_t *s_pre, uint32_t *s_base, uint32_t *s_d) {
     const uint32_t lane = threadIdx.x & 31;
-    const uint32_t units = nc + (qn + 31) / 32;
+    // a round with fewer 32-vertex groups than warps cuts each group's edges
+    // into `split` interleaved parts (128-edge batches i0 = part*128, +split*128,
+    // ...) so that its relaxations are not one warp's serial chain
+    const uint32_t groups = (qn + 31) / 32;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t split = groups ? max(1u, min(kSsspMaxSplit, nwarps / groups)) : 1u;
+    const uint32_t units = nc + groups * split;
     UnitDealer dealer(&cur->cursor);
     for (;;) {
         const uint32_t unit = dealer.take(units);
@@ -228,7 +235,8 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
                 rx.relax4(dq, eq, u, act);
             }
         } else {
-            const uint32_t qi = (unit - nc) * 32 + lane;
+            const uint32_t group = (unit - nc) / split, part = (unit - nc) % split;
+            const uint32_t qi = group * 32 + lane;
             uint32_t b = 0, deg = 0, d = 0;
             if (qi < qn) {
                 const uint32_t v = __ldcg(qin + qi);
@@ -249,7 +257,7 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
             __syncwarp();
             const uint32_t tot = s_pre[32];
             uint32_t k = 0;
-            for (uint32_t i0 = 0; i0 < tot; i0 += 128) {
+            for (uint32_t i0 = part * 128; i0 < tot; i0 += split * 128) {
                 uint32_t u[4], e[4], dd[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
@@ -293,6 +301,7 @@ __global__ void __launch_bounds__(kSsspThreads) sssp_persistent_kernel(SsspArgs 
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t nthreads = gridDim.x * blockDim.x;
     SsspState *st = a.st;
+    grid_barrier_init();
     uint32_t qn = 1, nh = 0, nc = 0, far_len = 0;
     {
         const uint32_t d0 = __ldg(a.outdeg + a.source);

@@ -7,12 +7,15 @@
 //   sssp_delta  bucket width of the near/far schedule
 //   pull_heavy_min  in-degree above which the pull engine (PR, SpMV) cuts a
 //               row into CTA-sized chunks (rows of 33 up to it get a warp)
-// None of them changes a result: BFS levels, processed_nodes and iteration
-// (= depth + 2, one step per level) and SSSP distances are the same for every
-// setting, and PR/SpMV sums only change their FP32 summation order (within
-// the 1e-6 relative L1 bound); only the time differs. gbx_autotune times
-// candidates on sample sources of the graph itself with CUDA events and keeps
-// the fastest.
+// SSSP distances are the same for every setting, and PR/SpMV sums only change
+// their FP32 summation order (within the 1e-6 relative L1 bound). BFS levels,
+// processed_nodes and iteration are the same for every bfs_alpha / bfs_beta
+// when the pull CSR is the inverse of the forward CSR (or the graph is
+// symmetric); without an inverse CSR the reference pulls over out-edges, and
+// on an asymmetric graph its levels then depend on the direction schedule, so
+// gbx_autotune leaves the BFS thresholds at the reference's values there.
+// gbx_autotune times candidates on sample sources of the graph itself with
+// CUDA events and keeps the fastest.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -109,7 +112,7 @@ extern "C" int gbx_autotune(gbx_graph *g, uint32_t flags, uint32_t num_samples, 
     GBX_TRY(sample_sources(g, num_samples, s, &src));
     DevBuf<uint32_t> out;
     GBX_TRY(out.alloc(g->V, s));
-    if (flags & 1u) {
+    if ((flags & 1u) && g->has_inverse()) {
         const uint32_t cands[] = {4, 15, 64, 256, 1024, 4096};
         float best = 1e30f;
         uint32_t best_a = g->bfs_alpha;
@@ -130,7 +133,7 @@ extern "C" int gbx_autotune(gbx_graph *g, uint32_t flags, uint32_t num_samples, 
         g->bfs_alpha = best_a;
     }
     if (flags & 2u) {
-        const uint32_t cands_w[] = {128, 512, 1024, 2048, 4096, 16384};
+        const uint32_t cands_w[] = {64, 128, 256, 512, 1024, 4096};
         const uint32_t cands_u[] = {1, 2, 4};
         const uint32_t *cands = g->weight ? cands_w : cands_u;
         const int nc = g->weight ? 6 : 3;

@@ -108,14 +108,18 @@ int gbx_graph_device_arrays(const gbx_graph *g, const uint32_t **offsets, const 
  * exceed unexplored edges / alpha; the reference fixes 15), "bfs_beta" (stay
  * bottom-up while the frontier exceeds V / beta; 18), "sssp_delta" (bucket
  * width, 0 = default), "pull_heavy_min" (in-degree above which PR/SpMV cut a
- * row into CTA-sized chunks; 4096). No knob changes an integer result; PR and
- * SpMV sums may change their FP32 summation order only. */
+ * row into CTA-sized chunks; 4096). SSSP distances never change; PR and SpMV
+ * sums may change their FP32 summation order only. BFS results do not depend
+ * on alpha/beta when the graph has an inverse CSR or is symmetric; without an
+ * inverse CSR the reference pulls over out-edges, and on an asymmetric graph
+ * its levels then follow the direction schedule (gbx_autotune does not touch
+ * alpha/beta on such graphs). */
 int gbx_graph_set_tuning(gbx_graph *g, const char *key, double value);
 int gbx_graph_get_tuning(const gbx_graph *g, const char *key, double *value);
 /* Time candidate settings on num_samples sources of this graph (CUDA
- * events) and keep the fastest: flags bit 0 BFS direction threshold, bit 1
- * SSSP bucket width, bit 2 the pull engine's heavy-row threshold (timed on
- * PageRank iterations). */
+ * events) and keep the fastest: flags bit 0 BFS direction threshold (graphs
+ * with an inverse CSR only), bit 1 SSSP bucket width, bit 2 the pull engine's
+ * heavy-row threshold (timed on PageRank iterations). */
 int gbx_autotune(gbx_graph *g, uint32_t flags, uint32_t num_samples, void *stream);
 
 /* ---- BFS --------------------------------------------------------------- */

@@ -300,3 +300,28 @@ def test_tuning_knobs_keep_results(gbx, cuda_device):
             with pytest.raises(gbx.GbxError) as e:
                 dg.set_tuning(key, bad)
             assert e.value.status == -1
+
+
+def test_bfs_pull_over_forward_with_sinks(gbx, cuda_device):
+    """No inverse CSR (the reference's DIRECTED 0 pull over out-edges) on a
+    directed RMAT graph whose out-neighbours include sinks: the bottom-up
+    frontier bitmap must then hold the frontier's out-degree-0 vertices too.
+    Levels here depend on the direction schedule, so the reference's
+    thresholds stay in place and the autotuner leaves them alone."""
+    scale = 14
+    src, dst = gbx.generate_rmat(scale, (1 << scale) * 8, seed=21)
+    V = 1 << scale
+    deg, idx, s, d, _ = gbx.csr_build(src, dst, num_vertices=V, dedup=True, sort=1)
+    assert np.any(deg[d] == 0)  # some out-neighbour is a sink
+    g = gbx.GraphCSR(V, int(s.shape[0]), deg, idx, d, s, None, np.arange(V, dtype=np.uint32),
+                     np.arange(V, dtype=np.uint32))
+    host = po.HostCSR(V, deg, idx, d)
+    rng = np.random.default_rng(3)
+    with gbx.DeviceGraph.from_graph_csr(g) as dg:
+        tuned = dg.autotune(bfs=True, sssp=False, samples=2)
+        assert (tuned["bfs_alpha"], tuned["bfs_beta"]) == (15, 18)
+        for r in [0] + [int(x) for x in rng.choice(np.nonzero(deg)[0], 6)]:
+            dd, _, proc, it = po.bfs(host, r, None)
+            st = gbx.breadth_first_search(dg, r)
+            np.testing.assert_array_equal(st.distances, dd)
+            assert (st.processed_nodes, st.iteration) == (proc, it)
