@@ -39,12 +39,34 @@ struct SsspRound {
     unsigned long long relaxed;
 };
 
+// Round trace (printed when GBX_TRACE is set): kind (0 start, 1 relax round,
+// 2 bucket move), near vertices / new threshold, relaxations / far pile, time.
+constexpr unsigned kSsspTraceMax = 256;
+struct SsspTraceRec {
+    unsigned kind, a;
+    unsigned long long b, ns;
+};
+
 struct SsspState {
     GridSync gs;
     SsspRound r[3];
     unsigned rounds, status;
     unsigned long long relaxed;
+    unsigned ntrace, pad;
+    SsspTraceRec trace[kSsspTraceMax];
 };
+
+__device__ __forceinline__ void sssp_trace(SsspState *st, unsigned kind, unsigned a, unsigned long long b) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && st->ntrace < kSsspTraceMax) {
+        unsigned long long t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        SsspTraceRec &r = st->trace[st->ntrace++];
+        r.kind = kind;
+        r.a = a;
+        r.b = b;
+        r.ns = t;
+    }
+}
 
 struct SsspArgs {
     const uint32_t *off, *dest, *outdeg;
@@ -313,6 +335,7 @@ __global__ void __launch_bounds__(kSsspThreads) sssp_persistent_kernel(SsspArgs 
     unsigned long long relaxed = 0;
     bool failed = false;
     const uint32_t max_rounds = 4 * a.V + 64;
+    sssp_trace(st, 0, 1, 0);
     for (uint32_t s = 0;; ++s) {
         SsspRound *cur = &st->r[s % 3];
         if (blockIdx.x == 0 && threadIdx.x == 0) zero_round(&st->r[(s + 1) % 3], 0);
@@ -336,6 +359,7 @@ __global__ void __launch_bounds__(kSsspThreads) sssp_persistent_kernel(SsspArgs 
             relax_phase(a, a.q[ib], qn, a.hv[ib], a.hc[ib], nh, nc, rx, cur, s_pre[wid], s_base[wid], s_d[wid]);
             if (!grid_barrier(&st->gs)) { failed = true; break; }
             relaxed += __ldcg(&cur->relaxed);
+            sssp_trace(st, 1, qn + nh, __ldcg(&cur->relaxed));
             qn = __ldcg(&cur->near_len);
             unsigned long long hb = __ldcg(&cur->near_hub);
             nh = (uint32_t)(hb >> 32);
@@ -392,6 +416,7 @@ __global__ void __launch_bounds__(kSsspThreads) sssp_persistent_kernel(SsspArgs 
         nh = (uint32_t)(hb >> 32);
         nc = (uint32_t)hb;
         far_len = __ldcg(&cur->far_len);
+        sssp_trace(st, 2, threshold > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)threshold, far_len);
         fb ^= 1;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -501,6 +526,14 @@ extern "C" int gbx_sssp(gbx_graph *g, uint32_t source, uint32_t delta, uint32_t 
     GBX_CUDA(cudaStreamSynchronize(s));
     GBX_REQUIRE(hs.gs.error == 0, GBX_ERR_DEVICE_TIMEOUT, "SSSP grid barrier wait expired");
     GBX_REQUIRE(hs.status == 0, GBX_ERR_ITER_CAP, "SSSP round cap reached");
+    if (trace_enabled()) {
+        fprintf(stderr, "| gbx_sssp source %u delta %u: %-6s | %-10s | %-12s | %-9s |\n", source, delta, "step",
+                "near/thr", "relaxed/far", "us");
+        static const char *names[] = {"start", "relax", "bucket"};
+        for (unsigned i = 1; i < hs.ntrace && i < kSsspTraceMax; ++i)
+            fprintf(stderr, "| %-30s | %-10u | %-12llu | %-9.2f |\n", names[hs.trace[i].kind % 3], hs.trace[i].a,
+                    hs.trace[i].b, (hs.trace[i].ns - hs.trace[i - 1].ns) * 1e-3);
+    }
     if (result) {
         result->reached = (uint32_t)hf[0];
         result->rounds = hs.rounds;
