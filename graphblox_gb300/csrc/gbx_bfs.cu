@@ -598,24 +598,34 @@ __global__ void bfs_finish_kernel(const uint32_t *level, const int32_t *parent, 
     }
 }
 
+// Working arrays of one traversal, carved from the graph's scratch arena;
+// the last two are staging for host-memory outputs.
 struct BfsWork {
-    DevBuf<uint32_t> level, visited, bm0, bm1, q0, q1, hv0, hv1, hc0, hc1;
-    DevBuf<int32_t> parent;
-    DevBuf<BfsState> st;
-    int alloc(uint32_t V, cudaStream_t s) {
-        uint32_t words = (V + 31) / 32;
-        GBX_TRY(level.alloc(V, s));
-        GBX_TRY(parent.alloc(V, s));
-        GBX_TRY(visited.alloc(words, s));
-        GBX_TRY(bm0.alloc(words, s));
-        GBX_TRY(bm1.alloc(words, s));
-        GBX_TRY(q0.alloc(V, s));
-        GBX_TRY(q1.alloc(V, s));
-        GBX_TRY(hv0.alloc(V, s));
-        GBX_TRY(hv1.alloc(V, s));
-        GBX_TRY(hc0.alloc(V, s));
-        GBX_TRY(hc1.alloc(V, s));
-        GBX_TRY(st.alloc(1, s));
+    uint32_t *level, *visited, *bm0, *bm1, *q0, *q1, *hv0, *hv1, *hc0, *hc1, *dist_stage;
+    int32_t *parent, *par_stage;
+    BfsState *st;
+    static size_t bytes(uint32_t V, bool stage) {
+        const size_t words = (V + 31) / 32, r = Scratch::round_up((size_t)V * 4);
+        return 8 * r + 3 * Scratch::round_up(words * 4) + (stage ? 2 * r : 0) +
+               Scratch::round_up(sizeof(BfsState));
+    }
+    int carve(Scratch &sc, uint32_t V, bool stage) {
+        const size_t words = (V + 31) / 32;
+        level = sc.carve<uint32_t>(V);
+        parent = sc.carve<int32_t>(V);
+        visited = sc.carve<uint32_t>(words);
+        bm0 = sc.carve<uint32_t>(words);
+        bm1 = sc.carve<uint32_t>(words);
+        q0 = sc.carve<uint32_t>(V);
+        q1 = sc.carve<uint32_t>(V);
+        hv0 = sc.carve<uint32_t>(V);
+        hv1 = sc.carve<uint32_t>(V);
+        hc0 = sc.carve<uint32_t>(V);
+        hc1 = sc.carve<uint32_t>(V);
+        dist_stage = stage ? sc.carve<uint32_t>(V) : nullptr;
+        par_stage = stage ? sc.carve<int32_t>(V) : nullptr;
+        st = sc.carve<BfsState>(1);
+        GBX_REQUIRE(st != nullptr, GBX_ERR_CUDA, "BFS scratch carve overflow");
         return GBX_OK;
     }
 };
@@ -633,12 +643,15 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
     GBX_TRY(ensure_device());
     cudaStream_t s = (cudaStream_t)stream;
     const uint32_t V = g->V, words = (V + 31) / 32;
+    const bool stage = (distances && !is_device_ptr(distances)) || (parents && !is_device_ptr(parents));
+    Scratch sc;
+    GBX_TRY(sc.take(g, BfsWork::bytes(V, stage), s));
     BfsWork w;
-    GBX_TRY(w.alloc(V, s));
+    GBX_TRY(w.carve(sc, V, stage));
     OutArray<uint32_t> dist;
     OutArray<int32_t> par;
-    GBX_TRY(dist.bind(distances, V, s));
-    GBX_TRY(par.bind(parents, V, s));
+    GBX_TRY(dist.bind(distances, V, s, w.dist_stage));
+    GBX_TRY(par.bind(parents, V, s, w.par_stage));
     const unsigned grid1 = std::min<unsigned>(ceil_div(V, 256), (unsigned)num_sms() * 8);
     if (g->pull_sources_live < 0) {
         DevBuf<uint32_t> bad;
@@ -654,11 +667,11 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
         GBX_CUDA(cudaStreamSynchronize(s));
         g->pull_sources_live = h ? 0 : 1;
     }
-    bfs_init_kernel<<<grid1, 256, 0, s>>>(w.level.p, w.parent.p, w.visited.p, w.bm0.p, w.bm1.p, V, words,
+    bfs_init_kernel<<<grid1, 256, 0, s>>>(w.level, w.parent, w.visited, w.bm0, w.bm1, V, words,
                                           source);
     GBX_LAUNCH_CHECK();
-    GBX_CUDA(cudaMemsetAsync(w.st.p, 0, sizeof(BfsState), s));
-    bfs_seed_kernel<<<1, 1, 0, s>>>(g->out_degree, source, w.q0.p, w.hv0.p, w.hc0.p, w.st.p);
+    GBX_CUDA(cudaMemsetAsync(w.st, 0, sizeof(BfsState), s));
+    bfs_seed_kernel<<<1, 1, 0, s>>>(g->out_degree, source, w.q0, w.hv0, w.hc0, w.st);
     GBX_LAUNCH_CHECK();
     BfsArgs a;
     a.off = g->offsets;
@@ -674,29 +687,30 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
     a.alpha = g->bfs_alpha;
     a.beta = g->bfs_beta;
     a.pull_live = g->pull_sources_live == 1 ? 1u : 0u;
-    a.level = w.level.p;
-    a.parent = w.parent.p;
-    a.visited = w.visited.p;
-    a.bm[0] = w.bm0.p;
-    a.bm[1] = w.bm1.p;
-    a.q[0] = w.q0.p;
-    a.q[1] = w.q1.p;
-    a.hv[0] = w.hv0.p;
-    a.hv[1] = w.hv1.p;
-    a.hc[0] = w.hc0.p;
-    a.hc[1] = w.hc1.p;
-    a.st = w.st.p;
+    a.level = w.level;
+    a.parent = w.parent;
+    a.visited = w.visited;
+    a.bm[0] = w.bm0;
+    a.bm[1] = w.bm1;
+    a.q[0] = w.q0;
+    a.q[1] = w.q1;
+    a.hv[0] = w.hv0;
+    a.hv[1] = w.hv1;
+    a.hc[0] = w.hc0;
+    a.hc[1] = w.hc1;
+    a.st = w.st;
     int grid = 0;
-    GBX_TRY(coop_grid(bfs_persistent_kernel, kBfsThreads, 0, &grid));
+    static int grid_cache[64] = {0};
+    GBX_TRY(coop_grid(bfs_persistent_kernel, kBfsThreads, 0, &grid, &grid_cache));
     void *args[] = {&a};
     GBX_CUDA(cudaLaunchCooperativeKernel((const void *)bfs_persistent_kernel, grid, kBfsThreads, args, 0, s));
     GBX_LAUNCH_CHECK();
-    bfs_finish_kernel<<<grid1, 256, 0, s>>>(w.level.p, w.parent.p, g->out_degree, V, dist.d, par.d);
+    bfs_finish_kernel<<<grid1, 256, 0, s>>>(w.level, w.parent, g->out_degree, V, dist.d, par.d);
     GBX_LAUNCH_CHECK();
     GBX_TRY(dist.finish(s));
     GBX_TRY(par.finish(s));
     BfsState hs;
-    GBX_CUDA(cudaMemcpyAsync(&hs, w.st.p, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    GBX_CUDA(cudaMemcpyAsync(&hs, w.st, sizeof(hs), cudaMemcpyDeviceToHost, s));
     GBX_CUDA(cudaStreamSynchronize(s));
     GBX_REQUIRE(hs.gs.error == 0, GBX_ERR_DEVICE_TIMEOUT, "BFS grid barrier wait expired");
     GBX_REQUIRE(hs.status == 0, GBX_ERR_ITER_CAP, "BFS step cap reached");

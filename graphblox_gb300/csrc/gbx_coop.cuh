@@ -129,13 +129,22 @@ struct UnitDealer {
     }
 };
 
-// Largest co-resident grid for `kernel` with `threads` per CTA.
+// Largest co-resident grid for `kernel` with `threads` per CTA. `cache`
+// (one per call site, indexed by device) keeps the answer after the first
+// occupancy query.
 template <class K>
-inline int coop_grid(K kernel, int threads, size_t smem, int *grid) {
+inline int coop_grid(K kernel, int threads, size_t smem, int *grid, int (*cache)[64] = nullptr) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cache && dev >= 0 && dev < 64 && (*cache)[dev] > 0) {
+        *grid = (*cache)[dev];
+        return GBX_OK;
+    }
     int per_sm = 0;
     GBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
     GBX_REQUIRE(per_sm > 0, GBX_ERR_CUDA, "kernel cannot be resident");
     *grid = per_sm * num_sms();
+    if (cache && dev >= 0 && dev < 64) (*cache)[dev] = *grid;
     return GBX_OK;
 }
 

@@ -124,7 +124,9 @@ struct OutArray {
     T *host = nullptr;
     size_t n = 0;
     DevBuf<T> owned;
-    int bind(T *dst, size_t count, cudaStream_t s) {
+    // staging (optional): device memory of count elements to use for a host
+    // destination instead of a new allocation
+    int bind(T *dst, size_t count, cudaStream_t s, T *staging = nullptr) {
         n = count;
         host = nullptr;
         if (dst == nullptr) {
@@ -136,6 +138,10 @@ struct OutArray {
             return GBX_OK;
         }
         host = dst;
+        if (staging) {
+            d = staging;
+            return GBX_OK;
+        }
         GBX_TRY(owned.alloc(count ? count : 1, s));
         d = owned.p;
         return GBX_OK;
@@ -229,6 +235,10 @@ struct gbx_graph {
     struct gbx_ms_plan *ms_plan = nullptr;
     // PageRank working memory and captured iteration loop (gbx_pagerank.cu)
     struct gbx_pr_cache *pr_cache = nullptr;
+    // device scratch lent to one synchronous call at a time (gbx::Scratch)
+    char *arena = nullptr;
+    size_t arena_bytes = 0;
+    int arena_busy = 0;
 
     bool has_inverse() const { return in_offsets != nullptr; }
     // CSR used by pull-direction kernels (reference: inverse when DIRECTED)
@@ -244,6 +254,60 @@ void gbx_free_ms_plan(struct gbx_ms_plan *p);
 void gbx_free_pr_cache(struct gbx_pr_cache *c);
 
 namespace gbx {
+// Device scratch for one synchronous call: carved from the graph's arena
+// (grown on demand, kept between calls), or from a single stream-ordered
+// allocation when another call holds the arena. The holder's stream is
+// synchronized before the arena is handed back.
+struct Scratch {
+    char *base = nullptr;
+    size_t used = 0, cap = 0;
+    gbx_graph *held = nullptr;
+    cudaStream_t stream = nullptr;
+    DevBuf<char> own;
+    Scratch() = default;
+    Scratch(const Scratch &) = delete;
+    Scratch &operator=(const Scratch &) = delete;
+    static size_t round_up(size_t b) { return (b + 255) & ~size_t(255); }
+    int take(gbx_graph *g, size_t bytes, cudaStream_t s) {
+        stream = s;
+        cap = bytes;
+        if (__atomic_exchange_n(&g->arena_busy, 1, __ATOMIC_ACQ_REL) == 0) {
+            held = g;
+            if (g->arena_bytes < bytes) {
+                cudaFree(g->arena);  // idle: every holder synchronized before release
+                g->arena = nullptr;
+                g->arena_bytes = 0;
+                if (cudaMalloc(&g->arena, bytes) != cudaSuccess) {
+                    (void)cudaGetLastError();
+                    g->arena = nullptr;
+                    set_error("device allocation of %zu bytes of scratch failed", bytes);
+                    return GBX_ERR_NOMEM;
+                }
+                g->arena_bytes = bytes;
+            }
+            base = g->arena;
+            return GBX_OK;
+        }
+        GBX_TRY(own.alloc(bytes, s));
+        base = own.p;
+        return GBX_OK;
+    }
+    // next count elements of T (256-byte aligned); the caller sized take()
+    // with round_up() of every carve
+    template <typename T>
+    T *carve(size_t count) {
+        T *p = reinterpret_cast<T *>(base + used);
+        used += round_up(count * sizeof(T));
+        return used <= cap ? p : nullptr;
+    }
+    ~Scratch() {
+        if (held) {
+            cudaStreamSynchronize(stream);
+            __atomic_store_n(&held->arena_busy, 0, __ATOMIC_RELEASE);
+        }
+    }
+};
+
 // plan for the pull CSR of g (built on first use, cached on the graph)
 int get_pull_plan(gbx_graph *g, cudaStream_t s, gbx_gather_plan **plan);
 void free_plan(gbx_gather_plan *p);

@@ -34,9 +34,11 @@ struct SsspRound {
     unsigned cursor;
     unsigned near_len;          // next near queue (degree in (0, hub])
     unsigned far_len;           // far pile length (carried across rounds)
-    unsigned far_min;
+    unsigned far_min;           // smallest distance pushed at or past the threshold
     unsigned long long near_hub;  // next near hubs: (count << 32) | chunks
     unsigned long long relaxed;
+    unsigned kept_min;          // smallest distance the far-pile split kept
+    unsigned pad;
 };
 
 // Round trace (printed when GBX_TRACE is set): kind (0 start, 1 relax round,
@@ -85,44 +87,6 @@ __device__ __forceinline__ uint32_t sssp_add(uint32_t d, float w) {
 
 __device__ __forceinline__ uint32_t sssp_chunks(uint32_t d) { return (d + kSsspHubChunk - 1) / kSsspHubChunk; }
 
-// push u into the next near generation (deduplicated per round by stamp)
-__device__ __forceinline__ void near_push(const SsspArgs &a, SsspRound *cnt, uint32_t *qout, uint32_t *hvout,
-                                          uint32_t *hcout, uint32_t u, bool want) {
-    bool push = false;
-    if (want) {
-        const uint32_t du = __ldg(a.outdeg + u);
-        if (du > kSsspHubDeg) {
-            unsigned long long old = atomicAdd(&cnt->near_hub, (1ull << 32) | sssp_chunks(du));
-            uint32_t slot = (uint32_t)(old >> 32);
-            hvout[slot] = u;
-            hcout[slot] = (uint32_t)old;
-        } else {
-            push = du > 0;
-        }
-    }
-    const uint32_t lane = threadIdx.x & 31;
-    const unsigned m = __ballot_sync(0xffffffffu, push);
-    if (m) {
-        uint32_t leader = __ffs(m) - 1;
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(&cnt->near_len, (unsigned)__popc(m));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (push) qout[base + __popc(m & ((1u << lane) - 1u))] = u;
-    }
-}
-
-__device__ __forceinline__ void far_push(const SsspArgs &a, SsspRound *cnt, uint32_t *far, uint32_t u, bool push) {
-    const uint32_t lane = threadIdx.x & 31;
-    const unsigned m = __ballot_sync(0xffffffffu, push);
-    if (m) {
-        uint32_t leader = __ffs(m) - 1;
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(&cnt->far_len, (unsigned)__popc(m));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (push) far[base + __popc(m & ((1u << lane) - 1u))] = u;
-    }
-}
-
 struct Relaxer {
     const SsspArgs &a;
     uint32_t threshold, round;
@@ -130,40 +94,10 @@ struct Relaxer {
     uint32_t *qout, *hvout, *hcout, *far;
     WarpQueue wnear, wfar;
     unsigned long long relaxed = 0;
+    uint32_t far_min = 0xFFFFFFFFu;  // smallest improvement at or past the threshold
     __device__ __forceinline__ Relaxer(const SsspArgs &a_, uint32_t t, uint32_t r, SsspRound *c, uint32_t *q,
                                        uint32_t *hv, uint32_t *hc, uint32_t *f, uint32_t *bn, uint32_t *bf)
         : a(a_), threshold(t), round(r), cnt(c), qout(q), hvout(hv), hcout(hc), far(f), wnear(bn), wfar(bf) {}
-    __device__ __forceinline__ void operator()(uint32_t d, uint32_t e, uint32_t u, bool active) {
-        bool to_near = false, to_far = false;
-        if (active) {
-            const float wt = a.w ? __ldcs(a.w + e) : 1.0f;
-            const uint32_t nd = sssp_add(d, wt);
-            relaxed++;
-            if (nd < __ldcg(a.dist + u)) {
-                const uint32_t old = atomicMin(a.dist + u, nd);
-                if (nd < old) {
-                    if (nd < threshold) to_near = atomicExch(a.stamp + u, round) != round;
-                    else to_far = atomicExch(a.in_far + u, 1u) == 0u;
-                }
-            }
-        }
-        // hubs go straight to the hub list; the rest through the warp buffers
-        bool hub = false;
-        if (to_near) {
-            const uint32_t du = __ldg(a.outdeg + u);
-            if (du > kSsspHubDeg) {
-                hub = true;
-                unsigned long long old = atomicAdd(&cnt->near_hub, (1ull << 32) | sssp_chunks(du));
-                uint32_t slot = (uint32_t)(old >> 32);
-                hvout[slot] = u;
-                hcout[slot] = (uint32_t)old;
-            } else if (du == 0) {
-                hub = true;  // nothing to relax from u
-            }
-        }
-        wnear.push(u, to_near && !hub, qout, &cnt->near_len);
-        wfar.push(u, to_far, far, &cnt->far_len);
-    }
     // Four relaxations per lane with their loads and atomics issued back to
     // back (independent), then the queue pushes.
     __device__ __forceinline__ void relax4(const uint32_t (&d)[4], const uint32_t (&e)[4], const uint32_t (&u)[4],
@@ -177,28 +111,31 @@ struct Relaxer {
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) old[q] = (act[q] && nd[q] < cur[q]) ? atomicMin(a.dist + u[q], nd[q]) : 0u;
-        bool to_near[4], to_far[4];
+        bool to_near[4], to_far[4], below[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             relaxed += act[q] ? 1u : 0u;
             const bool imp = act[q] && nd[q] < cur[q] && nd[q] < old[q];
-            to_near[q] = imp && nd[q] < threshold && atomicExch(a.stamp + u[q], round) != round;
+            below[q] = imp && nd[q] < threshold;
+            to_near[q] = below[q] && atomicExch(a.stamp + u[q], round) != round;
             to_far[q] = imp && nd[q] >= threshold && atomicExch(a.in_far + u[q], 1u) == 0u;
+            if (imp && nd[q] >= threshold) far_min = min(far_min, nd[q]);
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             bool hub = false;
-            if (to_near[q]) {
-                const uint32_t du = __ldg(a.outdeg + u[q]);
-                if (du > kSsspHubDeg) {
-                    hub = true;
-                    unsigned long long h = atomicAdd(&cnt->near_hub, (1ull << 32) | sssp_chunks(du));
-                    uint32_t slot = (uint32_t)(h >> 32);
-                    hvout[slot] = u[q];
-                    hcout[slot] = (uint32_t)h;
-                } else if (du == 0) {
-                    hub = true;
-                }
+            const uint32_t du = below[q] ? __ldg(a.outdeg + u[q]) : 1u;
+            if (du == 0) {
+                // nothing to expand: its snapshot is simply its distance, so
+                // a far entry it left behind is dropped, not re-bucketed
+                atomicMin(a.settled + u[q], nd[q]);
+                hub = true;
+            } else if (to_near[q] && du > kSsspHubDeg) {
+                hub = true;
+                unsigned long long h = atomicAdd(&cnt->near_hub, (1ull << 32) | sssp_chunks(du));
+                uint32_t slot = (uint32_t)(h >> 32);
+                hvout[slot] = u[q];
+                hcout[slot] = (uint32_t)h;
             }
             wnear.push(u[q], to_near[q] && !hub, qout, &cnt->near_len);
             wfar.push(u[q], to_far[q], far, &cnt->far_len);
@@ -209,6 +146,8 @@ struct Relaxer {
         wfar.flush(far, &cnt->far_len);
         unsigned long long r = warp_sum(relaxed);
         if ((threadIdx.x & 31) == 0 && r) atomicAdd(&cnt->relaxed, r);
+        const uint32_t m = warp_min(far_min);
+        if ((threadIdx.x & 31) == 0 && m != 0xFFFFFFFFu) atomicMin(&cnt->far_min, m);
     }
 };
 
@@ -250,7 +189,6 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
                     uint32_t j = j0 + q * 32 + lane;
                     u[q] = j < ce ? __ldcs(a.dest + j) : 0u;
                 }
-#pragma unroll
                 const uint32_t dq[4] = {d, d, d, d};
                 const uint32_t eq[4] = {j0 + lane, j0 + 32 + lane, j0 + 64 + lane, j0 + 96 + lane};
                 const bool act[4] = {eq[0] < ce, eq[1] < ce, eq[2] < ce, eq[3] < ce};
@@ -294,8 +232,8 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
                         u[q] = __ldcs(a.dest + e[q]);
                     }
                 }
-#pragma unroll
-                const bool act[4] = {i0 + lane < tot, i0 + 32 + lane < tot, i0 + 64 + lane < tot, i0 + 96 + lane < tot};
+                const bool act[4] = {i0 + lane < tot, i0 + 32 + lane < tot, i0 + 64 + lane < tot,
+                                     i0 + 96 + lane < tot};
                 rx.relax4(dd, e, u, act);
             }
             __syncwarp();
@@ -311,9 +249,10 @@ __device__ __forceinline__ void zero_round(SsspRound *r, uint32_t far_len) {
     r->far_min = 0xFFFFFFFFu;
     r->near_hub = 0;
     r->relaxed = 0;
+    r->kept_min = 0xFFFFFFFFu;
 }
 
-__global__ void __launch_bounds__(kSsspThreads) sssp_persistent_kernel(SsspArgs a) {
+__global__ void __launch_bounds__(kSsspThreads, 5) sssp_persistent_kernel(SsspArgs a) {
     __shared__ uint32_t s_pre[kSsspWarps][33];
     __shared__ uint32_t s_base[kSsspWarps][32];
     __shared__ uint32_t s_d[kSsspWarps][32];
@@ -331,10 +270,17 @@ __global__ void __launch_bounds__(kSsspThreads) sssp_persistent_kernel(SsspArgs 
         else if (d0 == 0) { qn = 0; }
     }
     uint64_t threshold = a.delta;
+    // lower bound of the far pile's smallest live distance: the smallest
+    // improvement pushed at or past the threshold since the pile was last
+    // split (whose split computed the kept entries' exact minimum)
+    uint32_t far_lb = 0xFFFFFFFFu;
     uint32_t round = 1, rounds = 0, fb = 0, gen = 0;
     unsigned long long relaxed = 0;
     bool failed = false;
     const uint32_t max_rounds = 4 * a.V + 64;
+    // round 0's counters (the host zeroed the state; the minima start at
+    // "none"); nothing touches them before the first grid barrier
+    if (blockIdx.x == 0 && threadIdx.x == 0) zero_round(&st->r[0], 0);
     sssp_trace(st, 0, 1, 0);
     for (uint32_t s = 0;; ++s) {
         SsspRound *cur = &st->r[s % 3];
@@ -365,13 +311,20 @@ __global__ void __launch_bounds__(kSsspThreads) sssp_persistent_kernel(SsspArgs 
             nh = (uint32_t)(hb >> 32);
             nc = (uint32_t)hb;
             far_len = __ldcg(&cur->far_len);
+            far_lb = min(far_lb, __ldcg(&cur->far_min));
             gen++;
             rounds++;
             continue;
         }
         if (far_len == 0) break;
-        // smallest far distance not yet expanded -> next threshold
-        {
+        // next threshold: one delta past the far pile's smallest live
+        // distance, taken from its lower bound. A bound left low by an entry
+        // that was expanded since costs at most one empty bucket move, after
+        // which the bound is exact again.
+        uint32_t fmin = far_lb;
+        if (fmin == 0xFFFFFFFFu) {
+            // no bound recorded (not expected: every far entry is pushed or
+            // kept with its distance); scan the pile
             uint32_t m = 0xFFFFFFFFu;
             for (uint32_t i = gtid; i < far_len; i += nthreads) {
                 uint32_t u = __ldcg(a.far[fb] + i);
@@ -380,19 +333,21 @@ __global__ void __launch_bounds__(kSsspThreads) sssp_persistent_kernel(SsspArgs 
             }
             m = __reduce_min_sync(0xffffffffu, m);
             if (lane == 0 && m != 0xFFFFFFFFu) atomicMin(&cur->far_min, m);
+            if (!grid_barrier(&st->gs)) { failed = true; break; }
+            fmin = __ldcg(&cur->far_min);
+            if (fmin == 0xFFFFFFFFu) break;  // every far entry is already expanded
         }
-        if (!grid_barrier(&st->gs)) { failed = true; break; }
-        const uint32_t fmin = __ldcg(&cur->far_min);
-        if (fmin == 0xFFFFFFFFu) break;  // every far entry is already expanded
         threshold = ((uint64_t)fmin / a.delta + 1) * a.delta;
         round++;
         {
             // split the far pile: below the threshold -> near, the rest stays
             const uint32_t ib = gen & 1;
             const uint32_t thr = threshold > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)threshold;
+            uint32_t kmin = 0xFFFFFFFFu;
+            WarpQueue wnear(s_wn[wid]), wfar(s_wf[wid]);
             for (uint32_t base = blockIdx.x * blockDim.x; base < far_len; base += nthreads) {
                 const uint32_t i = base + threadIdx.x;
-                bool to_near = false, keep = false;
+                bool to_near = false, keep = false, hub = false;
                 uint32_t u = 0;
                 if (i < far_len) {
                     u = __ldcg(a.far[fb] + i);
@@ -404,11 +359,31 @@ __global__ void __launch_bounds__(kSsspThreads) sssp_persistent_kernel(SsspArgs 
                         to_near = atomicExch(a.stamp + u, round) != round;
                     } else {
                         keep = true;
+                        kmin = min(kmin, d);
+                    }
+                    if (to_near) {
+                        const uint32_t du = __ldg(a.outdeg + u);
+                        if (du > kSsspHubDeg) {
+                            hub = true;
+                            const unsigned long long h =
+                                atomicAdd(&cur->near_hub, (1ull << 32) | sssp_chunks(du));
+                            const uint32_t slot = (uint32_t)(h >> 32);
+                            a.hv[ib][slot] = u;
+                            a.hc[ib][slot] = (uint32_t)h;
+                        } else if (du == 0) {
+                            // nothing to relax: settled right here
+                            hub = true;
+                            a.settled[u] = d;
+                        }
                     }
                 }
-                near_push(a, cur, a.q[ib], a.hv[ib], a.hc[ib], u, to_near);
-                far_push(a, cur, a.far[fb ^ 1], u, keep);
+                wnear.push(u, to_near && !hub, a.q[ib], &cur->near_len);
+                wfar.push(u, keep, a.far[fb ^ 1], &cur->far_len);
             }
+            wnear.flush(a.q[ib], &cur->near_len);
+            wfar.flush(a.far[fb ^ 1], &cur->far_len);
+            kmin = warp_min(kmin);
+            if (lane == 0 && kmin != 0xFFFFFFFFu) atomicMin(&cur->kept_min, kmin);
         }
         if (!grid_barrier(&st->gs)) { failed = true; break; }
         qn = __ldcg(&cur->near_len);
@@ -416,6 +391,7 @@ __global__ void __launch_bounds__(kSsspThreads) sssp_persistent_kernel(SsspArgs 
         nh = (uint32_t)(hb >> 32);
         nc = (uint32_t)hb;
         far_len = __ldcg(&cur->far_len);
+        far_lb = __ldcg(&cur->kept_min);
         sssp_trace(st, 2, threshold > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)threshold, far_len);
         fb ^= 1;
     }
@@ -475,20 +451,27 @@ extern "C" int gbx_sssp(gbx_graph *g, uint32_t source, uint32_t delta, uint32_t 
     cudaStream_t s = (cudaStream_t)stream;
     const uint32_t V = g->V;
     if (delta == 0) delta = g->sssp_delta ? g->sssp_delta : (g->weight ? 256u : 1u);
-    DevBuf<uint32_t> dist, settled, stamp, in_far, q0, q1, hv0, hv1, hc0, hc1, f0, f1;
-    DevBuf<SsspState> st;
-    DevBuf<unsigned long long> fin;
-    for (DevBuf<uint32_t> *b : {&dist, &settled, &stamp, &in_far, &q0, &q1, &hv0, &hv1, &hc0, &hc1, &f0, &f1})
-        GBX_TRY(b->alloc(V, s));
-    GBX_TRY(st.alloc(1, s));
-    GBX_TRY(fin.alloc(2, s));
+    // working arrays from the graph's scratch arena (plus staging for a
+    // host-memory result)
+    const bool stage = !is_device_ptr(distances);
+    const size_t r = Scratch::round_up((size_t)V * 4);
+    Scratch sc;
+    GBX_TRY(sc.take(g, (stage ? 13 : 12) * r + Scratch::round_up(sizeof(SsspState)) + Scratch::round_up(16), s));
+    uint32_t *dist = sc.carve<uint32_t>(V), *settled = sc.carve<uint32_t>(V), *stamp = sc.carve<uint32_t>(V);
+    uint32_t *in_far = sc.carve<uint32_t>(V), *q0 = sc.carve<uint32_t>(V), *q1 = sc.carve<uint32_t>(V);
+    uint32_t *hv0 = sc.carve<uint32_t>(V), *hv1 = sc.carve<uint32_t>(V), *hc0 = sc.carve<uint32_t>(V);
+    uint32_t *hc1 = sc.carve<uint32_t>(V), *f0 = sc.carve<uint32_t>(V), *f1 = sc.carve<uint32_t>(V);
+    uint32_t *out_stage = stage ? sc.carve<uint32_t>(V) : nullptr;
+    SsspState *st = sc.carve<SsspState>(1);
+    unsigned long long *fin = sc.carve<unsigned long long>(2);
+    GBX_REQUIRE(fin != nullptr, GBX_ERR_CUDA, "SSSP scratch carve overflow");
     OutArray<uint32_t> out;
-    GBX_TRY(out.bind(distances, V, s));
+    GBX_TRY(out.bind(distances, V, s, out_stage));
     const unsigned grid1 = std::min<unsigned>(ceil_div(V, 256), (unsigned)num_sms() * 8);
-    sssp_init_kernel<<<grid1, 256, 0, s>>>(dist.p, settled.p, stamp.p, in_far.p, V, source, g->out_degree,
-                                           q0.p, hv0.p, hc0.p);
+    sssp_init_kernel<<<grid1, 256, 0, s>>>(dist, settled, stamp, in_far, V, source, g->out_degree,
+                                           q0, hv0, hc0);
     GBX_LAUNCH_CHECK();
-    GBX_CUDA(cudaMemsetAsync(st.p, 0, sizeof(SsspState), s));
+    GBX_CUDA(cudaMemsetAsync(st, 0, sizeof(SsspState), s));
     SsspArgs a;
     a.off = g->offsets;
     a.dest = g->dest;
@@ -497,32 +480,33 @@ extern "C" int gbx_sssp(gbx_graph *g, uint32_t source, uint32_t delta, uint32_t 
     a.V = V;
     a.delta = delta;
     a.source = source;
-    a.dist = dist.p;
-    a.settled = settled.p;
-    a.stamp = stamp.p;
-    a.in_far = in_far.p;
-    a.q[0] = q0.p;
-    a.q[1] = q1.p;
-    a.hv[0] = hv0.p;
-    a.hv[1] = hv1.p;
-    a.hc[0] = hc0.p;
-    a.hc[1] = hc1.p;
-    a.far[0] = f0.p;
-    a.far[1] = f1.p;
-    a.st = st.p;
+    a.dist = dist;
+    a.settled = settled;
+    a.stamp = stamp;
+    a.in_far = in_far;
+    a.q[0] = q0;
+    a.q[1] = q1;
+    a.hv[0] = hv0;
+    a.hv[1] = hv1;
+    a.hc[0] = hc0;
+    a.hc[1] = hc1;
+    a.far[0] = f0;
+    a.far[1] = f1;
+    a.st = st;
     int grid = 0;
-    GBX_TRY(coop_grid(sssp_persistent_kernel, kSsspThreads, 0, &grid));
+    static int grid_cache[64] = {0};
+    GBX_TRY(coop_grid(sssp_persistent_kernel, kSsspThreads, 0, &grid, &grid_cache));
     void *args[] = {&a};
     GBX_CUDA(cudaLaunchCooperativeKernel((const void *)sssp_persistent_kernel, grid, kSsspThreads, args, 0, s));
     GBX_LAUNCH_CHECK();
-    GBX_CUDA(cudaMemsetAsync(fin.p, 0, 16, s));
-    sssp_finish_kernel<<<grid1, 256, 0, s>>>(dist.p, g->out_degree, V, out.d, fin.p);
+    GBX_CUDA(cudaMemsetAsync(fin, 0, 16, s));
+    sssp_finish_kernel<<<grid1, 256, 0, s>>>(dist, g->out_degree, V, out.d, fin);
     GBX_LAUNCH_CHECK();
     GBX_TRY(out.finish(s));
     SsspState hs;
     unsigned long long hf[2];
-    GBX_CUDA(cudaMemcpyAsync(&hs, st.p, sizeof(hs), cudaMemcpyDeviceToHost, s));
-    GBX_CUDA(cudaMemcpyAsync(hf, fin.p, 16, cudaMemcpyDeviceToHost, s));
+    GBX_CUDA(cudaMemcpyAsync(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    GBX_CUDA(cudaMemcpyAsync(hf, fin, 16, cudaMemcpyDeviceToHost, s));
     GBX_CUDA(cudaStreamSynchronize(s));
     GBX_REQUIRE(hs.gs.error == 0, GBX_ERR_DEVICE_TIMEOUT, "SSSP grid barrier wait expired");
     GBX_REQUIRE(hs.status == 0, GBX_ERR_ITER_CAP, "SSSP round cap reached");

@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(kTcThreads)
 // neighbours, N+(v) hashed once into a CTA-wide shared table of `slots`
 // entries (load factor <= 1/2), every warp streaming 32 upper neighbours'
 // prefixes at a time against it.
-constexpr int kWideThreads = 512;
+constexpr int kWideThreads = 1024;
 constexpr uint32_t kWideChunk = 2048;
 constexpr uint32_t kWideSlotsMax = 32768;  // 128 KiB: |N+(v)| <= 16384
 

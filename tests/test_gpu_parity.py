@@ -325,3 +325,19 @@ def test_bfs_pull_over_forward_with_sinks(gbx, cuda_device):
             st = gbx.breadth_first_search(dg, r)
             np.testing.assert_array_equal(st.distances, dd)
             assert (st.processed_nodes, st.iteration) == (proc, it)
+
+
+@pytest.mark.parametrize("delta", [1, 8, 64, 100, 200])
+def test_sssp_bucket_widths(gbx, cuda_device, delta):
+    """Weighted RMAT with hubs (rows longer than two work chunks): narrow
+    buckets (many bucket moves, far pile refills) to wide ones; the distances
+    are the unique fixed point whatever the schedule."""
+    g = _rmat_graph(gbx, 16, 16, 31, weights="int")
+    host, _ = host_views(g)
+    assert int(g.out_degree.max()) > 2048
+    rng = np.random.default_rng(delta)
+    roots = [0] + [int(r) for r in rng.choice(np.nonzero(g.out_degree)[0], 3)]
+    with gbx.DeviceGraph.from_graph_csr(g) as dg:
+        for r in roots:
+            st = gbx.sssp(dg, r, delta)
+            np.testing.assert_array_equal(st.distances, po.sssp(host, r, 64))
