@@ -242,12 +242,19 @@ __device__ __forceinline__ unsigned long long count_flat4(const uint32_t *__rest
         }
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
+            // the quad's elements inside [lo, hi) as a 4-bit mask; the
+            // membership bits of all four, then one popcount
             const uint32_t x[4] = {w[q].x, w[q].y, w[q].z, w[q].w};
+            const uint32_t from = lo[q] > e0[q] ? min(lo[q] - e0[q], 4u) : 0u;
+            const uint32_t to = hi[q] > e0[q] ? min(hi[q] - e0[q], 4u) : 0u;
+            const uint32_t valid = (0xFu >> (4u - to)) & (0xFu << from) & 0xFu;
+            uint32_t hit = 0;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const uint32_t e = e0[q] + j;
-                if (e >= lo[q] && e < hi[q] && member(x[j])) count++;
+                // a bitmap bit is cheaper to read than to branch around
+                if (Member::kProbeAll || ((valid >> j) & 1u)) hit |= member.bit(x[j]) << j;
             }
+            count += __popc(hit & valid);
         }
     }
     __syncwarp();
@@ -255,14 +262,26 @@ __device__ __forceinline__ unsigned long long count_flat4(const uint32_t *__rest
 }
 
 struct HashMember {
+    static constexpr bool kProbeAll = false;
     const uint32_t *table;
     uint32_t mask;
     __device__ __forceinline__ bool operator()(uint32_t w) const { return hash_contains(table, mask, w); }
+    __device__ __forceinline__ uint32_t bit(uint32_t w) const { return hash_contains(table, mask, w) ? 1u : 0u; }
 };
 
+// Exact bitmap over [0, nbits) with nbits a power of two. Ids are masked
+// into that range before the read: count_flat4 probes every id of a quad,
+// including ids outside the list (other rows, padding), whose bits it then
+// discards; a list's own ids are <= v < nbits and read their true bit.
 struct BitmapMember {
+    static constexpr bool kProbeAll = true;
     const uint32_t *bits;
-    __device__ __forceinline__ bool operator()(uint32_t w) const { return (bits[w >> 5] >> (w & 31)) & 1u; }
+    uint32_t id_mask;  // nbits - 1
+    __device__ __forceinline__ uint32_t bit(uint32_t w) const {
+        const uint32_t x = w & id_mask;
+        return (bits[x >> 5] >> (x & 31)) & 1u;
+    }
+    __device__ __forceinline__ bool operator()(uint32_t w) const { return bit(w) != 0u; }
 };
 
 // For the upper neighbours u in [ub, ue) of v's row nv, 32 at a time: the
@@ -288,10 +307,41 @@ __device__ __forceinline__ unsigned long long stream_pairs(const uint32_t *__res
     return count;
 }
 
+// stream_pairs for a CTA sharing one unit: warps take 32-neighbour chunks of
+// [ub, ue) from a shared-memory counter (zeroed before the CTA barrier that
+// precedes the call), so a warp with light prefixes takes more chunks and
+// the CTA's wait at the end of the unit is one chunk long.
+template <class Member>
+__device__ __forceinline__ unsigned long long stream_pairs_dealt(const uint32_t *__restrict__ off,
+                                                                const uint32_t *__restrict__ dest,
+                                                                const uint32_t *nv, uint32_t v, uint32_t ub,
+                                                                uint32_t ue, uint32_t *s_pre, uint32_t *s_base,
+                                                                uint32_t *s_end, const Member &m,
+                                                                unsigned *s_next) {
+    const uint32_t lane = threadIdx.x & 31;
+    unsigned long long count = 0;
+    for (;;) {
+        uint32_t c = 0;
+        if (lane == 0) c = atomicAdd(s_next, 1u);
+        const uint32_t a0 = ub + 32 * __shfl_sync(0xffffffffu, c, 0);
+        if (a0 >= ue) break;
+        uint32_t base = 0, len = 0;
+        if (a0 + lane < ue) {
+            const uint32_t u = __ldg(nv + a0 + lane);
+            base = __ldg(off + u);
+            len = count_le_front(dest + base, __ldg(off + u + 1) - base, v);
+        }
+        count += count_flat4(dest, base, len, s_pre, s_base, s_end, m);
+    }
+    return count;
+}
+
 struct SortedMember {
+    static constexpr bool kProbeAll = false;
     const uint32_t *list;
     uint32_t n;
     __device__ __forceinline__ bool operator()(uint32_t w) const { return sorted_contains(list, n, w); }
+    __device__ __forceinline__ uint32_t bit(uint32_t w) const { return sorted_contains(list, n, w) ? 1u : 0u; }
 };
 
 // One v, upper neighbours [ub, ue) of its row: build the membership test of
@@ -311,7 +361,8 @@ __device__ __forceinline__ unsigned long long v_unit(const uint32_t *__restrict_
             atomicOr(table + (w >> 5), 1u << (w & 31));
         }
         __syncwarp();
-        count = stream_pairs(off, dest, nv, v, ub, ue, s_pre, s_base, s_end, BitmapMember{table});
+        count = stream_pairs(off, dest, nv, v, ub, ue, s_pre, s_base, s_end,
+                             BitmapMember{table, kTcWarpSlots * 32 - 1});
         __syncwarp();
         for (uint32_t i = lane; i < pv; i += 32) table[__ldg(nv + i) >> 5] = 0u;
         __syncwarp();
@@ -335,7 +386,7 @@ struct TcBig {  // a v whose upper neighbours are dealt out in kUpperChunk units
     uint32_t v, ub, ue, first_unit;
 };
 
-__global__ void __launch_bounds__(kTcThreads)
+__global__ void __launch_bounds__(kTcThreads, 4)
     tc_vcentric_kernel(const uint32_t *__restrict__ off, const uint32_t *__restrict__ dest,
                        const uint32_t *__restrict__ low, const TcBig *__restrict__ big, uint32_t n_big,
                        uint32_t n_units, const uint8_t *__restrict__ is_big, uint32_t V, unsigned *cursor,
@@ -420,6 +471,8 @@ __global__ void __launch_bounds__(kTcThreads)
 constexpr int kWideThreads = 1024;
 constexpr uint32_t kWideChunk = 2048;
 constexpr uint32_t kWideSlotsMax = 32768;  // 128 KiB: |N+(v)| <= 16384
+static_assert((kWideSlotsMax & (kWideSlotsMax - 1)) == 0 && (kTcWarpSlots & (kTcWarpSlots - 1)) == 0,
+              "bitmap tables must cover a power-of-two id range (BitmapMember masks ids)");
 
 __global__ void __launch_bounds__(kWideThreads, 1)
     tc_wide_kernel(const uint32_t *__restrict__ off, const uint32_t *__restrict__ dest,
@@ -430,8 +483,9 @@ __global__ void __launch_bounds__(kWideThreads, 1)
     __shared__ uint32_t s_base[kWideThreads / 32][32];
     __shared__ uint32_t s_end[kWideThreads / 32][32];
     __shared__ uint32_t s_unit;
+    __shared__ unsigned s_next;
     __shared__ unsigned long long sred[32];
-    const uint32_t wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const uint32_t wid = threadIdx.x >> 5;
     unsigned long long count = 0;
     for (uint32_t i = threadIdx.x; i < slots; i += blockDim.x) s_table[i] = 0u;  // kept zero between units
     for (;;) {
@@ -450,6 +504,7 @@ __global__ void __launch_bounds__(kWideThreads, 1)
         const uint32_t ub = bg.ub + (unit - bg.first_unit) * kWideChunk;
         const uint32_t ue = min(ub + kWideChunk, bg.ue);
         const uint32_t *nv = dest + __ldg(off + v);
+        if (threadIdx.x == 0) s_next = 0;
         if (v < slots * 32) {
             // exact bitmap of N+(v) over [0, v]
             for (uint32_t i = threadIdx.x; i < pv; i += blockDim.x) {
@@ -457,8 +512,8 @@ __global__ void __launch_bounds__(kWideThreads, 1)
                 atomicOr(s_table + (w >> 5), 1u << (w & 31));
             }
             __syncthreads();
-            count += stream_pairs(off, dest, nv, v, ub + wid * 32, ue, s_pre[wid], s_base[wid], s_end[wid],
-                                  BitmapMember{s_table}, nwarps * 32, true);
+            count += stream_pairs_dealt(off, dest, nv, v, ub, ue, s_pre[wid], s_base[wid], s_end[wid],
+                                        BitmapMember{s_table, slots * 32 - 1}, &s_next);
             __syncthreads();
             for (uint32_t i = threadIdx.x; i < pv; i += blockDim.x) s_table[__ldg(nv + i) >> 5] = 0u;
         } else {
@@ -468,8 +523,8 @@ __global__ void __launch_bounds__(kWideThreads, 1)
             __syncthreads();
             for (uint32_t i = threadIdx.x; i < pv; i += blockDim.x) hash_insert(s_table, mask, __ldg(nv + i));
             __syncthreads();
-            count += stream_pairs(off, dest, nv, v, ub + wid * 32, ue, s_pre[wid], s_base[wid], s_end[wid],
-                                  HashMember{s_table, mask}, nwarps * 32, true);
+            count += stream_pairs_dealt(off, dest, nv, v, ub, ue, s_pre[wid], s_base[wid], s_end[wid],
+                                        HashMember{s_table, mask}, &s_next);
             __syncthreads();
             for (uint32_t i = threadIdx.x; i <= mask; i += blockDim.x) s_table[i] = 0u;
         }
