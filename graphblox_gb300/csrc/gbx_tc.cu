@@ -389,7 +389,7 @@ struct TcBig {  // a v whose upper neighbours are dealt out in kUpperChunk units
 __global__ void __launch_bounds__(kTcThreads, 4)
     tc_vcentric_kernel(const uint32_t *__restrict__ off, const uint32_t *__restrict__ dest,
                        const uint32_t *__restrict__ low, const TcBig *__restrict__ big, uint32_t n_big,
-                       uint32_t n_units, const uint8_t *__restrict__ is_big, uint32_t V, unsigned *cursor,
+                       uint32_t n_units, const TcBig *__restrict__ small, uint32_t n_small, unsigned *cursor,
                        unsigned long long *total) {
     __shared__ uint32_t tables[kTcWarps][kTcWarpSlots];
     __shared__ uint32_t s_pre[kTcWarps][33];
@@ -417,17 +417,14 @@ __global__ void __launch_bounds__(kTcThreads, 4)
         count += v_unit(off, dest, bg.v, __ldg(low + bg.v), ub, ue, tables[wid], s_pre[wid], s_base[wid],
                         s_end[wid]);
     }
-    // the other v's: one warp each
+    // the other pivots with work (the plan's compact list, with the first
+    // upper neighbour precomputed): one warp each
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t v = gw; v < V; v += nw) {
-        if (is_big[v]) continue;
-        const uint32_t pv = __ldg(low + v);
-        if (pv == 0) continue;
-        const uint32_t b = __ldg(off + v), d = __ldg(off + v + 1) - b;
-        const uint32_t ub = count_lt(dest + b, d, v);
-        if (ub >= d) continue;
-        count += v_unit(off, dest, v, pv, ub, d, tables[wid], s_pre[wid], s_base[wid], s_end[wid]);
+    for (uint32_t i = gw; i < n_small; i += nw) {
+        const TcBig sm = small[i];
+        count += v_unit(off, dest, sm.v, __ldg(low + sm.v), sm.ub, sm.ue, tables[wid], s_pre[wid], s_base[wid],
+                        s_end[wid]);
     }
     count = block_sum(count, sred);
     if (threadIdx.x == 0 && count) atomicAdd(total, count);
@@ -536,7 +533,9 @@ __global__ void __launch_bounds__(kWideThreads, 1)
 // Work lists of the v-centric count. kind 0: v's with more than kUpperChunk
 // upper neighbours and |N+(v)| within the warp table (units of kUpperChunk);
 // kind 1: v's with |N+(v)| above the warp table and within the CTA table
-// (units of kWideChunk, for tc_wide_kernel).
+// (units of kWideChunk, for tc_wide_kernel); kind 2: every other v with
+// N+(v) and an upper neighbour (one warp each). v's without both have no
+// pairs and are in no list.
 __global__ void tc_big_flags_kernel(const uint32_t *off, const uint32_t *dest, const uint32_t *low, uint32_t V,
                                     int kind, uint32_t *flag, uint32_t *units, uint32_t *ub_out) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
@@ -544,25 +543,19 @@ __global__ void tc_big_flags_kernel(const uint32_t *off, const uint32_t *dest, c
         const uint32_t ub = count_lt(dest + b, d, v);
         const uint32_t up = d - ub, pv = low[v];
         const bool wide = pv > kTcTableMax && pv <= kWideSlotsMax / 2;
-        const bool sel = pv > 0 && up > 0 &&
-                         (kind == 0 ? (!wide && (up > kUpperChunk || pv > kTcTableMax)) : wide);
+        const bool big = !wide && (up > kUpperChunk || pv > kTcTableMax);
+        const bool sel = pv > 0 && up > 0 && (kind == 0 ? big : kind == 1 ? wide : !wide && !big);
         const uint32_t chunk = kind == 0 ? kUpperChunk : kWideChunk;
         flag[v] = sel ? 1u : 0u;
-        units[v] = sel ? (up + chunk - 1) / chunk : 0u;
+        units[v] = !sel ? 0u : kind == 2 ? 1u : (up + chunk - 1) / chunk;
         ub_out[v] = ub;
     }
 }
 
 __global__ void tc_big_scatter_kernel(const uint32_t *off, const uint32_t *flag, const uint32_t *pos,
-                                      const uint32_t *unit_pre, const uint32_t *ub, uint32_t V, TcBig *big,
-                                      uint8_t *is_big, int first) {
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-        if (first) is_big[v] = 0;
-        if (flag[v]) {
-            is_big[v] = 1;
-            big[pos[v]] = TcBig{v, ub[v], off[v + 1] - off[v], unit_pre[v]};
-        }
-    }
+                                      const uint32_t *unit_pre, const uint32_t *ub, uint32_t V, TcBig *big) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+        if (flag[v]) big[pos[v]] = TcBig{v, ub[v], off[v + 1] - off[v], unit_pre[v]};
 }
 
 }  // namespace gbx
@@ -571,9 +564,10 @@ __global__ void tc_big_scatter_kernel(const uint32_t *off, const uint32_t *flag,
 struct gbx_tc_plan {
     gbx::TcBig *big = nullptr;   // warp-table v's with many upper neighbours
     gbx::TcBig *wide = nullptr;  // CTA-table v's (|N+(v)| above the warp table)
-    uint8_t *is_big = nullptr;   // v is in one of the lists
+    gbx::TcBig *small = nullptr; // the other v's with pairs, one warp each
     uint32_t n_big = 0, n_units = 0;
     uint32_t n_wide = 0, n_wunits = 0;
+    uint32_t n_small = 0;
 };
 
 using namespace gbx;
@@ -617,8 +611,7 @@ static int tc_prepare(gbx_graph *g, cudaStream_t s) {
         GBX_TRY(tot.alloc(2, s));
         gbx_tc_plan *p = new gbx_tc_plan();
         auto build = [&]() -> int {
-            GBX_CUDA(cudaMalloc(&p->is_big, V ? V : 1));
-            for (int kind = 0; kind < 2; ++kind) {
+            for (int kind = 0; kind < 3; ++kind) {
                 tc_big_flags_kernel<<<grid, 256, 0, s>>>(g->offsets, g->dest, g->low_count, V, kind, flag.p,
                                                          units.p, ub.p);
                 GBX_LAUNCH_CHECK();
@@ -627,12 +620,11 @@ static int tc_prepare(gbx_graph *g, cudaStream_t s) {
                 uint32_t h[2];
                 GBX_CUDA(cudaMemcpyAsync(h, tot.p, 8, cudaMemcpyDeviceToHost, s));
                 GBX_CUDA(cudaStreamSynchronize(s));
-                TcBig **list = kind == 0 ? &p->big : &p->wide;
-                (kind == 0 ? p->n_big : p->n_wide) = h[0];
-                (kind == 0 ? p->n_units : p->n_wunits) = h[1];
+                TcBig **list = kind == 0 ? &p->big : kind == 1 ? &p->wide : &p->small;
+                (kind == 0 ? p->n_big : kind == 1 ? p->n_wide : p->n_small) = h[0];
+                if (kind < 2) (kind == 0 ? p->n_units : p->n_wunits) = h[1];
                 GBX_CUDA(cudaMalloc(list, sizeof(TcBig) * (h[0] ? h[0] : 1)));
-                tc_big_scatter_kernel<<<grid, 256, 0, s>>>(g->offsets, flag.p, pos.p, unit_pre.p, ub.p, V, *list,
-                                                           p->is_big, kind == 0);
+                tc_big_scatter_kernel<<<grid, 256, 0, s>>>(g->offsets, flag.p, pos.p, unit_pre.p, ub.p, V, *list);
                 GBX_LAUNCH_CHECK();
             }
             return GBX_OK;
@@ -652,7 +644,7 @@ void gbx_free_tc_plan(gbx_tc_plan *p) {
     if (!p) return;
     cudaFree(p->big);
     cudaFree(p->wide);
-    cudaFree(p->is_big);
+    cudaFree(p->small);
     delete p;
 }
 
@@ -675,7 +667,8 @@ extern "C" int gbx_tc(gbx_graph *g, uint64_t *total, void *stream) {
         const unsigned grid = (unsigned)std::max(1, per_sm) * (unsigned)num_sms();
         const gbx_tc_plan *p = g->tc_plan;
         tc_vcentric_kernel<<<grid, kTcThreads, 0, s>>>(g->offsets, g->dest, g->low_count, p->big, p->n_big,
-                                                       p->n_big ? p->n_units : 0u, p->is_big, V, cursor.p, d.p);
+                                                       p->n_big ? p->n_units : 0u, p->small, p->n_small, cursor.p,
+                                                       d.p);
         GBX_LAUNCH_CHECK();
         if (p->n_wide) {
             const size_t smem = (size_t)kWideSlotsMax * 4;
