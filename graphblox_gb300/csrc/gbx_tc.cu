@@ -41,6 +41,12 @@ constexpr uint32_t kTcTableMax = 512;   // |N+(v)| that fits a per-warp table
 constexpr uint32_t kTcWarpSlots = 1024;  // hash slots per warp
 constexpr uint32_t kUpperChunk = 256;   // upper neighbours per work unit
 constexpr uint32_t kEmptySlot = 0xFFFFFFFFu;
+// hybrid membership for pivots above the bitmap range: ids below
+// kHybridSplit (the high-degree end of the degree order, which holds most of
+// N+(v) and of the streamed prefixes) in the warp's bitmap, the rest in a
+// second per-warp hash table of at most kHybridSlots slots
+constexpr uint32_t kHybridSplit = kTcWarpSlots * 32;
+constexpr uint32_t kHybridSlots = 256;
 
 // number of elements <= x (or < x) in sorted a[0..n)
 __device__ __forceinline__ uint32_t count_le(const uint32_t *a, uint32_t n, uint32_t x) {
@@ -273,6 +279,18 @@ struct HashMember {
 // into that range before the read: count_flat4 probes every id of a quad,
 // including ids outside the list (other rows, padding), whose bits it then
 // discards; a list's own ids are <= v < nbits and read their true bit.
+struct HybridMember {
+    static constexpr bool kProbeAll = true;  // both reads stay in range for any id
+    const uint32_t *bits;   // ids below kHybridSplit
+    const uint32_t *table;  // the others
+    uint32_t mask;
+    __device__ __forceinline__ uint32_t bit(uint32_t w) const {
+        if (w < kHybridSplit) return (bits[w >> 5] >> (w & 31)) & 1u;
+        return hash_contains(table, mask, w) ? 1u : 0u;
+    }
+    __device__ __forceinline__ bool operator()(uint32_t w) const { return bit(w) != 0u; }
+};
+
 struct BitmapMember {
     static constexpr bool kProbeAll = true;
     const uint32_t *bits;
@@ -348,8 +366,8 @@ struct SortedMember {
 // N+(v) (warp table, or the sorted list when it is too long) and count.
 __device__ __forceinline__ unsigned long long v_unit(const uint32_t *__restrict__ off,
                                                     const uint32_t *__restrict__ dest, uint32_t v, uint32_t pv,
-                                                    uint32_t ub, uint32_t ue, uint32_t *table, uint32_t *s_pre,
-                                                    uint32_t *s_base, uint32_t *s_end) {
+                                                    uint32_t ub, uint32_t ue, uint32_t *table, uint32_t *htable,
+                                                    uint32_t *s_pre, uint32_t *s_base, uint32_t *s_end) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t *nv = dest + __ldg(off + v);
     unsigned long long count = 0;
@@ -367,6 +385,30 @@ __device__ __forceinline__ unsigned long long v_unit(const uint32_t *__restrict_
         for (uint32_t i = lane; i < pv; i += 32) table[__ldg(nv + i) >> 5] = 0u;
         __syncwarp();
     } else if (pv <= kTcTableMax) {
+        uint32_t nh = 0;  // ids of N+(v) at or above kHybridSplit
+        for (uint32_t i = lane; i < pv; i += 32) nh += __ldg(nv + i) >= kHybridSplit ? 1u : 0u;
+        nh = warp_sum(nh);
+        if (2 * nh <= kHybridSlots) {
+            uint32_t hmask = 31;
+            while (hmask + 1 < 2 * nh) hmask = 2 * hmask + 1;
+            for (uint32_t i = lane; i <= hmask; i += 32) htable[i] = kEmptySlot;
+            __syncwarp();
+            for (uint32_t i = lane; i < pv; i += 32) {
+                const uint32_t w = __ldg(nv + i);
+                if (w < kHybridSplit) atomicOr(table + (w >> 5), 1u << (w & 31));
+                else hash_insert(htable, hmask, w);
+            }
+            __syncwarp();
+            count = stream_pairs(off, dest, nv, v, ub, ue, s_pre, s_base, s_end,
+                                 HybridMember{table, htable, hmask});
+            __syncwarp();
+            for (uint32_t i = lane; i < pv; i += 32) {
+                const uint32_t w = __ldg(nv + i);
+                if (w < kHybridSplit) table[w >> 5] = 0u;
+            }
+            __syncwarp();
+            return count;
+        }
         const uint32_t mask = table_mask(pv);
         for (uint32_t i = lane; i <= mask; i += 32) table[i] = kEmptySlot;
         __syncwarp();
@@ -392,6 +434,7 @@ __global__ void __launch_bounds__(kTcThreads, 4)
                        uint32_t n_units, const TcBig *__restrict__ small, uint32_t n_small, unsigned *cursor,
                        unsigned long long *total) {
     __shared__ uint32_t tables[kTcWarps][kTcWarpSlots];
+    __shared__ uint32_t htables[kTcWarps][kHybridSlots];
     __shared__ uint32_t s_pre[kTcWarps][33];
     __shared__ uint32_t s_base[kTcWarps][32];
     __shared__ uint32_t s_end[kTcWarps][32];
@@ -414,8 +457,8 @@ __global__ void __launch_bounds__(kTcThreads, 4)
         const TcBig bg = big[lo];
         const uint32_t ub = bg.ub + (unit - bg.first_unit) * kUpperChunk;
         const uint32_t ue = min(ub + kUpperChunk, bg.ue);
-        count += v_unit(off, dest, bg.v, __ldg(low + bg.v), ub, ue, tables[wid], s_pre[wid], s_base[wid],
-                        s_end[wid]);
+        count += v_unit(off, dest, bg.v, __ldg(low + bg.v), ub, ue, tables[wid], htables[wid], s_pre[wid],
+                        s_base[wid], s_end[wid]);
     }
     // the other pivots with work (the plan's compact list, with the first
     // upper neighbour precomputed): one warp each
@@ -423,8 +466,8 @@ __global__ void __launch_bounds__(kTcThreads, 4)
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t i = gw; i < n_small; i += nw) {
         const TcBig sm = small[i];
-        count += v_unit(off, dest, sm.v, __ldg(low + sm.v), sm.ub, sm.ue, tables[wid], s_pre[wid], s_base[wid],
-                        s_end[wid]);
+        count += v_unit(off, dest, sm.v, __ldg(low + sm.v), sm.ub, sm.ue, tables[wid], htables[wid], s_pre[wid],
+                        s_base[wid], s_end[wid]);
     }
     count = block_sum(count, sred);
     if (threadIdx.x == 0 && count) atomicAdd(total, count);
