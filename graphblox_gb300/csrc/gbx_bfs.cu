@@ -33,6 +33,7 @@
 // others still read the last one), which is what lets one barrier per step
 // suffice. processed_nodes and iteration therefore match the reference.
 #include <algorithm>
+#include <cstddef>
 
 #include "gbx_coop.cuh"
 
@@ -446,7 +447,7 @@ __global__ void __launch_bounds__(kBfsThreads) bfs_persistent_kernel(BfsArgs a) 
     uint32_t mu = a.E, mf = __ldg(a.outdeg + a.source), qsize = 1, nf_prev = 0, L = 0;
     uint32_t processed = 1, iteration = 1, td = 0, bu = 0;
     unsigned long long edges_total = __ldg(a.outdeg + a.source);
-    bool in_bu = false, last_was_bu = false, done = false, failed = false;
+    bool in_bu = false, done = false, failed = false;
     bool bm_clean[2] = {true, true};  // frontier bitmaps still all zero (cleared by bfs_init_kernel)
     const uint32_t max_steps = 2 * a.V + 16;
     // lists for step 0: prepared by the host in generation 0
@@ -514,7 +515,6 @@ __global__ void __launch_bounds__(kBfsThreads) bfs_persistent_kernel(BfsArgs a) 
                     mf = 1;
                 }
             }
-            last_was_bu = true;
         } else {
             mu -= mf;
             top_down_phase(a, a.q[ib], qn, a.hv[ib], a.hc[ib], nh, nc, cur, a.q[ob], a.hv[ob], a.hc[ob], L + 1,
@@ -534,10 +534,8 @@ __global__ void __launch_bounds__(kBfsThreads) bfs_persistent_kernel(BfsArgs a) 
             nc = (uint32_t)hb;
             if (nf) L++;
             if (qsize == 0) done = true;
-            last_was_bu = false;
         }
     }
-    (void)last_was_bu;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         st->processed = processed;
         st->iteration = iteration;
@@ -549,32 +547,44 @@ __global__ void __launch_bounds__(kBfsThreads) bfs_persistent_kernel(BfsArgs a) 
     }
 }
 
+// Per traversal: levels, parents, visited and both frontier bitmaps, the
+// traversal state (zeroed as 32-bit words by the grid), and the generation-0
+// lists: the source alone, as a hub when its degree is large. The state
+// words that hold those lists are written only by thread 0, after its own
+// share of the zeroing.
 __global__ void bfs_init_kernel(uint32_t *level, int32_t *parent, uint32_t *visited, uint32_t *bm0,
-                                uint32_t *bm1, uint32_t V, uint32_t words, uint32_t source) {
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+                                uint32_t *bm1, uint32_t V, uint32_t words, uint32_t source,
+                                const uint32_t *outdeg, uint32_t *q0, uint32_t *hv0, uint32_t *hc0,
+                                BfsState *st) {
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+    for (uint32_t v = tid; v < V; v += nt) {
         level[v] = v == source ? 0u : kInfLevel;
         parent[v] = v == source ? (int32_t)source : -1;
     }
-    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < words; w += gridDim.x * blockDim.x) {
+    for (uint32_t w = tid; w < words; w += nt) {
         visited[w] = (w == (source >> 5)) ? (1u << (source & 31)) : 0u;
         bm0[w] = 0;
         bm1[w] = 0;
     }
-}
-
-// generation-0 lists: the source alone (as a hub when its degree is large)
-__global__ void bfs_seed_kernel(const uint32_t *outdeg, uint32_t source, uint32_t *q0, uint32_t *hv0,
-                                uint32_t *hc0, BfsState *st) {
-    const uint32_t d = outdeg[source];
-    st->conv.qlen = 0;
-    st->conv.hub = 0;
-    if (d > kHubDeg) {
-        hv0[0] = source;
-        hc0[0] = 0;
-        st->conv.hub = (1ull << 32) | hub_chunks(d);
-    } else if (d > 0) {
-        q0[0] = source;
-        st->conv.qlen = 1;
+    static_assert(sizeof(BfsState) % 4 == 0, "state is zeroed as words");
+    constexpr uint32_t kStateWords = sizeof(BfsState) / 4;
+    uint32_t *sw = reinterpret_cast<uint32_t *>(st);
+    const uint32_t conv_lo = (uint32_t)(offsetof(BfsState, conv) / 4);
+    const uint32_t conv_hi = conv_lo + (uint32_t)(sizeof(BfsStep) / 4);
+    for (uint32_t i = tid; i < kStateWords; i += nt)
+        if (i < conv_lo || i >= conv_hi) sw[i] = 0u;
+    if (tid == 0) {
+        const uint32_t d = outdeg[source];
+        BfsStep c = {};
+        if (d > kHubDeg) {
+            hv0[0] = source;
+            hc0[0] = 0;
+            c.hub = (1ull << 32) | hub_chunks(d);
+        } else if (d > 0) {
+            q0[0] = source;
+            c.qlen = 1;
+        }
+        st->conv = c;
     }
 }
 
@@ -667,11 +677,8 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
         GBX_CUDA(cudaStreamSynchronize(s));
         g->pull_sources_live = h ? 0 : 1;
     }
-    bfs_init_kernel<<<grid1, 256, 0, s>>>(w.level, w.parent, w.visited, w.bm0, w.bm1, V, words,
-                                          source);
-    GBX_LAUNCH_CHECK();
-    GBX_CUDA(cudaMemsetAsync(w.st, 0, sizeof(BfsState), s));
-    bfs_seed_kernel<<<1, 1, 0, s>>>(g->out_degree, source, w.q0, w.hv0, w.hc0, w.st);
+    bfs_init_kernel<<<grid1, 256, 0, s>>>(w.level, w.parent, w.visited, w.bm0, w.bm1, V, words, source,
+                                          g->out_degree, w.q0, w.hv0, w.hc0, w.st);
     GBX_LAUNCH_CHECK();
     BfsArgs a;
     a.off = g->offsets;

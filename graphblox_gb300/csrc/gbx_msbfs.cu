@@ -57,10 +57,19 @@ __global__ void __launch_bounds__(kMsThreads)
         const uint32_t u = q[i];
         const uint32_t fu = F[(size_t)u * NW + k];
         if (!fu) continue;  // lane-local: other lanes of the group may still push
-        for (uint32_t e = off[u]; e < off[u + 1]; ++e) {
-            const uint32_t v = __ldg(dest + e);
-            const uint32_t add = fu & ~__ldg(seen + (size_t)v * NW + k);
-            if (add) atomicOr(Fn + (size_t)v * NW + k, add);
+        const uint32_t eb = off[u], ee = off[u + 1];
+        for (uint32_t e = eb; e < ee; e += 4) {
+            // four out-edges per round: targets, then their seen words
+            uint32_t v[4], sw[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v[q] = e + q < ee ? __ldg(dest + e + q) : 0u;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) sw[q] = e + q < ee ? __ldg(seen + (size_t)v[q] * NW + k) : 0xFFFFFFFFu;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint32_t add = fu & ~sw[q];
+                if (add) atomicOr(Fn + (size_t)v[q] * NW + k, add);
+            }
         }
     }
 }
@@ -92,9 +101,15 @@ __global__ void __launch_bounds__(kMsThreads)
         uint32_t j = b;
         while (__any_sync(0xFFFFFFFFu, open)) {
             if (open) {
-                const uint32_t u = __ldg(psrc + j);
-                acc |= __ldg(F + (size_t)u * NW + k);
-                ++j;
+                // four in-edges per round: their ids, then their mask words,
+                // in flight together (the early exit checks once per round)
+                uint32_t u[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) u[q] = j + q < e ? __ldg(psrc + j + q) : 0u;
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (j + q < e) acc |= __ldg(F + (size_t)u[q] * NW + k);
+                j += 4;
             }
             open = __ballot_sync(0xFFFFFFFFu, (need & ~acc) != 0 && j < e) & gmask;
         }
@@ -120,9 +135,17 @@ __global__ void __launch_bounds__(kMsThreads)
         const MsChunk ck = chunks[c];
         const uint32_t need = ~seen[(size_t)ck.row * NW + k] & ms_valid(k, S);
         uint32_t acc = 0;
-        for (uint32_t j0 = ck.eb; j0 < ck.ee; j0 += GPW) {
-            const uint32_t j = j0 + gi;
-            if (j < ck.ee) acc |= __ldg(F + (size_t)__ldg(psrc + j) * NW + k);
+        for (uint32_t j0 = ck.eb; j0 < ck.ee; j0 += 4 * GPW) {
+            // four edges per group per round, loads in flight together
+            uint32_t u[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint32_t j = j0 + q * GPW + gi;
+                u[q] = j < ck.ee ? __ldg(psrc + j) : 0u;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (j0 + q * GPW + gi < ck.ee) acc |= __ldg(F + (size_t)u[q] * NW + k);
             // OR across the groups, then stop once every needed bit is present
             uint32_t all = acc;
 #pragma unroll
