@@ -139,19 +139,32 @@ __device__ __forceinline__ unsigned long long pair_hash(uint32_t a, uint32_t b) 
 // equals its reverse (the CSR is symmetric); a non-symmetric CSR sums to zero
 // only by a 64-bit hash coincidence. One streaming pass instead of a search
 // per edge.
-__global__ void tc_shape_check_kernel(const uint32_t *off, const uint32_t *dest, uint32_t V, unsigned *flags,
-                                      unsigned long long *asym) {
+__global__ void tc_shape_check_kernel(const uint32_t *off, const uint32_t *dest, uint32_t V, uint32_t E,
+                                      unsigned *flags, unsigned long long *asym) {
+    // the edge array in fixed chunks per warp (rows of any length spread
+    // over many warps); each lane finds the row of its first edge by binary
+    // search over the offsets and then walks forward with its edges
+    constexpr uint32_t kChunk = 8192;
     const uint32_t lane = threadIdx.x & 31;
-    uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     unsigned f = 0;
     unsigned long long h = 0;
-    for (uint32_t v = gw; v < V; v += nw) {
-        uint32_t b = off[v], e = off[v + 1];
-        for (uint32_t j = b + lane; j < e; j += 32) {
-            uint32_t u = dest[j];
-            if (j > b && u == dest[j - 1]) f |= 1u;
-            h += pair_hash(v, u) - pair_hash(u, v);
+    for (uint64_t c0 = (uint64_t)gw * kChunk; c0 < E; c0 += (uint64_t)nw * kChunk) {
+        const uint32_t c1 = c0 + kChunk < (uint64_t)E ? (uint32_t)(c0 + kChunk) : E;
+        uint32_t j = (uint32_t)c0 + lane;
+        if (j >= c1) continue;
+        uint32_t lo = 0, hi = V - 1;  // last row r with off[r] <= j (E > j, so one exists)
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (__ldg(off + mid) <= j) lo = mid; else hi = mid - 1;
+        }
+        uint32_t r = lo;
+        for (; j < c1; j += 32) {
+            while (__ldg(off + r + 1) <= j) ++r;
+            const uint32_t u = __ldcs(dest + j);
+            if (j > __ldg(off + r) && u == __ldg(dest + j - 1)) f |= 1u;
+            h += pair_hash(r, u) - pair_hash(u, r);
         }
     }
     f = __reduce_or_sync(0xffffffffu, f);
@@ -579,26 +592,34 @@ __global__ void __launch_bounds__(kWideThreads, 1)
 // (units of kWideChunk, for tc_wide_kernel); kind 2: every other v with
 // N+(v) and an upper neighbour (one warp each). v's without both have no
 // pairs and are in no list.
-__global__ void tc_big_flags_kernel(const uint32_t *off, const uint32_t *dest, const uint32_t *low, uint32_t V,
-                                    int kind, uint32_t *flag, uint32_t *units, uint32_t *ub_out) {
+__global__ void tc_plan_flags_kernel(const uint32_t *off, const uint32_t *dest, const uint32_t *low, uint32_t V,
+                                     uint32_t *flag /* 3V: kinds 0, 1, 2 */, uint32_t *units /* 2V */,
+                                     uint32_t *ub_out) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
         const uint32_t b = off[v], d = off[v + 1] - b;
         const uint32_t ub = count_lt(dest + b, d, v);
         const uint32_t up = d - ub, pv = low[v];
         const bool wide = pv > kTcTableMax && pv <= kWideSlotsMax / 2;
         const bool big = !wide && (up > kUpperChunk || pv > kTcTableMax);
-        const bool sel = pv > 0 && up > 0 && (kind == 0 ? big : kind == 1 ? wide : !wide && !big);
-        const uint32_t chunk = kind == 0 ? kUpperChunk : kWideChunk;
-        flag[v] = sel ? 1u : 0u;
-        units[v] = !sel ? 0u : kind == 2 ? 1u : (up + chunk - 1) / chunk;
+        const bool pairs = pv > 0 && up > 0;
+        flag[v] = pairs && big ? 1u : 0u;
+        flag[(size_t)V + v] = pairs && wide ? 1u : 0u;
+        flag[2 * (size_t)V + v] = pairs && !big && !wide ? 1u : 0u;
+        units[v] = pairs && big ? (up + kUpperChunk - 1) / kUpperChunk : 0u;
+        units[(size_t)V + v] = pairs && wide ? (up + kWideChunk - 1) / kWideChunk : 0u;
         ub_out[v] = ub;
     }
 }
 
-__global__ void tc_big_scatter_kernel(const uint32_t *off, const uint32_t *flag, const uint32_t *pos,
-                                      const uint32_t *unit_pre, const uint32_t *ub, uint32_t V, TcBig *big) {
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
-        if (flag[v]) big[pos[v]] = TcBig{v, ub[v], off[v + 1] - off[v], unit_pre[v]};
+__global__ void tc_plan_scatter_kernel(const uint32_t *off, const uint32_t *flag, const uint32_t *pos,
+                                       const uint32_t *unit_pre, const uint32_t *ub, uint32_t V, TcBig *big,
+                                       TcBig *wide, TcBig *small) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        const uint32_t d = off[v + 1] - off[v];
+        if (flag[v]) big[pos[v]] = TcBig{v, ub[v], d, unit_pre[v]};
+        if (flag[(size_t)V + v]) wide[pos[(size_t)V + v]] = TcBig{v, ub[v], d, unit_pre[(size_t)V + v]};
+        if (flag[2 * (size_t)V + v]) small[pos[2 * (size_t)V + v]] = TcBig{v, ub[v], d, 0u};
+    }
 }
 
 }  // namespace gbx
@@ -635,7 +656,7 @@ static int tc_prepare(gbx_graph *g, cudaStream_t s) {
         DevBuf<unsigned long long> flags;  // [0] repeat flags, [1] asymmetry hash sum
         GBX_TRY(flags.alloc(2, s));
         GBX_CUDA(cudaMemsetAsync(flags.p, 0, 16, s));
-        tc_shape_check_kernel<<<wgrid, kTcThreads, 0, s>>>(g->offsets, g->dest, V,
+        tc_shape_check_kernel<<<wgrid, kTcThreads, 0, s>>>(g->offsets, g->dest, V, g->E,
                                                            reinterpret_cast<unsigned *>(flags.p), flags.p + 1);
         GBX_LAUNCH_CHECK();
         unsigned long long h[2] = {0, 0};
@@ -646,30 +667,36 @@ static int tc_prepare(gbx_graph *g, cudaStream_t s) {
     }
     if (g->simple_rows == 1 && g->symmetric == 1 && !g->tc_plan) {
         DevBuf<uint32_t> flag, pos, units, unit_pre, ub, tot;
-        GBX_TRY(flag.alloc(V, s));
-        GBX_TRY(pos.alloc(V, s));
-        GBX_TRY(units.alloc(V, s));
-        GBX_TRY(unit_pre.alloc(V, s));
+        GBX_TRY(flag.alloc(3 * (size_t)V, s));
+        GBX_TRY(pos.alloc(3 * (size_t)V, s));
+        GBX_TRY(units.alloc(2 * (size_t)V, s));
+        GBX_TRY(unit_pre.alloc(2 * (size_t)V, s));
         GBX_TRY(ub.alloc(V, s));
-        GBX_TRY(tot.alloc(2, s));
+        GBX_TRY(tot.alloc(5, s));
         gbx_tc_plan *p = new gbx_tc_plan();
         auto build = [&]() -> int {
-            for (int kind = 0; kind < 3; ++kind) {
-                tc_big_flags_kernel<<<grid, 256, 0, s>>>(g->offsets, g->dest, g->low_count, V, kind, flag.p,
-                                                         units.p, ub.p);
-                GBX_LAUNCH_CHECK();
-                GBX_TRY(exclusive_scan_u32(flag.p, pos.p, V, s, tot.p));
-                GBX_TRY(exclusive_scan_u32(units.p, unit_pre.p, V, s, tot.p + 1));
-                uint32_t h[2];
-                GBX_CUDA(cudaMemcpyAsync(h, tot.p, 8, cudaMemcpyDeviceToHost, s));
-                GBX_CUDA(cudaStreamSynchronize(s));
-                TcBig **list = kind == 0 ? &p->big : kind == 1 ? &p->wide : &p->small;
-                (kind == 0 ? p->n_big : kind == 1 ? p->n_wide : p->n_small) = h[0];
-                if (kind < 2) (kind == 0 ? p->n_units : p->n_wunits) = h[1];
-                GBX_CUDA(cudaMalloc(list, sizeof(TcBig) * (h[0] ? h[0] : 1)));
-                tc_big_scatter_kernel<<<grid, 256, 0, s>>>(g->offsets, flag.p, pos.p, unit_pre.p, ub.p, V, *list);
-                GBX_LAUNCH_CHECK();
-            }
+            // the three work lists in one classification pass, five scans
+            // and one host round trip for the list sizes
+            tc_plan_flags_kernel<<<grid, 256, 0, s>>>(g->offsets, g->dest, g->low_count, V, flag.p, units.p, ub.p);
+            GBX_LAUNCH_CHECK();
+            for (int k = 0; k < 3; ++k)
+                GBX_TRY(exclusive_scan_u32(flag.p + (size_t)k * V, pos.p + (size_t)k * V, V, s, tot.p + k));
+            for (int k = 0; k < 2; ++k)
+                GBX_TRY(exclusive_scan_u32(units.p + (size_t)k * V, unit_pre.p + (size_t)k * V, V, s, tot.p + 3 + k));
+            uint32_t h[5];
+            GBX_CUDA(cudaMemcpyAsync(h, tot.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+            GBX_CUDA(cudaStreamSynchronize(s));
+            p->n_big = h[0];
+            p->n_wide = h[1];
+            p->n_small = h[2];
+            p->n_units = h[3];
+            p->n_wunits = h[4];
+            GBX_CUDA(cudaMalloc(&p->big, sizeof(TcBig) * (h[0] ? h[0] : 1)));
+            GBX_CUDA(cudaMalloc(&p->wide, sizeof(TcBig) * (h[1] ? h[1] : 1)));
+            GBX_CUDA(cudaMalloc(&p->small, sizeof(TcBig) * (h[2] ? h[2] : 1)));
+            tc_plan_scatter_kernel<<<grid, 256, 0, s>>>(g->offsets, flag.p, pos.p, unit_pre.p, ub.p, V, p->big,
+                                                        p->wide, p->small);
+            GBX_LAUNCH_CHECK();
             return GBX_OK;
         };
         const int st = build();
