@@ -653,15 +653,17 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
     GBX_TRY(ensure_device());
     cudaStream_t s = (cudaStream_t)stream;
     const uint32_t V = g->V, words = (V + 31) / 32;
-    const bool stage = (distances && !is_device_ptr(distances)) || (parents && !is_device_ptr(parents));
+    const int dist_dev = distances ? (is_device_ptr(distances) ? 1 : 0) : 1;
+    const int par_dev = parents ? (is_device_ptr(parents) ? 1 : 0) : 1;
+    const bool stage = !dist_dev || !par_dev;
     Scratch sc;
     GBX_TRY(sc.take(g, BfsWork::bytes(V, stage), s));
     BfsWork w;
     GBX_TRY(w.carve(sc, V, stage));
     OutArray<uint32_t> dist;
     OutArray<int32_t> par;
-    GBX_TRY(dist.bind(distances, V, s, w.dist_stage));
-    GBX_TRY(par.bind(parents, V, s, w.par_stage));
+    GBX_TRY(dist.bind(distances, V, s, w.dist_stage, dist_dev));
+    GBX_TRY(par.bind(parents, V, s, w.par_stage, par_dev));
     const unsigned grid1 = std::min<unsigned>(ceil_div(V, 256), (unsigned)num_sms() * 8);
     if (g->pull_sources_live < 0) {
         DevBuf<uint32_t> bad;
@@ -716,8 +718,10 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
     GBX_LAUNCH_CHECK();
     GBX_TRY(dist.finish(s));
     GBX_TRY(par.finish(s));
+    // the counters (and the step trace only when it is printed)
     BfsState hs;
-    GBX_CUDA(cudaMemcpyAsync(&hs, w.st, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    GBX_CUDA(cudaMemcpyAsync(&hs, w.st, trace_enabled() ? sizeof(hs) : offsetof(BfsState, trace),
+                             cudaMemcpyDeviceToHost, s));
     GBX_CUDA(cudaStreamSynchronize(s));
     GBX_REQUIRE(hs.gs.error == 0, GBX_ERR_DEVICE_TIMEOUT, "BFS grid barrier wait expired");
     GBX_REQUIRE(hs.status == 0, GBX_ERR_ITER_CAP, "BFS step cap reached");

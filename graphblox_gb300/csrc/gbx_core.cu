@@ -53,8 +53,11 @@ static DevProps g_props[64];
 static std::once_flag g_props_once[64];
 
 int ensure_device() {
+    // a device this thread has already checked stays usable for the process
+    static thread_local int checked = -1;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess && dev == checked) return GBX_OK;
     if (e != cudaSuccess) {
         (void)cudaGetLastError();
         set_error("no usable CUDA device: %s", cudaGetErrorString(e));
@@ -90,6 +93,7 @@ int ensure_device() {
             g_props[dev].l2 = 50u << 20;
         }
     });
+    checked = dev;
     return GBX_OK;
 }
 

@@ -125,15 +125,16 @@ struct OutArray {
     size_t n = 0;
     DevBuf<T> owned;
     // staging (optional): device memory of count elements to use for a host
-    // destination instead of a new allocation
-    int bind(T *dst, size_t count, cudaStream_t s, T *staging = nullptr) {
+    // destination instead of a new allocation; on_device (optional): the
+    // caller's classification of dst, to skip a pointer-attribute query
+    int bind(T *dst, size_t count, cudaStream_t s, T *staging = nullptr, int on_device = -1) {
         n = count;
         host = nullptr;
         if (dst == nullptr) {
             d = nullptr;
             return GBX_OK;
         }
-        if (is_device_ptr(dst)) {
+        if (on_device == 1 || (on_device < 0 && is_device_ptr(dst))) {
             d = dst;
             return GBX_OK;
         }

@@ -19,6 +19,7 @@
 // with evict-first loads: they stream from HBM either way, and dist / stamp /
 // in_far (12 bytes per vertex) should keep the L2.
 #include <algorithm>
+#include <cstddef>
 
 #include "gbx_coop.cuh"
 
@@ -453,7 +454,8 @@ extern "C" int gbx_sssp(gbx_graph *g, uint32_t source, uint32_t delta, uint32_t 
     if (delta == 0) delta = g->sssp_delta ? g->sssp_delta : (g->weight ? 256u : 1u);
     // working arrays from the graph's scratch arena (plus staging for a
     // host-memory result)
-    const bool stage = !is_device_ptr(distances);
+    const int out_dev = is_device_ptr(distances) ? 1 : 0;
+    const bool stage = !out_dev;
     const size_t r = Scratch::round_up((size_t)V * 4);
     Scratch sc;
     GBX_TRY(sc.take(g, (stage ? 13 : 12) * r + Scratch::round_up(sizeof(SsspState)) + Scratch::round_up(16), s));
@@ -466,7 +468,7 @@ extern "C" int gbx_sssp(gbx_graph *g, uint32_t source, uint32_t delta, uint32_t 
     unsigned long long *fin = sc.carve<unsigned long long>(2);
     GBX_REQUIRE(fin != nullptr, GBX_ERR_CUDA, "SSSP scratch carve overflow");
     OutArray<uint32_t> out;
-    GBX_TRY(out.bind(distances, V, s, out_stage));
+    GBX_TRY(out.bind(distances, V, s, out_stage, out_dev));
     const unsigned grid1 = std::min<unsigned>(ceil_div(V, 256), (unsigned)num_sms() * 8);
     sssp_init_kernel<<<grid1, 256, 0, s>>>(dist, settled, stamp, in_far, V, source, g->out_degree,
                                            q0, hv0, hc0);
@@ -505,7 +507,8 @@ extern "C" int gbx_sssp(gbx_graph *g, uint32_t source, uint32_t delta, uint32_t 
     GBX_TRY(out.finish(s));
     SsspState hs;
     unsigned long long hf[2];
-    GBX_CUDA(cudaMemcpyAsync(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    GBX_CUDA(cudaMemcpyAsync(&hs, st, trace_enabled() ? sizeof(hs) : offsetof(SsspState, trace),
+                             cudaMemcpyDeviceToHost, s));
     GBX_CUDA(cudaMemcpyAsync(hf, fin, 16, cudaMemcpyDeviceToHost, s));
     GBX_CUDA(cudaStreamSynchronize(s));
     GBX_REQUIRE(hs.gs.error == 0, GBX_ERR_DEVICE_TIMEOUT, "SSSP grid barrier wait expired");
