@@ -48,7 +48,7 @@ PR_ITERS = 20
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each
 # kernel, from one `ncu --set full` capture of this workload on a GB300
 # (tc, spmv: one launch; pr: one iteration; bfs, sssp: one source).
-NCU_TRAFFIC_PER_LAUNCH = {"tc": 15.121e9, "pr": 0.4006e9, "bfs": 0.1761e9, "sssp": 5.334e9, "spmv": 0.6775e9}
+NCU_TRAFFIC_PER_LAUNCH = {"tc": 14.773e9, "pr": 0.4006e9, "bfs": 0.1761e9, "sssp": 1.427e9, "spmv": 0.6775e9}
 W_LO, W_HI = 1, 255
 # differentiable personalised PageRank: RMAT-20, 2^24 edges as generated,
 # lognormal(0,1) weights, 64 teleport columns of 32 seeds, d 0.85 to 1e-7 L1

@@ -4,7 +4,9 @@
 // cooperative kernel: the whole traversal, including the direction
 // decisions, runs on the device with one grid barrier per step.
 //
-// State in HBM: level[V] (0xFFFFFFFF = unvisited), parent[V], a visited
+// State in HBM: level[V] and parent[V] (the output arrays themselves, in the
+// reference's format from the start: unreached vertices keep level 0 and
+// parent -out_degree or -1, so no conversion pass follows), a visited
 // bitmap and two frontier bitmaps (V/8 bytes each, L2-resident), and two
 // generations of frontier lists: a queue of vertices with out-degree in
 // (0, kHubDeg] and a hub list for larger ones.
@@ -419,7 +421,10 @@ __device__ void level_to_bitmap_phase(const BfsArgs &a, uint32_t l, uint32_t *bm
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            const unsigned m = __ballot_sync(0xffffffffu, lv[q] == l);
+            // unreached vertices also hold level 0: the visited word keeps
+            // them out of level 0's frontier
+            const uint32_t vis = w0 + q * nw < a.words ? __ldcg(a.visited + w0 + q * nw) : 0u;
+            const unsigned m = __ballot_sync(0xffffffffu, lv[q] == l) & vis;
             if (lane == 0 && w0 + q * nw < a.words) bm[w0 + q * nw] = m;
         }
     }
@@ -558,8 +563,11 @@ __global__ void bfs_init_kernel(uint32_t *level, int32_t *parent, uint32_t *visi
                                 BfsState *st) {
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
     for (uint32_t v = tid; v < V; v += nt) {
-        level[v] = v == source ? 0u : kInfLevel;
-        parent[v] = v == source ? (int32_t)source : -1;
+        // the reference's values for unreached vertices (BFS.c:59-74); the
+        // traversal overwrites the reached ones
+        const uint32_t d = __ldg(outdeg + v);
+        level[v] = 0u;
+        parent[v] = v == source ? (int32_t)source : (d ? -(int32_t)d : -1);
     }
     for (uint32_t w = tid; w < words; w += nt) {
         visited[w] = (w == (source >> 5)) ? (1u << (source & 31)) : 0u;
@@ -594,18 +602,6 @@ __global__ void pull_live_kernel(const uint32_t *psrc, uint32_t E, const uint32_
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < E; j += gridDim.x * blockDim.x)
         dead |= __ldg(outdeg + __ldcs(psrc + j)) == 0;
     if (__any_sync(0xffffffffu, dead) && (threadIdx.x & 31) == 0) *bad = 1;
-}
-
-__global__ void bfs_finish_kernel(const uint32_t *level, const int32_t *parent, const uint32_t *outdeg,
-                                  uint32_t V, uint32_t *dist, int32_t *par_out) {
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-        uint32_t l = level[v];
-        if (dist) dist[v] = l == kInfLevel ? 0u : l;
-        if (par_out) {
-            uint32_t d = outdeg[v];
-            par_out[v] = l == kInfLevel ? (d ? -(int32_t)d : -1) : parent[v];
-        }
-    }
 }
 
 // Working arrays of one traversal, carved from the graph's scratch arena;
@@ -679,8 +675,12 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
         GBX_CUDA(cudaStreamSynchronize(s));
         g->pull_sources_live = h ? 0 : 1;
     }
-    bfs_init_kernel<<<grid1, 256, 0, s>>>(w.level, w.parent, w.visited, w.bm0, w.bm1, V, words, source,
-                                          g->out_degree, w.q0, w.hv0, w.hc0, w.st);
+    // levels and parents live in the output arrays (device memory, or their
+    // device staging) when the caller asked for them
+    uint32_t *lev = dist.d ? dist.d : w.level;
+    int32_t *parp = par.d ? par.d : w.parent;
+    bfs_init_kernel<<<grid1, 256, 0, s>>>(lev, parp, w.visited, w.bm0, w.bm1, V, words, source, g->out_degree,
+                                          w.q0, w.hv0, w.hc0, w.st);
     GBX_LAUNCH_CHECK();
     BfsArgs a;
     a.off = g->offsets;
@@ -696,8 +696,8 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
     a.alpha = g->bfs_alpha;
     a.beta = g->bfs_beta;
     a.pull_live = g->pull_sources_live == 1 ? 1u : 0u;
-    a.level = w.level;
-    a.parent = w.parent;
+    a.level = lev;
+    a.parent = parp;
     a.visited = w.visited;
     a.bm[0] = w.bm0;
     a.bm[1] = w.bm1;
@@ -713,8 +713,6 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
     GBX_TRY(coop_grid(bfs_persistent_kernel, kBfsThreads, 0, &grid, &grid_cache));
     void *args[] = {&a};
     GBX_CUDA(cudaLaunchCooperativeKernel((const void *)bfs_persistent_kernel, grid, kBfsThreads, args, 0, s));
-    GBX_LAUNCH_CHECK();
-    bfs_finish_kernel<<<grid1, 256, 0, s>>>(w.level, w.parent, g->out_degree, V, dist.d, par.d);
     GBX_LAUNCH_CHECK();
     GBX_TRY(dist.finish(s));
     GBX_TRY(par.finish(s));
