@@ -217,9 +217,9 @@ __device__ __forceinline__ unsigned long long count_flat(const uint32_t *__restr
 
 // Same count with 16-byte loads: each lane's list [base, base+len) is read as
 // the aligned quads that cover it (the neighbour array is 16-byte aligned and
-// padded by four ids), two quads per lane per step, and the elements of a
+// padded by four ids), four quads per lane per step, and the elements of a
 // quad outside the list are masked. Four times fewer load instructions and
-// twice the bytes in flight of count_flat.
+// four times the bytes in flight of count_flat.
 template <class Member>
 __device__ __forceinline__ unsigned long long count_flat4(const uint32_t *__restrict__ dest, uint32_t base,
                                                          uint32_t len, uint32_t *s_pre, uint32_t *s_base,
@@ -242,11 +242,11 @@ __device__ __forceinline__ unsigned long long count_flat4(const uint32_t *__rest
     const uint4 *d4 = reinterpret_cast<const uint4 *>(dest);
     unsigned long long count = 0;
     uint32_t k = 0;  // owner lane of this lane's current quad, advanced monotonically
-    for (uint32_t i0 = 0; i0 < tot; i0 += 64) {
-        uint4 w[2];
-        uint32_t e0[2], lo[2], hi[2];
+    for (uint32_t i0 = 0; i0 < tot; i0 += 128) {
+        uint4 w[4];
+        uint32_t e0[4], lo[4], hi[4];
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
+        for (int q = 0; q < 4; ++q) {
             const uint32_t i = i0 + q * 32 + lane;
             lo[q] = hi[q] = e0[q] = 0;
             w[q] = make_uint4(0u, 0u, 0u, 0u);
@@ -260,7 +260,7 @@ __device__ __forceinline__ unsigned long long count_flat4(const uint32_t *__rest
             }
         }
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
+        for (int q = 0; q < 4; ++q) {
             // the quad's elements inside [lo, hi) as a 4-bit mask; the
             // membership bits of all four, then one popcount
             const uint32_t x[4] = {w[q].x, w[q].y, w[q].z, w[q].w};

@@ -3,8 +3,9 @@
  * vertex-centric CSR kernels.
  *
  * Two layers sit on this ABI:
- *   - the drop-in "cuda" integration (graphblox_gb300/integration/*.c,
- *     headers in include/algorithms/cuda/), which exports the same symbols
+ *   - the drop-in "cuda" integration (the C files in
+ *     graphblox_gb300/integration/, headers in include/algorithms/cuda/),
+ *     which exports the same symbols
  *     and Stats structs as the reference's 01_host/include/algorithms/openmp
  *     headers so that 01_host/src/utils_graph/graphRun.c links unchanged;
  *   - the Python host mirror (graphblox_gb300/), which binds it with ctypes.

@@ -341,3 +341,47 @@ def test_sssp_bucket_widths(gbx, cuda_device, delta):
         for r in roots:
             st = gbx.sssp(dg, r, delta)
             np.testing.assert_array_equal(st.distances, po.sssp(host, r, 64))
+
+
+def _bottom_up_levels(deg, idx, dest, V, source):
+    """Pull-only BFS over out-edges (the reference's DIRECTED 0 bottom-up
+    step, BFS.c:562-613, run from the first level): v joins level L+1 when
+    one of its out-neighbours is in level L."""
+    dist = np.zeros(V, np.int64)
+    seen = np.zeros(V, bool)
+    seen[source] = True
+    frontier = np.zeros(V, bool)
+    frontier[source] = True
+    level = 0
+    while True:
+        nxt = np.zeros(V, bool)
+        for v in np.nonzero(~seen)[0]:
+            row = dest[idx[v]:idx[v] + deg[v]]
+            if row.size and frontier[row].any():
+                nxt[v] = True
+        if not nxt.any():
+            return dist, int(seen.sum())
+        level += 1
+        dist[nxt] = level
+        seen |= nxt
+        frontier = nxt
+
+
+def test_bfs_pull_only_level_scan(gbx, cuda_device):
+    """Mode 0 (bottom-up from the first step) on an asymmetric graph without
+    an inverse CSR and with sinks: the first frontier bitmap comes from the
+    level scan, where unreached vertices (level 0 in the output format) must
+    not count as level-0 frontier."""
+    scale = 10
+    src, dst = gbx.generate_rmat(scale, (1 << scale) * 8, seed=23)
+    V = 1 << scale
+    deg, idx, s, d, _ = gbx.csr_build(src, dst, num_vertices=V, dedup=True, sort=1)
+    assert np.any(deg[d] == 0)
+    g = gbx.GraphCSR(V, int(s.shape[0]), deg, idx, d, s, None, np.arange(V, dtype=np.uint32),
+                     np.arange(V, dtype=np.uint32))
+    with gbx.DeviceGraph.from_graph_csr(g) as dg:
+        for r in [0, 5, int(np.nonzero(deg)[0][-1])]:
+            ref, reached = _bottom_up_levels(deg, idx, d, V, r)
+            st = gbx.breadth_first_search(dg, r, 0)
+            np.testing.assert_array_equal(np.asarray(st.distances).astype(np.int64), ref)
+            assert st.processed_nodes == reached
