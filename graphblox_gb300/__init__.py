@@ -21,6 +21,9 @@ from .graph import (  # noqa: F401
     connected_components,
     csr_build,
     degree_reorder,
+    read_label_file,
+    relabel,
+    relabel_from_file,
     generate_chung_lu,
     generate_rmat,
     generate_rmat_batch,

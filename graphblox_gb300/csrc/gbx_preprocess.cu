@@ -137,6 +137,58 @@ __global__ void compose_labels_kernel(uint32_t *labels, uint32_t *inv, uint32_t 
     }
 }
 
+// ---- bucketed reorder modes (DBG, HUBSort, HUBCluster, Corder) -------------
+struct BucketThresholds {
+    uint32_t t[11];
+    uint32_t n;
+};
+
+// key[v] = n-1 - bucket(v): a stable ascending sort of (key, id) lists the
+// highest bucket first, ids ascending inside a bucket (reorder.c:439-572)
+__global__ void bucket_key_kernel(const uint32_t *deg, uint32_t V, BucketThresholds th, uint32_t *key) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        uint32_t i = 0;
+        while (deg[v] > th.t[i]) ++i;  // th.t[th.n-1] = UINT32_MAX ends the scan
+        key[v] = th.n - 1 - i;
+    }
+}
+
+// newlab[sorted[i]] = i
+__global__ void rank_labels_kernel(const uint32_t *sorted, uint32_t n, uint32_t *newlab) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        newlab[sorted[i]] = i;
+}
+
+// HUBSort: hot flag (degree above t0) per vertex
+__global__ void hot_flag_kernel(const uint32_t *deg, uint32_t V, uint32_t t0, uint32_t *flag) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+        flag[v] = deg[v] > t0 ? 1u : 0u;
+}
+
+// hot vertices (ascending ids) and their degrees at their rank; cold vertices
+// labelled H + (their rank among cold vertices) = H + v - (hot before v)
+__global__ void hot_split_kernel(const uint32_t *deg, const uint32_t *flag, const uint32_t *pos, uint32_t V,
+                                 const uint32_t *hot_total, uint32_t *hot_ids, uint32_t *hot_deg,
+                                 uint32_t *newlab) {
+    const uint32_t H = *hot_total;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        if (flag[v]) {
+            hot_ids[pos[v]] = v;
+            hot_deg[pos[v]] = deg[v];
+        } else {
+            newlab[v] = H + v - pos[v];
+        }
+    }
+}
+
+// bad[0] counts labels out of range or taken twice (seen[] starts zeroed)
+__global__ void permutation_check_kernel(const uint32_t *lab, uint32_t V, uint32_t *seen, unsigned *bad) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        const uint32_t l = lab[v];
+        if (l >= V || atomicExch(seen + l, 1u) != 0u) atomicAdd(bad, 1u);
+    }
+}
+
 static int bits_for(uint32_t maxv) {
     int b = 0;
     while (b < 32 && (maxv >> b)) ++b;
@@ -272,7 +324,12 @@ extern "C" int gbx_degree_reorder(uint32_t num_vertices, uint32_t num_edges, uin
     GBX_REQUIRE(num_vertices > 0, GBX_ERR_INVALID, "num_vertices must be > 0");
     GBX_REQUIRE(num_edges == 0 || (src && dst), GBX_ERR_INVALID, "src/dst is NULL");
     GBX_REQUIRE(labels && inverse_labels, GBX_ERR_INVALID, "labels is NULL");
-    GBX_REQUIRE(lmode >= 1 && lmode <= 3, GBX_ERR_INVALID, "lmode must be 1, 2 or 3");
+    GBX_REQUIRE(lmode != 10, GBX_ERR_UNSUPPORTED,
+                "lmode 10 (random order) draws per-thread random degrees in the reference and is not "
+                "reproducible; relabel with explicit labels (gbx_relabel) instead");
+    GBX_REQUIRE(lmode != 11, GBX_ERR_INVALID, "lmode 11 (labels from a file): call gbx_relabel with the labels");
+    GBX_REQUIRE((lmode >= 1 && lmode <= 9) || lmode == 12 || lmode == 13, GBX_ERR_INVALID,
+                "lmode must be 1-9, 12 or 13");
     GBX_TRY(ensure_device());
     cudaStream_t s = (cudaStream_t)stream;
     const uint32_t V = num_vertices, E = num_edges;
@@ -290,8 +347,12 @@ extern "C" int gbx_degree_reorder(uint32_t num_vertices, uint32_t num_edges, uin
     GBX_TRY(newlab.alloc(V, s));
     GBX_TRY(mx.alloc(1, s));
     GBX_CUDA(cudaMemsetAsync(deg.p, 0, (size_t)V * 4, s));
+    // reorderGraphGenerateInOutDegrees (reorder.c:1483-1552): in-degrees for
+    // 2, 5, 7, 9, in + out for 3, out-degrees for every other mode
+    const bool in_deg = lmode == 2 || lmode == 5 || lmode == 7 || lmode == 9;
+    const int count_mode = in_deg ? 2 : (lmode == 3 ? 3 : 1);
     if (E) {
-        degree_count_kernel<<<grid1d(E), 256, 0, s>>>(os.d, od.d, E, lmode, deg.p);
+        degree_count_kernel<<<grid1d(E), 256, 0, s>>>(os.d, od.d, E, count_mode, deg.p);
         GBX_LAUNCH_CHECK();
     }
     GBX_CUDA(cudaMemsetAsync(mx.p, 0, 4, s));
@@ -300,16 +361,108 @@ extern "C" int gbx_degree_reorder(uint32_t num_vertices, uint32_t num_edges, uin
     uint32_t hmax = 0;
     GBX_CUDA(cudaMemcpyAsync(&hmax, mx.p, 4, cudaMemcpyDeviceToHost, s));
     GBX_CUDA(cudaStreamSynchronize(s));
-    iota_kernel<<<grid1d(V), 256, 0, s>>>(ids.p, V);
-    GBX_LAUNCH_CHECK();
-    GBX_TRY(radix_sort_pairs(deg.p, ids.p, V, bits_for(hmax), s));
-    new_labels_kernel<<<grid1d(V), 256, 0, s>>>(ids.p, V, newlab.p);
-    GBX_LAUNCH_CHECK();
+    // thresholds of the bucketed modes: t0 = avg <= 1 ? 1 : avg/2 (HUBCluster:
+    // avg), doubling, last UINT32_MAX; avg = E/V in uint32 as the reference's
+    // EdgeList.avg_degree
+    BucketThresholds th{};
+    th.n = (lmode == 4 || lmode == 5 || lmode == 12 || lmode == 13) ? 11u : (lmode >= 6 && lmode <= 9 ? 2u : 0u);
+    if (th.n) {
+        const uint32_t avg = E / V;
+        th.t[0] = (lmode == 8 || lmode == 9) ? avg : (avg <= 1 ? 1u : avg / 2);
+        for (uint32_t i = 1; i + 1 < th.n; ++i) th.t[i] = th.t[i - 1] * 2u;
+        th.t[th.n - 1] = 0xFFFFFFFFu;
+    }
+    if (th.n == 0) {
+        // reorderGraphListDegree (reorder.c:296-380): stable ascending sort of
+        // (degree, id), label N-1-rank
+        iota_kernel<<<grid1d(V), 256, 0, s>>>(ids.p, V);
+        GBX_LAUNCH_CHECK();
+        GBX_TRY(radix_sort_pairs(deg.p, ids.p, V, bits_for(hmax), s));
+        new_labels_kernel<<<grid1d(V), 256, 0, s>>>(ids.p, V, newlab.p);
+        GBX_LAUNCH_CHECK();
+    } else if (lmode == 6 || lmode == 7) {
+        // HUBSort (reorder.c:814-982): hot vertices (degree above t0) stably
+        // sorted by degree and labelled in reverse, cold ones after, in id order
+        DevBuf<uint32_t> flag, pos, hot_deg, tot;
+        GBX_TRY(flag.alloc(V, s));
+        GBX_TRY(pos.alloc(V, s));
+        GBX_TRY(hot_deg.alloc(V, s));
+        GBX_TRY(tot.alloc(1, s));
+        hot_flag_kernel<<<grid1d(V), 256, 0, s>>>(deg.p, V, th.t[0], flag.p);
+        GBX_LAUNCH_CHECK();
+        GBX_TRY(exclusive_scan_u32(flag.p, pos.p, V, s, tot.p));
+        hot_split_kernel<<<grid1d(V), 256, 0, s>>>(deg.p, flag.p, pos.p, V, tot.p, ids.p, hot_deg.p, newlab.p);
+        GBX_LAUNCH_CHECK();
+        uint32_t H = 0;
+        GBX_CUDA(cudaMemcpyAsync(&H, tot.p, 4, cudaMemcpyDeviceToHost, s));
+        GBX_CUDA(cudaStreamSynchronize(s));
+        GBX_TRY(radix_sort_pairs(hot_deg.p, ids.p, H, bits_for(hmax), s));
+        if (H) {
+            new_labels_kernel<<<grid1d(H), 256, 0, s>>>(ids.p, H, newlab.p);
+            GBX_LAUNCH_CHECK();
+        }
+    } else {
+        // DBG / Corder (11 buckets) and HUBCluster (2): buckets from the
+        // highest, ids ascending inside a bucket
+        bucket_key_kernel<<<grid1d(V), 256, 0, s>>>(deg.p, V, th, deg.p);
+        GBX_LAUNCH_CHECK();
+        iota_kernel<<<grid1d(V), 256, 0, s>>>(ids.p, V);
+        GBX_LAUNCH_CHECK();
+        GBX_TRY(radix_sort_pairs(deg.p, ids.p, V, bits_for(th.n - 1), s));
+        rank_labels_kernel<<<grid1d(V), 256, 0, s>>>(ids.p, V, newlab.p);
+        GBX_LAUNCH_CHECK();
+    }
     if (E) {
         relabel_edges_kernel<<<grid1d(E), 256, 0, s>>>(os.d, od.d, E, newlab.p);
         GBX_LAUNCH_CHECK();
     }
     compose_labels_kernel<<<grid1d(V), 256, 0, s>>>(ol.d, oi.d, V, newlab.p);
+    GBX_LAUNCH_CHECK();
+    GBX_TRY(os.finish(s));
+    GBX_TRY(od.finish(s));
+    GBX_TRY(ol.finish(s));
+    GBX_TRY(oi.finish(s));
+    GBX_CUDA(cudaStreamSynchronize(s));
+    return GBX_OK;
+}
+
+extern "C" int gbx_relabel(uint32_t num_vertices, uint32_t num_edges, uint32_t *src, uint32_t *dst,
+                           const uint32_t *new_labels, uint32_t *labels, uint32_t *inverse_labels, void *stream) {
+    clear_error();
+    GBX_REQUIRE(num_vertices > 0, GBX_ERR_INVALID, "num_vertices must be > 0");
+    GBX_REQUIRE(num_edges == 0 || (src && dst), GBX_ERR_INVALID, "src/dst is NULL");
+    GBX_REQUIRE(new_labels && labels && inverse_labels, GBX_ERR_INVALID, "labels is NULL");
+    GBX_TRY(ensure_device());
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t V = num_vertices, E = num_edges;
+    InArray<uint32_t> nl;
+    GBX_TRY(nl.bind(new_labels, V, s));
+    DevBuf<uint32_t> seen;
+    DevBuf<unsigned> bad;
+    GBX_TRY(seen.alloc(V, s));
+    GBX_TRY(bad.alloc(1, s));
+    GBX_CUDA(cudaMemsetAsync(seen.p, 0, (size_t)V * 4, s));
+    GBX_CUDA(cudaMemsetAsync(bad.p, 0, 4, s));
+    permutation_check_kernel<<<grid1d(V), 256, 0, s>>>(nl.d, V, seen.p, bad.p);
+    GBX_LAUNCH_CHECK();
+    unsigned hbad = 0;
+    GBX_CUDA(cudaMemcpyAsync(&hbad, bad.p, 4, cudaMemcpyDeviceToHost, s));
+    GBX_CUDA(cudaStreamSynchronize(s));
+    GBX_REQUIRE(hbad == 0, GBX_ERR_INVALID, "new_labels is not a permutation of [0, %u): %u bad entries", V,
+                hbad);
+    OutArray<uint32_t> os, od, ol, oi;
+    GBX_TRY(os.bind(src, E, s));
+    GBX_TRY(od.bind(dst, E, s));
+    GBX_TRY(ol.bind(labels, V, s));
+    GBX_TRY(oi.bind(inverse_labels, V, s));
+    if (os.to_host() && E) GBX_CUDA(cudaMemcpyAsync(os.d, src, (size_t)E * 4, cudaMemcpyHostToDevice, s));
+    if (od.to_host() && E) GBX_CUDA(cudaMemcpyAsync(od.d, dst, (size_t)E * 4, cudaMemcpyHostToDevice, s));
+    if (ol.to_host()) GBX_CUDA(cudaMemcpyAsync(ol.d, labels, (size_t)V * 4, cudaMemcpyHostToDevice, s));
+    if (E) {
+        relabel_edges_kernel<<<grid1d(E), 256, 0, s>>>(os.d, od.d, E, nl.d);
+        GBX_LAUNCH_CHECK();
+    }
+    compose_labels_kernel<<<grid1d(V), 256, 0, s>>>(ol.d, oi.d, V, nl.d);
     GBX_LAUNCH_CHECK();
     GBX_TRY(os.finish(s));
     GBX_TRY(od.finish(s));

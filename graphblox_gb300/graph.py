@@ -152,8 +152,10 @@ def csr_build(src, dst, weight=None, *, num_vertices: int, symmetric: bool = Fal
 
 
 def degree_reorder(el: EdgeList, lmode: int = 1, stream=None) -> EdgeList:
-    """reorderGraphProcessDegree on the GPU: relabels el.src/el.dst in place
-    and composes el.label_array / el.inverse_label_array."""
+    """reorderGraphProcess on the GPU for lmode 1-9, 12, 13 (degree, DBG,
+    HUBSort, HUBCluster, Corder): relabels el.src/el.dst in place and
+    composes el.label_array / el.inverse_label_array. lmode 11 is
+    relabel_from_file; lmode 10 (random) is not reproducible and rejected."""
     V = el.num_vertices
     if el.label_array is None:
         el.label_array = np.arange(V, dtype=np.uint32)
@@ -164,6 +166,41 @@ def degree_reorder(el: EdgeList, lmode: int = 1, stream=None) -> EdgeList:
     call("gbx_degree_reorder", V, el.num_edges, _ptr(el.src), _ptr(el.dst), int(lmode),
          _ptr(el.label_array), _ptr(el.inverse_label_array), stream)
     return el
+
+
+def relabel(el: EdgeList, new_labels, stream=None) -> EdgeList:
+    """gbx_relabel: new_labels[v] is the new id of v (a permutation of
+    [0, V)); relabels el.src/el.dst in place and composes the label arrays
+    (relabelEdgeList + label composition, reorder.c:1618-1637,1703-1709)."""
+    V = el.num_vertices
+    if el.label_array is None:
+        el.label_array = np.arange(V, dtype=np.uint32)
+    if el.inverse_label_array is None:
+        el.inverse_label_array = np.arange(V, dtype=np.uint32)
+    el.src = _u32(el.src)
+    el.dst = _u32(el.dst)
+    nl = _u32(new_labels)
+    if nl.shape[0] != V:
+        raise ValueError(f"{nl.shape[0]} labels for {V} vertices")
+    call("gbx_relabel", V, el.num_edges, _ptr(el.src), _ptr(el.dst), _ptr(nl), _ptr(el.label_array),
+         _ptr(el.inverse_label_array), stream)
+    return el
+
+
+def read_label_file(path: str, num_vertices: int) -> np.ndarray:
+    """The reference's label file (lmode 11, relabelEdgeListFromFile,
+    reorder.c:1662-1700): one unsigned label per line, read up to
+    num_vertices of them; fewer is an error here (the reference leaves the
+    rest uninitialised)."""
+    lab = np.loadtxt(path, dtype=np.int64, ndmin=1)[:num_vertices]
+    if lab.shape[0] != num_vertices:
+        raise ValueError(f"{path}: {lab.shape[0]} labels for {num_vertices} vertices")
+    return lab.astype(np.uint32)
+
+
+def relabel_from_file(el: EdgeList, path: str, stream=None) -> EdgeList:
+    """lmode 11: relabel with the labels of the reference's label file."""
+    return relabel(el, read_label_file(path, el.num_vertices), stream)
 
 
 def graph_csr_preprocessing(el: EdgeList, *, sort: int = 0, dedup: bool = False, lmode: int = 0,

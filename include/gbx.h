@@ -37,7 +37,10 @@
  *   gbx_csr_build             -> graphCSRPreProcessingStep's sort/dedup/map
  *                                (01_host/src/structures/graphCSR.c:243-327,
  *                                 radixsort.c:231-339, edgeList.c:255-321, vertex.c:204-328)
- *   gbx_degree_reorder        -> reorderGraphProcessDegree (01_host/src/preprocess/reorder.c:275-380,1483-1552,1618-1637)
+ *   gbx_degree_reorder        -> reorderGraphProcess (01_host/src/preprocess/reorder.c:1556-1614): degree
+ *                                (:275-380), DBG (:387-572), HUBSort (:762-982), HUBCluster (:984-1170),
+ *                                Corder (:574-624), degrees (:1483-1552), relabel (:1618-1637)
+ *   gbx_relabel               -> relabelEdgeListFromFile's relabelling (01_host/src/preprocess/reorder.c:1662-1714)
  * Extension entry points (batched, multi-source, personalised PageRank and
  * its adjoint, generators) have no reference counterpart.
  */
@@ -301,13 +304,34 @@ int gbx_csr_build(uint32_t num_edges, const uint32_t *src, const uint32_t *dst, 
                   uint32_t *out_degree, uint32_t *edges_idx, uint32_t *src_out, uint32_t *dst_out,
                   float *w_out, uint32_t *num_edges_out, void *stream);
 
-/* Degree reordering (lmode 1 out, 2 in, 3 in+out): stable ascending sort
- * of (degree, id), new label of the i-th = N-1-i; composes labels[] and
- * inverse_labels[] in place (identity on a fresh graph) and relabels
- * src/dst in place. The caller re-sorts with gbx_csr_build, as the
- * reference re-runs sortRunAlgorithms. */
+/* Reordering by the reference's lmode (its -l flag). Degrees: in-degree for
+ * lmode 2, 5, 7, 9, in + out for 3, out-degree otherwise (12 and 13 both
+ * count out-degrees, as the reference's degree routine does).
+ *   1, 2, 3      stable ascending sort of (degree, id), new label of the i-th
+ *                = N-1-i (highest degree first, larger id first on ties)
+ *   4, 5, 12, 13 DBG (12/13: Corder, which runs the DBG routine in the
+ *                reference): 11 buckets, thresholds t0 = avg <= 1 ? 1 :
+ *                avg/2 (avg = E/V, integer), doubling, last UINT32_MAX;
+ *                labels bucket by bucket from the highest, ids ascending
+ *   6, 7         HUBSort: vertices above t0 sorted by degree as in mode 1,
+ *                then the others in id order
+ *   8, 9         HUBCluster: vertices above avg, then the others, both in
+ *                id order
+ * lmode 10 (random) is GBX_ERR_UNSUPPORTED: the reference draws per-thread
+ * random keys, so its order depends on its thread count. lmode 11 (labels
+ * from a file) is gbx_relabel. Composes labels[] and inverse_labels[] in
+ * place (identity on a fresh graph) and relabels src/dst in place. The
+ * caller re-sorts with gbx_csr_build, as the reference re-runs
+ * sortRunAlgorithms. */
 int gbx_degree_reorder(uint32_t num_vertices, uint32_t num_edges, uint32_t *src, uint32_t *dst,
                        int lmode, uint32_t *labels, uint32_t *inverse_labels, void *stream);
+/* Relabel with explicit new labels (new_labels[v] = label of v; the
+ * reference's lmode 11 reads them from a text file, one per line):
+ * GBX_ERR_INVALID unless new_labels is a permutation of [0, num_vertices).
+ * Relabels src/dst and composes labels[] / inverse_labels[] like
+ * gbx_degree_reorder. */
+int gbx_relabel(uint32_t num_vertices, uint32_t num_edges, uint32_t *src, uint32_t *dst,
+                const uint32_t *new_labels, uint32_t *labels, uint32_t *inverse_labels, void *stream);
 
 /* ---- synthetic inputs (no reference counterpart) ------------------------ */
 /* R-MAT edge list: 2^scale vertices, num_edges edges, quadrant

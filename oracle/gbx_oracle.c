@@ -121,31 +121,101 @@ void orc_map_vertices(uint32_t num_vertices, uint32_t num_edges, const uint32_t 
 /* degree reordering                                                        */
 /* ------------------------------------------------------------------------ */
 
-/* reorderGraphGenerateInOutDegrees + reorderGraphListDegree: stable
- * ascending sort of (degree, id), label of the i-th smallest = N-1-i, so the
- * largest degree gets label 0 and, within a degree, the larger old id gets
- * the smaller new label (reorder.c:342-348). Then label composition
- * (reorder.c:368-373) and relabelEdgeList (reorder.c:1618-1637). */
+/* reorderGraphProcess (reorder.c:1556-1614) for the deterministic modes.
+ *
+ * Degrees (reorderGraphGenerateInOutDegrees, reorder.c:1483-1552): lmodes
+ * 2, 5, 7, 9 count in-degrees, 3 in + out, every other mode (1, 4, 6, 8 and,
+ * through the switch's default, 12 and 13) out-degrees.
+ *
+ * lmode 1-3 (reorderGraphListDegree, :296-380): stable ascending sort of
+ * (degree, id); the i-th smallest gets label N-1-i, so the largest degree
+ * gets label 0 and, within a degree, the larger old id the smaller label.
+ *
+ * Bucketed modes: thresholds t0 = avg <= 1 ? 1 : avg/2 (avg = E/V, uint32;
+ * HUBCluster takes t0 = avg itself, :1001), t_i = 2 t_{i-1}, last =
+ * UINT32_MAX; v goes to the first bucket with degree <= t_i. lmode 4, 5 (DBG, :387-572) and 12, 13 (Corder, whose
+ * process function calls the DBG list routine, :574-624) use 11 buckets,
+ * lmode 8, 9 (HUBCluster, :984-1170) two: labels are given bucket by bucket
+ * from the highest, in ascending id order inside a bucket. lmode 6, 7
+ * (HUBSort, :762-982), two buckets: the hot bucket's vertices (ascending
+ * ids) are stably sorted by degree and labelled in reverse (hot size - 1 -
+ * position), the cold ones follow in id order.
+ *
+ * Then label composition (:368-373) and relabelEdgeList (:1618-1637).
+ * lmode 10 (random) draws from per-thread generators and depends on the
+ * thread count, so it is not restated. */
+static uint32_t reorder_buckets(int lmode) {
+    switch (lmode) {
+    case 4: case 5: case 12: case 13: return 11;
+    case 6: case 7: case 8: case 9: return 2;
+    default: return 0;
+    }
+}
+
 void orc_degree_reorder(uint32_t num_vertices, uint32_t num_edges, uint32_t *src, uint32_t *dst,
                         int lmode, uint32_t *labels, uint32_t *inverse_labels, int num_threads) {
     set_threads(num_threads);
     uint32_t n = num_vertices;
     uint32_t *deg = (uint32_t *)calloc((size_t)n + 1, 4);
     if (!deg) abort();
+    const int in = lmode == 2 || lmode == 5 || lmode == 7 || lmode == 9;
     for (uint32_t i = 0; i < num_edges; ++i) {
-        if (lmode == 2) deg[dst[i]]++;
+        if (in) deg[dst[i]]++;
         else if (lmode == 3) { deg[dst[i]]++; deg[src[i]]++; }
         else deg[src[i]]++;
     }
-    uint32_t maxdeg = 0;
-    for (uint32_t v = 0; v < n; ++v) if (deg[v] > maxdeg) maxdeg = deg[v];
-    uint32_t *ids = (uint32_t *)calloc((size_t)n + 1, 4);
-    if (!ids) abort();
-    uint32_t *sorted = (uint32_t *)xmalloc((size_t)n * 4 + 4);
-    for (uint32_t v = 0; v < n; ++v) ids[v] = v;
-    counting_pass(n, deg, maxdeg + 1, ids, sorted);
     uint32_t *newlab = (uint32_t *)xmalloc((size_t)n * 4 + 4);
-    for (uint32_t i = 0; i < n; ++i) newlab[sorted[i]] = n - 1 - i;
+    const uint32_t nb = reorder_buckets(lmode);
+    if (nb == 0) {
+        uint32_t maxdeg = 0;
+        for (uint32_t v = 0; v < n; ++v) if (deg[v] > maxdeg) maxdeg = deg[v];
+        uint32_t *ids = (uint32_t *)calloc((size_t)n + 1, 4);
+        uint32_t *sorted = (uint32_t *)xmalloc((size_t)n * 4 + 4);
+        if (!ids) abort();
+        for (uint32_t v = 0; v < n; ++v) ids[v] = v;
+        counting_pass(n, deg, maxdeg + 1, ids, sorted);
+        for (uint32_t i = 0; i < n; ++i) newlab[sorted[i]] = n - 1 - i;
+        free(sorted);
+        free(ids);
+    } else {
+        uint32_t th[11];
+        const uint32_t avg = n ? num_edges / n : 0;
+        th[0] = (lmode == 8 || lmode == 9) ? avg : (avg <= 1 ? 1u : avg / 2);
+        for (uint32_t i = 1; i + 1 < nb; ++i) th[i] = th[i - 1] * 2u;
+        th[nb - 1] = 0xFFFFFFFFu;
+        uint8_t *bk = (uint8_t *)xmalloc((size_t)n + 1);
+        uint32_t size[11] = {0};
+        for (uint32_t v = 0; v < n; ++v) {
+            uint32_t i = 0;
+            while (deg[v] > th[i]) ++i;
+            bk[v] = (uint8_t)i;
+            size[i]++;
+        }
+        if (lmode == 6 || lmode == 7) {
+            const uint32_t hot = size[1];
+            uint32_t *hid = (uint32_t *)xmalloc((size_t)hot * 4 + 4);
+            uint32_t *hs = (uint32_t *)xmalloc((size_t)hot * 4 + 4);
+            uint32_t h = 0, c = 0, maxdeg = 0;
+            for (uint32_t v = 0; v < n; ++v) {
+                if (bk[v] == 1) {
+                    hid[h++] = v;
+                    if (deg[v] > maxdeg) maxdeg = deg[v];
+                } else {
+                    newlab[v] = hot + c++;
+                }
+            }
+            counting_pass(hot, deg, maxdeg + 1, hid, hs);
+            for (uint32_t i = 0; i < hot; ++i) newlab[hs[i]] = hot - 1 - i;
+            free(hs);
+            free(hid);
+        } else {
+            uint32_t start[11];
+            uint32_t acc = 0;
+            for (int j = (int)nb - 1; j >= 0; --j) { start[j] = acc; acc += size[j]; }
+            for (uint32_t v = 0; v < n; ++v) newlab[v] = start[bk[v]]++;
+        }
+        free(bk);
+    }
     #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < (int64_t)num_edges; ++i) {
         src[i] = newlab[src[i]];
@@ -156,8 +226,6 @@ void orc_degree_reorder(uint32_t num_vertices, uint32_t num_edges, uint32_t *src
         inverse_labels[labels[v]] = v;
     }
     free(newlab);
-    free(sorted);
-    free(ids);
     free(deg);
 }
 

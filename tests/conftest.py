@@ -9,11 +9,19 @@ if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-GOLDEN_GRAPHS = sorted(p.stem for p in GOLDEN.glob("*.npz"))
+# one fixture per test graph; reorder_modes.npz holds the labels of the
+# reorder modes for all of them
+GOLDEN_GRAPHS = sorted(p.stem for p in GOLDEN.glob("*.npz") if p.stem != "reorder_modes")
+REORDER_MODES = [2, 3, 4, 5, 6, 7, 8, 9, 12, 13]
 
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (run on the GB300 host)")
+
+
+def load_reorder_modes() -> dict:
+    with np.load(GOLDEN / "reorder_modes.npz") as z:
+        return {k: z[k] for k in z.files}
 
 
 def load_golden(name: str) -> dict:

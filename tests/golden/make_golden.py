@@ -12,7 +12,8 @@ its build (oracle/build_ref.sh). For every test graph the reference ships in
 The GPU host has no reference tree, so the parity tests read only these
 fixtures there.
 
-Usage: python tests/golden/make_golden.py [REFERENCE_ROOT]
+Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [reorder]
+("reorder" writes only reorder_modes.npz, the labels of the reorder modes.)
 """
 from __future__ import annotations
 
@@ -105,5 +106,37 @@ def main(ref_root: str) -> None:
         print(f"wrote {name}.npz")
 
 
+REORDER_MODES = [2, 3, 4, 5, 6, 7, 8, 9, 12, 13]
+
+
+def reorder_modes(ref_root: str) -> None:
+    """tests/golden/reorder_modes.npz: the reference's label_array after each
+    deterministic reorder mode (in/in+out degree, DBG, HUBSort, HUBCluster,
+    Corder) on every test graph and build variant (keys
+    <graph>_<variant>_l<mode>); the CSR it reorders is <variant>_src /
+    _dest / _num_vertices of <graph>.npz."""
+    test_dir = Path(ref_root) / "03_data" / "TEST"
+    fx: dict[str, np.ndarray] = {}
+    for name in GRAPHS:
+        gdir = test_dir / name
+        weighted = (gdir / "graph.wbin").exists() and not (gdir / "graph.bin").exists()
+        f = gdir / ("graph.wbin" if weighted else "graph.bin")
+        wflag = ["-w"] if weighted else []
+        for variant, flags in (("u", ["-s", "-k"]), ("dw", [])):
+            exe = "u" if variant == "u" else "dw"
+            fl = ["-o", "1", *wflag, *flags]
+            key = f"{name}_{variant}"
+            for lm in REORDER_MODES:
+                fx[f"{key}_l{lm}"] = po.ref_run(f, exe, -1, [*fl, "-l", str(lm)])["label"]
+    out = Path(__file__).resolve().parent / "reorder_modes.npz"
+    np.savez_compressed(out, **fx)
+    print(f"wrote {out.name}")
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) > 2 and sys.argv[2] == "reorder":
+        reorder_modes(root)
+    else:
+        main(root)
+        reorder_modes(root)

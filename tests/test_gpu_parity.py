@@ -8,7 +8,7 @@ relative L1 of the FP64 restatement (the tolerance the spec states).
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_GRAPHS, load_golden
+from conftest import GOLDEN_GRAPHS, REORDER_MODES, load_golden, load_reorder_modes
 from oracle import pyoracle as po
 
 pytestmark = pytest.mark.gpu
@@ -385,3 +385,65 @@ def test_bfs_pull_only_level_scan(gbx, cuda_device):
             st = gbx.breadth_first_search(dg, r, 0)
             np.testing.assert_array_equal(np.asarray(st.distances).astype(np.int64), ref)
             assert st.processed_nodes == reached
+
+
+@pytest.mark.parametrize("name", GOLDEN_GRAPHS)
+@pytest.mark.parametrize("variant", ["u", "dw"])
+def test_reorder_modes_golden(gbx, cuda_device, name, variant):
+    """In/in+out degree, DBG, HUBSort, HUBCluster and Corder on the GPU
+    against the reference's labels, on the CSR the reference reorders."""
+    fx = load_golden(name)
+    rm = load_reorder_modes()
+    V = int(fx[f"{variant}_num_vertices"])
+    for lm in REORDER_MODES:
+        el = gbx.EdgeList(V, fx[f"{variant}_src"].copy(), fx[f"{variant}_dest"].copy())
+        gbx.degree_reorder(el, lm)
+        lab = rm[f"{name}_{variant}_l{lm}"]
+        np.testing.assert_array_equal(el.label_array, lab, err_msg=f"lmode {lm}")
+        np.testing.assert_array_equal(el.inverse_label_array[lab], np.arange(V, dtype=np.uint32))
+        np.testing.assert_array_equal(el.src, lab[fx[f"{variant}_src"]])
+        np.testing.assert_array_equal(el.dst, lab[fx[f"{variant}_dest"]])
+
+
+@pytest.mark.parametrize("lmode", [1, 2, 3, 4, 5, 6, 7, 8, 9, 12, 13])
+def test_reorder_modes_rmat(gbx, cuda_device, lmode):
+    """Every mode on a deduplicated RMAT-16 edge list (hubs above all DBG
+    thresholds, many degree-0 vertices) against the oracle."""
+    src, dst = gbx.generate_rmat(16, (1 << 16) * 16, seed=41)
+    V = 1 << 16
+    _, _, s, d, _ = gbx.csr_build(src, dst, num_vertices=V, dedup=True, sort=1)
+    rs, rd, rlab, rinv = po.degree_reorder(V, s, d, lmode=lmode)
+    el = gbx.EdgeList(V, s.copy(), d.copy())
+    gbx.degree_reorder(el, lmode)
+    np.testing.assert_array_equal(el.label_array, rlab)
+    np.testing.assert_array_equal(el.inverse_label_array, rinv)
+    np.testing.assert_array_equal(el.src, rs)
+    np.testing.assert_array_equal(el.dst, rd)
+
+
+def test_relabel_explicit_and_rejected(gbx, cuda_device, tmp_path):
+    """lmode 11: labels from the reference's label file; a label list that
+    is not a permutation, and the non-reproducible random mode, are errors."""
+    src, dst = gbx.generate_rmat(12, 1 << 15, seed=43)
+    V = 1 << 12
+    perm = np.random.default_rng(4).permutation(V).astype(np.uint32)
+    f = tmp_path / "labels.txt"
+    f.write_text("".join(f"{x}\n" for x in perm))
+    el = gbx.relabel_from_file(gbx.EdgeList(V, src.copy(), dst.copy()), str(f))
+    np.testing.assert_array_equal(el.src, perm[src])
+    np.testing.assert_array_equal(el.dst, perm[dst])
+    np.testing.assert_array_equal(el.label_array, perm)
+    np.testing.assert_array_equal(el.inverse_label_array[perm], np.arange(V, dtype=np.uint32))
+    # composition: a second relabelling maps the composed labels
+    perm2 = np.roll(np.arange(V, dtype=np.uint32), 5)
+    gbx.relabel(el, perm2)
+    np.testing.assert_array_equal(el.label_array, perm2[perm])
+    np.testing.assert_array_equal(el.src, perm2[perm[src]])
+    bad = perm.copy()
+    bad[7] = bad[8]
+    with pytest.raises(gbx.GbxError) as e:
+        gbx.relabel(gbx.EdgeList(V, src.copy(), dst.copy()), bad)
+    assert e.value.status == -1
+    with pytest.raises(gbx.GbxError) as e:
+        gbx.degree_reorder(gbx.EdgeList(V, src.copy(), dst.copy()), 10)
+    assert e.value.status == -6

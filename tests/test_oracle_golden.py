@@ -7,7 +7,7 @@ tests/golden/*.npz by tests/golden/make_golden.py.
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_GRAPHS, load_golden
+from conftest import GOLDEN_GRAPHS, REORDER_MODES, load_golden, load_reorder_modes
 from oracle import pyoracle as po
 
 VARIANTS = [("u", True, True), ("dw", False, False), ("dwk", False, True)]
@@ -103,6 +103,22 @@ def test_oracle_degree_reorder(name, variant, symmetric, dedup):
     g2 = po.build_csr(V, s, d, sort_mode=1)
     np.testing.assert_array_equal(g2.dest, fx[f"{variant}_reorder_dest"])
     np.testing.assert_array_equal(g2.out_degree, fx[f"{variant}_reorder_out_degree"])
+
+
+@pytest.mark.parametrize("name", GOLDEN_GRAPHS)
+@pytest.mark.parametrize("variant", ["u", "dw"])
+def test_oracle_reorder_modes(name, variant):
+    """In/in+out degree, DBG, HUBSort, HUBCluster and Corder labels of the
+    reference on the CSR it reorders (the reference's own build output)."""
+    fx = load_golden(name)
+    rm = load_reorder_modes()
+    V = int(fx[f"{variant}_num_vertices"])
+    for lm in REORDER_MODES:
+        s, d, lab, inv = po.degree_reorder(V, fx[f"{variant}_src"], fx[f"{variant}_dest"], lmode=lm)
+        np.testing.assert_array_equal(lab, rm[f"{name}_{variant}_l{lm}"], err_msg=f"lmode {lm}")
+        np.testing.assert_array_equal(inv[lab], np.arange(V, dtype=np.uint32))
+        np.testing.assert_array_equal(s, lab[fx[f"{variant}_src"]])
+        np.testing.assert_array_equal(d, lab[fx[f"{variant}_dest"]])
 
 
 @pytest.mark.skipif(not po.ref_available("dw"), reason="reference build (oracle/_ref) not present")
