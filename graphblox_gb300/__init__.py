@@ -34,10 +34,12 @@ from .graph import (  # noqa: F401
     ppr_adjoint,
     ppr_forward,
     read_edge_list_bin,
+    read_graph_csr_bin,
     spmv,
     sssp,
     triangle_count,
     write_edge_list_bin,
+    write_graph_csr_bin,
 )
 
 __version__ = "0.1.0"

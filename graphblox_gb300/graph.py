@@ -118,6 +118,8 @@ class GraphCSR:
     inverse_edges_idx: Optional[np.ndarray] = None
     inverse_dest: Optional[np.ndarray] = None
     inverse_weight: Optional[np.ndarray] = None
+    inverse_src: Optional[np.ndarray] = None
+    max_weight: float = 0.0
 
     @property
     def avg_degree(self) -> int:
@@ -222,9 +224,124 @@ def graph_csr_preprocessing(el: EdgeList, *, sort: int = 0, dedup: bool = False,
         labels, inv_labels = tmp.label_array, tmp.inverse_label_array
         deg, idx, s, d, ww = csr_build(tmp.src, tmp.dst, ww, num_vertices=V, sort=sort, stream=stream)
     g = GraphCSR(V, int(s.shape[0]), deg, idx, d, s, ww, labels, inv_labels)
+    # max over the weights as read (edgeList.c:673-684), kept through dedup
+    if el.weight is not None and el.num_edges:
+        g.max_weight = float(max(0.0, float(np.max(el.weight))))
     if directed:
         ideg, iidx, isrc, idst, iw = csr_build(d, s, ww, num_vertices=V, sort=sort, stream=stream)
         g.inverse_out_degree, g.inverse_edges_idx, g.inverse_dest, g.inverse_weight = ideg, iidx, idst, iw
+        g.inverse_src = isrc
+    return g
+
+
+# ---------------------------------------------------------------------------
+# the reference's binary CSR file (.csr)
+
+
+def _csr_record_types(weighted: bool, directed: bool):
+    """Record layouts of the .csr file: one vertex record per vertex
+    (graphCSR.c:486-500), then one edge record per edge (graphCSR.c:502-524);
+    the inverse fields exist in DIRECTED builds, the weights in WEIGHTED
+    builds. All fields are 4 bytes, native (little-endian) order, packed."""
+    u4, f4 = np.dtype("<u4"), np.dtype("<f4")
+    vf = [("out_degree", u4), ("in_degree", u4), ("edges_idx", u4)]
+    ef = [("src", u4), ("dest", u4)] + ([("weight", f4)] if weighted else [])
+    if directed:
+        vf += [("inv_out_degree", u4), ("inv_in_degree", u4), ("inv_edges_idx", u4)]
+        ef += [("inv_src", u4), ("inv_dest", u4)] + ([("inv_weight", f4)] if weighted else [])
+    return np.dtype(vf), np.dtype(ef)
+
+
+def _csr_file_size(V: int, E: int, weighted: bool, directed: bool) -> int:
+    vt, et = _csr_record_types(weighted, directed)
+    return 8 + (4 if weighted else 0) + V * vt.itemsize + E * et.itemsize
+
+
+def write_graph_csr_bin(fname: str, g: GraphCSR, *, weighted: Optional[bool] = None,
+                        directed: Optional[bool] = None) -> str:
+    """writeToBinFileGraphCSR (graphCSR.c:458-529): writes `fname + ".csr"`
+    and returns that path. Header: num_edges, num_vertices (uint32) and, in
+    a WEIGHTED build, max_weight (float32); then the vertex and the edge
+    records of _csr_record_types. in_degree is the other direction's
+    out-degree in a DIRECTED build (vertex.c:291-310) and 0 otherwise.
+    weighted / directed name the reference build whose file is written
+    (default: what g holds)."""
+    weighted = (g.weight is not None) if weighted is None else bool(weighted)
+    directed = g.directed if directed is None else bool(directed)
+    if weighted and g.weight is None:
+        raise ValueError("a WEIGHTED .csr needs edge weights")
+    if directed and (g.inverse_dest is None or g.inverse_out_degree is None or g.inverse_edges_idx is None):
+        raise ValueError("a DIRECTED .csr needs the inverse CSR")
+    V, E = int(g.num_vertices), int(g.num_edges)
+    vt, et = _csr_record_types(weighted, directed)
+    vrec = np.zeros(V, dtype=vt)
+    vrec["out_degree"] = g.out_degree[:V]
+    vrec["edges_idx"] = g.edges_idx[:V]
+    erec = np.zeros(E, dtype=et)
+    erec["src"] = g.src[:E]
+    erec["dest"] = g.dest[:E]
+    if weighted:
+        erec["weight"] = g.weight[:E]
+    if directed:
+        ideg = _u32(g.inverse_out_degree[:V])
+        vrec["in_degree"] = ideg
+        vrec["inv_out_degree"] = ideg
+        vrec["inv_in_degree"] = g.out_degree[:V]
+        vrec["inv_edges_idx"] = g.inverse_edges_idx[:V]
+        isrc = g.inverse_src if g.inverse_src is not None else np.repeat(np.arange(V, dtype=np.uint32), ideg)
+        erec["inv_src"] = isrc[:E]
+        erec["inv_dest"] = g.inverse_dest[:E]
+        if weighted:
+            iw = g.inverse_weight if g.inverse_weight is not None else np.ones(E, np.float32)
+            erec["inv_weight"] = iw[:E]
+    path = fname + ".csr"
+    with open(path, "wb") as f:
+        f.write(np.array([E, V], dtype="<u4").tobytes())
+        if weighted:
+            f.write(np.array([g.max_weight], dtype="<f4").tobytes())
+        f.write(vrec.tobytes())
+        f.write(erec.tobytes())
+    return path
+
+
+def read_graph_csr_bin(path: str, *, weighted: Optional[bool] = None,
+                       directed: Optional[bool] = None) -> GraphCSR:
+    """readFromBinFileGraphCSR (graphCSR.c:638-744). The file does not name
+    its build; weighted / directed default to the one layout whose size
+    matches the header's counts (the four sizes differ for any V >= 1). A
+    size that matches no layout, or not the one asked for, is an error (the
+    reference reads on past the end). Labels start as the identity."""
+    raw = np.fromfile(path, dtype=np.uint8)
+    if raw.shape[0] < 8:
+        raise ValueError(f"{path}: {raw.shape[0]} bytes, no .csr header")
+    E, V = (int(x) for x in raw[:8].view("<u4"))
+    combos = [(w, d) for w in (False, True) for d in (False, True)
+              if (weighted is None or w == weighted) and (directed is None or d == directed)]
+    match = [(w, d) for w, d in combos if _csr_file_size(V, E, w, d) == raw.shape[0]]
+    if len(match) != 1:
+        raise ValueError(f"{path}: {raw.shape[0]} bytes fit no .csr layout for V={V} E={E}"
+                         f" (weighted={weighted}, directed={directed})")
+    weighted, directed = match[0]
+    vt, et = _csr_record_types(weighted, directed)
+    off = 8
+    max_weight = 0.0
+    if weighted:
+        max_weight = float(raw[8:12].view("<f4")[0])
+        off = 12
+    vrec = raw[off:off + V * vt.itemsize].view(vt)
+    off += V * vt.itemsize
+    erec = raw[off:off + E * et.itemsize].view(et)
+    ident = np.arange(V, dtype=np.uint32)
+    g = GraphCSR(V, E, vrec["out_degree"].astype(np.uint32), vrec["edges_idx"].astype(np.uint32),
+                 erec["dest"].astype(np.uint32), erec["src"].astype(np.uint32),
+                 erec["weight"].astype(np.float32) if weighted else None, ident.copy(), ident.copy(),
+                 max_weight=max_weight)
+    if directed:
+        g.inverse_out_degree = vrec["inv_out_degree"].astype(np.uint32)
+        g.inverse_edges_idx = vrec["inv_edges_idx"].astype(np.uint32)
+        g.inverse_dest = erec["inv_dest"].astype(np.uint32)
+        g.inverse_src = erec["inv_src"].astype(np.uint32)
+        g.inverse_weight = erec["inv_weight"].astype(np.float32) if weighted else None
     return g
 
 

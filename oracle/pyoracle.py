@@ -228,6 +228,6 @@ def ref_run(graph_file, variant="dw", algorithm=-1, flags=(), threads=4):
                     out[k] = float(v) if ("." in v or "e" in v) else int(v)
             else:
                 stem, ext = f.name.rsplit(".", 1)
-                dt = {"u32": np.uint32, "i32": np.int32, "f32": np.float32}[ext]
+                dt = {"u32": np.uint32, "i32": np.int32, "f32": np.float32, "csr": np.uint8}[ext]
                 out[stem] = np.fromfile(f, dtype=dt)
         return out

@@ -21,6 +21,7 @@
 //   -p PP   pushpull variant        -s symmetric      -k dedup (+sort 1)
 //   -w      weighted .wbin input    -o SORT           -l LMODE
 //   -r ROOT -i ITERS -e EPS -b DELTA -n THREADS
+//   -W      also write the reference's binary CSR file (graph.csr)
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -58,6 +59,7 @@ int main(int argc, char **argv) {
     std::string out = argv[2];
     int alg = -1;
     int threads = omp_get_max_threads();
+    bool write_csr = false;
     for (int i = 3; i < argc; ++i) {
         std::string f = argv[i];
         auto next = [&](void) -> const char * {
@@ -76,6 +78,7 @@ int main(int argc, char **argv) {
         else if (f == "-e") a->epsilon = std::atof(next());
         else if (f == "-b") a->delta = (uint32_t)std::atoi(next());
         else if (f == "-n") threads = std::atoi(next());
+        else if (f == "-W") write_csr = true;
         else { std::fprintf(stderr, "unknown flag %s\n", f.c_str()); return 2; }
     }
     a->pre_numThreads = threads;
@@ -86,6 +89,10 @@ int main(int argc, char **argv) {
 
     struct GraphCSR *g = (struct GraphCSR *)generateGraphDataStructure(a);
     omp_set_num_threads(threads);
+
+    // the reference's binary CSR file (writeToBinFileGraphCSR, graphCSR.c:458-529):
+    // OUTDIR/graph.csr
+    if (write_csr) writeToBinFileGraphCSR((out + "/graph").c_str(), g);
 
     FILE *sc = std::fopen((out + "/scalars.txt").c_str(), "w");
     if (!sc) { std::perror("scalars"); return 2; }

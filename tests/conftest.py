@@ -10,8 +10,8 @@ if str(ROOT) not in sys.path:
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 # one fixture per test graph; reorder_modes.npz holds the labels of the
-# reorder modes for all of them
-GOLDEN_GRAPHS = sorted(p.stem for p in GOLDEN.glob("*.npz") if p.stem != "reorder_modes")
+# reorder modes for all of them, csr_files.npz the reference's .csr files
+GOLDEN_GRAPHS = sorted(p.stem for p in GOLDEN.glob("*.npz") if p.stem not in ("reorder_modes", "csr_files"))
 REORDER_MODES = [2, 3, 4, 5, 6, 7, 8, 9, 12, 13]
 
 
@@ -21,6 +21,11 @@ def pytest_configure(config):
 
 def load_reorder_modes() -> dict:
     with np.load(GOLDEN / "reorder_modes.npz") as z:
+        return {k: z[k] for k in z.files}
+
+
+def load_csr_files() -> dict:
+    with np.load(GOLDEN / "csr_files.npz") as z:
         return {k: z[k] for k in z.files}
 
 

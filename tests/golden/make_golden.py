@@ -12,8 +12,9 @@ its build (oracle/build_ref.sh). For every test graph the reference ships in
 The GPU host has no reference tree, so the parity tests read only these
 fixtures there.
 
-Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [reorder]
-("reorder" writes only reorder_modes.npz, the labels of the reorder modes.)
+Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [reorder|csr]
+("reorder" writes only reorder_modes.npz, the labels of the reorder modes;
+"csr" writes only csr_files.npz, the reference's .csr files.)
 """
 from __future__ import annotations
 
@@ -133,10 +134,36 @@ def reorder_modes(ref_root: str) -> None:
     print(f"wrote {out.name}")
 
 
+CSR_FILE_GRAPHS = ["v51_e1021", "v300_e2730", "v500_e500", "v1024_e4096", "test"]
+
+
+def csr_files(ref_root: str) -> None:
+    """tests/golden/csr_files.npz: the bytes of the .csr file the reference
+    writes (writeToBinFileGraphCSR) for a few test graphs, in the shipped
+    build (u: -s -k, no weights, no inverse), the DIRECTED 1 / WEIGHTED 1
+    build on the graph as read (dw) and the same with dedup (dwk). Keys
+    <graph>_<variant>."""
+    test_dir = Path(ref_root) / "03_data" / "TEST"
+    fx: dict[str, np.ndarray] = {}
+    for name in CSR_FILE_GRAPHS:
+        gdir = test_dir / name
+        weighted = (gdir / "graph.wbin").exists() and not (gdir / "graph.bin").exists()
+        f = gdir / ("graph.wbin" if weighted else "graph.bin")
+        wflag = ["-w"] if weighted else []
+        for variant, flags in (("u", ["-s", "-k"]), ("dw", []), ("dwk", ["-k"])):
+            exe = "u" if variant == "u" else "dw"
+            fx[f"{name}_{variant}"] = po.ref_run(f, exe, -1, ["-o", "1", *wflag, *flags, "-W"])["graph"]
+    out = Path(__file__).resolve().parent / "csr_files.npz"
+    np.savez_compressed(out, **fx)
+    print(f"wrote {out.name}")
+
+
 if __name__ == "__main__":
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     if len(sys.argv) > 2 and sys.argv[2] == "reorder":
         reorder_modes(root)
+    elif len(sys.argv) > 2 and sys.argv[2] == "csr":
+        csr_files(root)
     else:
         main(root)
         reorder_modes(root)
