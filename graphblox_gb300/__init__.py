@@ -28,6 +28,7 @@ from .graph import (  # noqa: F401
     generate_rmat,
     generate_rmat_batch,
     generate_values,
+    mask_graph,
     graph_csr_preprocessing,
     pack_graphs,
     page_rank,

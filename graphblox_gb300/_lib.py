@@ -73,6 +73,7 @@ SIGNATURES = {
                                 C.POINTER(u32), vp]),
     "gbx_degree_reorder": (C.c_int, [u32, u32, vp, vp, C.c_int, vp, vp, vp]),
     "gbx_relabel": (C.c_int, [u32, u32, vp, vp, vp, vp, vp, vp]),
+    "gbx_mask_graph": (C.c_int, [u32, u32, vp, vp, C.c_int, u32, vp, vp]),
     "gbx_generate_rmat": (C.c_int, [u32, u64, C.c_double, C.c_double, C.c_double, u64, vp, vp]),
     "gbx_generate_values": (C.c_int, [u64, C.c_int, u32, u32, u64, vp]),
     "gbx_generate_chung_lu": (C.c_int, [u32, u64, C.c_double, u32, C.c_double, u64, vp, vp, vp]),

@@ -133,12 +133,34 @@ __global__ void degree_from_offsets_kernel(const uint32_t *off, uint32_t *deg, u
         deg[v] = off[v + 1] - off[v];
 }
 
-// The reference layout is edges_idx + out_degree over a source-sorted array;
-// it must equal the prefix-sum offsets wherever the degree is non-zero.
+// The reference layout is edges_idx + out_degree: the edges of v are the run
+// ids[edges_idx[v] .. +deg[v]). bad[0] counts vertices whose run does not
+// start at the prefix-sum offset (runs out of vertex order, as in the
+// inverse CSR the reference sorts on masked ids), bad[2] runs that end past
+// the E edges.
 __global__ void check_layout_kernel(const uint32_t *edges_idx, const uint32_t *deg,
-                                    const uint32_t *off, uint32_t V, unsigned *bad) {
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
-        if (deg[v] && edges_idx[v] != off[v]) atomicAdd(bad, 1u);
+                                    const uint32_t *off, uint32_t V, uint32_t E, unsigned *bad) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        if (!deg[v]) continue;
+        if (edges_idx[v] != off[v]) atomicAdd(bad, 1u);
+        if ((uint64_t)edges_idx[v] + deg[v] > E) atomicAdd(bad + 2, 1u);
+    }
+}
+
+// Moves every run to its prefix-sum position, keeping the order inside the
+// run (one warp per vertex; runs checked in bounds by check_layout_kernel).
+__global__ void repack_runs_kernel(const uint32_t *edges_idx, const uint32_t *deg,
+                                   const uint32_t *off, uint32_t V, const uint32_t *ids,
+                                   const float *w, uint32_t *ids_out, float *w_out) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < V; v += warps) {
+        const uint32_t n = deg[v], from = edges_idx[v], to = off[v];
+        for (uint32_t k = lane; k < n; k += 32) {
+            ids_out[to + k] = ids[from + k];
+            if (w) w_out[to + k] = w[from + k];
+        }
+    }
 }
 
 __global__ void check_offsets_kernel(const uint32_t *off, uint32_t V, uint32_t E, unsigned *bad) {
@@ -192,8 +214,10 @@ static int fill_direction(uint32_t V, uint32_t E, const uint32_t *edges_idx, con
     GBX_CUDA(cudaMemsetAsync(*d_ids + E, 0, 16, s));
     if (w) GBX_TRY(dmalloc((void **)d_w, (size_t)E * 4));
     DevBuf<unsigned> bad;
-    GBX_TRY(bad.alloc(2, s));
-    GBX_CUDA(cudaMemsetAsync(bad.p, 0, 8, s));
+    GBX_TRY(bad.alloc(3, s));
+    GBX_CUDA(cudaMemsetAsync(bad.p, 0, 12, s));
+    bool repack = false;
+    InArray<uint32_t> eidx;
     if (offsets) {
         GBX_TRY(copy_in(*d_off, offsets, (size_t)(V + 1) * 4, s));
         check_offsets_kernel<<<grid_for(V), 256, 0, s>>>(*d_off, V, E, bad.p);
@@ -208,30 +232,45 @@ static int fill_direction(uint32_t V, uint32_t E, const uint32_t *edges_idx, con
         total = tot.p;
         GBX_TRY(exclusive_scan_u32(*d_deg, *d_off, V, s, total));
         GBX_CUDA(cudaMemcpyAsync(*d_off + V, total, 4, cudaMemcpyDeviceToDevice, s));
-        InArray<uint32_t> eidx;
         GBX_TRY(eidx.bind(edges_idx, V, s));
-        check_layout_kernel<<<grid_for(V), 256, 0, s>>>(eidx.d, *d_deg, *d_off, V, bad.p);
+        check_layout_kernel<<<grid_for(V), 256, 0, s>>>(eidx.d, *d_deg, *d_off, V, E, bad.p);
         GBX_LAUNCH_CHECK();
         uint32_t hv = 0;
+        unsigned hl[3] = {0, 0, 0};
         GBX_CUDA(cudaMemcpyAsync(&hv, total, 4, cudaMemcpyDeviceToHost, s));
+        GBX_CUDA(cudaMemcpyAsync(hl, bad.p, 12, cudaMemcpyDeviceToHost, s));
         GBX_CUDA(cudaStreamSynchronize(s));
         GBX_REQUIRE(hv == E, GBX_ERR_INVALID, "sum of degrees (%u) != num_edges (%u)", hv, E);
+        GBX_REQUIRE(hl[2] == 0, GBX_ERR_INVALID,
+                    "%u vertices whose edges_idx + out_degree exceeds num_edges (%u)", hl[2], E);
+        repack = hl[0] != 0;
+        GBX_CUDA(cudaMemsetAsync(bad.p, 0, 4, s));
     }
-    GBX_TRY(copy_in(*d_ids, ids, (size_t)E * 4, s));
+    if (repack) {
+        // runs out of vertex order: gather them into offset order
+        InArray<uint32_t> raw_ids;
+        InArray<float> raw_w;
+        GBX_TRY(raw_ids.bind(ids, E, s));
+        GBX_TRY(raw_w.bind(w, E, s));
+        repack_runs_kernel<<<grid_for((uint64_t)V * 32), 256, 0, s>>>(eidx.d, *d_deg, *d_off, V, raw_ids.d,
+                                                                     w ? raw_w.d : nullptr, *d_ids,
+                                                                     w ? *d_w : nullptr);
+        GBX_LAUNCH_CHECK();
+        GBX_CUDA(cudaStreamSynchronize(s));
+    } else {
+        GBX_TRY(copy_in(*d_ids, ids, (size_t)E * 4, s));
+        if (w) GBX_TRY(copy_in(*d_w, w, (size_t)E * 4, s));
+    }
     if (E) {
         mask_ids_kernel<<<grid_for(E), 256, 0, s>>>(*d_ids, E);
         GBX_LAUNCH_CHECK();
     }
-    if (w) GBX_TRY(copy_in(*d_w, w, (size_t)E * 4, s));
     max_u32_kernel<<<grid_for(V), 256, 0, s>>>(*d_deg, V, bad.p + 1);
     GBX_LAUNCH_CHECK();
     unsigned hb[2] = {0, 0};
     GBX_CUDA(cudaMemcpyAsync(hb, bad.p, 8, cudaMemcpyDeviceToHost, s));
     GBX_CUDA(cudaStreamSynchronize(s));
-    GBX_REQUIRE(hb[0] == 0, GBX_ERR_UNSUPPORTED,
-                "CSR layout rejected: %u vertices whose edges_idx is not the prefix sum of the "
-                "degrees (edges must be a source-sorted contiguous array)",
-                hb[0]);
+    GBX_REQUIRE(hb[0] == 0, GBX_ERR_INVALID, "offsets are not non-decreasing from 0 to num_edges");
     *max_deg = hb[1];
     return GBX_OK;
 }

@@ -42,6 +42,40 @@ __global__ void max_id_kernel(const uint32_t *s, const uint32_t *d, uint32_t n, 
     if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
+// out[0] = largest id, out[1] = largest id without the mask bits
+__global__ void id_range_kernel(const uint32_t *s, const uint32_t *d, uint32_t n, uint32_t *out) {
+    uint32_t m = 0, mm = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t a = s[i], b = d[i];
+        m = max(m, max(a, b));
+        mm = max(mm, max(a & kIdMask, b & kIdMask));
+    }
+    m = __reduce_max_sync(0xffffffffu, m);
+    mm = __reduce_max_sync(0xffffffffu, mm);
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(out, m);
+        atomicMax(out + 1, mm);
+    }
+}
+
+// Largest id of an edge list (device scalar read back), 0 for no edges.
+static int max_edge_id(const uint32_t *s, const uint32_t *d, uint32_t n, cudaStream_t st, uint32_t *full,
+                       uint32_t *masked) {
+    *full = *masked = 0;
+    if (!n) return GBX_OK;
+    DevBuf<uint32_t> r;
+    GBX_TRY(r.alloc(2, st));
+    GBX_CUDA(cudaMemsetAsync(r.p, 0, 8, st));
+    id_range_kernel<<<grid1d(n), 256, 0, st>>>(s, d, n, r.p);
+    GBX_LAUNCH_CHECK();
+    uint32_t h[2];
+    GBX_CUDA(cudaMemcpyAsync(h, r.p, 8, cudaMemcpyDeviceToHost, st));
+    GBX_CUDA(cudaStreamSynchronize(st));
+    *full = h[0];
+    *masked = h[1];
+    return GBX_OK;
+}
+
 __global__ void gather_u32_kernel(const uint32_t *in, const uint32_t *perm, uint32_t n, uint32_t *out) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         out[i] = in[perm[i]];
@@ -189,6 +223,25 @@ __global__ void permutation_check_kernel(const uint32_t *lab, uint32_t V, uint32
     }
 }
 
+// ---- mask mode (maskGraphProcess, reorder.c:1164-1475) --------------------
+// The vertex at position i of the bucket order takes the first region with
+// room left (reorder.c:1408-1436): HOT below e0, WARM below e1, LUKEWARM
+// below e2 (cumulative region ends), COLD after.
+__global__ void mask_hints_kernel(const uint32_t *sorted, uint32_t V, uint64_t e0, uint64_t e1, uint64_t e2,
+                                  uint32_t *mask) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < V; i += gridDim.x * blockDim.x)
+        mask[sorted[i]] = i < e0 ? 0xC0000000u : i < e1 ? 0x80000000u : i < e2 ? 0x40000000u : 0u;
+}
+
+// maskEdgeList (reorder.c:1639-1657): every id ORed with its vertex's hint
+__global__ void mask_edges_kernel(uint32_t *s, uint32_t *d, uint32_t n, const uint32_t *mask) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t a = s[i], b = d[i];
+        s[i] = a | mask[a];
+        d[i] = b | mask[b];
+    }
+}
+
 static int bits_for(uint32_t maxv) {
     int b = 0;
     while (b < 32 && (maxv >> b)) ++b;
@@ -220,28 +273,23 @@ extern "C" int gbx_csr_build(uint32_t num_edges, const uint32_t *src, const uint
     GBX_TRY(idst.bind(dst, E, s));
     GBX_TRY(iw.bind(w, E, s));
     const bool want_w = w_out != nullptr;
-    DevBuf<uint32_t> es, ed, perm, keys, maxid;
+    DevBuf<uint32_t> es, ed, perm, keys;
     DevBuf<float> ew;
     GBX_TRY(es.alloc(E2, s));
     GBX_TRY(ed.alloc(E2, s));
     GBX_TRY(perm.alloc(E2, s));
     GBX_TRY(keys.alloc(E2, s));
-    GBX_TRY(maxid.alloc(1, s));
     if (want_w) GBX_TRY(ew.alloc(E2, s));
     if (E) {
         stage_edges_kernel<<<grid1d(E), 256, 0, s>>>(isrc.d, idst.d, iw.d, E, symmetric, es.p, ed.p,
                                                      want_w ? ew.p : nullptr);
         GBX_LAUNCH_CHECK();
     }
-    GBX_CUDA(cudaMemsetAsync(maxid.p, 0, 4, s));
-    if (E2) {
-        max_id_kernel<<<grid1d(E2), 256, 0, s>>>(es.p, ed.p, E2, maxid.p);
-        GBX_LAUNCH_CHECK();
-    }
-    uint32_t hmax = 0;
-    GBX_CUDA(cudaMemcpyAsync(&hmax, maxid.p, 4, cudaMemcpyDeviceToHost, s));
-    GBX_CUDA(cudaStreamSynchronize(s));
-    GBX_REQUIRE(E2 == 0 || hmax < V, GBX_ERR_INVALID, "vertex id %u >= num_vertices %u", hmax, V);
+    // ids may carry the mask bits of mask mode: the vertex is the id without
+    // them, the sort key the whole id (the reference radix-sorts all 32 bits)
+    uint32_t hmax = 0, hmasked = 0;
+    GBX_TRY(max_edge_id(es.p, ed.p, E2, s, &hmax, &hmasked));
+    GBX_REQUIRE(E2 == 0 || hmasked < V, GBX_ERR_INVALID, "vertex id %u >= num_vertices %u", hmasked, V);
     const int bits = bits_for(hmax);
     // stable sort: destination pass(es) first, then source (LSD on the pair)
     iota_kernel<<<grid1d(E2), 256, 0, s>>>(perm.p, E2);
@@ -341,6 +389,9 @@ extern "C" int gbx_degree_reorder(uint32_t num_vertices, uint32_t num_edges, uin
     if (os.to_host() && E) GBX_CUDA(cudaMemcpyAsync(os.d, src, (size_t)E * 4, cudaMemcpyHostToDevice, s));
     if (od.to_host() && E) GBX_CUDA(cudaMemcpyAsync(od.d, dst, (size_t)E * 4, cudaMemcpyHostToDevice, s));
     if (ol.to_host()) GBX_CUDA(cudaMemcpyAsync(ol.d, labels, (size_t)V * 4, cudaMemcpyHostToDevice, s));
+    uint32_t id_max = 0, id_masked = 0;
+    GBX_TRY(max_edge_id(os.d, od.d, E, s, &id_max, &id_masked));
+    GBX_REQUIRE(E == 0 || id_max < V, GBX_ERR_INVALID, "vertex id %u >= num_vertices %u", id_max, V);
     DevBuf<uint32_t> deg, ids, newlab, mx;
     GBX_TRY(deg.alloc(V, s));
     GBX_TRY(ids.alloc(V, s));
@@ -458,6 +509,9 @@ extern "C" int gbx_relabel(uint32_t num_vertices, uint32_t num_edges, uint32_t *
     if (os.to_host() && E) GBX_CUDA(cudaMemcpyAsync(os.d, src, (size_t)E * 4, cudaMemcpyHostToDevice, s));
     if (od.to_host() && E) GBX_CUDA(cudaMemcpyAsync(od.d, dst, (size_t)E * 4, cudaMemcpyHostToDevice, s));
     if (ol.to_host()) GBX_CUDA(cudaMemcpyAsync(ol.d, labels, (size_t)V * 4, cudaMemcpyHostToDevice, s));
+    uint32_t id_max = 0, id_masked = 0;
+    GBX_TRY(max_edge_id(os.d, od.d, E, s, &id_max, &id_masked));
+    GBX_REQUIRE(E == 0 || id_max < V, GBX_ERR_INVALID, "vertex id %u >= num_vertices %u", id_max, V);
     if (E) {
         relabel_edges_kernel<<<grid1d(E), 256, 0, s>>>(os.d, od.d, E, nl.d);
         GBX_LAUNCH_CHECK();
@@ -468,6 +522,74 @@ extern "C" int gbx_relabel(uint32_t num_vertices, uint32_t num_edges, uint32_t *
     GBX_TRY(od.finish(s));
     GBX_TRY(ol.finish(s));
     GBX_TRY(oi.finish(s));
+    GBX_CUDA(cudaStreamSynchronize(s));
+    return GBX_OK;
+}
+
+extern "C" int gbx_mask_graph(uint32_t num_vertices, uint32_t num_edges, uint32_t *src, uint32_t *dst,
+                              int mmode, uint32_t cache_size, uint32_t *mask_array, void *stream) {
+    clear_error();
+    GBX_REQUIRE(num_vertices > 0, GBX_ERR_INVALID, "num_vertices must be > 0");
+    GBX_REQUIRE(num_edges == 0 || (src && dst), GBX_ERR_INVALID, "src/dst is NULL");
+    GBX_REQUIRE(mask_array, GBX_ERR_INVALID, "mask_array is NULL");
+    GBX_REQUIRE(mmode >= 1 && mmode <= 6, GBX_ERR_INVALID, "mmode must be 1-6");
+    GBX_TRY(ensure_device());
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t V = num_vertices, E = num_edges;
+    OutArray<uint32_t> os, od, om;
+    GBX_TRY(os.bind(src, E, s));
+    GBX_TRY(od.bind(dst, E, s));
+    GBX_TRY(om.bind(mask_array, V, s));
+    if (os.to_host() && E) GBX_CUDA(cudaMemcpyAsync(os.d, src, (size_t)E * 4, cudaMemcpyHostToDevice, s));
+    if (od.to_host() && E) GBX_CUDA(cudaMemcpyAsync(od.d, dst, (size_t)E * 4, cudaMemcpyHostToDevice, s));
+    uint32_t id_max = 0, id_masked = 0;
+    GBX_TRY(max_edge_id(os.d, od.d, E, s, &id_max, &id_masked));
+    GBX_REQUIRE(E == 0 || id_max < V, GBX_ERR_INVALID,
+                "vertex id %u >= num_vertices %u (ids must not carry mask bits yet)", id_max, V);
+    DevBuf<uint32_t> key, ids;
+    GBX_TRY(key.alloc(V, s));
+    GBX_TRY(ids.alloc(V, s));
+    GBX_CUDA(cudaMemsetAsync(key.p, 0, (size_t)V * 4, s));
+    // maskGraphProcessGenerateInOutDegrees (reorder.c:1260-1306): in-degrees
+    // for 2, 4, in + out for 5, 6, out-degrees otherwise
+    const int count_mode = (mmode == 2 || mmode == 4) ? 2 : (mmode == 5 || mmode == 6) ? 3 : 1;
+    if (E) {
+        degree_count_kernel<<<grid1d(E), 256, 0, s>>>(os.d, od.d, E, count_mode, key.p);
+        GBX_LAUNCH_CHECK();
+    }
+    // DBG's 11 buckets (reorder.c:1214-1228), highest first, ids ascending
+    BucketThresholds th{};
+    th.n = 11;
+    const uint32_t avg = E / V;
+    th.t[0] = avg <= 1 ? 1u : avg / 2;
+    for (uint32_t i = 1; i + 1 < th.n; ++i) th.t[i] = th.t[i - 1] * 2u;
+    th.t[th.n - 1] = 0xFFFFFFFFu;
+    bucket_key_kernel<<<grid1d(V), 256, 0, s>>>(key.p, V, th, key.p);
+    GBX_LAUNCH_CHECK();
+    iota_kernel<<<grid1d(V), 256, 0, s>>>(ids.p, V);
+    GBX_LAUNCH_CHECK();
+    GBX_TRY(radix_sort_pairs(key.p, ids.p, V, bits_for(th.n - 1), s));
+    // region sizes (reorder.c:1329-1345) with cs = cache_size / 4: V/4 each
+    // when V - cs < 2 cs, else cs*8, *4, *4 in uint32 as the reference
+    const uint32_t cs = cache_size >> 2;
+    uint32_t r0, r1, r2;
+    if ((int64_t)V - (int64_t)cs < 2 * (int64_t)cs) {
+        r0 = r1 = r2 = V / 4;
+    } else {
+        r0 = cs * 8u;
+        r1 = r0 * 4u;
+        r2 = r1 * 4u;
+    }
+    const uint64_t e0 = r0, e1 = e0 + r1, e2 = e1 + r2;
+    mask_hints_kernel<<<grid1d(V), 256, 0, s>>>(ids.p, V, e0, e1, e2, om.d);
+    GBX_LAUNCH_CHECK();
+    GBX_TRY(om.finish(s));
+    if ((mmode == 1 || mmode == 2) && E) {
+        mask_edges_kernel<<<grid1d(E), 256, 0, s>>>(os.d, od.d, E, om.d);
+        GBX_LAUNCH_CHECK();
+        GBX_TRY(os.finish(s));
+        GBX_TRY(od.finish(s));
+    }
     GBX_CUDA(cudaStreamSynchronize(s));
     return GBX_OK;
 }

@@ -61,6 +61,7 @@ class EdgeList:
     weight: Optional[np.ndarray] = None
     label_array: Optional[np.ndarray] = None
     inverse_label_array: Optional[np.ndarray] = None
+    mask_array: Optional[np.ndarray] = None
 
     @property
     def num_edges(self) -> int:
@@ -120,6 +121,7 @@ class GraphCSR:
     inverse_weight: Optional[np.ndarray] = None
     inverse_src: Optional[np.ndarray] = None
     max_weight: float = 0.0
+    mask_array: Optional[np.ndarray] = None
 
     @property
     def avg_degree(self) -> int:
@@ -189,6 +191,20 @@ def relabel(el: EdgeList, new_labels, stream=None) -> EdgeList:
     return el
 
 
+def mask_graph(el: EdgeList, mmode: int = 1, cache_size: int = 32768, stream=None) -> EdgeList:
+    """maskGraphProcess (the reference's -M, -C): el.mask_array gets the
+    hot/warm/lukewarm/cold hint of every vertex (top two id bits); mmode 1
+    and 2 also OR the hints into el.src / el.dst. Run after the last sort;
+    see gbx_mask_graph for the assignment."""
+    el.src = _u32(el.src)
+    el.dst = _u32(el.dst)
+    mask = np.zeros(el.num_vertices, np.uint32)
+    call("gbx_mask_graph", el.num_vertices, el.num_edges, _ptr(el.src), _ptr(el.dst), int(mmode),
+         int(cache_size), _ptr(mask), stream)
+    el.mask_array = mask
+    return el
+
+
 def read_label_file(path: str, num_vertices: int) -> np.ndarray:
     """The reference's label file (lmode 11, relabelEdgeListFromFile,
     reorder.c:1662-1700): one unsigned label per line, read up to
@@ -206,11 +222,13 @@ def relabel_from_file(el: EdgeList, path: str, stream=None) -> EdgeList:
 
 
 def graph_csr_preprocessing(el: EdgeList, *, sort: int = 0, dedup: bool = False, lmode: int = 0,
-                            directed: bool = True, keep_weights: bool = True, stream=None) -> GraphCSR:
+                            directed: bool = True, keep_weights: bool = True, mmode: int = 0,
+                            cache_size: int = 32768, stream=None) -> GraphCSR:
     """graphCSRPreProcessingStep (graphCSR.c:243-327) on the GPU: sort, dedup
-    (-k forces sort 1, GraphBlox.c:355-356), degree reorder + re-sort, CSR
-    map, and for directed graphs the inverse CSR built from the swapped
-    edges with the same sort."""
+    (-k forces sort 1, GraphBlox.c:355-356), degree reorder + re-sort, mask
+    mode (mmode, after the last sort, :285-286), CSR map, and for directed
+    graphs the inverse CSR built from the swapped edges with the same sort
+    (on the masked ids when mmode is 1 or 2)."""
     if dedup:
         sort = 1
     V = el.num_vertices
@@ -223,7 +241,12 @@ def graph_csr_preprocessing(el: EdgeList, *, sort: int = 0, dedup: bool = False,
         degree_reorder(tmp, lmode, stream)
         labels, inv_labels = tmp.label_array, tmp.inverse_label_array
         deg, idx, s, d, ww = csr_build(tmp.src, tmp.dst, ww, num_vertices=V, sort=sort, stream=stream)
-    g = GraphCSR(V, int(s.shape[0]), deg, idx, d, s, ww, labels, inv_labels)
+    mask = None
+    if mmode:
+        # the map strips the mask bits, so deg / idx of the sorted list stand
+        m = mask_graph(EdgeList(V, s, d), mmode, cache_size, stream)
+        s, d, mask = m.src, m.dst, m.mask_array
+    g = GraphCSR(V, int(s.shape[0]), deg, idx, d, s, ww, labels, inv_labels, mask_array=mask)
     # max over the weights as read (edgeList.c:673-684), kept through dedup
     if el.weight is not None and el.num_edges:
         g.max_weight = float(max(0.0, float(np.max(el.weight))))

@@ -41,6 +41,8 @@
  *                                (:275-380), DBG (:387-572), HUBSort (:762-982), HUBCluster (:984-1170),
  *                                Corder (:574-624), degrees (:1483-1552), relabel (:1618-1637)
  *   gbx_relabel               -> relabelEdgeListFromFile's relabelling (01_host/src/preprocess/reorder.c:1662-1714)
+ *   gbx_mask_graph            -> maskGraphProcess (01_host/src/preprocess/reorder.c:1164-1475) and
+ *                                maskEdgeList (:1639-1657), the -M mask mode
  * Extension entry points (batched, multi-source, personalised PageRank and
  * its adjoint, generators) have no reference counterpart.
  */
@@ -80,10 +82,12 @@ typedef struct gbx_graph gbx_graph;
 /* Copy a CSR in the reference's layout to the device.
  *   edges_idx[v], out_degree[v]: first edge position and degree of v (the
  *     reference's struct Vertex, vertex.h:17-23; edges_idx is 0 for
- *     degree-0 vertices). The edges of v must be the contiguous run
- *     dest[edges_idx[v] .. +out_degree[v]) of a source-sorted edge array,
- *     which is what the reference's CSR build produces; other layouts are
- *     rejected with GBX_ERR_UNSUPPORTED.
+ *     degree-0 vertices). The edges of v are the run dest[edges_idx[v] ..
+ *     +out_degree[v]). Runs in vertex order (the reference's CSR build) are
+ *     copied as they are; runs in any other order (the inverse CSR of a
+ *     masked edge list, sorted on the masked ids) are gathered into vertex
+ *     order on the device, keeping the order inside each run. A run that
+ *     ends past num_edges is GBX_ERR_INVALID.
  *   dest[E], weight[E] (weight may be NULL).
  *   in_*: the inverse CSR (in-edges; the reference's DIRECTED 1 build), or
  *     all NULL. Pull-direction kernels use it when present, else they pull
@@ -295,7 +299,10 @@ int gbx_spmv(gbx_graph *g, const float *values, float default_value, const float
  * by source (sort_mode 0) or by (source,destination) (sort_mode 1), then
  * optional removal of self loops and adjacent duplicates (dedup; requires
  * sort_mode 1, keeps the first weight truncated through uint32 as the
- * reference does). num_vertices = max id + 1 over the input.
+ * reference does). num_vertices = max id + 1 over the input. Ids may carry
+ * the mask bits of gbx_mask_graph (top two bits): the vertex is the id
+ * without them and the sort key the whole id, as in the reference's radix
+ * sort, so the runs of such a CSR are not in vertex order.
  * Outputs (caller-allocated; capacity = 2*num_edges when symmetric):
  * out_degree[V], edges_idx[V], src_out[E'], dst_out[E'], w_out[E'] (may be
  * NULL), *num_edges_out = E'. */
@@ -332,6 +339,20 @@ int gbx_degree_reorder(uint32_t num_vertices, uint32_t num_edges, uint32_t *src,
  * gbx_degree_reorder. */
 int gbx_relabel(uint32_t num_vertices, uint32_t num_edges, uint32_t *src, uint32_t *dst,
                 const uint32_t *new_labels, uint32_t *labels, uint32_t *inverse_labels, void *stream);
+/* Mask mode (the reference's -M, run after the last sort): hot/cold hints
+ * 0xC0000000 HOT, 0x80000000 WARM, 0x40000000 LUKEWARM, 0 COLD per vertex
+ * into mask_array[V]. Degrees: in-degree for mmode 2, 4, in + out for 5, 6,
+ * out-degree for 1, 3. Vertices in DBG order (11 buckets, t0 = avg <= 1 ?
+ * 1 : avg/2, highest bucket first, ids ascending) fill the regions in turn;
+ * with cs = cache_size / 4 (the reference's -C, default 32768) the regions
+ * are V/4 HOT, V/4 WARM, V/4 LUKEWARM when V - cs < 2 cs, else cs*8, cs*32,
+ * cs*128 (uint32 products); the rest are COLD. This is the reference's
+ * assignment run by one thread (with several, its threads take the regions
+ * concurrently and the hints depend on the schedule). mmode 1, 2 also OR the
+ * hints into src/dst in place (every kernel of this library clears them);
+ * 3-6 leave the edges unchanged. Ids must be below num_vertices on entry. */
+int gbx_mask_graph(uint32_t num_vertices, uint32_t num_edges, uint32_t *src, uint32_t *dst,
+                   int mmode, uint32_t cache_size, uint32_t *mask_array, void *stream);
 
 /* ---- synthetic inputs (no reference counterpart) ------------------------ */
 /* R-MAT edge list: 2^scale vertices, num_edges edges, quadrant

@@ -44,8 +44,28 @@ static void counting_pass(uint32_t n, const uint32_t *key, uint32_t nkeys,
     free(cnt);
 }
 
+/* A stable sort of perm_in by key[] into perm_out: one counting pass for
+ * keys below 2^24, else two 16-bit digit passes (ids that carry the mask
+ * bits of mask mode reach 2^32 - 1). */
+static void stable_key_sort(uint32_t n, const uint32_t *key, uint32_t maxkey,
+                            uint32_t *perm_in, uint32_t *perm_out) {
+    if (maxkey < (1u << 24)) {
+        counting_pass(n, key, maxkey + 1, perm_in, perm_out);
+        return;
+    }
+    uint32_t *digit = (uint32_t *)calloc((size_t)n + 1, 4);
+    if (!digit) abort();
+    for (uint32_t i = 0; i < n; ++i) digit[i] = key[i] & 0xFFFFu;
+    counting_pass(n, digit, 1u << 16, perm_in, perm_out);
+    for (uint32_t i = 0; i < n; ++i) digit[i] = key[i] >> 16;
+    counting_pass(n, digit, 1u << 16, perm_out, perm_in);
+    memcpy(perm_out, perm_in, (size_t)n * 4);
+    free(digit);
+}
+
 /* radixSortEdgesBySource / ...BySourceAndDestination (radixsort.c:231-339):
- * LSD order -- destination pass first, then a stable source pass. */
+ * LSD order -- destination pass first, then a stable source pass, on the
+ * full 32-bit ids. */
 void orc_sort_edges(uint32_t num_edges, uint32_t *src, uint32_t *dst, float *w,
                     int sort_mode, int num_threads) {
     (void)num_threads;
@@ -55,16 +75,15 @@ void orc_sort_edges(uint32_t num_edges, uint32_t *src, uint32_t *dst, float *w,
         if (src[i] > maxid) maxid = src[i];
         if (dst[i] > maxid) maxid = dst[i];
     }
-    uint32_t nkeys = maxid + 1;
     uint32_t *p0 = (uint32_t *)xmalloc((size_t)num_edges * 4);
     uint32_t *p1 = (uint32_t *)xmalloc((size_t)num_edges * 4);
     for (uint32_t i = 0; i < num_edges; ++i) p0[i] = i;
     uint32_t *cur = p0, *nxt = p1;
     if (sort_mode == 1 || sort_mode == 3) {
-        counting_pass(num_edges, dst, nkeys, cur, nxt);
+        stable_key_sort(num_edges, dst, maxid, cur, nxt);
         uint32_t *t = cur; cur = nxt; nxt = t;
     }
-    counting_pass(num_edges, src, nkeys, cur, nxt);
+    stable_key_sort(num_edges, src, maxid, cur, nxt);
     cur = nxt;
     uint32_t *ts = (uint32_t *)xmalloc((size_t)num_edges * 4);
     for (uint32_t i = 0; i < num_edges; ++i) ts[i] = src[cur[i]];
@@ -226,6 +245,70 @@ void orc_degree_reorder(uint32_t num_vertices, uint32_t num_edges, uint32_t *src
         inverse_labels[labels[v]] = v;
     }
     free(newlab);
+    free(deg);
+}
+
+/* maskGraphProcess (reorder.c:1164-1475) run by one thread.
+ *
+ * Degrees (maskGraphProcessGenerateInOutDegrees, :1260-1306): mmode 2, 4
+ * count in-degrees, 5, 6 in + out, every other mode out-degrees. Buckets as
+ * DBG: 11 thresholds t0 = avg <= 1 ? 1 : avg/2 (avg = E/V, uint32),
+ * doubling, last UINT32_MAX. Regions (:1329-1345), cs = cache_size / 4:
+ * V/4 HOT, V/4 WARM, V/4 LUKEWARM when V - cs < 2 cs, else cs*8 HOT, cs*32
+ * WARM, cs*128 LUKEWARM (uint32 products); the rest COLD. Vertices take the
+ * regions in order, buckets from the highest and ascending ids inside a
+ * bucket (:1408-1436). With more than one thread the reference's regions
+ * are taken by the threads concurrently, so which vertex gets which hint
+ * then depends on the schedule; the one-thread order is the one restated.
+ * mmode 1, 2 then OR the hints into the edge list's ids (maskEdgeList,
+ * :1639-1657); every mode returns the hints per vertex. */
+void orc_mask_graph(uint32_t num_vertices, uint32_t num_edges, uint32_t *src, uint32_t *dst,
+                    int mmode, uint32_t cache_size, uint32_t *mask) {
+    const uint32_t n = num_vertices;
+    uint32_t *deg = (uint32_t *)calloc((size_t)n + 1, 4);
+    if (!deg) abort();
+    for (uint32_t i = 0; i < num_edges; ++i) {
+        if (mmode == 2 || mmode == 4) deg[dst[i]]++;
+        else if (mmode == 5 || mmode == 6) { deg[dst[i]]++; deg[src[i]]++; }
+        else deg[src[i]]++;
+    }
+    uint32_t th[11];
+    const uint32_t avg = n ? num_edges / n : 0;
+    th[0] = avg <= 1 ? 1u : avg / 2;
+    for (int i = 1; i < 10; ++i) th[i] = th[i - 1] * 2u;
+    th[10] = 0xFFFFFFFFu;
+    uint8_t *bk = (uint8_t *)xmalloc((size_t)n + 1);
+    for (uint32_t v = 0; v < n; ++v) {
+        uint32_t i = 0;
+        while (deg[v] > th[i]) ++i;
+        bk[v] = (uint8_t)i;
+    }
+    const uint32_t cs = cache_size >> 2;
+    uint32_t region[3];
+    if ((int64_t)n - (int64_t)cs < 2 * (int64_t)cs) {
+        region[0] = region[1] = region[2] = n / 4;
+    } else {
+        region[0] = cs * 8u;
+        region[1] = region[0] * 4u;
+        region[2] = region[1] * 4u;
+    }
+    static const uint32_t hint[4] = {0xC0000000u, 0x80000000u, 0x40000000u, 0u};
+    for (int j = 10; j >= 0; --j) {
+        for (uint32_t v = 0; v < n; ++v) {
+            if (bk[v] != j) continue;
+            int r = 0;
+            while (r < 3 && region[r] == 0) ++r;
+            if (r < 3) region[r]--;
+            mask[v] = hint[r];
+        }
+    }
+    if (mmode == 1 || mmode == 2) {
+        for (uint32_t i = 0; i < num_edges; ++i) {
+            src[i] |= mask[src[i]];
+            dst[i] |= mask[dst[i]];
+        }
+    }
+    free(bk);
     free(deg);
 }
 

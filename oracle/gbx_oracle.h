@@ -49,6 +49,10 @@ void orc_map_vertices(uint32_t num_vertices, uint32_t num_edges, const uint32_t 
 void orc_degree_reorder(uint32_t num_vertices, uint32_t num_edges, uint32_t *src, uint32_t *dst,
                         int lmode, uint32_t *labels, uint32_t *inverse_labels, int num_threads);
 
+/* ---- mask mode (maskGraphProcess, reorder.c:1164-1475) ------------------ */
+void orc_mask_graph(uint32_t num_vertices, uint32_t num_edges, uint32_t *src, uint32_t *dst,
+                    int mmode, uint32_t cache_size, uint32_t *mask);
+
 /* ---- BFS (BFS.c:42-78, :335-613) -------------------------------------- */
 /* Direction-optimising BFS (alpha 15, beta 18). distances: level, 0 for
  * the source and for unreached vertices; parents: -out_degree (or -1) for

@@ -38,6 +38,7 @@ def load():
             "orc_dedup_edges": (u32, [u32, vp, vp, vp]),
             "orc_map_vertices": (None, [u32, u32, vp, vp, vp]),
             "orc_degree_reorder": (None, [u32, u32, vp, vp, C.c_int, vp, vp, C.c_int]),
+            "orc_mask_graph": (None, [u32, u32, vp, vp, C.c_int, u32, vp]),
             "orc_bfs": (None, [u32, u32, vp, vp, vp, vp, vp, vp, u32, vp, vp, vp, vp, C.c_int]),
             "orc_pagerank_pull": (None, [u32, vp, vp, vp, vp, u32, C.c_double, vp, vp, vp, C.c_int]),
             "orc_pagerank_pull_f64": (None, [u32, vp, vp, vp, vp, u32, C.c_double, vp, vp, C.c_int]),
@@ -106,6 +107,15 @@ def degree_reorder(num_vertices, src, dst, lmode=1, labels=None, inverse_labels=
     inv = np.arange(num_vertices, dtype=np.uint32) if inverse_labels is None else _u32(inverse_labels).copy()
     load().orc_degree_reorder(num_vertices, s.shape[0], _p(s), _p(d), lmode, _p(lab), _p(inv), threads)
     return s, d, lab, inv
+
+
+def mask_graph(num_vertices, src, dst, mmode=1, cache_size=32768):
+    """Mask mode: returns (src, dst, mask); src/dst carry the hints for mmode 1, 2."""
+    s = _u32(src).copy()
+    d = _u32(dst).copy()
+    m = np.zeros(num_vertices, np.uint32)
+    load().orc_mask_graph(num_vertices, s.shape[0], _p(s), _p(d), int(mmode), int(cache_size), _p(m))
+    return s, d, m
 
 
 def bfs(g: HostCSR, source, pull: Optional[HostCSR] = None, threads=0):

@@ -79,6 +79,8 @@ int main(int argc, char **argv) {
         else if (f == "-b") a->delta = (uint32_t)std::atoi(next());
         else if (f == "-n") threads = std::atoi(next());
         else if (f == "-W") write_csr = true;
+        else if (f == "-M") a->mmode = (uint32_t)std::atoi(next());
+        else if (f == "-C") a->cache_size = (uint32_t)std::strtoul(next(), nullptr, 10);
         else { std::fprintf(stderr, "unknown flag %s\n", f.c_str()); return 2; }
     }
     a->pre_numThreads = threads;
@@ -105,6 +107,9 @@ int main(int argc, char **argv) {
     dump(out, "src.u32", g->sorted_edges_array->edges_array_src, E * 4ull);
     dump(out, "label.u32", g->sorted_edges_array->label_array, V * 4ull);
     dump(out, "inverse_label.u32", g->sorted_edges_array->inverse_label_array, V * 4ull);
+    // hot/warm/lukewarm/cold hints of mask mode (maskGraphProcess, reorder.c:1164-1475)
+    if (a->mmode && g->sorted_edges_array->mask_array)
+        dump(out, "mask.u32", g->sorted_edges_array->mask_array, V * 4ull);
 #if WEIGHTED
     dump(out, "weight.f32", g->sorted_edges_array->edges_array_weight, E * 4ull);
 #endif

@@ -10,8 +10,10 @@ if str(ROOT) not in sys.path:
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 # one fixture per test graph; reorder_modes.npz holds the labels of the
-# reorder modes for all of them, csr_files.npz the reference's .csr files
-GOLDEN_GRAPHS = sorted(p.stem for p in GOLDEN.glob("*.npz") if p.stem not in ("reorder_modes", "csr_files"))
+# reorder modes for all of them, csr_files.npz the reference's .csr files,
+# mask_modes.npz its mask mode
+GOLDEN_GRAPHS = sorted(p.stem for p in GOLDEN.glob("*.npz")
+                       if p.stem not in ("reorder_modes", "csr_files", "mask_modes"))
 REORDER_MODES = [2, 3, 4, 5, 6, 7, 8, 9, 12, 13]
 
 
@@ -26,6 +28,11 @@ def load_reorder_modes() -> dict:
 
 def load_csr_files() -> dict:
     with np.load(GOLDEN / "csr_files.npz") as z:
+        return {k: z[k] for k in z.files}
+
+
+def load_mask_modes() -> dict:
+    with np.load(GOLDEN / "mask_modes.npz") as z:
         return {k: z[k] for k in z.files}
 
 

@@ -12,9 +12,10 @@ its build (oracle/build_ref.sh). For every test graph the reference ships in
 The GPU host has no reference tree, so the parity tests read only these
 fixtures there.
 
-Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [reorder|csr]
+Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [reorder|csr|mask]
 ("reorder" writes only reorder_modes.npz, the labels of the reorder modes;
-"csr" writes only csr_files.npz, the reference's .csr files.)
+"csr" writes only csr_files.npz, the reference's .csr files; "mask" writes
+only mask_modes.npz, the reference's mask mode.)
 """
 from __future__ import annotations
 
@@ -158,12 +159,58 @@ def csr_files(ref_root: str) -> None:
     print(f"wrote {out.name}")
 
 
+MASK_MODES = [1, 2, 3, 4, 5, 6]
+MASK_CACHE_SIZES = [32768, 256]
+MASK_CSR_GRAPHS = ["v51_e1021", "v300_e2730", "test"]
+
+
+def mask_modes(ref_root: str) -> None:
+    """tests/golden/mask_modes.npz: the reference's mask mode (-M, -C) run
+    with one thread (its hint assignment is schedule-dependent with more).
+    Keys: <graph>_<variant>_m<mode>_c<cache_size> = hint per vertex (id >>
+    30, uint8) for every test graph, build variant (u, dw), mode 1-6 and two
+    cache sizes (the default, whose regions are V/4 on these graphs, and 256,
+    whose regions are cs*8, *4, *4 on the larger ones); <graph>_<variant>_m<mode>_csr
+    = the .csr file the reference writes for modes 1, 2 (ids carry the hints;
+    the DIRECTED build's inverse CSR is sorted on them) on three graphs; and
+    <graph>_dw_m1_bfs1 / _pr20 = BFS levels from vertex 1 and 20 PageRank
+    iterations on the masked dw graph."""
+    test_dir = Path(ref_root) / "03_data" / "TEST"
+    fx: dict[str, np.ndarray] = {}
+    for name in GRAPHS:
+        gdir = test_dir / name
+        weighted = (gdir / "graph.wbin").exists() and not (gdir / "graph.bin").exists()
+        f = gdir / ("graph.wbin" if weighted else "graph.bin")
+        wflag = ["-w"] if weighted else []
+        for variant, flags in (("u", ["-s", "-k"]), ("dw", [])):
+            exe = "u" if variant == "u" else "dw"
+            fl = ["-o", "1", *wflag, *flags]
+            for m in MASK_MODES:
+                for cs in MASK_CACHE_SIZES:
+                    out = po.ref_run(f, exe, -1, [*fl, "-M", str(m), "-C", str(cs)], threads=1)
+                    fx[f"{name}_{variant}_m{m}_c{cs}"] = (out["mask"] >> 30).astype(np.uint8)
+                if m in (1, 2) and name in MASK_CSR_GRAPHS:
+                    out = po.ref_run(f, exe, -1, [*fl, "-M", str(m), "-W"], threads=1)
+                    fx[f"{name}_{variant}_m{m}_csr"] = out["graph"]
+        if name in MASK_CSR_GRAPHS:
+            fl = ["-o", "1", *wflag, "-M", "1"]
+            out = po.ref_run(f, "dw", 0, [*fl, "-p", "2", "-r", "1"], threads=1)
+            fx[f"{name}_dw_m1_bfs1"] = out["bfs_distances"]
+            out = po.ref_run(f, "dw", 1, [*fl, "-i", "20", "-e", "0"], threads=1)
+            fx[f"{name}_dw_m1_pr20"] = out["pr_ranks"]
+    out = Path(__file__).resolve().parent / "mask_modes.npz"
+    np.savez_compressed(out, **fx)
+    print(f"wrote {out.name}")
+
+
 if __name__ == "__main__":
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     if len(sys.argv) > 2 and sys.argv[2] == "reorder":
         reorder_modes(root)
     elif len(sys.argv) > 2 and sys.argv[2] == "csr":
         csr_files(root)
+    elif len(sys.argv) > 2 and sys.argv[2] == "mask":
+        mask_modes(root)
     else:
         main(root)
         reorder_modes(root)

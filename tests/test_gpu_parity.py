@@ -236,14 +236,54 @@ def test_edge_cases(gbx, cuda_device):
         np.testing.assert_array_equal(comp, po.cc(host, 2))
 
 
-def test_layout_rejected(gbx, cuda_device):
-    # edges_idx that is not the prefix sum of the degrees
-    g = gbx.GraphCSR(3, 2, np.array([1, 1, 0], np.uint32), np.array([1, 0, 0], np.uint32),
-                     np.array([1, 2], np.uint32), np.array([0, 1], np.uint32), None,
+def _runs_reversed(deg, idx, ids, w):
+    """The same CSR with every vertex's run stored in reverse vertex order
+    (edges_idx no longer the prefix sum of the degrees)."""
+    V = deg.shape[0]
+    new_idx = np.zeros(V, np.uint32)
+    parts, wparts, at = [], [], 0
+    for v in range(V - 1, -1, -1):
+        n = int(deg[v])
+        if n:
+            new_idx[v] = at
+            parts.append(ids[idx[v]: idx[v] + n])
+            if w is not None:
+                wparts.append(w[idx[v]: idx[v] + n])
+            at += n
+    cat = np.concatenate(parts).astype(np.uint32)
+    return new_idx, cat, (None if w is None else np.concatenate(wparts).astype(np.float32))
+
+
+def test_layout_runs_out_of_vertex_order(gbx, cuda_device):
+    g = _rmat_graph(gbx, 12, 8, 9, weights="int")
+    host, pull = host_views(g)
+    V = g.num_vertices
+    fidx, fdest, fw = _runs_reversed(g.out_degree, g.edges_idx, g.dest, g.weight)
+    iidx, idest, iw = _runs_reversed(g.inverse_out_degree, g.inverse_edges_idx, g.inverse_dest,
+                                     g.inverse_weight)
+    assert np.any(np.diff(fidx[g.out_degree > 0].astype(np.int64)) < 0)
+    g2 = gbx.GraphCSR(V, g.num_edges, g.out_degree, fidx, fdest, g.src, fw, g.label_array,
+                      g.inverse_label_array, g.inverse_out_degree, iidx, idest, iw)
+    with gbx.DeviceGraph.from_graph_csr(g2) as dg:
+        for r in (0, 5):
+            d, _, proc, it = po.bfs(host, r, pull)
+            st = gbx.breadth_first_search(dg, r)
+            np.testing.assert_array_equal(st.distances, d)
+            assert (st.processed_nodes, st.iteration) == (proc, it)
+        np.testing.assert_array_equal(gbx.sssp(dg, 0, 64).distances, po.sssp(host, 0, 64))
+        pr = gbx.page_rank(dg, 20, 0.0)
+        ref64, _, _ = po.pagerank(host, 20, 0.0, pull, fp64=True)
+        assert po.fp32_close(np.asarray(pr.pageRanks), ref64, REL_L1_TOL)[0]
+
+
+def test_layout_run_past_edges_rejected(gbx, cuda_device):
+    # vertex 0's run starts at 1 and holds two edges: it ends past E = 2
+    g = gbx.GraphCSR(3, 2, np.array([2, 0, 0], np.uint32), np.array([1, 0, 0], np.uint32),
+                     np.array([1, 2], np.uint32), np.array([0, 0], np.uint32), None,
                      np.arange(3, dtype=np.uint32), np.arange(3, dtype=np.uint32))
     with pytest.raises(gbx.GbxError) as e:
         gbx.DeviceGraph.from_graph_csr(g)
-    assert e.value.status == -6
+    assert e.value.status == -1
 
 
 def test_device_resident_outputs(gbx, cuda_device):
