@@ -6,7 +6,10 @@ graph-load and algorithm interfaces; see graph.py.
 """
 from ._lib import GbxError, load  # noqa: F401
 from .graph import (  # noqa: F401
+    BellmanFordStats,
+    BetweennessCentralityStats,
     BFSStats,
+    DFSStats,
     DeviceGraph,
     EdgeList,
     GraphBatch,
@@ -16,12 +19,16 @@ from .graph import (  # noqa: F401
     PPRAdjointStats,
     PPRStats,
     SSSPStats,
+    bellman_ford,
+    betweenness_centrality,
     bfs_multisource,
     breadth_first_search,
     connected_components,
     csr_build,
     degree_reorder,
+    depth_first_search,
     read_label_file,
+    reference_roots,
     relabel,
     relabel_from_file,
     generate_chung_lu,

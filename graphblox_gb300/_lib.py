@@ -37,6 +37,10 @@ class SsspResult(C.Structure):
     _fields_ = [("reached", u32), ("rounds", u32), ("edges_relaxed", u64), ("edges_traversed", u64)]
 
 
+class BcResult(C.Structure):
+    _fields_ = [("iteration", u32), ("processed_nodes", u32), ("levels", u32)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "gbx_status_string": (C.c_char_p, [C.c_int]),
@@ -66,6 +70,10 @@ SIGNATURES = {
     "gbx_ppr_adjoint": (C.c_int, [vp, u32, vp, vp, vp, C.c_double, C.c_double, u32, vp, vp,
                                   C.POINTER(PprResult), vp]),
     "gbx_sssp": (C.c_int, [vp, u32, u32, vp, C.POINTER(SsspResult), vp]),
+    "gbx_bellman_ford": (C.c_int, [vp, u32, vp, vp, C.POINTER(SsspResult), vp]),
+    "gbx_dfs": (C.c_int, [vp, u32, vp, vp, C.POINTER(u32), vp]),
+    "gbx_betweenness": (C.c_int, [vp, u32, vp, vp, vp, vp, vp, C.POINTER(BcResult), vp]),
+    "gbx_reference_roots": (C.c_int, [vp, u32, u32, vp]),
     "gbx_cc": (C.c_int, [vp, C.c_int, vp, C.POINTER(u32), vp]),
     "gbx_tc": (C.c_int, [vp, C.POINTER(u64), vp]),
     "gbx_spmv": (C.c_int, [vp, vp, C.c_float, vp, vp, u32, vp]),

@@ -1,0 +1,552 @@
+// Betweenness centrality (Brandes), Bellman-Ford and the stack DFS of the
+// reference host (betweennessCentrality.c, bellmanFord.c, DFS.c).
+//
+// Brandes needs, from a vertex v, the vertices w whose pull row holds v
+// (its successors in the shortest-path DAG), in ascending id order: the
+// reference folds the dependency contributions into v from the top of its
+// stack down, i.e. in descending (level, id) order of w, and float addition
+// is not associative. That successor CSR is the forward CSR when the graph
+// has an inverse and its rows are sorted, otherwise the transpose of the
+// pull CSR built here once per graph by a stable sort on the neighbour id.
+#include "gbx_internal.cuh"
+
+#include <cstring>
+#include <vector>
+
+struct gbx_bc_cache {
+    uint32_t *succ_off = nullptr;  // V+1, owned when built here
+    uint32_t *succ_ids = nullptr;  // E
+    bool owned = false;
+};
+
+void gbx_free_bc_cache(struct gbx_bc_cache *c) {
+    if (!c) return;
+    if (c->owned) {
+        cudaFree(c->succ_off);
+        cudaFree(c->succ_ids);
+    }
+    delete c;
+}
+
+namespace gbx {
+
+static unsigned grid_sm(uint64_t n, int threads = 256) {
+    const uint64_t b = (n + threads - 1) / threads;
+    const uint64_t cap = (uint64_t)num_sms() * 8;
+    return (unsigned)(b == 0 ? 1 : (b > cap ? cap : b));
+}
+
+// flag[0] = 1 when some row of (off, ids) is not ascending
+__global__ void rows_sorted_kernel(const uint32_t *off, const uint32_t *ids, uint32_t V, unsigned *flag) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < V; v += warps) {
+        const uint32_t b = off[v], e = off[v + 1];
+        bool bad = false;
+        for (uint32_t j = b + 1 + lane; j < e; j += 32)
+            bad |= (ids[j - 1] & kIdMask) > (ids[j] & kIdMask);
+        if (__any_sync(0xffffffffu, bad)) {
+            if (lane == 0) atomicOr(flag, 1u);
+        }
+    }
+}
+
+// keys[j] = neighbour id of entry j, vals[j] = the vertex whose row holds j
+// (rows are in vertex order, so a stable sort on keys keeps vals ascending)
+__global__ void transpose_pairs_kernel(const uint32_t *off, const uint32_t *ids, uint32_t V, uint32_t E,
+                                       uint32_t *keys, uint32_t *vals) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < E; j += gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = V;  // last v with off[v] <= j
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (off[mid] <= j) lo = mid; else hi = mid;
+        }
+        keys[j] = ids[j] & kIdMask;
+        vals[j] = lo;
+    }
+}
+
+// run starts of a sorted key array -> per-key counts (deg[k] = run length)
+__global__ void run_lengths_kernel(const uint32_t *keys, uint32_t E, uint32_t *deg) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < E; i += gridDim.x * blockDim.x) {
+        const uint32_t k = keys[i];
+        if (i + 1 == E || keys[i + 1] != k) {
+            // the run of k ends here; find its start by the previous key's end
+            uint32_t lo = 0, hi = i;  // first index with keys[idx] == k
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (keys[mid] < k) lo = mid + 1; else hi = mid;
+            }
+            deg[k] = i + 1 - lo;
+        }
+    }
+}
+
+// transpose of the pull CSR into toff (V+1) / tids (E + 4 zeroed ids)
+static int build_transpose(const gbx_graph *g, uint32_t *toff, uint32_t *tids, cudaStream_t s) {
+    const uint32_t V = g->V, E = g->E;
+    DevBuf<uint32_t> keys, deg, tot;
+    GBX_TRY(keys.alloc(E ? E : 1, s));
+    GBX_TRY(deg.alloc(V, s));
+    GBX_TRY(tot.alloc(1, s));
+    GBX_CUDA(cudaMemsetAsync(deg.p, 0, (size_t)V * 4, s));
+    GBX_CUDA(cudaMemsetAsync(tids + E, 0, 16, s));
+    if (E) {
+        transpose_pairs_kernel<<<grid_sm(E), 256, 0, s>>>(g->pull_offsets(), g->pull_src(), V, E, keys.p, tids);
+        GBX_LAUNCH_CHECK();
+        int bits = 0;
+        while (bits < 32 && ((V - 1) >> bits)) ++bits;
+        GBX_TRY(radix_sort_pairs(keys.p, tids, E, bits, s));
+        run_lengths_kernel<<<grid_sm(E), 256, 0, s>>>(keys.p, E, deg.p);
+        GBX_LAUNCH_CHECK();
+    }
+    GBX_TRY(exclusive_scan_u32(deg.p, toff, V, s, tot.p));
+    GBX_CUDA(cudaMemcpyAsync(toff + V, tot.p, 4, cudaMemcpyDeviceToDevice, s));
+    GBX_CUDA(cudaStreamSynchronize(s));
+    return GBX_OK;
+}
+
+static int bc_successors(gbx_graph *g, cudaStream_t s, const uint32_t **off, const uint32_t **ids) {
+    if (!g->bc_cache) {
+        const uint32_t V = g->V, E = g->E;
+        bool use_forward = false;
+        if (g->has_inverse()) {
+            DevBuf<unsigned> flag;
+            GBX_TRY(flag.alloc(1, s));
+            GBX_CUDA(cudaMemsetAsync(flag.p, 0, 4, s));
+            rows_sorted_kernel<<<grid_sm((uint64_t)V * 32), 256, 0, s>>>(g->offsets, g->dest, V, flag.p);
+            GBX_LAUNCH_CHECK();
+            unsigned h = 0;
+            GBX_CUDA(cudaMemcpyAsync(&h, flag.p, 4, cudaMemcpyDeviceToHost, s));
+            GBX_CUDA(cudaStreamSynchronize(s));
+            use_forward = h == 0;
+        }
+        gbx_bc_cache *c = new gbx_bc_cache();
+        if (use_forward) {
+            c->succ_off = g->offsets;
+            c->succ_ids = g->dest;
+        } else {
+            uint32_t *toff = nullptr, *tids = nullptr;
+            int st = GBX_OK;
+            if (cudaMalloc(&toff, ((size_t)V + 1) * 4) != cudaSuccess ||
+                cudaMalloc(&tids, ((size_t)E + 4) * 4) != cudaSuccess) {
+                (void)cudaGetLastError();
+                set_error("device allocation of the successor CSR failed");
+                st = GBX_ERR_NOMEM;
+            }
+            if (st == GBX_OK) st = build_transpose(g, toff, tids, s);
+            if (st != GBX_OK) {
+                cudaStreamSynchronize(s);
+                cudaFree(toff);
+                cudaFree(tids);
+                delete c;
+                return st;
+            }
+            c->succ_off = toff;
+            c->succ_ids = tids;
+            c->owned = true;
+        }
+        g->bc_cache = c;
+    }
+    *off = g->bc_cache->succ_off;
+    *ids = g->bc_cache->succ_ids;
+    return GBX_OK;
+}
+
+}  // namespace gbx
+
+// ---- betweenness centrality --------------------------------------------------
+namespace gbx {
+
+__global__ void bc_root_kernel(uint32_t root, uint32_t *dist, int32_t *sigma, uint32_t *stack) {
+    dist[root] = 0;
+    sigma[root] = 1;
+    stack[0] = root;
+}
+
+// One level of the forward sweep, pushed over the successor CSR from the
+// level-L vertices level[0..n): a successor v not reached yet is claimed for
+// level L+1 (its claimer appends it to next[]), and every successor at level
+// L+1 adds sigma[u] -- the reference's sigma[v] += sigma[u] over the
+// frontier entries of v's pull row (betweennessCentrality.c:322-336); int
+// addition wraps and is associative, so the order does not matter.
+// counts[0] = size of the next level, counts[1] += those entries.
+__global__ void bc_forward_kernel(const uint32_t *off, const uint32_t *ids, const uint32_t *level, uint32_t n,
+                                  uint32_t L, uint32_t *dist, int32_t *sigma, uint32_t *next,
+                                  unsigned *counts) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    unsigned entries = 0;
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+        const uint32_t u = level[i];
+        const unsigned su = (unsigned)sigma[u];
+        const uint32_t b = off[u], e = off[u + 1];
+        for (uint32_t base = b; base < e; base += 32) {
+            const uint32_t j = base + lane;
+            bool fresh = false, hit = false;
+            uint32_t v = 0;
+            if (j < e) {
+                v = ids[j] & kIdMask;
+                const uint32_t old = atomicCAS(dist + v, kInfLevel, L + 1);
+                fresh = old == kInfLevel;
+                hit = fresh || old == L + 1;
+                if (hit) atomicAdd(reinterpret_cast<unsigned *>(sigma) + v, su);
+            }
+            const unsigned fm = __ballot_sync(0xffffffffu, fresh);
+            const unsigned hm = __ballot_sync(0xffffffffu, hit);
+            if (fm) {
+                uint32_t pos = 0;
+                if (lane == 0) pos = atomicAdd(counts, (unsigned)__popc(fm));
+                pos = __shfl_sync(0xffffffffu, pos, 0);
+                if (fresh) next[pos + __popc(fm & ((1u << lane) - 1u))] = v;
+            }
+            entries += (unsigned)__popc(hm);
+        }
+    }
+    if (lane == 0 && entries) atomicAdd(counts + 1, entries);
+}
+
+// One level of the backward sweep. Each level-L vertex v folds the
+// contributions of its successors w at level L+1 in descending id order, as
+// the reference's walk down its stack reaches them
+// (betweennessCentrality.c:432-455): for sigma[w] != 0,
+//   dep = float(double(dep) + (sigma[v] * 1.0 / sigma[w]) * double(1.0f + dep[w]))
+// with every operation rounded on its own (no fused multiply-add); then
+// bc[v] += dep / 2 unless v is the root. A warp loads 32 successors at a
+// time from the end of v's ascending row and folds them lane by lane.
+__global__ void bc_backward_kernel(const uint32_t *off, const uint32_t *ids, const uint32_t *level, uint32_t n,
+                                   uint32_t L, uint32_t root, const uint32_t *dist, const int32_t *sigma,
+                                   float *dep, float *bc) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+        const uint32_t v = level[i];
+        const double sv = (double)sigma[v];
+        const uint32_t b = off[v];
+        float acc = 0.0f;
+        for (uint32_t top = off[v + 1]; top > b;) {
+            const uint32_t avail = top - b;
+            bool ok = false;
+            double term = 0.0;
+            if (lane < avail) {
+                const uint32_t w = ids[top - 1 - lane] & kIdMask;
+                if (dist[w] == L + 1) {
+                    const int32_t sw = sigma[w];
+                    if (sw != 0) {
+                        ok = true;
+                        const float one_plus = __fadd_rn(1.0f, dep[w]);
+                        term = __dmul_rn(__ddiv_rn(sv, (double)sw), (double)one_plus);
+                    }
+                }
+            }
+            unsigned m = __ballot_sync(0xffffffffu, ok);
+            while (m) {
+                const int k = __ffs(m) - 1;  // lowest lane = largest successor
+                const double t = __shfl_sync(0xffffffffu, term, k);
+                acc = __double2float_rn(__dadd_rn((double)acc, t));
+                m &= m - 1u;
+            }
+            top = avail > 32u ? top - 32u : b;
+        }
+        if (lane == 0) {
+            dep[v] = acc;
+            if (v != root) bc[v] = __fadd_rn(bc[v], __fdiv_rn(acc, 2.0f));
+        }
+    }
+}
+
+static unsigned warp_grid(uint64_t items) { return grid_sm(items * 32); }
+
+}  // namespace gbx
+
+using namespace gbx;
+
+extern "C" int gbx_betweenness(gbx_graph *g, uint32_t num_roots, const uint32_t *roots, float *centrality,
+                               uint32_t *distances, int32_t *sigma_out, float *dependency,
+                               gbx_bc_result *result, void *stream) {
+    clear_error();
+    GBX_REQUIRE(g != nullptr, GBX_ERR_INVALID, "graph is NULL");
+    GBX_REQUIRE(centrality != nullptr, GBX_ERR_INVALID, "centrality is NULL");
+    GBX_REQUIRE(num_roots == 0 || roots != nullptr, GBX_ERR_INVALID, "roots is NULL");
+    GBX_TRY(ensure_device());
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t V = g->V;
+    std::vector<uint32_t> hroots(num_roots);
+    if (num_roots) {
+        if (is_device_ptr(roots)) {
+            GBX_CUDA(cudaMemcpyAsync(hroots.data(), roots, (size_t)num_roots * 4, cudaMemcpyDeviceToHost, s));
+            GBX_CUDA(cudaStreamSynchronize(s));
+        } else {
+            std::memcpy(hroots.data(), roots, (size_t)num_roots * 4);
+        }
+    }
+    for (uint32_t r = 0; r < num_roots; ++r)
+        GBX_REQUIRE(hroots[r] < V, GBX_ERR_INVALID, "root %u (%u) out of range [0, %u)", r, hroots[r], V);
+    const uint32_t *soff = nullptr, *sids = nullptr;
+    GBX_TRY(bc_successors(g, s, &soff, &sids));
+    Scratch sc;
+    const size_t bytes = 4 * Scratch::round_up((size_t)V * 4) + Scratch::round_up(16);
+    GBX_TRY(sc.take(g, bytes, s));
+    uint32_t *dist = sc.carve<uint32_t>(V);
+    int32_t *sigma = sc.carve<int32_t>(V);
+    float *dep = sc.carve<float>(V);
+    uint32_t *stack = sc.carve<uint32_t>(V);
+    unsigned *counts = sc.carve<unsigned>(4);
+    OutArray<float> obc;
+    GBX_TRY(obc.bind(centrality, V, s));
+    if (obc.to_host()) GBX_CUDA(cudaMemcpyAsync(obc.d, centrality, (size_t)V * 4, cudaMemcpyHostToDevice, s));
+    uint32_t levels = 0;
+    std::vector<uint32_t> start;
+    for (uint32_t r = 0; r < num_roots; ++r) {
+        const uint32_t root = hroots[r];
+        GBX_CUDA(cudaMemsetAsync(dist, 0xFF, (size_t)V * 4, s));
+        GBX_CUDA(cudaMemsetAsync(sigma, 0, (size_t)V * 4, s));
+        GBX_CUDA(cudaMemsetAsync(dep, 0, (size_t)V * 4, s));
+        GBX_CUDA(cudaMemsetAsync(counts, 0, 16, s));
+        bc_root_kernel<<<1, 1, 0, s>>>(root, dist, sigma, stack);
+        GBX_LAUNCH_CHECK();
+        start.assign({0u, 1u});
+        for (uint32_t L = 0;; ++L) {
+            const uint32_t n = start[L + 1] - start[L];
+            GBX_CUDA(cudaMemsetAsync(counts, 0, 4, s));
+            bc_forward_kernel<<<warp_grid(n), 256, 0, s>>>(soff, sids, stack + start[L], n, L, dist, sigma,
+                                                           stack + start[L + 1], counts);
+            GBX_LAUNCH_CHECK();
+            unsigned nn = 0;
+            GBX_CUDA(cudaMemcpyAsync(&nn, counts, 4, cudaMemcpyDeviceToHost, s));
+            GBX_CUDA(cudaStreamSynchronize(s));
+            if (nn == 0) break;
+            start.push_back(start[L + 1] + nn);
+        }
+        levels = (uint32_t)start.size() - 1;  // levels 0 .. levels-1 are non-empty
+        for (int L = (int)levels - 2; L >= 0; --L) {
+            const uint32_t n = start[L + 1] - start[L];
+            bc_backward_kernel<<<warp_grid(n), 256, 0, s>>>(soff, sids, stack + start[L], n, (uint32_t)L, root,
+                                                            dist, sigma, dep, obc.d);
+            GBX_LAUNCH_CHECK();
+        }
+    }
+    GBX_TRY(obc.finish(s));
+    unsigned processed = 0;
+    if (num_roots) GBX_CUDA(cudaMemcpyAsync(&processed, counts + 1, 4, cudaMemcpyDeviceToHost, s));
+    if (num_roots && distances) {
+        OutArray<uint32_t> o;
+        GBX_TRY(o.bind(distances, V, s));
+        GBX_CUDA(cudaMemcpyAsync(o.d, dist, (size_t)V * 4, cudaMemcpyDeviceToDevice, s));
+        GBX_TRY(o.finish(s));
+        GBX_CUDA(cudaStreamSynchronize(s));
+    }
+    if (num_roots && sigma_out) {
+        OutArray<int32_t> o;
+        GBX_TRY(o.bind(sigma_out, V, s));
+        GBX_CUDA(cudaMemcpyAsync(o.d, sigma, (size_t)V * 4, cudaMemcpyDeviceToDevice, s));
+        GBX_TRY(o.finish(s));
+        GBX_CUDA(cudaStreamSynchronize(s));
+    }
+    if (num_roots && dependency) {
+        OutArray<float> o;
+        GBX_TRY(o.bind(dependency, V, s));
+        GBX_CUDA(cudaMemcpyAsync(o.d, dep, (size_t)V * 4, cudaMemcpyDeviceToDevice, s));
+        GBX_TRY(o.finish(s));
+        GBX_CUDA(cudaStreamSynchronize(s));
+    }
+    GBX_CUDA(cudaStreamSynchronize(s));
+    if (result) {
+        result->iteration = num_roots;
+        result->processed_nodes = processed;
+        result->levels = num_roots ? levels : 0;
+    }
+    return GBX_OK;
+}
+
+// ---- Bellman-Ford and DFS -----------------------------------------------------
+namespace gbx {
+
+// Parents of the shortest-path tree: the smallest u with an edge u->v and
+// (uint32)((float)dist[u] + w) == dist[v]. The reference keeps whichever
+// relaxation wrote last (bellmanFord.c:134-227), so its parents depend on
+// the schedule; every such u is a valid parent and the smallest is the
+// deterministic choice. par[] starts at UINT32_MAX (unreached).
+__global__ void bf_parents_kernel(const uint32_t *off, const uint32_t *dest, const float *w, uint32_t V,
+                                  const uint32_t *dist, uint32_t source, uint32_t *par) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < V; u += warps) {
+        const uint32_t du = dist[u];
+        if (du == kSsspInf) continue;
+        const float fu = __uint2float_rn(du);
+        for (uint32_t j = off[u] + lane; j < off[u + 1]; j += 32) {
+            const uint32_t v = dest[j] & kIdMask;
+            const float wt = w ? w[j] : 1.0f;
+            if (v != source && __float2uint_rz(__fadd_rn(fu, wt)) == dist[v]) atomicMin(par + v, u);
+        }
+    }
+}
+
+__global__ void set_u32_kernel(uint32_t *a, uint32_t i, uint32_t value) { a[i] = value; }
+
+// The reference's stack DFS (DFS.c:156-205) run by one warp, since each pop
+// depends on every earlier one: pop v, scan its row in CSR order 32 entries
+// at a time; a neighbour whose parent is still negative is taken by the
+// first lane holding it (a repeated neighbour in the same chunk resolves to
+// its first copy, as in the sequential loop), gets parent v and distance
+// dist[v] + 1 and is pushed in row order. A vertex is pushed at most once,
+// so the stack never holds more than V entries and the loop ends after at
+// most V pops.
+__global__ void dfs_warp_kernel(const uint32_t *off, const uint32_t *dest, uint32_t source, uint32_t *dist,
+                                int32_t *par, uint32_t *stack, uint32_t *processed) {
+    const uint32_t lane = threadIdx.x & 31;
+    if (lane == 0) {
+        stack[0] = source;
+        par[source] = (int32_t)source;
+    }
+    __syncwarp();
+    uint32_t top = 1, pops = 0;
+    while (top > 0) {
+        const uint32_t v = stack[--top];
+        ++pops;
+        const uint32_t dv = dist[v] + 1u;
+        const uint32_t e = off[v + 1];
+        for (uint32_t base = off[v]; base < e; base += 32) {
+            const uint32_t j = base + lane;
+            const uint32_t u = j < e ? (dest[j] & kIdMask) : 0xFFFFFFFFu;
+            bool take = j < e && par[u] < 0;
+            const unsigned peers = __match_any_sync(0xffffffffu, u);
+            take = take && lane == (uint32_t)(__ffs(peers) - 1);
+            const unsigned m = __ballot_sync(0xffffffffu, take);
+            if (take) {
+                par[u] = (int32_t)v;
+                dist[u] = dv;
+                stack[top + __popc(m & ((1u << lane) - 1u))] = u;
+            }
+            top += (uint32_t)__popc(m);
+            __syncwarp();
+        }
+    }
+    if (lane == 0) *processed = pops;
+}
+
+}  // namespace gbx
+
+extern "C" int gbx_bellman_ford(gbx_graph *g, uint32_t source, uint32_t *distances, uint32_t *parents,
+                                gbx_sssp_result *result, void *stream) {
+    clear_error();
+    GBX_REQUIRE(g != nullptr, GBX_ERR_INVALID, "graph is NULL");
+    GBX_REQUIRE(distances != nullptr, GBX_ERR_INVALID, "distances is NULL");
+    GBX_REQUIRE(source < g->V, GBX_ERR_INVALID, "source %u out of range [0, %u)", source, g->V);
+    GBX_TRY(ensure_device());
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t V = g->V;
+    OutArray<uint32_t> od;
+    GBX_TRY(od.bind(distances, V, s));
+    gbx_sssp_result r{};
+    GBX_TRY(gbx_sssp(g, source, 0, od.d, &r, stream));
+    if (parents) {
+        OutArray<uint32_t> op;
+        GBX_TRY(op.bind(parents, V, s));
+        GBX_CUDA(cudaMemsetAsync(op.d, 0xFF, (size_t)V * 4, s));
+        bf_parents_kernel<<<warp_grid(V), 256, 0, s>>>(g->offsets, g->dest, g->weight, V, od.d, source, op.d);
+        GBX_LAUNCH_CHECK();
+        set_u32_kernel<<<1, 1, 0, s>>>(op.d, source, source);
+        GBX_LAUNCH_CHECK();
+        GBX_TRY(op.finish(s));
+        GBX_CUDA(cudaStreamSynchronize(s));
+    }
+    GBX_TRY(od.finish(s));
+    GBX_CUDA(cudaStreamSynchronize(s));
+    if (result) *result = r;
+    return GBX_OK;
+}
+
+extern "C" int gbx_dfs(gbx_graph *g, uint32_t source, uint32_t *distances, int32_t *parents,
+                       uint32_t *processed_nodes, void *stream) {
+    clear_error();
+    GBX_REQUIRE(g != nullptr, GBX_ERR_INVALID, "graph is NULL");
+    GBX_REQUIRE(distances != nullptr && parents != nullptr, GBX_ERR_INVALID, "distances/parents is NULL");
+    GBX_REQUIRE(source < g->V, GBX_ERR_INVALID, "source %u out of range [0, %u)", source, g->V);
+    GBX_TRY(ensure_device());
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t V = g->V;
+    OutArray<uint32_t> od;
+    OutArray<int32_t> op;
+    GBX_TRY(od.bind(distances, V, s));
+    GBX_TRY(op.bind(parents, V, s));
+    DevBuf<uint32_t> stack, pops;
+    GBX_TRY(stack.alloc((size_t)V + 1, s));
+    GBX_TRY(pops.alloc(1, s));
+    GBX_CUDA(cudaMemsetAsync(od.d, 0, (size_t)V * 4, s));
+    GBX_CUDA(cudaMemsetAsync(op.d, 0xFF, (size_t)V * 4, s));
+    dfs_warp_kernel<<<1, 32, 0, s>>>(g->offsets, g->dest, source, od.d, op.d, stack.p, pops.p);
+    GBX_LAUNCH_CHECK();
+    uint32_t hp = 0;
+    GBX_CUDA(cudaMemcpyAsync(&hp, pops.p, 4, cudaMemcpyDeviceToHost, s));
+    GBX_TRY(od.finish(s));
+    GBX_TRY(op.finish(s));
+    GBX_CUDA(cudaStreamSynchronize(s));
+    if (processed_nodes) *processed_nodes = hp;
+    return GBX_OK;
+}
+
+// ---- the reference's random roots ------------------------------------------------
+// Host code: the Mersenne Twister MT19937 (Matsumoto and Nishimura, 1998)
+// with the seeding of its first release (Knuth's LCG x <- 69069 x + 1, the
+// upper 16 bits of two draws per state word), as the reference's
+// mt19937.c seeds it (graphConfig.c:84 uses 27491095), and the rejection
+// loop of generateRandomRootBetweennessCentrality (betweennessCentrality.c:
+// 172-189): draw until the value is a vertex whose out-degree exceeds E/V.
+namespace {
+
+struct Mt19937 {
+    uint32_t mt[624];
+    int mti = 624;
+    explicit Mt19937(uint32_t seed) {
+        for (int i = 0; i < 624; ++i) {
+            mt[i] = seed & 0xffff0000u;
+            seed = 69069u * seed + 1u;
+            mt[i] |= (seed & 0xffff0000u) >> 16;
+            seed = 69069u * seed + 1u;
+        }
+    }
+    uint32_t next() {
+        if (mti >= 624) {
+            for (int k = 0; k < 624; ++k) {
+                const uint32_t y = (mt[k] & 0x80000000u) | (mt[(k + 1) % 624] & 0x7fffffffu);
+                mt[k] = mt[(k + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+            }
+            mti = 0;
+        }
+        uint32_t y = mt[mti++];
+        y ^= y >> 11;
+        y ^= (y << 7) & 0x9d2c5680u;
+        y ^= (y << 15) & 0xefc60000u;
+        y ^= y >> 18;
+        return y;
+    }
+};
+
+}  // namespace
+
+extern "C" int gbx_reference_roots(gbx_graph *g, uint32_t seed, uint32_t n, uint32_t *roots) {
+    clear_error();
+    GBX_REQUIRE(g != nullptr, GBX_ERR_INVALID, "graph is NULL");
+    GBX_REQUIRE(n == 0 || roots != nullptr, GBX_ERR_INVALID, "roots is NULL");
+    GBX_TRY(ensure_device());
+    const uint32_t V = g->V, avg = g->E / g->V;
+    std::vector<uint32_t> deg(V);
+    GBX_CUDA(cudaMemcpy(deg.data(), g->out_degree, (size_t)V * 4, cudaMemcpyDeviceToHost));
+    uint32_t maxdeg = 0;
+    for (uint32_t d : deg) maxdeg = d > maxdeg ? d : maxdeg;
+    GBX_REQUIRE(n == 0 || maxdeg > avg, GBX_ERR_INVALID,
+                "no vertex has an out-degree above the average (%u): the draw would not end", avg);
+    Mt19937 m(seed);
+    for (uint32_t i = 0; i < n; ++i) {
+        for (;;) {
+            const uint32_t r = m.next();
+            if (r < V && deg[r] > avg) {
+                roots[i] = r;
+                break;
+            }
+        }
+    }
+    return GBX_OK;
+}

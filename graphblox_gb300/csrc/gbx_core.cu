@@ -384,6 +384,7 @@ int gbx_graph_destroy(gbx_graph *g) {
     gbx_free_ppr_cache(g->ppr);
     gbx_free_ms_plan(g->ms_plan);
     gbx_free_pr_cache(g->pr_cache);
+    gbx_free_bc_cache(g->bc_cache);
     cudaFree(g->arena);
     free_plan(g->plan_fwd);
     free_plan(g->plan_inv);

@@ -236,6 +236,8 @@ struct gbx_graph {
     struct gbx_ms_plan *ms_plan = nullptr;
     // PageRank working memory and captured iteration loop (gbx_pagerank.cu)
     struct gbx_pr_cache *pr_cache = nullptr;
+    // betweenness centrality: successor CSR with ascending rows (gbx_bc.cu)
+    struct gbx_bc_cache *bc_cache = nullptr;
     // device scratch lent to one synchronous call at a time (gbx::Scratch)
     char *arena = nullptr;
     size_t arena_bytes = 0;
@@ -253,6 +255,7 @@ void gbx_free_tc_plan(struct gbx_tc_plan *p);
 void gbx_free_ppr_cache(struct gbx_ppr_cache *c);
 void gbx_free_ms_plan(struct gbx_ms_plan *p);
 void gbx_free_pr_cache(struct gbx_pr_cache *c);
+void gbx_free_bc_cache(struct gbx_bc_cache *c);
 
 namespace gbx {
 // Device scratch for one synchronous call: carved from the graph's arena

@@ -20,7 +20,7 @@ from typing import Optional
 import numpy as np
 
 from . import _lib
-from ._lib import BfsResult, PrResult, SsspResult, call
+from ._lib import BcResult, BfsResult, PrResult, SsspResult, call
 
 ID_MASK = np.uint32(0x3FFFFFFF)  # EXTRACT_VALUE, reorder.h:23
 
@@ -582,6 +582,94 @@ def sssp(dg: DeviceGraph, source: int, delta: int = 0, distances=None, stream=No
     r = SsspResult()
     call("gbx_sssp", dg.handle, src, int(delta), _ptr(distances), C.byref(r), stream)
     return SSSPStats(distances, r.reached, r.rounds, r.edges_relaxed, r.edges_traversed, src)
+
+
+@dataclass
+class BellmanFordStats:
+    distances: object
+    parents: object
+    processed_nodes: int
+    source: int
+
+
+def bellman_ford(dg: DeviceGraph, source: int, distances=None, parents=None, stream=None,
+                 map_source: bool = True) -> BellmanFordStats:
+    """bellmanFordGraphCSR: the reference's distances (UINT32_MAX/2 when
+    unreached) and a shortest-path parent per vertex (the smallest valid
+    one; UINT32_MAX when unreached). processed_nodes = vertices reached."""
+    src = _map_source(dg, source) if map_source else int(source)
+    V = dg.num_vertices
+    if distances is None:
+        distances = np.zeros(V, np.uint32)
+    if parents is None:
+        parents = np.zeros(V, np.uint32)
+    r = SsspResult()
+    call("gbx_bellman_ford", dg.handle, src, _ptr(distances), _ptr(parents), C.byref(r), stream)
+    return BellmanFordStats(distances, parents, r.reached, src)
+
+
+@dataclass
+class DFSStats:
+    distances: object
+    parents: object
+    processed_nodes: int
+
+
+def depth_first_search(dg: DeviceGraph, source: int, distances=None, parents=None,
+                       stream=None) -> DFSStats:
+    """depthFirstSearchGraphCSR: the reference's stack traversal (its source
+    is used as given, without the label remapping of BFS/SSSP)."""
+    V = dg.num_vertices
+    if distances is None:
+        distances = np.zeros(V, np.uint32)
+    if parents is None:
+        parents = np.zeros(V, np.int32)
+    n = _lib.u32(0)
+    call("gbx_dfs", dg.handle, int(source), _ptr(distances), _ptr(parents), C.byref(n), stream)
+    return DFSStats(distances, parents, n.value)
+
+
+BC_SEED = 27491095  # the reference's generator seed, graphConfig.c:84
+
+
+@dataclass
+class BetweennessCentralityStats:
+    betweennessCentrality: object
+    distances: object
+    sigma: object
+    dependency: object
+    iteration: int
+    processed_nodes: int
+    roots: np.ndarray
+
+
+def reference_roots(dg: DeviceGraph, n: int, seed: int = BC_SEED) -> np.ndarray:
+    """The n roots the reference's Brandes draws from a freshly seeded
+    generator (gbx_reference_roots)."""
+    roots = np.zeros(max(int(n), 1), np.uint32)
+    call("gbx_reference_roots", dg.handle, int(seed), int(n), _ptr(roots))
+    return roots[:n]
+
+
+def betweenness_centrality(dg: DeviceGraph, iterations: int = 20, roots=None, centrality=None,
+                           seed: int = BC_SEED, stream=None) -> BetweennessCentralityStats:
+    """betweennessCentralityBrandesGraphCSR: Brandes from `iterations` roots
+    drawn like the reference's (or the given roots), centrality accumulated
+    from zero (or into the given array). distances / sigma / dependency are
+    the last root's."""
+    if roots is None:
+        roots = reference_roots(dg, iterations, seed)
+    roots = _u32(roots)
+    V = dg.num_vertices
+    if centrality is None:
+        centrality = np.zeros(V, np.float32)
+    dist = np.zeros(V, np.uint32)
+    sig = np.zeros(V, np.int32)
+    dep = np.zeros(V, np.float32)
+    r = BcResult()
+    call("gbx_betweenness", dg.handle, roots.shape[0], _ptr(roots), _ptr(centrality), _ptr(dist), _ptr(sig),
+         _ptr(dep), C.byref(r), stream)
+    return BetweennessCentralityStats(centrality, dist, sig, dep, r.iteration, r.processed_nodes, roots)
 
 
 def connected_components(dg: DeviceGraph, variant: int = 1, components=None, stream=None):

@@ -41,6 +41,9 @@
  *                                (:275-380), DBG (:387-572), HUBSort (:762-982), HUBCluster (:984-1170),
  *                                Corder (:574-624), degrees (:1483-1552), relabel (:1618-1637)
  *   gbx_relabel               -> relabelEdgeListFromFile's relabelling (01_host/src/preprocess/reorder.c:1662-1714)
+ *   gbx_bellman_ford          -> bellmanFordGraphCSR (01_host/src/algorithms/openmp/bellmanFord.c:419-738)
+ *   gbx_dfs                   -> depthFirstSearchGraphCSR (01_host/src/algorithms/openmp/DFS.c:156-205)
+ *   gbx_betweenness           -> betweennessCentralityGraphCSR (01_host/src/algorithms/openmp/betweennessCentrality.c:230-466)
  *   gbx_mask_graph            -> maskGraphProcess (01_host/src/preprocess/reorder.c:1164-1475) and
  *                                maskEdgeList (:1639-1657), the -M mask mode
  * Extension entry points (batched, multi-source, personalised PageRank and
@@ -271,6 +274,51 @@ typedef struct gbx_sssp_result {
  * delta: bucket width of the near/far schedule (0 = autotuned). */
 int gbx_sssp(gbx_graph *g, uint32_t source, uint32_t delta, uint32_t *distances,
              gbx_sssp_result *result, void *stream);
+
+/* Bellman-Ford: the reference's distances (its pull and push variants and
+ * SSSP all reach the same fixpoint of (uint32)((float)d + w)), computed by
+ * the SSSP engine; parents[v] = the smallest u with an edge u->v on a
+ * shortest path (the reference keeps the last racing writer), the source
+ * its own parent, UINT32_MAX when unreached. parents may be NULL. The
+ * result counts the SSSP engine's work, not the reference's active-vertex
+ * sum, which depends on its relaxation order. */
+int gbx_bellman_ford(gbx_graph *g, uint32_t source, uint32_t *distances, uint32_t *parents,
+                     gbx_sssp_result *result, void *stream);
+
+/* ---- depth-first search ---------------------------------------------------- */
+/* The reference's stack traversal over the forward CSR: pop v, push every
+ * out-neighbour whose parent is still -1 (parent v, distance d[v] + 1), in
+ * row order; the source is its own parent. Unreached vertices keep
+ * distance 0 and parent -1; *processed_nodes = vertices popped. Each pop
+ * depends on the previous ones, so one warp runs it (latency-bound). */
+int gbx_dfs(gbx_graph *g, uint32_t source, uint32_t *distances, int32_t *parents,
+            uint32_t *processed_nodes, void *stream);
+
+/* ---- betweenness centrality ------------------------------------------------ */
+typedef struct gbx_bc_result {
+    uint32_t iteration;        /* roots processed */
+    uint32_t processed_nodes;  /* last root: predecessor entries (DAG edges) */
+    uint32_t levels;           /* last root: BFS levels */
+} gbx_bc_result;
+
+/* Brandes from each of roots[0..num_roots) in turn (the reference draws them
+ * from its generator: out-degree above the average), ADDING each root's
+ * dependency / 2 into centrality[V] (zero it for a fresh run, as the
+ * reference's new stats are). Levels come from the pull CSR (inverse when
+ * present), sigma is int32 (wrapping), and the dependency fold follows the
+ * reference's order and rounding exactly, so centrality is bit-identical to
+ * the reference's. distances (UINT32_MAX unreached), sigma and dependency
+ * of the last root are written when not NULL. */
+int gbx_betweenness(gbx_graph *g, uint32_t num_roots, const uint32_t *roots, float *centrality,
+                    uint32_t *distances, int32_t *sigma, float *dependency, gbx_bc_result *result,
+                    void *stream);
+/* The n roots the reference's Brandes draws from a generator seeded with
+ * seed (the reference seeds 27491095 and draws its trial roots from the same
+ * stream, so a run that drew those first continues from a later state):
+ * MT19937 values, kept when below num_vertices with an out-degree above
+ * num_edges / num_vertices. Host computation; roots is host memory.
+ * GBX_ERR_INVALID when no vertex qualifies. */
+int gbx_reference_roots(gbx_graph *g, uint32_t seed, uint32_t n, uint32_t *roots);
 
 /* ---- connected components ---------------------------------------------- */
 /* components[v] = smallest vertex id in v's component. variant 0 SV-style

@@ -871,3 +871,177 @@ void orc_spmv_pull_f64(uint32_t num_vertices, const uint32_t *pull_degree, const
         }
     }
 }
+
+/* ------------------------------------------------------------------------ */
+/* random roots (mt19937.c, betweennessCentrality.c:172-189)                */
+/* ------------------------------------------------------------------------ */
+
+/* The Mersenne Twister MT19937 (Matsumoto and Nishimura, 1998) with the
+ * seeding of its first release (Knuth's LCG x <- 69069 x + 1, two draws
+ * per state word, the upper 16 bits of each), which is the generator the
+ * reference seeds with 27491095 (graphConfig.c:84). */
+typedef struct { uint32_t mt[624]; int mti; } orc_mt;
+
+static void orc_mt_seed(orc_mt *m, uint32_t seed) {
+    for (int i = 0; i < 624; ++i) {
+        m->mt[i] = seed & 0xffff0000u;
+        seed = 69069u * seed + 1u;
+        m->mt[i] |= (seed & 0xffff0000u) >> 16;
+        seed = 69069u * seed + 1u;
+    }
+    m->mti = 624;
+}
+
+static uint32_t orc_mt_next(orc_mt *m) {
+    if (m->mti >= 624) {
+        for (int k = 0; k < 624; ++k) {
+            const uint32_t y = (m->mt[k] & 0x80000000u) | (m->mt[(k + 1) % 624] & 0x7fffffffu);
+            m->mt[k] = m->mt[(k + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+        }
+        m->mti = 0;
+    }
+    uint32_t y = m->mt[m->mti++];
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= y >> 18;
+    return y;
+}
+
+/* generateRandomRootBetweennessCentrality, n times from one seeded state:
+ * draw until the value is a vertex whose out-degree exceeds avg_degree. */
+void orc_random_roots(uint32_t seed, uint32_t n, uint32_t num_vertices, const uint32_t *out_degree,
+                      uint32_t avg_degree, uint32_t *roots) {
+    orc_mt m;
+    orc_mt_seed(&m, seed);
+    for (uint32_t i = 0; i < n; ++i) {
+        for (;;) {
+            const uint32_t r = orc_mt_next(&m);
+            if (r < num_vertices && out_degree[r] > avg_degree) { roots[i] = r; break; }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* betweenness centrality (betweennessCentrality.c:230-466)                 */
+/* ------------------------------------------------------------------------ */
+
+/* Brandes from each root in turn, accumulating into bc[] (which the caller
+ * zeroes, as newBetweennessCentralityStatsGraphCSR does). Per root: a
+ * level-synchronous pull BFS over the pull CSR (the inverse CSR in a
+ * DIRECTED build, the forward one otherwise): an unreached v whose pull
+ * row holds frontier vertices gets level + 1, sigma[v] = the sum of their
+ * sigma (int) and the list of those entries as its predecessors, in row
+ * order (:289-347). The stack holds the levels in order, ids ascending
+ * inside a level (copyBitmapToStack, :205-217). Then, for the stack from
+ * the top down to (not including) the root, each predecessor v of w takes
+ * dependency[v] += (sigma[v] * 1.0 / sigma[w]) * (1 + dependency[w]) --
+ * a double product of the double ratio and the float 1 + dependency[w],
+ * added in double and stored as float -- when sigma[w] != 0, and
+ * bc[w] += dependency[w] / 2 for w != root (:432-455). Returns, for the
+ * last root, its distances (UINT32_MAX unreached), sigma, dependency and
+ * processed_nodes = the number of predecessor entries. */
+void orc_betweenness(uint32_t num_vertices, const uint32_t *pull_degree, const uint32_t *pull_idx,
+                     const uint32_t *pull_src, uint32_t num_roots, const uint32_t *roots, float *bc,
+                     uint32_t *distances, int32_t *sigma, float *dependency, uint32_t *processed_nodes) {
+    const uint32_t n = num_vertices;
+    uint64_t E = 0;
+    for (uint32_t v = 0; v < n; ++v) E += pull_degree[v];
+    uint32_t *pred_off = (uint32_t *)xmalloc(((size_t)n + 1) * 4);
+    uint32_t *pred_cnt = (uint32_t *)xmalloc((size_t)n * 4 + 4);
+    uint32_t *preds = (uint32_t *)xmalloc((size_t)E * 4 + 4);
+    uint32_t *stack = (uint32_t *)xmalloc((size_t)n * 4 + 4);
+    uint8_t *frontier = (uint8_t *)xmalloc((size_t)n + 1);
+    uint8_t *next = (uint8_t *)xmalloc((size_t)n + 1);
+    pred_off[0] = 0;
+    for (uint32_t v = 0; v < n; ++v) pred_off[v + 1] = pred_off[v] + pull_degree[v];
+    for (uint32_t r = 0; r < num_roots; ++r) {
+        const uint32_t s = roots[r];
+        uint32_t processed = 0, top = 0;
+        for (uint32_t v = 0; v < n; ++v) {
+            distances[v] = 0xFFFFFFFFu;
+            dependency[v] = 0.0f;
+            sigma[v] = 0;
+            pred_cnt[v] = 0;
+            frontier[v] = 0;
+        }
+        distances[s] = 0;
+        sigma[s] = 1;
+        frontier[s] = 1;
+        stack[top++] = s;
+        uint32_t nf = 1;
+        while (nf) {
+            nf = 0;
+            memset(next, 0, n);
+            for (uint32_t v = 0; v < n; ++v) {
+                if (distances[v] != 0xFFFFFFFFu) continue;
+                for (uint32_t j = pull_idx[v]; j < pull_idx[v] + pull_degree[v]; ++j) {
+                    const uint32_t u = pull_src[j] & 0x3FFFFFFFu;
+                    if (!frontier[u]) continue;
+                    distances[v] = distances[u] + 1;
+                    sigma[v] = (int32_t)((uint32_t)sigma[v] + (uint32_t)sigma[u]);
+                    preds[pred_off[v] + pred_cnt[v]++] = u;
+                    next[v] = 1;
+                    ++nf;
+                }
+            }
+            /* the loop above reads distances[] of frontier vertices only and
+             * writes those of unreached ones, so its order does not matter */
+            for (uint32_t v = 0; v < n; ++v) if (next[v]) stack[top++] = v;
+            processed += nf;
+            uint8_t *t = frontier; frontier = next; next = t;
+        }
+        for (uint32_t t = top - 1; t > 0; --t) {
+            const uint32_t w = stack[t];
+            for (uint32_t k = 0; k < pred_cnt[w]; ++k) {
+                const uint32_t v = preds[pred_off[w] + k];
+                if (sigma[w] != 0) {
+                    const double ratio = (double)sigma[v] * 1.0 / (double)sigma[w];
+                    const float one_plus = 1.0f + dependency[w];
+                    dependency[v] = (float)((double)dependency[v] + ratio * (double)one_plus);
+                }
+            }
+            if (w != s) bc[w] += dependency[w] / 2;
+        }
+        *processed_nodes = processed;
+    }
+    free(next);
+    free(frontier);
+    free(stack);
+    free(preds);
+    free(pred_cnt);
+    free(pred_off);
+}
+
+/* ------------------------------------------------------------------------ */
+/* depth-first search (DFS.c:156-205)                                       */
+/* ------------------------------------------------------------------------ */
+
+/* One LIFO stack, a vertex marked when pushed: pop v, then for v's
+ * out-edges in CSR order push every u whose parent is still negative, with
+ * parent v and distance distance[v] + 1. distances start 0, parents -1,
+ * the root is its own parent; processed_nodes counts pops. */
+void orc_dfs(uint32_t num_vertices, const uint32_t *out_degree, const uint32_t *edges_idx,
+             const uint32_t *dest, uint32_t source, uint32_t *distances, int32_t *parents,
+             uint32_t *processed_nodes) {
+    const uint32_t n = num_vertices;
+    uint32_t *stack = (uint32_t *)xmalloc((size_t)n * 4 + 4);
+    for (uint32_t v = 0; v < n; ++v) { distances[v] = 0; parents[v] = -1; }
+    uint32_t top = 0, processed = 0;
+    stack[top++] = source;
+    parents[source] = (int32_t)source;
+    while (top) {
+        const uint32_t v = stack[--top];
+        ++processed;
+        for (uint32_t j = edges_idx[v]; j < edges_idx[v] + out_degree[v]; ++j) {
+            const uint32_t u = dest[j] & 0x3FFFFFFFu;
+            if (parents[u] < 0) {
+                parents[u] = (int32_t)v;
+                distances[u] = distances[v] + 1;
+                stack[top++] = u;
+            }
+        }
+    }
+    *processed_nodes = processed;
+    free(stack);
+}

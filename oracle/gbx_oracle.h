@@ -111,6 +111,20 @@ void orc_spmv_pull_f64(uint32_t num_vertices, const uint32_t *pull_degree, const
                        const uint32_t *pull_src, const float *weights, float default_weight,
                        const float *x, double *y, uint32_t iterations, int num_threads);
 
+/* ---- random roots (mt19937.c, betweennessCentrality.c:172-189) -------- */
+void orc_random_roots(uint32_t seed, uint32_t n, uint32_t num_vertices, const uint32_t *out_degree,
+                      uint32_t avg_degree, uint32_t *roots);
+
+/* ---- betweenness centrality (betweennessCentrality.c:230-466) ---------- */
+void orc_betweenness(uint32_t num_vertices, const uint32_t *pull_degree, const uint32_t *pull_idx,
+                     const uint32_t *pull_src, uint32_t num_roots, const uint32_t *roots, float *bc,
+                     uint32_t *distances, int32_t *sigma, float *dependency, uint32_t *processed_nodes);
+
+/* ---- depth-first search (DFS.c:156-205) -------------------------------- */
+void orc_dfs(uint32_t num_vertices, const uint32_t *out_degree, const uint32_t *edges_idx,
+             const uint32_t *dest, uint32_t source, uint32_t *distances, int32_t *parents,
+             uint32_t *processed_nodes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -39,6 +39,9 @@ def load():
             "orc_map_vertices": (None, [u32, u32, vp, vp, vp]),
             "orc_degree_reorder": (None, [u32, u32, vp, vp, C.c_int, vp, vp, C.c_int]),
             "orc_mask_graph": (None, [u32, u32, vp, vp, C.c_int, u32, vp]),
+            "orc_random_roots": (None, [u32, u32, u32, vp, u32, vp]),
+            "orc_betweenness": (None, [u32, vp, vp, vp, u32, vp, vp, vp, vp, vp, vp]),
+            "orc_dfs": (None, [u32, vp, vp, vp, u32, vp, vp, vp]),
             "orc_bfs": (None, [u32, u32, vp, vp, vp, vp, vp, vp, u32, vp, vp, vp, vp, C.c_int]),
             "orc_pagerank_pull": (None, [u32, vp, vp, vp, vp, u32, C.c_double, vp, vp, vp, C.c_int]),
             "orc_pagerank_pull_f64": (None, [u32, vp, vp, vp, vp, u32, C.c_double, vp, vp, C.c_int]),
@@ -116,6 +119,44 @@ def mask_graph(num_vertices, src, dst, mmode=1, cache_size=32768):
     m = np.zeros(num_vertices, np.uint32)
     load().orc_mask_graph(num_vertices, s.shape[0], _p(s), _p(d), int(mmode), int(cache_size), _p(m))
     return s, d, m
+
+
+BC_SEED = 27491095  # graphConfig.c:84
+
+
+def random_roots(g: HostCSR, n, seed=BC_SEED):
+    """The roots the reference's Brandes draws (n of them, from a fresh generator)."""
+    roots = np.zeros(max(int(n), 1), np.uint32)
+    avg = g.num_edges // g.num_vertices if g.num_vertices else 0
+    load().orc_random_roots(int(seed), int(n), g.num_vertices, _p(g.out_degree), avg, _p(roots))
+    return roots[:n]
+
+
+def betweenness(g: HostCSR, roots, pull: Optional[HostCSR] = None):
+    """Returns (bc, distances, sigma, dependency, processed_nodes) -- the last
+    four for the last root."""
+    pull = pull or g
+    V = g.num_vertices
+    r = _u32(roots)
+    bc = np.zeros(V, np.float32)
+    dist = np.zeros(V, np.uint32)
+    sig = np.zeros(V, np.int32)
+    dep = np.zeros(V, np.float32)
+    proc = u32(0)
+    load().orc_betweenness(V, _p(pull.out_degree), _p(pull.edges_idx), _p(pull.dest), r.shape[0], _p(r),
+                           _p(bc), _p(dist), _p(sig), _p(dep), C.byref(proc))
+    return bc, dist, sig, dep, proc.value
+
+
+def dfs(g: HostCSR, source):
+    """Returns (distances, parents, processed_nodes)."""
+    V = g.num_vertices
+    dist = np.zeros(V, np.uint32)
+    par = np.zeros(V, np.int32)
+    proc = u32(0)
+    load().orc_dfs(V, _p(g.out_degree), _p(g.edges_idx), _p(g.dest), int(source), _p(dist), _p(par),
+                   C.byref(proc))
+    return dist, par, proc.value
 
 
 def bfs(g: HostCSR, source, pull: Optional[HostCSR] = None, threads=0):

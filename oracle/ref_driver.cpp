@@ -38,6 +38,9 @@ extern "C" {
 #include "SSSP.h"
 #include "connectedComponents.h"
 #include "triangleCount.h"
+#include "bellmanFord.h"
+#include "DFS.h"
+#include "betweennessCentrality.h"
 #include "SPMV.h"
 }
 
@@ -144,6 +147,39 @@ int main(int argc, char **argv) {
                      a->source, s->processed_nodes, s->time_total);
         dump(out, "sssp_distances.u32", s->distances, V * 4ull);
         freeSSSPStats(s);
+    } break;
+    case 3: {
+        struct BellmanFordStats *s = bellmanFordGraphCSR(a, g);
+        std::fprintf(sc, "source %u\nprocessed_nodes %u\ntime_total %.9f\n",
+                     a->source, s->processed_nodes, s->time_total);
+        dump(out, "bf_distances.u32", s->distances, V * 4ull);
+        dump(out, "bf_parents.u32", s->parents, V * 4ull);
+        freeBellmanFordStats(s);
+    } break;
+    case 4: {
+        struct DFSStats *s = depthFirstSearchGraphCSR(a, g);
+        std::fprintf(sc, "source %u\nprocessed_nodes %u\ntime_total %.9f\n",
+                     a->source, s->processed_nodes, s->time_total);
+        dump(out, "dfs_distances.u32", s->distances, V * 4ull);
+        dump(out, "dfs_parents.i32", s->parents, V * 4ull);
+        freeDFSStats(s);
+    } break;
+    case 7: {
+        // the roots Brandes will draw, from a copy of the generator state
+        mt19937state rng = a->mt19937var;
+        uint32_t *roots = (uint32_t *)std::malloc((a->iterations + 1) * 4ull);
+        for (uint32_t i = 0; i < a->iterations; ++i)
+            roots[i] = generateRandomRootBetweennessCentrality(&rng, g);
+        dump(out, "bc_roots.u32", roots, a->iterations * 4ull);
+        std::free(roots);
+        struct BetweennessCentralityStats *s = betweennessCentralityGraphCSR(a, g);
+        std::fprintf(sc, "iteration %u\nprocessed_nodes %u\ntime_total %.9f\n",
+                     s->iteration, s->processed_nodes, s->time_total);
+        dump(out, "bc_centrality.f32", s->betweennessCentrality, V * 4ull);
+        dump(out, "bc_distances.u32", s->distances, V * 4ull);
+        dump(out, "bc_sigma.i32", s->sigma, V * 4ull);
+        dump(out, "bc_dependency.f32", s->dependency, V * 4ull);
+        freeBetweennessCentralityStats(s);
     } break;
     case 5: {
         struct SPMVStats *s = SPMVGraphCSR(a, g);

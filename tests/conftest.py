@@ -11,9 +11,10 @@ if str(ROOT) not in sys.path:
 GOLDEN = Path(__file__).resolve().parent / "golden"
 # one fixture per test graph; reorder_modes.npz holds the labels of the
 # reorder modes for all of them, csr_files.npz the reference's .csr files,
-# mask_modes.npz its mask mode
+# mask_modes.npz its mask mode, bf_dfs_bc.npz Bellman-Ford, DFS and
+# betweenness centrality
 GOLDEN_GRAPHS = sorted(p.stem for p in GOLDEN.glob("*.npz")
-                       if p.stem not in ("reorder_modes", "csr_files", "mask_modes"))
+                       if p.stem not in ("reorder_modes", "csr_files", "mask_modes", "bf_dfs_bc"))
 REORDER_MODES = [2, 3, 4, 5, 6, 7, 8, 9, 12, 13]
 
 
@@ -28,6 +29,11 @@ def load_reorder_modes() -> dict:
 
 def load_csr_files() -> dict:
     with np.load(GOLDEN / "csr_files.npz") as z:
+        return {k: z[k] for k in z.files}
+
+
+def load_bf_dfs_bc() -> dict:
+    with np.load(GOLDEN / "bf_dfs_bc.npz") as z:
         return {k: z[k] for k in z.files}
 
 

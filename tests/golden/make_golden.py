@@ -12,10 +12,11 @@ its build (oracle/build_ref.sh). For every test graph the reference ships in
 The GPU host has no reference tree, so the parity tests read only these
 fixtures there.
 
-Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [reorder|csr|mask]
+Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [reorder|csr|mask|more]
 ("reorder" writes only reorder_modes.npz, the labels of the reorder modes;
 "csr" writes only csr_files.npz, the reference's .csr files; "mask" writes
-only mask_modes.npz, the reference's mask mode.)
+only mask_modes.npz, the reference's mask mode; "more" writes only
+bf_dfs_bc.npz, Bellman-Ford, DFS and betweenness centrality.)
 """
 from __future__ import annotations
 
@@ -203,6 +204,50 @@ def mask_modes(ref_root: str) -> None:
     print(f"wrote {out.name}")
 
 
+BC_ROOTS = 4
+
+
+def more_algorithms(ref_root: str) -> None:
+    """tests/golden/bf_dfs_bc.npz: Bellman-Ford, DFS and betweenness
+    centrality of the reference host on every test graph. Keys
+    <graph>_<variant>_...: bf_r<root> (distances; the parents depend on the
+    thread schedule), dfs_r<root> / dfs_parents_r<root> / dfs_processed_r<root>
+    for roots 0 and 1, and for the DIRECTED 1 build (dw, dwk) bc_roots,
+    bc (centrality after BC_ROOTS roots), bc_distances / bc_sigma /
+    bc_dependency / bc_processed of the last root. The DIRECTED 0 build's
+    Brandes writes past its predecessor lists (sized by in_degree, which
+    that build leaves 0) and aborts, so it has no BC keys."""
+    test_dir = Path(ref_root) / "03_data" / "TEST"
+    fx: dict[str, np.ndarray] = {}
+    for name in GRAPHS:
+        gdir = test_dir / name
+        weighted = (gdir / "graph.wbin").exists() and not (gdir / "graph.bin").exists()
+        f = gdir / ("graph.wbin" if weighted else "graph.bin")
+        wflag = ["-w"] if weighted else []
+        for variant, flags in (("u", ["-s", "-k"]), ("dw", []), ("dwk", ["-k"])):
+            exe = "u" if variant == "u" else "dw"
+            fl = ["-o", "1", *wflag, *flags]
+            key = f"{name}_{variant}"
+            out = po.ref_run(f, exe, 3, [*fl, "-r", "1", "-p", "1"])
+            fx[f"{key}_bf_r1"] = out["bf_distances"]
+            for r in (0, 1):
+                out = po.ref_run(f, exe, 4, [*fl, "-r", str(r)], threads=1)
+                fx[f"{key}_dfs_r{r}"] = out["dfs_distances"]
+                fx[f"{key}_dfs_parents_r{r}"] = out["dfs_parents"]
+                fx[f"{key}_dfs_processed_r{r}"] = np.array(out["processed_nodes"])
+            if exe == "dw":
+                out = po.ref_run(f, exe, 7, [*fl, "-i", str(BC_ROOTS)])
+                fx[f"{key}_bc_roots"] = out["bc_roots"]
+                fx[f"{key}_bc"] = out["bc_centrality"]
+                fx[f"{key}_bc_distances"] = out["bc_distances"]
+                fx[f"{key}_bc_sigma"] = out["bc_sigma"]
+                fx[f"{key}_bc_dependency"] = out["bc_dependency"]
+                fx[f"{key}_bc_processed"] = np.array(out["processed_nodes"])
+    out_path = Path(__file__).resolve().parent / "bf_dfs_bc.npz"
+    np.savez_compressed(out_path, **fx)
+    print(f"wrote {out_path.name}")
+
+
 if __name__ == "__main__":
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     if len(sys.argv) > 2 and sys.argv[2] == "reorder":
@@ -211,6 +256,8 @@ if __name__ == "__main__":
         csr_files(root)
     elif len(sys.argv) > 2 and sys.argv[2] == "mask":
         mask_modes(root)
+    elif len(sys.argv) > 2 and sys.argv[2] == "more":
+        more_algorithms(root)
     else:
         main(root)
         reorder_modes(root)

@@ -203,3 +203,113 @@ def test_reference_entry_points_undirected(gbx, cuda_device, name):
     s = lib.connectedComponentsGraphCSR(C.byref(a), g)
     np.testing.assert_array_equal(_arr(s.contents.components, b.V, np.uint32), fx["u_cc"])
     lib.freeCCStats(s)
+
+
+class BellmanFordStats(C.Structure):
+    _fields_ = [("distances", P(u32)), ("parents", P(u32)), ("processed_nodes", u32), ("num_vertices", u32),
+                ("time_total", C.c_double)]
+
+
+class DFSStats(C.Structure):
+    _fields_ = [("distances", P(u32)), ("parents", P(C.c_int)), ("processed_nodes", u32), ("num_vertices", u32),
+                ("time_total", C.c_double)]
+
+
+class Predecessor(C.Structure):
+    _fields_ = [("nodes", P(u32)), ("degree", u32)]
+
+
+class BCStats(C.Structure):
+    _fields_ = [("stack", P(Predecessor)), ("distances", P(u32)), ("realRanks", P(u32)), ("parents", P(C.c_int)),
+                ("sigma", P(C.c_int)), ("dependency", P(C.c_float)), ("betweennessCentrality", P(C.c_float)),
+                ("predecessors", P(Predecessor)), ("iteration", u32), ("processed_nodes", u32),
+                ("num_vertices", u32), ("time_total", C.c_double)]
+
+
+def _seed_mt(a, seed=27491095):
+    """initializeMersenneState (mt19937.c:55-67) into a.mt19937var."""
+    for i in range(624):
+        hi = seed & 0xFFFF0000
+        seed = (69069 * seed + 1) & 0xFFFFFFFF
+        a.mt19937var.mt[i] = hi | ((seed & 0xFFFF0000) >> 16)
+        seed = (69069 * seed + 1) & 0xFFFFFFFF
+    a.mt19937var.mti = 624
+
+
+def _lib_more(gbx, name):
+    import graphblox_gb300._build as b
+
+    b.build_integration()
+    lib = C.CDLL(str(b.PKG / f"libgbx_graphblox_{name}.so"))
+    gtype = GraphCSRdw if name == "dw" else GraphCSRu
+    for fn, st in (("bellmanFordGraphCSR", BellmanFordStats), ("depthFirstSearchGraphCSR", DFSStats),
+                   ("betweennessCentralityGraphCSR", BCStats)):
+        f = getattr(lib, fn)
+        f.restype = P(st)
+        f.argtypes = [P(Arguments), P(gtype)]
+    for fn in ("freeBellmanFordStats", "freeDFSStats", "freeBetweennessCentralityStats"):
+        getattr(lib, fn).argtypes = [C.c_void_p]
+    return lib
+
+
+@pytest.mark.parametrize("name", ["v300_e2730", "v1000_e10000", "v8192_e32768"])
+def test_reference_bf_dfs_bc_directed_weighted(gbx, cuda_device, name):
+    from conftest import load_bf_dfs_bc
+
+    more = load_bf_dfs_bc()
+    fx = load_golden(name)
+    b = Built(fx, "dw", directed=True)
+    lib = _lib_more(gbx, "dw")
+    g = C.byref(b.g)
+    key = f"{name}_dw"
+    a = _args(source=1, pushpull=1)
+    s = lib.bellmanFordGraphCSR(C.byref(a), g)
+    assert s, "NULL BellmanFordStats"
+    np.testing.assert_array_equal(_arr(s.contents.distances, b.V, np.uint32), more[f"{key}_bf_r1"])
+    assert a.iterations == b.V - 1  # bellmanFord.c:449 side effect kept
+    lib.freeBellmanFordStats(s)
+    for r in (0, 1):
+        a = _args(source=r)
+        s = lib.depthFirstSearchGraphCSR(C.byref(a), g)
+        np.testing.assert_array_equal(_arr(s.contents.distances, b.V, np.uint32), more[f"{key}_dfs_r{r}"])
+        np.testing.assert_array_equal(_arr(s.contents.parents, b.V, np.int32), more[f"{key}_dfs_parents_r{r}"])
+        assert s.contents.processed_nodes == int(more[f"{key}_dfs_processed_r{r}"])
+        lib.freeDFSStats(s)
+    roots = more[f"{key}_bc_roots"]
+    a = _args(iterations=len(roots))
+    _seed_mt(a)
+    s = lib.betweennessCentralityGraphCSR(C.byref(a), g)
+    assert s, "NULL BetweennessCentralityStats"
+    bc = _arr(s.contents.betweennessCentrality, b.V, np.float32)
+    np.testing.assert_array_equal(bc.view(np.uint32), more[f"{key}_bc"].view(np.uint32))
+    np.testing.assert_array_equal(_arr(s.contents.distances, b.V, np.uint32), more[f"{key}_bc_distances"])
+    np.testing.assert_array_equal(_arr(s.contents.sigma, b.V, np.int32), more[f"{key}_bc_sigma"])
+    assert (s.contents.iteration, s.contents.processed_nodes) == (len(roots), int(more[f"{key}_bc_processed"]))
+    reached = int(np.count_nonzero(more[f"{key}_bc_distances"] != 0xFFFFFFFF))
+    stack = _arr(s.contents.stack.contents.nodes, b.V, np.uint32)[:reached]
+    assert s.contents.stack.contents.degree == reached
+    lv = more[f"{key}_bc_distances"][stack].astype(np.int64)
+    assert np.all(np.diff(lv) >= 0) and stack[0] == roots[-1]
+    lib.freeBetweennessCentralityStats(s)
+
+
+@pytest.mark.parametrize("name", ["v51_e1021", "v8192_e32768", "graphbrew"])
+def test_reference_bf_dfs_undirected(gbx, cuda_device, name):
+    from conftest import load_bf_dfs_bc
+
+    more = load_bf_dfs_bc()
+    fx = load_golden(name)
+    b = Built(fx, "u", directed=False)
+    lib = _lib_more(gbx, "u")
+    g = C.byref(b.g)
+    key = f"{name}_u"
+    a = _args(source=1, pushpull=1)
+    s = lib.bellmanFordGraphCSR(C.byref(a), g)
+    np.testing.assert_array_equal(_arr(s.contents.distances, b.V, np.uint32), more[f"{key}_bf_r1"])
+    lib.freeBellmanFordStats(s)
+    for r in (0, 1):
+        a = _args(source=r)
+        s = lib.depthFirstSearchGraphCSR(C.byref(a), g)
+        np.testing.assert_array_equal(_arr(s.contents.parents, b.V, np.int32), more[f"{key}_dfs_parents_r{r}"])
+        assert s.contents.processed_nodes == int(more[f"{key}_dfs_processed_r{r}"])
+        lib.freeDFSStats(s)
