@@ -354,6 +354,9 @@ def run_gpu(args):
     if not args.no_batched and (not args.only or "batched" in args.only.split(",")):
         batched = run_batched(args, torch, gbx, _lib, dev, stream, peak)
         batched["multisource"] = run_multisource(args, torch, gbx, _lib, dg, W, dev, stream, peak)
+    more = None
+    if not args.no_more and (not args.only or "more" in args.only.split(",")):
+        more = run_more(args, torch, gbx, dg, g, stream, peak)
     c5 = None
     if args.c5:
         dg.close(), dgs.close(), dgr.close()
@@ -378,13 +381,104 @@ def run_gpu(args):
                    "dag_edges": e_plus, "bfs_roots": N_ROOTS, "sssp_roots": N_SSSP_ROOTS,
                    "pr_iterations": PR_ITERS, "l2": "flushed (256 MiB write) before every kernel",
                    "parallelism": "replicas" if world > 1 else "single GPU", "tuning": tuning},
-        "kernels": per, "batched": batched, "ppr_adjoint": ppr, "c5": c5, "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk,
+        "kernels": per, "batched": batched, "ppr_adjoint": ppr, "more": more, "c5": c5, "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk,
         "gpu_launches": int(launches), "wall_ms_timed_region": round(wall_ms, 3),
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+BC_ROOTS = 20  # the reference's default -i for Brandes (graphConfig.c:59)
+
+
+def run_more(args, torch, gbx, dg, g, stream, peak):
+    """Betweenness centrality, Bellman-Ford and DFS (outside the headline
+    kernel set). Brandes runs the reference's default 20 roots on the RMAT-22
+    graph, one gbx_betweenness call per root so each root's reached edges
+    can be counted; per root the algorithmic bytes are 16 E_r + 12 P + 44 V_r
+    + 12 V (E_r: successor entries of reached vertices, read forward and
+    backward with a level check each; P: DAG edges, which add sigma forward
+    and read sigma and dependency backward; V_r: reached vertices; the three
+    per-root arrays cleared). DFS walks one vertex at a time, so it runs on a
+    small RMAT-16 graph."""
+    from oracle import pyoracle as po
+
+    sp = stream.cuda_stream
+    V = g.num_vertices
+    dev = stream.device
+    deg = torch.from_numpy(g.out_degree.astype(np.int64)).to(dev)
+    roots = gbx.reference_roots(dg, BC_ROOTS)
+    bc = torch.zeros(V, dtype=torch.float32, device=dev)
+    dist = torch.empty(V, dtype=torch.int32, device=dev)
+    sig = torch.empty(V, dtype=torch.int32, device=dev)
+    dep = torch.empty(V, dtype=torch.float32, device=dev)
+    out = dict(centrality=bc, distances=dist, sigma=sig, dependency=dep, stream=sp)
+    gbx.betweenness_centrality(dg, roots=roots[:2], **out)  # warm-up (the successor CSR check runs once)
+    bc.zero_()
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    e_r = p_tot = v_r = 0
+    ms = 0.0
+    for r in roots:
+        a.record(stream)
+        st = gbx.betweenness_centrality(dg, roots=[r], **out)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms += a.elapsed_time(b)
+        reached = dist != -1
+        e_r += int(deg[reached].sum().item())
+        v_r += int(reached.sum().item())
+        p_tot += st.processed_nodes
+    alg = 16 * e_r + 12 * p_tot + 44 * v_r + 12 * V * len(roots)
+    bc_sec = {"roots": len(roots), "ms": round(ms, 3), "ms_per_root": round(ms / len(roots), 3),
+              "gteps": round(2 * e_r / (ms * 1e-3) / 1e9, 3), "achieved_gbs": round(alg / (ms * 1e-3) / 1e9, 1),
+              "frac": round(alg / (ms * 1e-3) / 1e9 / peak, 3), "alg_bytes": int(alg)}
+    if not args.no_cpu_baseline:
+        host = po.HostCSR(V, g.out_degree, g.edges_idx, g.dest, None, g.src)
+        pull = po.HostCSR(V, g.inverse_out_degree, g.inverse_edges_idx, g.inverse_dest)
+        t0 = time.time()
+        po.betweenness(host, roots[:1], pull)
+        bc_sec["cpu_ms_per_root"] = round((time.time() - t0) * 1e3, 1)
+        bc_sec["cpu"] = "oracle/gbx_oracle.c Brandes, one root, one thread (the reference's Brandes loop is serial)"
+    # Bellman-Ford: the SSSP engine plus the parent pass, 4 roots
+    bf_roots = roots[:4]
+    par = torch.empty(V, dtype=torch.int32, device=dev)
+    a.record(stream)
+    for r in bf_roots:
+        gbx.bellman_ford(dg, int(r), distances=dist, parents=par, stream=sp, map_source=False)
+    b.record(stream)
+    torch.cuda.synchronize()
+    bf_sec = {"roots": len(bf_roots), "ms_per_root": round(a.elapsed_time(b) / len(bf_roots), 3),
+              "note": "SSSP engine (distances) + one parent pass over the forward CSR"}
+    # DFS on RMAT-16
+    Vs = 1 << 16
+    src, dst = gbx.generate_rmat(16, Vs * 16, seed=5)
+    gd = gbx.graph_csr_preprocessing(gbx.EdgeList(Vs, src, dst), sort=1, dedup=True, directed=False,
+                                     keep_weights=False)
+    dfs_sec = {}
+    with gbx.DeviceGraph.from_graph_csr(gd, use_weights=False, stream=sp) as dd:
+        nz = [int(v) for v in np.nonzero(gd.out_degree)[0][:4]]
+        gbx.depth_first_search(dd, nz[0], stream=sp)
+        torch.cuda.synchronize()
+        a.record(stream)
+        pops = 0
+        for r in nz:
+            pops += gbx.depth_first_search(dd, r, stream=sp).processed_nodes
+        b.record(stream)
+        torch.cuda.synchronize()
+        dms = a.elapsed_time(b)
+        dfs_sec = {"graph": "rmat16 directed", "roots": len(nz), "ms_per_root": round(dms / len(nz), 3),
+                   "ns_per_pop": round(dms * 1e6 / max(pops, 1), 1)}
+        if not args.no_cpu_baseline:
+            hd = po.HostCSR(Vs, gd.out_degree, gd.edges_idx, gd.dest)
+            t0 = time.time()
+            for r in nz:
+                po.dfs(hd, r)
+            dfs_sec["cpu_ms_per_root"] = round((time.time() - t0) * 1e3 / len(nz), 3)
+    return {"betweenness": bc_sec, "bellman_ford": bf_sec, "dfs": dfs_sec}
 
 
 def run_ppr(args, torch, gbx, dev, stream, peak):
@@ -912,6 +1006,8 @@ def main():
     ap.add_argument("--only", default="", help="comma-separated kernel subset (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-ppr", action="store_true", help="skip the personalised PageRank forward/adjoint section")
+    ap.add_argument("--no-more", action="store_true",
+                    help="skip the betweenness / Bellman-Ford / DFS section")
     ap.add_argument("--no-batched", action="store_true", help="skip the 2,048-graph batched section")
     ap.add_argument("--ppr-scale", type=int, default=PPR_SCALE, help="RMAT scale of the PPR section (20 is the workload)")
     ap.add_argument("--batch-graphs", type=int, default=BATCH_GRAPHS, help="graphs in the batched section (2048)")

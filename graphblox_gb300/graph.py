@@ -652,20 +652,21 @@ def reference_roots(dg: DeviceGraph, n: int, seed: int = BC_SEED) -> np.ndarray:
 
 
 def betweenness_centrality(dg: DeviceGraph, iterations: int = 20, roots=None, centrality=None,
-                           seed: int = BC_SEED, stream=None) -> BetweennessCentralityStats:
+                           seed: int = BC_SEED, distances=None, sigma=None, dependency=None,
+                           stream=None) -> BetweennessCentralityStats:
     """betweennessCentralityBrandesGraphCSR: Brandes from `iterations` roots
     drawn like the reference's (or the given roots), centrality accumulated
     from zero (or into the given array). distances / sigma / dependency are
-    the last root's."""
+    the last root's (host arrays unless given)."""
     if roots is None:
         roots = reference_roots(dg, iterations, seed)
     roots = _u32(roots)
     V = dg.num_vertices
     if centrality is None:
         centrality = np.zeros(V, np.float32)
-    dist = np.zeros(V, np.uint32)
-    sig = np.zeros(V, np.int32)
-    dep = np.zeros(V, np.float32)
+    dist = np.zeros(V, np.uint32) if distances is None else distances
+    sig = np.zeros(V, np.int32) if sigma is None else sigma
+    dep = np.zeros(V, np.float32) if dependency is None else dependency
     r = BcResult()
     call("gbx_betweenness", dg.handle, roots.shape[0], _ptr(roots), _ptr(centrality), _ptr(dist), _ptr(sig),
          _ptr(dep), C.byref(r), stream)
