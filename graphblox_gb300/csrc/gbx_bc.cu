@@ -11,6 +11,8 @@
 #include "gbx_internal.cuh"
 
 #include <cstring>
+#include <string>
+#include <thread>
 #include <vector>
 
 struct gbx_bc_cache {
@@ -158,104 +160,350 @@ static int bc_successors(gbx_graph *g, cudaStream_t s, const uint32_t **off, con
 // ---- betweenness centrality --------------------------------------------------
 namespace gbx {
 
-__global__ void bc_root_kernel(uint32_t root, uint32_t *dist, int32_t *sigma, uint32_t *stack) {
+// Vertices whose successor row is longer than this are "heavy": their rows
+// are cut across the whole grid (forward pushes and backward terms), while
+// a warp handles each lighter row. The packed per-level counter gives every
+// heavy vertex its list slot (high half) and its term-buffer base (low
+// half) in one atomic, so the list is ordered by base.
+constexpr uint32_t kBcHeavy = 1024;
+
+struct BcCounters {
+    unsigned long long next;   // vertices claimed for the next level
+    unsigned long long dag;    // predecessor entries (DAG edges) of this root
+    unsigned long long heavy;  // next level's heavy vertices << 32 | their row total
+    unsigned long long pad;
+};
+
+__device__ __forceinline__ void bc_note_heavy(const uint32_t *off, uint32_t v, BcCounters *c, uint2 *heavy) {
+    const uint32_t d = off[v + 1] - off[v];
+    if (d > kBcHeavy) {
+        const unsigned long long old = atomicAdd(&c->heavy, (1ull << 32) | d);
+        heavy[old >> 32] = make_uint2(v, (uint32_t)old);
+    }
+}
+
+__global__ void bc_root_kernel(const uint32_t *off, uint32_t root, uint32_t *dist, int32_t *sigma,
+                               uint32_t *stack, BcCounters *c, uint2 *heavy) {
     dist[root] = 0;
     sigma[root] = 1;
     stack[0] = root;
+    bc_note_heavy(off, root, c, heavy);
 }
 
-// One level of the forward sweep, pushed over the successor CSR from the
-// level-L vertices level[0..n): a successor v not reached yet is claimed for
-// level L+1 (its claimer appends it to next[]), and every successor at level
-// L+1 adds sigma[u] -- the reference's sigma[v] += sigma[u] over the
+// claim v for level L+1 from a level-L vertex with sigma su; returns true
+// when v is a successor (claimed now or earlier in this level)
+__device__ __forceinline__ bool bc_claim(uint32_t v, uint32_t L, unsigned su, uint32_t *dist, int32_t *sigma,
+                                         bool &fresh) {
+    const uint32_t old = atomicCAS(dist + v, kInfLevel, L + 1);
+    fresh = old == kInfLevel;
+    const bool hit = fresh || old == L + 1;
+    if (hit) atomicAdd(reinterpret_cast<unsigned *>(sigma) + v, su);
+    return hit;
+}
+
+// warp-aggregated append of the lanes' fresh vertices to the next level
+__device__ __forceinline__ void bc_append(bool fresh, uint32_t v, const uint32_t *off, uint32_t *next,
+                                          BcCounters *c, uint2 *heavy_next) {
+    const uint32_t lane = threadIdx.x & 31;
+    const unsigned fm = __ballot_sync(0xffffffffu, fresh);
+    if (!fm) return;
+    uint32_t pos = 0;
+    if (lane == 0) pos = (uint32_t)atomicAdd(&c->next, (unsigned long long)__popc(fm));
+    pos = __shfl_sync(0xffffffffu, pos, 0);
+    if (fresh) {
+        next[pos + __popc(fm & ((1u << lane) - 1u))] = v;
+        bc_note_heavy(off, v, c, heavy_next);
+    }
+}
+
+// One forward level for the light vertices of level[0..n), a warp per
+// vertex, pushed over the successor CSR: a successor v not reached yet is
+// claimed for level L+1 and appended to next[], and every successor at
+// level L+1 adds sigma[u] -- the reference's sigma[v] += sigma[u] over the
 // frontier entries of v's pull row (betweennessCentrality.c:322-336); int
 // addition wraps and is associative, so the order does not matter.
-// counts[0] = size of the next level, counts[1] += those entries.
 __global__ void bc_forward_kernel(const uint32_t *off, const uint32_t *ids, const uint32_t *level, uint32_t n,
-                                  uint32_t L, uint32_t *dist, int32_t *sigma, uint32_t *next,
-                                  unsigned *counts) {
+                                  uint32_t L, uint32_t *dist, int32_t *sigma, uint32_t *next, BcCounters *c,
+                                  uint2 *heavy_next) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     unsigned entries = 0;
     for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
         const uint32_t u = level[i];
-        const unsigned su = (unsigned)sigma[u];
         const uint32_t b = off[u], e = off[u + 1];
+        if (e - b > kBcHeavy) continue;  // bc_forward_heavy_kernel
+        const unsigned su = (unsigned)sigma[u];
         for (uint32_t base = b; base < e; base += 32) {
             const uint32_t j = base + lane;
             bool fresh = false, hit = false;
             uint32_t v = 0;
             if (j < e) {
                 v = ids[j] & kIdMask;
-                const uint32_t old = atomicCAS(dist + v, kInfLevel, L + 1);
-                fresh = old == kInfLevel;
-                hit = fresh || old == L + 1;
-                if (hit) atomicAdd(reinterpret_cast<unsigned *>(sigma) + v, su);
+                hit = bc_claim(v, L, su, dist, sigma, fresh);
             }
-            const unsigned fm = __ballot_sync(0xffffffffu, fresh);
-            const unsigned hm = __ballot_sync(0xffffffffu, hit);
-            if (fm) {
-                uint32_t pos = 0;
-                if (lane == 0) pos = atomicAdd(counts, (unsigned)__popc(fm));
-                pos = __shfl_sync(0xffffffffu, pos, 0);
-                if (fresh) next[pos + __popc(fm & ((1u << lane) - 1u))] = v;
-            }
-            entries += (unsigned)__popc(hm);
+            entries += (unsigned)__popc(__ballot_sync(0xffffffffu, hit));
+            bc_append(fresh, v, off, next, c, heavy_next);
         }
     }
-    if (lane == 0 && entries) atomicAdd(counts + 1, entries);
+    if (lane == 0 && entries) atomicAdd(&c->dag, (unsigned long long)entries);
 }
 
-// One level of the backward sweep. Each level-L vertex v folds the
-// contributions of its successors w at level L+1 in descending id order, as
-// the reference's walk down its stack reaches them
-// (betweennessCentrality.c:432-455): for sigma[w] != 0,
-//   dep = float(double(dep) + (sigma[v] * 1.0 / sigma[w]) * double(1.0f + dep[w]))
-// with every operation rounded on its own (no fused multiply-add); then
-// bc[v] += dep / 2 unless v is the root. A warp loads 32 successors at a
-// time from the end of v's ascending row and folds them lane by lane.
+// last i in [0, n) with heavy[i].y <= e (the bases ascend with i)
+__device__ __forceinline__ uint32_t bc_heavy_owner(const uint2 *heavy, uint32_t n, uint32_t e) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (heavy[mid].y <= e) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// The heavy vertices' rows of one forward level, one entry per thread over
+// the concatenated rows [0, total).
+__global__ void bc_forward_heavy_kernel(const uint32_t *off, const uint32_t *ids, const uint2 *heavy, uint32_t nh,
+                                        uint32_t total, uint32_t L, uint32_t *dist, int32_t *sigma,
+                                        uint32_t *next, BcCounters *c, uint2 *heavy_next) {
+    const uint32_t lane = threadIdx.x & 31;
+    unsigned entries = 0;
+    const uint32_t stride = gridDim.x * blockDim.x;  // a multiple of 32
+    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < total; base += stride) {
+        const uint32_t e = base + lane;
+        bool fresh = false, hit = false;
+        uint32_t v = 0;
+        if (e < total) {
+            const uint2 h = heavy[bc_heavy_owner(heavy, nh, e)];
+            v = ids[off[h.x] + (e - h.y)] & kIdMask;
+            hit = bc_claim(v, L, (unsigned)sigma[h.x], dist, sigma, fresh);
+        }
+        entries += (unsigned)__popc(__ballot_sync(0xffffffffu, hit));
+        bc_append(fresh, v, off, next, c, heavy_next);
+    }
+    if (lane == 0 && entries) atomicAdd(&c->dag, (unsigned long long)entries);
+}
+
+// term of successor w of v (sv = sigma[v]), 0 when w is not a successor:
+// (sigma[v] * 1.0 / sigma[w]) * double(1.0f + dep[w]), each step rounded on
+// its own (betweennessCentrality.c:445-449)
+__device__ __forceinline__ double bc_term(double sv, uint32_t w, uint32_t L, const uint32_t *dist,
+                                          const int32_t *sigma, const float *dep) {
+    if (dist[w] != L + 1) return 0.0;
+    const int32_t sw = sigma[w];
+    if (sw == 0) return 0.0;
+    return __dmul_rn(__ddiv_rn(sv, (double)sw), (double)__fadd_rn(1.0f, dep[w]));
+}
+
+// acc <- float(double(acc) + t) for the lanes' nonzero terms, lane 0 first.
+// A zero term is the identity of this step (acc is never -0), so skipping
+// non-successors keeps the reference's result.
+__device__ __forceinline__ float bc_fold(float acc, double term) {
+    unsigned m = __ballot_sync(0xffffffffu, term != 0.0);
+    while (m) {
+        const int k = __ffs(m) - 1;
+        const double t = __shfl_sync(0xffffffffu, term, k);
+        acc = __double2float_rn(__dadd_rn((double)acc, t));
+        m &= m - 1u;
+    }
+    return acc;
+}
+
+// bc[v] += dep[v] / 2 for every v but the root, one root after another in
+// the caller's order (the reference adds each root's dependencies as its
+// stack unwinds; unreached vertices and the deepest level add +0, which
+// leaves bc unchanged)
+__global__ void bc_accumulate_kernel(float *bc, const float *dep, uint32_t V, uint32_t root) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+        if (v != root) bc[v] = __fadd_rn(bc[v], __fdiv_rn(dep[v], 2.0f));
+}
+
+// One backward level for the light vertices of level[0..n). Each folds its
+// successors at level L+1 in descending id order, as the reference's walk
+// down its stack reaches them (betweennessCentrality.c:432-455), then
+// dep[v] is the result (bc_accumulate_kernel adds it). A warp loads 32
+// entries at a time from the end of v's ascending row.
 __global__ void bc_backward_kernel(const uint32_t *off, const uint32_t *ids, const uint32_t *level, uint32_t n,
-                                   uint32_t L, uint32_t root, const uint32_t *dist, const int32_t *sigma,
-                                   float *dep, float *bc) {
+                                   uint32_t L, const uint32_t *dist, const int32_t *sigma, float *dep) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
         const uint32_t v = level[i];
+        const uint32_t b = off[v], e = off[v + 1];
+        if (e - b > kBcHeavy) continue;  // bc_terms_kernel + bc_fold_heavy_kernel
         const double sv = (double)sigma[v];
-        const uint32_t b = off[v];
         float acc = 0.0f;
-        for (uint32_t top = off[v + 1]; top > b;) {
+        for (uint32_t top = e; top > b;) {
             const uint32_t avail = top - b;
-            bool ok = false;
-            double term = 0.0;
-            if (lane < avail) {
-                const uint32_t w = ids[top - 1 - lane] & kIdMask;
-                if (dist[w] == L + 1) {
-                    const int32_t sw = sigma[w];
-                    if (sw != 0) {
-                        ok = true;
-                        const float one_plus = __fadd_rn(1.0f, dep[w]);
-                        term = __dmul_rn(__ddiv_rn(sv, (double)sw), (double)one_plus);
-                    }
-                }
-            }
-            unsigned m = __ballot_sync(0xffffffffu, ok);
-            while (m) {
-                const int k = __ffs(m) - 1;  // lowest lane = largest successor
-                const double t = __shfl_sync(0xffffffffu, term, k);
-                acc = __double2float_rn(__dadd_rn((double)acc, t));
-                m &= m - 1u;
-            }
+            const double term = lane < avail ? bc_term(sv, ids[top - 1 - lane] & kIdMask, L, dist, sigma, dep) : 0.0;
+            acc = bc_fold(acc, term);
             top = avail > 32u ? top - 32u : b;
         }
-        if (lane == 0) {
-            dep[v] = acc;
-            if (v != root) bc[v] = __fadd_rn(bc[v], __fdiv_rn(acc, 2.0f));
+        if (lane == 0) dep[v] = acc;
+    }
+}
+
+// The heavy vertices' rows of one backward level, one entry per thread over
+// the concatenated rows [0, total): flag[e] = 1 when the entry is a
+// successor with sigma != 0 (the only entries whose terms can be nonzero)...
+__global__ void bc_flags_kernel(const uint32_t *off, const uint32_t *ids, const uint2 *heavy, uint32_t nh,
+                                uint32_t total, uint32_t L, const uint32_t *dist, const int32_t *sigma,
+                                uint32_t *flag) {
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        const uint2 h = heavy[bc_heavy_owner(heavy, nh, e)];
+        const uint32_t w = ids[off[h.x] + (e - h.y)] & kIdMask;
+        flag[e] = (dist[w] == L + 1 && sigma[w] != 0) ? 1u : 0u;
+    }
+}
+
+// ... then their terms, compacted in row order at pos[e] (exclusive scan of flag)
+__global__ void bc_terms_kernel(const uint32_t *off, const uint32_t *ids, const uint2 *heavy, uint32_t nh,
+                                uint32_t total, uint32_t L, const uint32_t *dist, const int32_t *sigma,
+                                const float *dep, const uint32_t *flag, const uint32_t *pos, double *terms) {
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        if (!flag[e]) continue;
+        const uint2 h = heavy[bc_heavy_owner(heavy, nh, e)];
+        terms[pos[e]] = bc_term((double)sigma[h.x], ids[off[h.x] + (e - h.y)] & kIdMask, L, dist, sigma, dep);
+    }
+}
+
+// ... and their folds: a warp per heavy vertex over its compacted terms
+// [pos[base], pos[base + row length]), from the end
+__global__ void bc_fold_heavy_kernel(const uint32_t *off, const uint2 *heavy, uint32_t nh, const uint32_t *pos,
+                                     const double *terms, float *dep) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nh; i += warps) {
+        const uint2 h = heavy[i];
+        const uint32_t b = pos[h.y], e = pos[h.y + (off[h.x + 1] - off[h.x])];
+        float acc = 0.0f;
+        uint32_t top = e;
+        double cur = (top > b && lane < top - b) ? terms[top - 1 - lane] : 0.0;
+        while (top > b) {
+            const uint32_t avail = top - b;
+            const uint32_t nxt = avail > 32u ? top - 32u : b;
+            // load the next chunk before folding this one
+            const double ahead = (nxt > b && lane < nxt - b) ? terms[nxt - 1 - lane] : 0.0;
+            acc = bc_fold(acc, cur);
+            cur = ahead;
+            top = nxt;
         }
+        if (lane == 0) dep[h.x] = acc;
     }
 }
 
 static unsigned warp_grid(uint64_t items) { return grid_sm(items * 32); }
+
+// Per-root working memory of one worker.
+struct BcRoot {
+    DevBuf<uint32_t> dist, stack, flag, pos;
+    DevBuf<int32_t> sigma;
+    DevBuf<float> dep;
+    DevBuf<uint2> heavy;
+    DevBuf<BcCounters> ctr;
+    DevBuf<double> terms;
+    uint32_t levels = 0;
+    unsigned long long dag = 0;
+    void release() {
+        dist.release();
+        stack.release();
+        flag.release();
+        pos.release();
+        sigma.release();
+        dep.release();
+        heavy.release();
+        ctr.release();
+        terms.release();
+    }
+    int alloc(uint32_t V, cudaStream_t s) {
+        GBX_TRY(dist.alloc(V, s));
+        GBX_TRY(stack.alloc(V, s));
+        GBX_TRY(sigma.alloc(V, s));
+        GBX_TRY(dep.alloc(V, s));
+        GBX_TRY(heavy.alloc(V, s));
+        GBX_TRY(ctr.alloc(1, s));
+        return GBX_OK;
+    }
+};
+
+// Brandes for one root on stream s: dist, sigma and dep of every vertex
+// (dep is what bc_accumulate_kernel adds); one host sync per forward level.
+static int bc_one_root(const uint32_t *soff, const uint32_t *sids, uint32_t V, uint32_t root, BcRoot &w,
+                       cudaStream_t s) {
+    uint32_t *dist = w.dist.p, *stack = w.stack.p;
+    int32_t *sigma = w.sigma.p;
+    float *dep = w.dep.p;
+    uint2 *heavy = w.heavy.p;
+    BcCounters *ctr = w.ctr.p;
+    GBX_CUDA(cudaMemsetAsync(dist, 0xFF, (size_t)V * 4, s));
+    GBX_CUDA(cudaMemsetAsync(sigma, 0, (size_t)V * 4, s));
+    GBX_CUDA(cudaMemsetAsync(dep, 0, (size_t)V * 4, s));
+    GBX_CUDA(cudaMemsetAsync(ctr, 0, sizeof(BcCounters), s));
+    bc_root_kernel<<<1, 1, 0, s>>>(soff, root, dist, sigma, stack, ctr, heavy);
+    GBX_LAUNCH_CHECK();
+    BcCounters hc{};
+    GBX_CUDA(cudaMemcpyAsync(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, s));
+    GBX_CUDA(cudaStreamSynchronize(s));
+    std::vector<uint32_t> start{0u, 1u}, hstart{0u, (uint32_t)(hc.heavy >> 32)}, htotal{(uint32_t)hc.heavy};
+    size_t max_total = htotal[0];
+    for (uint32_t L = 0;; ++L) {
+        const uint32_t n = start[L + 1] - start[L];
+        const uint32_t nh = hstart[L + 1] - hstart[L];
+        GBX_CUDA(cudaMemsetAsync(&ctr->next, 0, 8, s));
+        GBX_CUDA(cudaMemsetAsync(&ctr->heavy, 0, 8, s));
+        uint32_t *next = stack + start[L + 1];
+        uint2 *heavy_next = heavy + hstart[L + 1];
+        bc_forward_kernel<<<warp_grid(n), 256, 0, s>>>(soff, sids, stack + start[L], n, L, dist, sigma, next, ctr,
+                                                       heavy_next);
+        GBX_LAUNCH_CHECK();
+        if (nh) {
+            bc_forward_heavy_kernel<<<grid_sm(htotal[L]), 256, 0, s>>>(soff, sids, heavy + hstart[L], nh, htotal[L],
+                                                                       L, dist, sigma, next, ctr, heavy_next);
+            GBX_LAUNCH_CHECK();
+        }
+        GBX_CUDA(cudaMemcpyAsync(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, s));
+        GBX_CUDA(cudaStreamSynchronize(s));
+        if (hc.next == 0) break;
+        start.push_back(start[L + 1] + (uint32_t)hc.next);
+        hstart.push_back(hstart[L + 1] + (uint32_t)(hc.heavy >> 32));
+        htotal.push_back((uint32_t)hc.heavy);
+        if (htotal.back() > max_total) max_total = htotal.back();
+    }
+    w.dag = hc.dag;
+    w.levels = (uint32_t)start.size() - 1;  // levels 0 .. levels-1 are non-empty
+    if (max_total > w.flag.n) {
+        GBX_TRY(w.flag.alloc(max_total, s));
+        GBX_TRY(w.pos.alloc(max_total + 1, s));
+    }
+    for (int L = (int)w.levels - 2; L >= 0; --L) {
+        const uint32_t n = start[L + 1] - start[L];
+        const uint32_t nh = hstart[L + 1] - hstart[L];
+        bc_backward_kernel<<<warp_grid(n), 256, 0, s>>>(soff, sids, stack + start[L], n, (uint32_t)L, dist, sigma,
+                                                        dep);
+        GBX_LAUNCH_CHECK();
+        if (!nh) continue;
+        const uint32_t tot = htotal[L];
+        uint2 *hl = heavy + hstart[L];
+        bc_flags_kernel<<<grid_sm(tot), 256, 0, s>>>(soff, sids, hl, nh, tot, (uint32_t)L, dist, sigma, w.flag.p);
+        GBX_LAUNCH_CHECK();
+        GBX_TRY(exclusive_scan_u32(w.flag.p, w.pos.p, tot, s, w.pos.p + tot));
+        uint32_t nvalid = 0;
+        GBX_CUDA(cudaMemcpyAsync(&nvalid, w.pos.p + tot, 4, cudaMemcpyDeviceToHost, s));
+        GBX_CUDA(cudaStreamSynchronize(s));
+        if (nvalid > w.terms.n) GBX_TRY(w.terms.alloc(nvalid, s));
+        if (nvalid) {
+            bc_terms_kernel<<<grid_sm(tot), 256, 0, s>>>(soff, sids, hl, nh, tot, (uint32_t)L, dist, sigma, dep,
+                                                         w.flag.p, w.pos.p, w.terms.p);
+            GBX_LAUNCH_CHECK();
+        }
+        bc_fold_heavy_kernel<<<warp_grid(nh), 256, 0, s>>>(soff, hl, nh, w.pos.p, w.terms.p, dep);
+        GBX_LAUNCH_CHECK();
+    }
+    GBX_CUDA(cudaStreamSynchronize(s));
+    return GBX_OK;
+}
+
+// Roots in flight at once: each root's longest dependency fold is serial
+// (one hub's successors in order), so independent roots overlap their folds
+// with one another's level sweeps.
+constexpr uint32_t kBcConcurrentRoots = 4;
 
 }  // namespace gbx
 
@@ -284,79 +532,91 @@ extern "C" int gbx_betweenness(gbx_graph *g, uint32_t num_roots, const uint32_t 
         GBX_REQUIRE(hroots[r] < V, GBX_ERR_INVALID, "root %u (%u) out of range [0, %u)", r, hroots[r], V);
     const uint32_t *soff = nullptr, *sids = nullptr;
     GBX_TRY(bc_successors(g, s, &soff, &sids));
-    Scratch sc;
-    const size_t bytes = 4 * Scratch::round_up((size_t)V * 4) + Scratch::round_up(16);
-    GBX_TRY(sc.take(g, bytes, s));
-    uint32_t *dist = sc.carve<uint32_t>(V);
-    int32_t *sigma = sc.carve<int32_t>(V);
-    float *dep = sc.carve<float>(V);
-    uint32_t *stack = sc.carve<uint32_t>(V);
-    unsigned *counts = sc.carve<unsigned>(4);
     OutArray<float> obc;
     GBX_TRY(obc.bind(centrality, V, s));
     if (obc.to_host()) GBX_CUDA(cudaMemcpyAsync(obc.d, centrality, (size_t)V * 4, cudaMemcpyHostToDevice, s));
-    uint32_t levels = 0;
-    std::vector<uint32_t> start;
-    for (uint32_t r = 0; r < num_roots; ++r) {
-        const uint32_t root = hroots[r];
-        GBX_CUDA(cudaMemsetAsync(dist, 0xFF, (size_t)V * 4, s));
-        GBX_CUDA(cudaMemsetAsync(sigma, 0, (size_t)V * 4, s));
-        GBX_CUDA(cudaMemsetAsync(dep, 0, (size_t)V * 4, s));
-        GBX_CUDA(cudaMemsetAsync(counts, 0, 16, s));
-        bc_root_kernel<<<1, 1, 0, s>>>(root, dist, sigma, stack);
-        GBX_LAUNCH_CHECK();
-        start.assign({0u, 1u});
-        for (uint32_t L = 0;; ++L) {
-            const uint32_t n = start[L + 1] - start[L];
-            GBX_CUDA(cudaMemsetAsync(counts, 0, 4, s));
-            bc_forward_kernel<<<warp_grid(n), 256, 0, s>>>(soff, sids, stack + start[L], n, L, dist, sigma,
-                                                           stack + start[L + 1], counts);
-            GBX_LAUNCH_CHECK();
-            unsigned nn = 0;
-            GBX_CUDA(cudaMemcpyAsync(&nn, counts, 4, cudaMemcpyDeviceToHost, s));
-            GBX_CUDA(cudaStreamSynchronize(s));
-            if (nn == 0) break;
-            start.push_back(start[L + 1] + nn);
+    const uint32_t K = num_roots < kBcConcurrentRoots ? num_roots : kBcConcurrentRoots;
+    std::vector<cudaStream_t> ws(K, nullptr);
+    std::vector<BcRoot> work(K);
+    int st = GBX_OK;
+    for (uint32_t k = 0; k < K && st == GBX_OK; ++k) {
+        if (cudaStreamCreateWithFlags(&ws[k], cudaStreamNonBlocking) != cudaSuccess) {
+            (void)cudaGetLastError();
+            set_error("stream creation failed");
+            st = GBX_ERR_CUDA;
         }
-        levels = (uint32_t)start.size() - 1;  // levels 0 .. levels-1 are non-empty
-        for (int L = (int)levels - 2; L >= 0; --L) {
-            const uint32_t n = start[L + 1] - start[L];
-            bc_backward_kernel<<<warp_grid(n), 256, 0, s>>>(soff, sids, stack + start[L], n, (uint32_t)L, root,
-                                                            dist, sigma, dep, obc.d);
-            GBX_LAUNCH_CHECK();
+        if (st == GBX_OK) st = work[k].alloc(V, ws[k]);
+    }
+    // the caller's pending work on s (the centrality upload) before the workers
+    if (st == GBX_OK && cudaStreamSynchronize(s) != cudaSuccess) st = GBX_ERR_CUDA;
+    const int device = g->device;
+    for (uint32_t w0 = 0; w0 < num_roots && st == GBX_OK; w0 += K) {
+        const uint32_t nw = num_roots - w0 < K ? num_roots - w0 : K;
+        std::vector<int> rs(nw, GBX_OK);
+        std::vector<std::string> msg(nw);
+        std::vector<std::thread> th;
+        for (uint32_t k = 0; k < nw; ++k)
+            th.emplace_back([&, k] {
+                cudaSetDevice(device);
+                rs[k] = bc_one_root(soff, sids, V, hroots[w0 + k], work[k], ws[k]);
+                if (rs[k] != GBX_OK) msg[k] = gbx_last_error();  // the message is per thread
+            });
+        for (auto &t : th) t.join();
+        for (uint32_t k = 0; k < nw; ++k)
+            if (rs[k] != GBX_OK && st == GBX_OK) {
+                st = rs[k];
+                set_error("betweenness root %u: %s", hroots[w0 + k], msg[k].c_str());
+            }
+        if (st != GBX_OK) break;
+        for (uint32_t k = 0; k < nw && st == GBX_OK; ++k) {
+            bc_accumulate_kernel<<<grid_sm(V), 256, 0, s>>>(obc.d, work[k].dep.p, V, hroots[w0 + k]);
+            note_launch();
+            if (cudaGetLastError() != cudaSuccess) st = GBX_ERR_CUDA;
+        }
+        if (st == GBX_OK && cudaStreamSynchronize(s) != cudaSuccess) st = GBX_ERR_CUDA;
+    }
+    const uint32_t last = num_roots ? (num_roots - 1) % (K ? K : 1) : 0;
+    if (st == GBX_OK) st = obc.finish(s);
+    if (st == GBX_OK && num_roots) {
+        BcRoot &w = work[last];
+        if (distances) {
+            OutArray<uint32_t> o;
+            if ((st = o.bind(distances, V, s)) == GBX_OK) {
+                cudaMemcpyAsync(o.d, w.dist.p, (size_t)V * 4, cudaMemcpyDeviceToDevice, s);
+                st = o.finish(s);
+                cudaStreamSynchronize(s);
+            }
+        }
+        if (st == GBX_OK && sigma_out) {
+            OutArray<int32_t> o;
+            if ((st = o.bind(sigma_out, V, s)) == GBX_OK) {
+                cudaMemcpyAsync(o.d, w.sigma.p, (size_t)V * 4, cudaMemcpyDeviceToDevice, s);
+                st = o.finish(s);
+                cudaStreamSynchronize(s);
+            }
+        }
+        if (st == GBX_OK && dependency) {
+            OutArray<float> o;
+            if ((st = o.bind(dependency, V, s)) == GBX_OK) {
+                cudaMemcpyAsync(o.d, w.dep.p, (size_t)V * 4, cudaMemcpyDeviceToDevice, s);
+                st = o.finish(s);
+                cudaStreamSynchronize(s);
+            }
         }
     }
-    GBX_TRY(obc.finish(s));
-    unsigned processed = 0;
-    if (num_roots) GBX_CUDA(cudaMemcpyAsync(&processed, counts + 1, 4, cudaMemcpyDeviceToHost, s));
-    if (num_roots && distances) {
-        OutArray<uint32_t> o;
-        GBX_TRY(o.bind(distances, V, s));
-        GBX_CUDA(cudaMemcpyAsync(o.d, dist, (size_t)V * 4, cudaMemcpyDeviceToDevice, s));
-        GBX_TRY(o.finish(s));
-        GBX_CUDA(cudaStreamSynchronize(s));
-    }
-    if (num_roots && sigma_out) {
-        OutArray<int32_t> o;
-        GBX_TRY(o.bind(sigma_out, V, s));
-        GBX_CUDA(cudaMemcpyAsync(o.d, sigma, (size_t)V * 4, cudaMemcpyDeviceToDevice, s));
-        GBX_TRY(o.finish(s));
-        GBX_CUDA(cudaStreamSynchronize(s));
-    }
-    if (num_roots && dependency) {
-        OutArray<float> o;
-        GBX_TRY(o.bind(dependency, V, s));
-        GBX_CUDA(cudaMemcpyAsync(o.d, dep, (size_t)V * 4, cudaMemcpyDeviceToDevice, s));
-        GBX_TRY(o.finish(s));
-        GBX_CUDA(cudaStreamSynchronize(s));
-    }
-    GBX_CUDA(cudaStreamSynchronize(s));
-    if (result) {
+    if (cudaStreamSynchronize(s) != cudaSuccess && st == GBX_OK) st = GBX_ERR_CUDA;
+    if (st == GBX_OK && result) {
         result->iteration = num_roots;
-        result->processed_nodes = processed;
-        result->levels = num_roots ? levels : 0;
+        result->processed_nodes = num_roots ? (uint32_t)work[last].dag : 0;
+        result->levels = num_roots ? work[last].levels : 0;
     }
-    return GBX_OK;
+    for (uint32_t k = 0; k < K; ++k) {
+        if (ws[k]) cudaStreamSynchronize(ws[k]);
+        work[k].release();  // frees on ws[k], before the stream goes
+    }
+    for (uint32_t k = 0; k < K; ++k)
+        if (ws[k]) cudaStreamDestroy(ws[k]);
+    return st;
 }
 
 // ---- Bellman-Ford and DFS -----------------------------------------------------
