@@ -626,19 +626,29 @@ namespace gbx {
 // (uint32)((float)dist[u] + w) == dist[v]. The reference keeps whichever
 // relaxation wrote last (bellmanFord.c:134-227), so its parents depend on
 // the schedule; every such u is a valid parent and the smallest is the
-// deterministic choice. par[] starts at UINT32_MAX (unreached).
+// deterministic choice. par[] starts at UINT32_MAX (unreached). Each thread
+// takes kBfEdges consecutive edges (hub rows spread over many threads):
+// one binary search for the first edge's source, then a walk forward.
+constexpr uint32_t kBfEdges = 16;
+
 __global__ void bf_parents_kernel(const uint32_t *off, const uint32_t *dest, const float *w, uint32_t V,
-                                  const uint32_t *dist, uint32_t source, uint32_t *par) {
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < V; u += warps) {
-        const uint32_t du = dist[u];
-        if (du == kSsspInf) continue;
-        const float fu = __uint2float_rn(du);
-        for (uint32_t j = off[u] + lane; j < off[u + 1]; j += 32) {
+                                  uint32_t E, const uint32_t *dist, uint32_t source, uint32_t *par) {
+    const uint32_t chunks = (E + kBfEdges - 1) / kBfEdges;
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < chunks; c += gridDim.x * blockDim.x) {
+        const uint32_t e0 = c * kBfEdges, e1 = e0 + kBfEdges < E ? e0 + kBfEdges : E;
+        uint32_t lo = 0, hi = V;  // last u with off[u] <= e0
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (off[mid] <= e0) lo = mid; else hi = mid;
+        }
+        uint32_t u = lo, uend = off[u + 1];
+        for (uint32_t j = e0; j < e1; ++j) {
+            while (j >= uend) uend = off[++u + 1];
+            const uint32_t du = dist[u];
+            if (du == kSsspInf) continue;
             const uint32_t v = dest[j] & kIdMask;
             const float wt = w ? w[j] : 1.0f;
-            if (v != source && __float2uint_rz(__fadd_rn(fu, wt)) == dist[v]) atomicMin(par + v, u);
+            if (v != source && __float2uint_rz(__fadd_rn(__uint2float_rn(du), wt)) == dist[v]) atomicMin(par + v, u);
         }
     }
 }
@@ -705,7 +715,8 @@ extern "C" int gbx_bellman_ford(gbx_graph *g, uint32_t source, uint32_t *distanc
         OutArray<uint32_t> op;
         GBX_TRY(op.bind(parents, V, s));
         GBX_CUDA(cudaMemsetAsync(op.d, 0xFF, (size_t)V * 4, s));
-        bf_parents_kernel<<<warp_grid(V), 256, 0, s>>>(g->offsets, g->dest, g->weight, V, od.d, source, op.d);
+        bf_parents_kernel<<<grid_sm(((uint64_t)g->E + kBfEdges - 1) / kBfEdges), 256, 0, s>>>(
+            g->offsets, g->dest, g->weight, V, g->E, od.d, source, op.d);
         GBX_LAUNCH_CHECK();
         set_u32_kernel<<<1, 1, 0, s>>>(op.d, source, source);
         GBX_LAUNCH_CHECK();

@@ -121,7 +121,7 @@ def test_ppr_autograd_function(gbx, cuda_device, sub2048):
         direct = gg.ppr_adjoint(dg, w, R.detach().cpu().numpy(), W, D, TOL)
     np.testing.assert_array_equal(wt.grad.cpu().numpy(), direct.grad_weights)
     np.testing.assert_array_equal(Tt.grad.cpu().numpy(), direct.grad_teleport)
-    assert float(loss) == pytest.approx(direct.loss, rel=1e-12)
+    assert float(loss.detach()) == pytest.approx(direct.loss, rel=1e-12)
 
 
 @pytest.mark.parametrize("K", [32, 128, 256])
