@@ -10,7 +10,10 @@
 // pull CSR built here once per graph by a stable sort on the neighbour id.
 #include "gbx_internal.cuh"
 
+#include <atomic>
+#include <condition_variable>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -503,7 +506,7 @@ static int bc_one_root(const uint32_t *soff, const uint32_t *sids, uint32_t V, u
 // Roots in flight at once: each root's longest dependency fold is serial
 // (one hub's successors in order), so independent roots overlap their folds
 // with one another's level sweeps.
-constexpr uint32_t kBcConcurrentRoots = 4;
+constexpr uint32_t kBcConcurrentRoots = 8;
 
 }  // namespace gbx
 
@@ -549,33 +552,71 @@ extern "C" int gbx_betweenness(gbx_graph *g, uint32_t num_roots, const uint32_t 
     }
     // the caller's pending work on s (the centrality upload) before the workers
     if (st == GBX_OK && cudaStreamSynchronize(s) != cudaSuccess) st = GBX_ERR_CUDA;
+    // Workers take roots in order as they free up; each root's dependencies
+    // are added to bc in root order: a worker waits for the previous root's
+    // turn (host token) and makes its add wait for the previous add (event).
     const int device = g->device;
-    for (uint32_t w0 = 0; w0 < num_roots && st == GBX_OK; w0 += K) {
-        const uint32_t nw = num_roots - w0 < K ? num_roots - w0 : K;
-        std::vector<int> rs(nw, GBX_OK);
-        std::vector<std::string> msg(nw);
-        std::vector<std::thread> th;
-        for (uint32_t k = 0; k < nw; ++k)
-            th.emplace_back([&, k] {
-                cudaSetDevice(device);
-                rs[k] = bc_one_root(soff, sids, V, hroots[w0 + k], work[k], ws[k]);
-                if (rs[k] != GBX_OK) msg[k] = gbx_last_error();  // the message is per thread
-            });
-        for (auto &t : th) t.join();
-        for (uint32_t k = 0; k < nw; ++k)
-            if (rs[k] != GBX_OK && st == GBX_OK) {
-                st = rs[k];
-                set_error("betweenness root %u: %s", hroots[w0 + k], msg[k].c_str());
-            }
-        if (st != GBX_OK) break;
-        for (uint32_t k = 0; k < nw && st == GBX_OK; ++k) {
-            bc_accumulate_kernel<<<grid_sm(V), 256, 0, s>>>(obc.d, work[k].dep.p, V, hroots[w0 + k]);
-            note_launch();
-            if (cudaGetLastError() != cudaSuccess) st = GBX_ERR_CUDA;
+    std::vector<cudaEvent_t> ev(K, nullptr);
+    for (uint32_t k = 0; k < K && st == GBX_OK; ++k)
+        if (cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming) != cudaSuccess) {
+            (void)cudaGetLastError();
+            set_error("event creation failed");
+            st = GBX_ERR_CUDA;
         }
-        if (st == GBX_OK && cudaStreamSynchronize(s) != cudaSuccess) st = GBX_ERR_CUDA;
+    std::mutex mu;
+    std::condition_variable turn;
+    uint32_t next_add = 0;               // root whose add goes next
+    cudaEvent_t prev_add = nullptr;      // event after the previous root's add
+    std::atomic<uint32_t> next_root{0};
+    std::atomic<bool> failed{st != GBX_OK};
+    std::vector<int> rs(K, GBX_OK);
+    std::vector<std::string> msg(K);
+    std::vector<uint32_t> last_of(K, UINT32_MAX);
+    std::vector<std::thread> th;
+    for (uint32_t k = 0; k < K && st == GBX_OK; ++k)
+        th.emplace_back([&, k] {
+            cudaSetDevice(device);
+            for (;;) {
+                const uint32_t r = next_root.fetch_add(1);
+                if (r >= num_roots) break;
+                int rc = failed.load() ? GBX_ERR_CUDA : bc_one_root(soff, sids, V, hroots[r], work[k], ws[k]);
+                std::unique_lock<std::mutex> lk(mu);
+                turn.wait(lk, [&] { return next_add == r; });
+                if (rc == GBX_OK && !failed.load()) {
+                    if (prev_add) cudaStreamWaitEvent(ws[k], prev_add, 0);
+                    bc_accumulate_kernel<<<grid_sm(V), 256, 0, ws[k]>>>(obc.d, work[k].dep.p, V, hroots[r]);
+                    note_launch();
+                    if (cudaGetLastError() != cudaSuccess || cudaEventRecord(ev[k], ws[k]) != cudaSuccess) {
+                        set_error("betweenness accumulation launch failed");
+                        rc = GBX_ERR_CUDA;
+                    }
+                    prev_add = ev[k];
+                }
+                if (rc != GBX_OK && rs[k] == GBX_OK) {
+                    rs[k] = rc;
+                    msg[k] = gbx_last_error();  // the message is per thread
+                    failed.store(true);
+                }
+                last_of[k] = r;
+                next_add = r + 1;
+                lk.unlock();
+                turn.notify_all();
+                if (rc != GBX_OK) break;
+            }
+        });
+    for (auto &t : th) t.join();
+    for (uint32_t k = 0; k < K; ++k) {
+        if (ws[k] && cudaStreamSynchronize(ws[k]) != cudaSuccess && st == GBX_OK) st = GBX_ERR_CUDA;
+        if (rs[k] != GBX_OK && st == GBX_OK) {
+            st = rs[k];
+            set_error("betweenness: %s", msg[k].c_str());
+        }
     }
-    const uint32_t last = num_roots ? (num_roots - 1) % (K ? K : 1) : 0;
+    for (uint32_t k = 0; k < K; ++k)
+        if (ev[k]) cudaEventDestroy(ev[k]);
+    uint32_t last = 0;  // the worker that ran the last root holds its state
+    for (uint32_t k = 0; k < K; ++k)
+        if (num_roots && last_of[k] == num_roots - 1) last = k;
     if (st == GBX_OK) st = obc.finish(s);
     if (st == GBX_OK && num_roots) {
         BcRoot &w = work[last];
