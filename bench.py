@@ -31,6 +31,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -117,7 +118,8 @@ def dag_stats(gsr):
 class ClockSampler:
     def __init__(self):
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        # raw nvidia-smi samples; their summary goes into the JSON line
+        self.path = Path(tempfile.gettempdir()) / f"gbx_clocks_{os.getpid()}.csv"
 
     def start(self):
         try:
