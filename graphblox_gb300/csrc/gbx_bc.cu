@@ -698,37 +698,68 @@ __global__ void set_u32_kernel(uint32_t *a, uint32_t i, uint32_t value) { a[i] =
 
 // The reference's stack DFS (DFS.c:156-205) run by one warp, since each pop
 // depends on every earlier one: pop v, scan its row in CSR order 32 entries
-// at a time; a neighbour whose parent is still negative is taken by the
-// first lane holding it (a repeated neighbour in the same chunk resolves to
-// its first copy, as in the sequential loop), gets parent v and distance
-// dist[v] + 1 and is pushed in row order. A vertex is pushed at most once,
-// so the stack never holds more than V entries and the loop ends after at
-// most V pops.
-__global__ void dfs_warp_kernel(const uint32_t *off, const uint32_t *dest, uint32_t source, uint32_t *dist,
-                                int32_t *par, uint32_t *stack, uint32_t *processed) {
+// at a time; a neighbour not visited yet is taken by the first lane holding
+// it (a repeated neighbour in the same chunk resolves to its first copy, as
+// in the sequential loop), gets parent v and distance dist[v] + 1 and is
+// pushed in row order. A vertex is pushed at most once, so the stacks never
+// hold more than V entries and the loop ends after at most V pops.
+// Each pop is a chain of dependent loads, so the kernel keeps that chain
+// short: the visited set is a shared-memory bitmap when V fits (else the
+// parents array is read), distances travel on the stack beside the ids, and
+// the entry on top after a push is kept in registers.
+constexpr uint32_t kDfsSmemBits = 1536u * 1024u;  // 192 KB of bitmap
+
+__global__ void dfs_warp_kernel(const uint32_t *off, const uint32_t *dest, uint32_t V, uint32_t source,
+                                uint32_t *dist, int32_t *par, uint32_t *stack, uint32_t *stack_dist,
+                                uint32_t *processed) {
+    extern __shared__ uint32_t seen[];
     const uint32_t lane = threadIdx.x & 31;
-    if (lane == 0) {
-        stack[0] = source;
-        par[source] = (int32_t)source;
+    const bool in_smem = V <= kDfsSmemBits;
+    if (in_smem) {
+        for (uint32_t i = lane; i < (V + 31) / 32; i += 32) seen[i] = 0;
+        __syncwarp();
+        if (lane == 0) seen[source >> 5] |= 1u << (source & 31);
     }
+    if (lane == 0) par[source] = (int32_t)source;
     __syncwarp();
     uint32_t top = 1, pops = 0;
+    uint32_t cv = source, cd = 0;  // the top entry, valid when cached
+    bool cached = true;
     while (top > 0) {
-        const uint32_t v = stack[--top];
+        uint32_t v, d;
+        if (cached) {
+            v = cv;
+            d = cd;
+        } else {
+            v = stack[top - 1];
+            d = stack_dist[top - 1];
+        }
+        --top;
+        cached = false;
         ++pops;
-        const uint32_t dv = dist[v] + 1u;
         const uint32_t e = off[v + 1];
         for (uint32_t base = off[v]; base < e; base += 32) {
             const uint32_t j = base + lane;
             const uint32_t u = j < e ? (dest[j] & kIdMask) : 0xFFFFFFFFu;
-            bool take = j < e && par[u] < 0;
+            bool take = false;
+            if (j < e) take = in_smem ? !((seen[u >> 5] >> (u & 31)) & 1u) : par[u] < 0;
             const unsigned peers = __match_any_sync(0xffffffffu, u);
             take = take && lane == (uint32_t)(__ffs(peers) - 1);
             const unsigned m = __ballot_sync(0xffffffffu, take);
             if (take) {
+                if (in_smem) atomicOr(&seen[u >> 5], 1u << (u & 31));
                 par[u] = (int32_t)v;
-                dist[u] = dv;
-                stack[top + __popc(m & ((1u << lane) - 1u))] = u;
+                dist[u] = d + 1u;
+                const uint32_t at = top + __popc(m & ((1u << lane) - 1u));
+                stack[at] = u;
+                stack_dist[at] = d + 1u;
+            }
+            if (m) {
+                // the last pushed entry (highest lane) is the new top
+                const int hi = 31 - __clz(m);
+                cv = __shfl_sync(0xffffffffu, u, hi);
+                cd = d + 1u;
+                cached = true;
             }
             top += (uint32_t)__popc(m);
             __syncwarp();
@@ -783,12 +814,16 @@ extern "C" int gbx_dfs(gbx_graph *g, uint32_t source, uint32_t *distances, int32
     OutArray<int32_t> op;
     GBX_TRY(od.bind(distances, V, s));
     GBX_TRY(op.bind(parents, V, s));
-    DevBuf<uint32_t> stack, pops;
+    DevBuf<uint32_t> stack, stack_dist, pops;
     GBX_TRY(stack.alloc((size_t)V + 1, s));
+    GBX_TRY(stack_dist.alloc((size_t)V + 1, s));
     GBX_TRY(pops.alloc(1, s));
     GBX_CUDA(cudaMemsetAsync(od.d, 0, (size_t)V * 4, s));
     GBX_CUDA(cudaMemsetAsync(op.d, 0xFF, (size_t)V * 4, s));
-    dfs_warp_kernel<<<1, 32, 0, s>>>(g->offsets, g->dest, source, od.d, op.d, stack.p, pops.p);
+    const size_t smem = V <= kDfsSmemBits ? (size_t)((V + 31) / 32) * 4 : 0;
+    if (smem > 48 * 1024)
+        GBX_CUDA(cudaFuncSetAttribute(dfs_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dfs_warp_kernel<<<1, 32, smem, s>>>(g->offsets, g->dest, V, source, od.d, op.d, stack.p, stack_dist.p, pops.p);
     GBX_LAUNCH_CHECK();
     uint32_t hp = 0;
     GBX_CUDA(cudaMemcpyAsync(&hp, pops.p, 4, cudaMemcpyDeviceToHost, s));
