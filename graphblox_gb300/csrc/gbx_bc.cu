@@ -569,8 +569,18 @@ extern "C" int gbx_betweenness(gbx_graph *g, uint32_t num_roots, const uint32_t 
     cudaEvent_t prev_add = nullptr;      // event after the previous root's add
     std::atomic<uint32_t> next_root{0};
     std::atomic<bool> failed{st != GBX_OK};
-    std::vector<int> rs(K, GBX_OK);
-    std::vector<std::string> msg(K);
+    // the first failure (in time) is the one reported; workers that give up
+    // their roots after it record nothing
+    int first_rc = GBX_OK;
+    std::string first_msg;
+    constexpr int kSkipped = 1;
+    auto record_failure = [&](int rc) {  // caller holds mu
+        if (first_rc == GBX_OK) {
+            first_rc = rc;
+            first_msg = gbx_last_error();  // the message is per thread
+        }
+        failed.store(true);
+    };
     std::vector<uint32_t> last_of(K, UINT32_MAX);
     std::vector<std::thread> th;
     for (uint32_t k = 0; k < K && st == GBX_OK; ++k)
@@ -579,8 +589,9 @@ extern "C" int gbx_betweenness(gbx_graph *g, uint32_t num_roots, const uint32_t 
             for (;;) {
                 const uint32_t r = next_root.fetch_add(1);
                 if (r >= num_roots) break;
-                int rc = failed.load() ? GBX_ERR_CUDA : bc_one_root(soff, sids, V, hroots[r], work[k], ws[k]);
+                int rc = failed.load() ? kSkipped : bc_one_root(soff, sids, V, hroots[r], work[k], ws[k]);
                 std::unique_lock<std::mutex> lk(mu);
+                if (rc != GBX_OK && rc != kSkipped) record_failure(rc);
                 turn.wait(lk, [&] { return next_add == r; });
                 if (rc == GBX_OK && !failed.load()) {
                     if (prev_add) cudaStreamWaitEvent(ws[k], prev_add, 0);
@@ -589,13 +600,9 @@ extern "C" int gbx_betweenness(gbx_graph *g, uint32_t num_roots, const uint32_t 
                     if (cudaGetLastError() != cudaSuccess || cudaEventRecord(ev[k], ws[k]) != cudaSuccess) {
                         set_error("betweenness accumulation launch failed");
                         rc = GBX_ERR_CUDA;
+                        record_failure(rc);
                     }
                     prev_add = ev[k];
-                }
-                if (rc != GBX_OK && rs[k] == GBX_OK) {
-                    rs[k] = rc;
-                    msg[k] = gbx_last_error();  // the message is per thread
-                    failed.store(true);
                 }
                 last_of[k] = r;
                 next_add = r + 1;
@@ -605,13 +612,15 @@ extern "C" int gbx_betweenness(gbx_graph *g, uint32_t num_roots, const uint32_t 
             }
         });
     for (auto &t : th) t.join();
-    for (uint32_t k = 0; k < K; ++k) {
-        if (ws[k] && cudaStreamSynchronize(ws[k]) != cudaSuccess && st == GBX_OK) st = GBX_ERR_CUDA;
-        if (rs[k] != GBX_OK && st == GBX_OK) {
-            st = rs[k];
-            set_error("betweenness: %s", msg[k].c_str());
-        }
+    if (first_rc != GBX_OK && st == GBX_OK) {
+        st = first_rc;
+        set_error("betweenness: %s", first_msg.c_str());
     }
+    for (uint32_t k = 0; k < K; ++k)
+        if (ws[k] && cudaStreamSynchronize(ws[k]) != cudaSuccess && st == GBX_OK) {
+            st = GBX_ERR_CUDA;
+            set_error("betweenness: a worker stream failed");
+        }
     for (uint32_t k = 0; k < K; ++k)
         if (ev[k]) cudaEventDestroy(ev[k]);
     uint32_t last = 0;  // the worker that ran the last root holds its state

@@ -1,24 +1,27 @@
 // Pull PageRank for callers that cannot allocate device memory.
 //
-// Some callers cannot call cudaMalloc: code running while a CUDA graph is
-// being captured on their stream, allocators that own all device memory, or
-// hosts that must not grow the CUDA heap after start-up. gbx_pagerank_pull
-// allocates its working buffers (stream-ordered) and builds a per-graph
-// degree plan; this variant allocates nothing. Its working memory is one
-// file-scope __device__ array, g_pr_scratch, sized for graphs of at most
-// kNoAllocMaxVertices vertices and kNoAllocMaxIterations iterations
+// Some callers cannot call cudaMalloc: hosts whose own allocator has taken
+// all device memory at start-up (a serving process or a framework's caching
+// pool), and real-time hosts that must not grow the CUDA heap once they are
+// running, since an allocation may block or fail at any time there.
+// gbx_pagerank_pull allocates its working buffers (stream-ordered) and builds
+// a per-graph degree plan; this variant allocates nothing. Its working memory
+// is one file-scope __device__ array, g_pr_scratch, sized for graphs of at
+// most kNoAllocMaxVertices vertices and kNoAllocMaxIterations iterations
 // (about 64 MiB, held by every GPU that loads the library until the process
 // exits). The caller passes the pull CSR, the out-degrees and the output, all
 // in device memory.
 //
 // In host code the name g_pr_scratch is only a host-side stand-in for the
 // device array; its device address is looked up with cudaGetSymbolAddress
-// once per device, on the first call made with that device current. That
-// first call therefore does the set-up and should come before any stream
-// capture. Every call reuses the same array and keeps the previous call's
-// contents; the iteration counters are cleared at the start of each call.
-// Calls that overlap on the GPU (two streams, or two host threads) race on
-// the array: serialise them.
+// once per device, on the first call made with that device current (a lookup
+// that failed is retried by the next call). That first call therefore does
+// the set-up and should come before any stream capture. Every call reuses
+// the same array and keeps the previous call's contents; the iteration
+// counters are cleared at the start of each call. Calls that overlap on the
+// GPU (two streams, or two host threads) race on the array: serialise them.
+// With a non-NULL result the call copies the result to the host and
+// synchronises the stream before it returns.
 //
 // The computation is the reference's pageRankPullGraphCSR recurrence
 // (pageRank.c:245-368), as in gbx_pagerank_pull, with a plan-free row mapping:
@@ -54,12 +57,9 @@ struct NaScratch {
 
 static __device__ __align__(256) NaScratch g_pr_scratch;
 
-struct NaDevice {
-    std::once_flag once;
-    NaScratch *ptr = nullptr;
-    cudaError_t err = cudaSuccess;
-};
-static NaDevice g_na_dev[64];
+// Device address of g_pr_scratch per device; only a successful lookup is kept.
+static std::mutex g_na_mutex;
+static NaScratch *g_na_ptr[64] = {};
 
 __device__ __forceinline__ float na_warp_sum(float v) {
 #pragma unroll
@@ -206,20 +206,21 @@ __global__ void na_finish_kernel(NaScratch *sc, uint32_t max_it, uint32_t can_st
     }
 }
 
-// Device address of g_pr_scratch on the current device (set-up on first use).
+// Device address of g_pr_scratch on the current device (set-up on first use;
+// a failed lookup leaves the slot empty, so a later call tries again).
 int scratch_for_current_device(NaScratch **out) {
     int dev = 0;
     GBX_CUDA(cudaGetDevice(&dev));
     GBX_REQUIRE(dev >= 0 && dev < 64, GBX_ERR_INVALID, "device index %d out of range", dev);
-    NaDevice &d = g_na_dev[dev];
-    std::call_once(d.once, [&d]() {
+    std::lock_guard<std::mutex> lock(g_na_mutex);
+    if (!g_na_ptr[dev]) {
         void *p = nullptr;
-        d.err = cudaGetSymbolAddress(&p, g_pr_scratch);
-        d.ptr = (NaScratch *)p;
-    });
-    if (d.err != cudaSuccess) return cuda_fail(d.err, "cudaGetSymbolAddress(g_pr_scratch)", __FILE__, __LINE__);
-    GBX_REQUIRE(d.ptr != nullptr, GBX_ERR_CUDA, "no device address for the PageRank scratch array");
-    *out = d.ptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_pr_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_pr_scratch)", __FILE__, __LINE__);
+        GBX_REQUIRE(p != nullptr, GBX_ERR_CUDA, "no device address for the PageRank scratch array");
+        g_na_ptr[dev] = (NaScratch *)p;
+    }
+    *out = g_na_ptr[dev];
     return GBX_OK;
 }
 

@@ -168,16 +168,17 @@ int gbx_pagerank_pull(gbx_graph *g, uint32_t max_iterations, double epsilon, flo
                       gbx_pr_result *result, void *stream);
 
 /* Pull PageRank that allocates no memory. No counterpart in the reference.
- * For callers that cannot call cudaMalloc (inside stream capture, under an
- * allocator that owns all device memory, or after start-up): the working
- * memory is a fixed file-scope device array (about 64 MiB per GPU that loads
- * the library, held until exit), so num_vertices <= 4,194,304 and
- * max_iterations <= 1024; larger sizes fail with GBX_ERR_INVALID.
- * pull_offsets (num_vertices+1), pull_src, out_degree and ranks must be
- * device memory. The first call on a device looks up the array's address
- * (make it before any stream capture). All calls share the array: calls
- * that overlap on the GPU race, so serialise them. Same recurrence and
- * result as gbx_pagerank_pull. */
+ * For callers that cannot call cudaMalloc: hosts whose own allocator took all
+ * device memory at start-up, and real-time hosts that must not grow the CUDA
+ * heap while they run. The working memory is a fixed file-scope device array
+ * (about 64 MiB per GPU that loads the library, held until exit), so
+ * num_vertices <= 4,194,304 and max_iterations <= 1024; larger sizes fail
+ * with GBX_ERR_INVALID. pull_offsets (num_vertices+1), pull_src, out_degree
+ * and ranks must be device memory. The first call on a device looks up the
+ * array's address (make it before any stream capture). All calls share the
+ * array: calls that overlap on the GPU race, so serialise them. A non-NULL
+ * result is copied to the host and the stream synchronised before return.
+ * Same recurrence and result as gbx_pagerank_pull. */
 int gbx_pagerank_pull_noalloc(uint32_t num_vertices, const uint32_t *pull_offsets,
                               const uint32_t *pull_src, const uint32_t *out_degree,
                               uint32_t max_iterations, double epsilon, float *ranks,
