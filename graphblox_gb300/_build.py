@@ -124,12 +124,21 @@ def build_oracle(verbose: bool = False) -> Path:
     return ROOT / "oracle" / "liboracle.so"
 
 
-def build_reference(verbose: bool = False) -> bool:
-    """Compile the reference host into oracle/_ref/ when its sources are present."""
-    ref = Path("/root/reference/01_host/src")
-    if not ref.exists():
+def build_reference(verbose: bool = False, reference_root: str | None = None) -> bool:
+    """Compile the reference host into oracle/_ref/ when its sources are present.
+
+    The tree is `reference_root`, else $GBX_REFERENCE_ROOT, else the recipe's
+    own default (oracle/build_ref.sh); the recipe exits 2 when no tree is there
+    (the GPU host has none), which is not an error."""
+    cmd = ["bash", str(ROOT / "oracle" / "build_ref.sh")]
+    root = reference_root or os.environ.get("GBX_REFERENCE_ROOT")
+    if root:
+        cmd.append(root)
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode == 2:
         return False
-    _run(["bash", str(ROOT / "oracle" / "build_ref.sh")])
+    if res.returncode != 0:
+        raise RuntimeError(f"reference build failed ({res.returncode}): {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
     return True
 
 

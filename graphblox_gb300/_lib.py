@@ -74,6 +74,7 @@ SIGNATURES = {
     "gbx_dfs": (C.c_int, [vp, u32, vp, vp, C.POINTER(u32), vp]),
     "gbx_betweenness": (C.c_int, [vp, u32, vp, vp, vp, vp, vp, C.POINTER(BcResult), vp]),
     "gbx_reference_roots": (C.c_int, [vp, u32, u32, vp]),
+    "gbx_mt19937_next": (u32, [C.POINTER(C.c_ulong), C.POINTER(C.c_int)]),
     "gbx_cc": (C.c_int, [vp, C.c_int, vp, C.POINTER(u32), vp]),
     "gbx_tc": (C.c_int, [vp, C.POINTER(u64), vp]),
     "gbx_spmv": (C.c_int, [vp, vp, C.c_float, vp, vp, u32, vp]),

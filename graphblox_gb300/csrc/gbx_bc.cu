@@ -852,8 +852,10 @@ extern "C" int gbx_dfs(gbx_graph *g, uint32_t source, uint32_t *distances, int32
 // 172-189): draw until the value is a vertex whose out-degree exceeds E/V.
 namespace {
 
+// The generator state in the reference's layout (624 unsigned long words and
+// the index, mt19937.h:58-62), stepped by gbx_mt19937_next.
 struct Mt19937 {
-    uint32_t mt[624];
+    unsigned long mt[624];
     int mti = 624;
     explicit Mt19937(uint32_t seed) {
         for (int i = 0; i < 624; ++i) {
@@ -863,24 +865,29 @@ struct Mt19937 {
             seed = 69069u * seed + 1u;
         }
     }
-    uint32_t next() {
-        if (mti >= 624) {
-            for (int k = 0; k < 624; ++k) {
-                const uint32_t y = (mt[k] & 0x80000000u) | (mt[(k + 1) % 624] & 0x7fffffffu);
-                mt[k] = mt[(k + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
-            }
-            mti = 0;
-        }
-        uint32_t y = mt[mti++];
-        y ^= y >> 11;
-        y ^= (y << 7) & 0x9d2c5680u;
-        y ^= (y << 15) & 0xefc60000u;
-        y ^= y >> 18;
-        return y;
-    }
+    uint32_t next() { return gbx_mt19937_next(mt, &mti); }
 };
 
 }  // namespace
+
+// One draw: regenerate the 624 words when they are used up (the twist), then
+// temper the next one. The words hold 32-bit values in 64-bit slots, as the
+// reference's do.
+extern "C" uint32_t gbx_mt19937_next(unsigned long *mt, int *mti) {
+    if (*mti >= 624) {
+        for (int k = 0; k < 624; ++k) {
+            const unsigned long y = (mt[k] & 0x80000000UL) | (mt[(k + 1) % 624] & 0x7fffffffUL);
+            mt[k] = mt[(k + 397) % 624] ^ (y >> 1) ^ ((y & 1UL) ? 0x9908b0dfUL : 0UL);
+        }
+        *mti = 0;
+    }
+    unsigned long y = mt[(*mti)++];
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680UL;
+    y ^= (y << 15) & 0xefc60000UL;
+    y ^= y >> 18;
+    return (uint32_t)y;
+}
 
 extern "C" int gbx_reference_roots(gbx_graph *g, uint32_t seed, uint32_t n, uint32_t *roots) {
     clear_error();

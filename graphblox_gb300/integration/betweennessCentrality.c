@@ -6,25 +6,11 @@
 #include "betweennessCentrality.h"
 #include "gbx_shim.h"
 
-/* One value of the generator in the caller's state: the Mersenne Twister
- * MT19937 (Matsumoto and Nishimura, 1998) stepped on the reference's
- * mt19937state (01_host/include/utils_graph/mt19937.h:58-62), so the stream
- * continues exactly as the reference's generateRandInt would continue it. */
-static unsigned long mt_next(mt19937state *m) {
-    if (m->mti >= 624) {
-        for (int k = 0; k < 624; ++k) {
-            const unsigned long y = (m->mt[k] & 0x80000000UL) | (m->mt[(k + 1) % 624] & 0x7fffffffUL);
-            m->mt[k] = m->mt[(k + 397) % 624] ^ (y >> 1) ^ ((y & 1UL) ? 0x9908b0dfUL : 0UL);
-        }
-        m->mti = 0;
-    }
-    unsigned long y = m->mt[m->mti++];
-    y ^= y >> 11;
-    y ^= (y << 7) & 0x9d2c5680UL;
-    y ^= (y << 15) & 0xefc60000UL;
-    y ^= y >> 18;
-    return y;
-}
+/* One value of the generator in the caller's state: gbx_mt19937_next steps
+ * the reference's mt19937state (01_host/include/utils_graph/mt19937.h:58-62)
+ * in place, so the stream continues exactly as the reference's
+ * generateRandInt would continue it. */
+static unsigned long mt_next(mt19937state *m) { return gbx_mt19937_next(m->mt, &m->mti); }
 
 /* betweennessCentrality.c:172-189: draw until a vertex with out-degree above
  * the average */

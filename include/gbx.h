@@ -321,6 +321,13 @@ int gbx_betweenness(gbx_graph *g, uint32_t num_roots, const uint32_t *roots, flo
  * GBX_ERR_INVALID when no vertex qualifies. */
 int gbx_reference_roots(gbx_graph *g, uint32_t seed, uint32_t n, uint32_t *roots);
 
+/* One draw of the Mersenne Twister MT19937 (Matsumoto and Nishimura, 1998)
+ * from a state laid out like the reference's mt19937state (624 unsigned long
+ * words and the index; mt19937.h:58-62), which it advances in place: the
+ * value the reference's generateRandInt (mt19937.c) returns from that state.
+ * gbx_reference_roots and the drop-in betweenness draw with it. */
+uint32_t gbx_mt19937_next(unsigned long *mt, int *mti);
+
 /* ---- connected components ---------------------------------------------- */
 /* components[v] = smallest vertex id in v's component. variant 0 SV-style
  * hooking sweeps, 1 Afforest (default), 2 label propagation. All variants

@@ -11,17 +11,22 @@
 # only by a graphConfig.h whose three macros are rewritten with sed into
 # oracle/_ref/cfg_<variant>/, which precedes the reference include dirs.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   REFERENCE_ROOT defaults to $GBX_REFERENCE_ROOT, else /root/reference.
+#   Exits 2 (nothing built) when the reference sources are not there.
+#   The tree it compiled from is recorded in oracle/_ref/reference_root, where
+#   the tests that read the reference sources look it up.
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${GBX_REFERENCE_ROOT:-/root/reference}}"
 HOST="$REF/01_host"
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -d "$HOST/src" ]; then
     echo "reference host sources not found under $HOST" >&2
-    exit 1
+    exit 2
 fi
 mkdir -p "$OUT"
+printf '%s\n' "$(cd "$REF" && pwd)" > "$OUT/reference_root"
 CXX="${CXX:-g++}"
 JOBS="$(nproc)"
 SRCS=$(ls "$HOST"/src/algorithms/openmp/*.c "$HOST"/src/structures/*.c \

@@ -9,6 +9,20 @@ if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def reference_root():
+    """The reference tree the tests may read (None where there is none): the
+    GBX_REFERENCE_ROOT environment variable, else the tree oracle/build_ref.sh
+    compiled oracle/_ref from."""
+    import os
+
+    env = os.environ.get("GBX_REFERENCE_ROOT")
+    if env:
+        return Path(env)
+    rec = ROOT / "oracle" / "_ref" / "reference_root"
+    return Path(rec.read_text().strip()) if rec.exists() else None
+
 # one fixture per test graph; reorder_modes.npz holds the labels of the
 # reorder modes for all of them, csr_files.npz the reference's .csr files,
 # mask_modes.npz its mask mode, bf_dfs_bc.npz Bellman-Ford, DFS and

@@ -1,6 +1,7 @@
 """Generate the golden fixtures in tests/golden/*.npz.
 
-Run in a container that has the reference tree (default /root/reference) and
+Run in a container that has the reference tree (the first argument, or
+$GBX_REFERENCE_ROOT, or the tree oracle/_ref was built from) and
 its build (oracle/build_ref.sh). For every test graph the reference ships in
 03_data/TEST, the fixture stores:
   - the input edge list (graph.bin / graph.wbin records),
@@ -20,6 +21,7 @@ bf_dfs_bc.npz, Bellman-Ford, DFS and betweenness centrality.)
 """
 from __future__ import annotations
 
+import os
 import sys
 from pathlib import Path
 
@@ -249,7 +251,13 @@ def more_algorithms(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    # the reference tree: the first argument, else $GBX_REFERENCE_ROOT, else
+    # the tree oracle/build_ref.sh compiled oracle/_ref from
+    rec = Path(__file__).resolve().parents[2] / "oracle" / "_ref" / "reference_root"
+    root = (sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GBX_REFERENCE_ROOT")
+            or (rec.read_text().strip() if rec.exists() else ""))
+    if not root:
+        sys.exit("usage: make_golden.py REFERENCE_ROOT [reorder|csr|mask|more] (or set GBX_REFERENCE_ROOT)")
     if len(sys.argv) > 2 and sys.argv[2] == "reorder":
         reorder_modes(root)
     elif len(sys.argv) > 2 and sys.argv[2] == "csr":

@@ -10,8 +10,11 @@ from pathlib import Path
 
 import pytest
 
+from conftest import reference_root
+
 ROOT = Path(__file__).resolve().parents[1]
-REF = Path("/root/reference/01_host")
+_root = reference_root()
+REF = (_root / "01_host") if _root else Path("reference-tree-not-present")
 CFG = ROOT / "oracle" / "_ref" / "cfg_dw"
 
 pytestmark = pytest.mark.skipif(not (REF / "src").exists() or not (CFG / "graphConfig.h").exists(),
