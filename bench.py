@@ -77,6 +77,8 @@ def peaks():
 
 
 def build_workload(gbx, scale=SCALE, ef=EDGE_FACTOR, seed=SEED):
+    """The RMAT workload generated and built on the GPU (the library's own
+    generator and gbx_csr_build / gbx_degree_reorder)."""
     V = 1 << scale
     t0 = time.time()
     src, dst = gbx.generate_rmat(scale, V * ef, seed=seed)
@@ -91,24 +93,72 @@ def build_workload(gbx, scale=SCALE, ef=EDGE_FACTOR, seed=SEED):
     gsr = gbx.graph_csr_preprocessing(elr, sort=1, directed=False, keep_weights=False)
     x = gbx.generate_values(V, 2, seed=seed + 21)
     vals = gbx.generate_values(g.num_edges, 1, seed=seed + 31)
-    rng = np.random.default_rng(seed)
-    nz = np.nonzero(g.out_degree)[0]
-    roots = [int(r) for r in rng.choice(nz, N_ROOTS, replace=False)]
+    roots = pick_roots(g.out_degree, seed)
     log(f"workload built in {time.time() - t0:.1f}s: V={V} E={g.num_edges} Esym={gs.num_edges}")
-    return dict(V=V, g=g, gs=gs, gsr=gsr, x=x, vals=vals, roots=roots, edges_src=g.src, edges_dst=g.dest)
+    return dict(V=V, g=g, gs=gs, gsr=gsr, x=x, vals=vals, roots=roots, edges_src=g.src, edges_dst=g.dest,
+                reorder_labels=(elr.label_array, elr.inverse_label_array))
 
 
-def dag_stats(gsr):
-    """|E+| and the TC algorithmic bytes sum over DAG edges of 4(d+u + d+v),
-    with d+(u) = number of neighbours with id <= u (ids are degree order)."""
+def pick_roots(out_degree, seed=SEED):
+    rng = np.random.default_rng(seed)
+    nz = np.nonzero(out_degree)[0]
+    return [int(r) for r in rng.choice(nz, N_ROOTS, replace=False)]
+
+
+class HostGraph:
+    """A CSR in the reference's layout, built on the CPU by the oracle."""
+
+    def __init__(self, V, csr, inverse=None):
+        self.num_vertices = V
+        self.num_edges = int(csr.dest.shape[0])
+        self.out_degree, self.edges_idx, self.dest, self.src, self.weight = (
+            csr.out_degree, csr.edges_idx, csr.dest, csr.src, csr.weight)
+        self.inverse_out_degree = self.inverse_edges_idx = self.inverse_dest = self.inverse_weight = None
+        if inverse is not None:
+            self.inverse_out_degree, self.inverse_edges_idx = inverse.out_degree, inverse.edges_idx
+            self.inverse_dest, self.inverse_weight = inverse.dest, inverse.weight
+
+
+def build_workload_oracle(scale=SCALE, ef=EDGE_FACTOR, seed=SEED):
+    """The same workload generated and built on the host cores by the oracle
+    (oracle/gbx_oracle.c: the same generator streams, the reference's sort /
+    dedup / map and degree reordering), without the GPU library."""
+    from oracle import pyoracle as po
+
+    V = 1 << scale
+    t0 = time.time()
+    src, dst = po.generate_rmat(scale, V * ef, seed=seed)
+    w = po.generate_values(src.shape[0], 0, W_LO, W_HI, seed=seed + 11)
+    fwd = po.build_csr(V, src, dst, w, sort_mode=1, dedup=True)
+    inv = po.build_csr(V, fwd.dest, fwd.src, fwd.weight, sort_mode=1)
+    g = HostGraph(V, fwd, inv)
+    sym = po.build_csr(V, np.concatenate([src, dst]), np.concatenate([dst, src]), None, sort_mode=1, dedup=True)
+    gs = HostGraph(V, sym)
+    rs, rd, lab, ilab = po.degree_reorder(V, sym.src, sym.dest, 1)
+    gsr = HostGraph(V, po.build_csr(V, rs, rd, None, sort_mode=1))
+    x = po.generate_values(V, 2, seed=seed + 21)
+    vals = po.generate_values(g.num_edges, 1, seed=seed + 31)
+    roots = pick_roots(g.out_degree, seed)
+    log(f"oracle workload built on the host cores in {time.time() - t0:.1f}s")
+    return dict(V=V, g=g, gs=gs, gsr=gsr, x=x, vals=vals, roots=roots, edges_src=g.src, edges_dst=g.dest,
+                reorder_labels=(lab, ilab))
+
+
+def tc_stats(gsr):
+    """|E+| (DAG edges: neighbours with a smaller degree-order id) and the
+    triangle count's byte figures: `compulsory` = the DAG read once,
+    4(V+1) + 4|E+|, the roofline's bytes; `merge` = sum over DAG edges of
+    4(d+u + d+v), what a merge-based intersection would stream (reported
+    beside it, not used for the roofline)."""
     deg = gsr.out_degree.astype(np.int64)
-    src = gsr.src.astype(np.int64)
+    src = np.repeat(np.arange(gsr.num_vertices, dtype=np.int64), deg)
     dst = gsr.dest.astype(np.int64)
     lower = dst <= src
     dplus = np.bincount(src[lower], minlength=gsr.num_vertices).astype(np.int64)
     e_plus = int(lower.sum())
-    tc_bytes = 4 * (gsr.num_vertices + 1) + 4 * e_plus + int((4 * (dplus[src[lower]] + dplus[dst[lower]])).sum())
-    return e_plus, tc_bytes
+    compulsory = 4 * (gsr.num_vertices + 1) + 4 * e_plus
+    merge = compulsory + int((4 * (dplus[src[lower]] + dplus[dst[lower]])).sum())
+    return e_plus, compulsory, merge
 
 
 # ---------------------------------------------------------------------------
@@ -182,6 +232,25 @@ def reduce_over_ranks(dist, local_ms, local_edges, device=None):
     return ms, (world * local_edges / (ms * 1e-3) / 1e9 if ms else 0.0)
 
 
+def shard(n, rank, world):
+    """The contiguous share [lo, hi) of n independent units (graphs of a
+    batch, BFS sources) that rank `rank` of `world` runs."""
+    return n * rank // world, n * (rank + 1) // world
+
+
+def job_reduce(dist, ms, edges, device=None):
+    """(slowest rank's ms, every rank's edges summed) for sharded work."""
+    if not dist or not dist.is_initialized() or dist.get_world_size() == 1:
+        return ms, edges
+    import torch
+
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    e = torch.tensor([float(edges)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(e, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(e.item())
+
+
 # ---------------------------------------------------------------------------
 # GPU arm
 
@@ -242,7 +311,7 @@ def run_gpu(args):
     lab_d = torch.empty(V, dtype=torch.int32, device=dev)
     inv_d = torch.empty(V, dtype=torch.int32, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    e_plus, tc_bytes = dag_stats(gsr)
+    e_plus, tc_bytes, tc_merge_bytes = tc_stats(gsr)
     roots = W["roots"]
     sssp_roots = roots[:N_SSSP_ROOTS]
     ident = torch.arange(V, dtype=torch.int32, device=dev)
@@ -339,6 +408,14 @@ def run_gpu(args):
         per[n] = {"ms": round(ms, 4), "gteps": round(te / (ms * 1e-3) / 1e9, 3),
                   "achieved_gbs": round(tb / (ms * 1e-3) / 1e9, 1),
                   "frac": round(tb / (ms * 1e-3) / 1e9 / peak, 3), "edges": int(te), "alg_bytes": int(tb)}
+        if n in NCU_TRAFFIC_PER_LAUNCH:
+            # DRAM bytes one launch moved under ncu, over this run's time per launch
+            launches = {"bfs": len(roots), "sssp": len(sssp_roots), "pr": PR_ITERS}.get(n, 1)
+            per[n]["dram_frac"] = round(NCU_TRAFFIC_PER_LAUNCH[n] * launches / (ms * 1e-3) / 1e9 / peak, 3)
+        if n == "tc":
+            per[n]["merge_bytes"] = int(tc_merge_bytes)
+            per[n]["note"] = ("alg_bytes = the DAG read once, 4(V+1) + 4|E+|; merge_bytes = what a merge "
+                              "intersection would stream; the kernel probes shared-memory tables instead")
         tot_edges += te
         tot_ms += ms
     ms_step, gteps = reduce_over_ranks(dist, tot_ms, tot_edges, torch.device("cuda", local) if dist else None)
@@ -354,8 +431,9 @@ def run_gpu(args):
         ppr = run_ppr(args, torch, gbx, dev, stream, peak)
     batched = None
     if not args.no_batched and (not args.only or "batched" in args.only.split(",")):
-        batched = run_batched(args, torch, gbx, _lib, dev, stream, peak)
-        batched["multisource"] = run_multisource(args, torch, gbx, _lib, dg, W, dev, stream, peak)
+        batched = run_batched(args, torch, gbx, _lib, dev, stream, peak, dist, rank, world)
+        batched["multisource"] = run_multisource(args, torch, gbx, _lib, dg, W, dev, stream, peak, dist, rank,
+                                                 world)
     more = None
     if not args.no_more and (not args.only or "more" in args.only.split(",")):
         more = run_more(args, torch, gbx, dg, g, stream, peak)
@@ -368,9 +446,20 @@ def run_gpu(args):
         dgs = gbx.DeviceGraph.from_graph_csr(gs, use_weights=False, stream=sp)
         dgr = gbx.DeviceGraph.from_graph_csr(gsr, use_weights=False, stream=sp)
     e2e = None if args.no_e2e else run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp, tuning)
-    cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(W, args, roots)
+    cpu = parity = None
+    if rank == 0 and not (args.no_cpu_baseline and args.no_parity):
+        Wc = build_workload_oracle(scale=args.scale)
+        if args.no_cpu_baseline:
+            from oracle import pyoracle as po
+
+            tri_oracle = po.triangle_count(po.HostCSR(V, Wc["gsr"].out_degree, Wc["gsr"].edges_idx, Wc["gsr"].dest))
+        else:
+            cpu, tri_oracle = cpu_baseline(Wc)
+        if not args.no_parity:
+            t0 = time.time()
+            parity = parity_kernel_set(torch, gbx, W, Wc, dg, dgs, dgr, tri_oracle, stream)
+            log(f"parity checked in {time.time() - t0:.1f}s: all exact {parity['all_exact']}")
+        del Wc
     dg.close(), dgs.close(), dgr.close()
     line = {
         "metric": "GTEPS per kernel (aggregate over the kernel set) & %HBM-peak per kernel",
@@ -378,12 +467,8 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32 (ids, levels, distances) + f32 (ranks, SpMV)",
         "data": "synthetic",
-        "config": {"workload": f"rmat{args.scale}_full_kernel_set", "scale": args.scale, "num_vertices": V,
-                   "edges_generated": V * EDGE_FACTOR, "num_edges": E, "num_edges_symmetric": gs.num_edges,
-                   "dag_edges": e_plus, "bfs_roots": N_ROOTS, "sssp_roots": N_SSSP_ROOTS,
-                   "pr_iterations": PR_ITERS, "l2": "flushed (256 MiB write) before every kernel",
-                   "parallelism": "replicas" if world > 1 else "single GPU", "tuning": tuning},
-        "kernels": per, "batched": batched, "ppr_adjoint": ppr, "more": more, "c5": c5, "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk,
+        "config": workload_config(args, V, E, gs.num_edges, e_plus, world), "tuning": tuning,
+        "kernels": per, "parity": parity, "batched": batched, "ppr_adjoint": ppr, "more": more, "c5": c5, "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk,
         "gpu_launches": int(launches), "wall_ms_timed_region": round(wall_ms, 3),
     }
     if rank == 0:
@@ -547,15 +632,20 @@ def run_ppr(args, torch, gbx, dev, stream, peak):
             "note": "adjoint_ms includes dL/dw (one more gather pass), dL/dT and the FP64 loss"}
 
 
-def run_batched(args, torch, gbx, _lib, dev, stream, peak):
+def run_batched(args, torch, gbx, _lib, dev, stream, peak, dist=None, rank=0, world=1):
     """2,048 RMAT graphs (scale ~U[8,15], V = floor(2^s), edge factor
     ~U[4,32]) packed back to back: one step = BFS from vertex 0 plus 30
     PageRank iterations on every graph. Batched: gbx_bfs_batched +
     gbx_pr_batched (two persistent launches). Per instance: gbx_bfs +
     gbx_pagerank_pull called once per graph on resident single graphs, the
-    same device output arrays. Both timed with CUDA events, mean of `steps`."""
+    same device output arrays. Both timed with CUDA events, mean of `steps`.
+    With several ranks each takes a contiguous share of the graphs (the
+    work queue's natural shard, no collective on the data path); the job's
+    time is the slowest rank's and its edges are every rank's."""
     t0 = time.time()
     gl = gbx.generate_rmat_batch(args.batch_graphs, seed=SEED)
+    lo, hi = shard(len(gl), rank, world)
+    gl = gl[lo:hi]
     packed = gbx.pack_graphs(gl)
     del gl
     G = packed.num_graphs
@@ -610,6 +700,11 @@ def run_batched(args, torch, gbx, _lib, dev, stream, peak):
     l0 = _lib.load().gbx_kernel_launches()
     p_ms = timed(per_instance, max(1, min(args.steps, 2)))
     p_launches = (_lib.load().gbx_kernel_launches() - l0) // max(1, min(args.steps, 2))
+    parity = None
+    if not args.no_parity:
+        batched()
+        torch.cuda.synchronize()
+        parity = batched_parity(packed, dist_d.cpu().numpy().view(np.uint32), ranks_d.cpu().numpy(), bres, pres)
     m_reach = sum(int(r.edges_traversed) for r in bres)
     nv = np.diff(vb)
     edges = m_reach + BATCH_PR_ITERS * Et
@@ -617,7 +712,12 @@ def run_batched(args, torch, gbx, _lib, dev, stream, peak):
     for dg in singles:
         dg.close()
     batch.close()
-    return {"workload": f"rmat_batch_{G}_graphs", "num_graphs": G, "num_vertices": Vt, "num_edges": Et,
+    dev_r = dev if dist else None
+    b_job, e_job = job_reduce(dist, b_ms, edges, dev_r)
+    p_job, _ = job_reduce(dist, p_ms, 0, dev_r)
+    return {"workload": f"rmat_batch_{args.batch_graphs}_graphs", "num_graphs": G, "num_vertices": Vt,
+            "num_edges": Et, "rank_graphs": [int(lo), int(hi)], "job_batched_ms": round(b_job, 3),
+            "job_per_instance_ms": round(p_job, 3), "job_batched_gteps": round(e_job / (b_job * 1e-3) / 1e9, 3),
             "graph_vertices_min_max": [int(nv.min()), int(nv.max())], "pr_iterations": BATCH_PR_ITERS,
             "batched_ms": round(b_ms, 3), "per_instance_ms": round(p_ms, 3),
             "speedup_vs_per_instance": round(p_ms / b_ms, 2),
@@ -626,27 +726,67 @@ def run_batched(args, torch, gbx, _lib, dev, stream, peak):
             "batched_achieved_gbs": round(alg / (b_ms * 1e-3) / 1e9, 1),
             "batched_frac": round(alg / (b_ms * 1e-3) / 1e9 / peak, 3),
             "launches_batched": int(b_launches), "launches_per_instance": int(p_launches),
-            "edges_per_step": int(edges), "alg_bytes_per_step": int(alg)}
+            "edges_per_step": int(edges), "alg_bytes_per_step": int(alg), "parity": parity}
 
 
-def run_multisource(args, torch, gbx, _lib, dg, W, dev, stream, peak):
+def batched_parity(packed, dist, ranks, bres, pres, n_check=64, n_largest=10):
+    """Per-graph results of the batched launches against the oracle run on
+    each graph alone, for the n_largest largest graphs and graphs spread
+    evenly over the rest (n_check in all): BFS levels, processed_nodes and
+    iteration bit-exact; PageRank (BATCH_PR_ITERS iterations) within 1e-6
+    relative L1 of the FP64 restatement."""
+    from oracle import pyoracle as po
+
+    G = packed.num_graphs
+    vb = packed.vertex_base.astype(np.int64)
+    nv = np.diff(vb)
+    largest = [int(x) for x in np.argsort(-nv, kind="stable")[:n_largest]]
+    rest = [g for g in np.linspace(0, G - 1, n_check - n_largest).astype(int).tolist() if g not in largest]
+    pick = sorted(set(largest + rest))
+    bad_bfs, bad_pr, worst = [], [], 0.0
+    for g in pick:
+        V, off, dest, ioff, isrc = packed.graph(g)
+        deg = np.diff(off.astype(np.int64)).astype(np.uint32)
+        ideg = np.diff(ioff.astype(np.int64)).astype(np.uint32)
+        host = po.HostCSR(V, deg, off[:-1], dest)
+        pull = po.HostCSR(V, ideg, ioff[:-1], isrc)
+        d, _, proc, it = po.bfs(host, 0, pull)
+        b, e = int(vb[g]), int(vb[g + 1])
+        if not (np.array_equal(dist[b:e], d) and bres[g].processed_nodes == proc and bres[g].iteration == it):
+            bad_bfs.append(g)
+        r64, _, _ = po.pagerank(host, BATCH_PR_ITERS, 0.0, pull, fp64=True)
+        ok, err, _ = po.fp32_close(ranks[b:e], r64, 1e-6)
+        worst = max(worst, err)
+        if not ok:
+            bad_pr.append(g)
+    return {"graphs_checked": len(pick), "largest_checked": n_largest,
+            "largest_vertices": int(nv[largest[0]]), "bfs_exact": not bad_bfs, "bfs_mismatched": bad_bfs,
+            "pr_worst_rel_l1_vs_fp64": float(f"{worst:.3e}"), "pr_within_1e-6": not bad_pr,
+            "pr_mismatched": bad_pr}
+
+
+def run_multisource(args, torch, gbx, _lib, dg, W, dev, stream, peak, dist=None, rank=0, world=1):
     """256-source BFS on the RMAT-22 graph: one gbx_bfs_multisource call
     (bitmask sweep) against 256 gbx_bfs calls, same sources (seeded,
-    non-isolated), device outputs. Mean CUDA-event time of `steps` calls."""
+    non-isolated), device outputs. Mean CUDA-event time of `steps` calls.
+    With several ranks each takes a contiguous share of the sources."""
     V = W["V"]
     g = W["g"]
     rng = np.random.default_rng(SEED + 5)
     nz = np.nonzero(g.out_degree)[0]
     src = rng.choice(nz, MS_SOURCES, replace=False).astype(np.uint32)
+    lo, hi = shard(MS_SOURCES, rank, world)
+    src = src[lo:hi]
+    n_src = int(src.shape[0])
     sp = stream.cuda_stream
     src_d = torch.from_numpy(src.view(np.int32)).to(dev)
-    dist_d = torch.empty((V, MS_SOURCES), dtype=torch.int32, device=dev)
+    dist_d = torch.empty((V, n_src), dtype=torch.int32, device=dev)
     d1 = torch.empty(V, dtype=torch.int32, device=dev)
-    res = (_lib.BfsResult * MS_SOURCES)()
+    res = (_lib.BfsResult * n_src)()
     r1 = _lib.BfsResult()
 
     def multi():
-        _lib.call("gbx_bfs_multisource", dg.handle, MS_SOURCES, src_d.data_ptr(), dist_d.data_ptr(), res, sp)
+        _lib.call("gbx_bfs_multisource", dg.handle, n_src, src_d.data_ptr(), dist_d.data_ptr(), res, sp)
 
     def singles():
         for s in src:
@@ -671,14 +811,34 @@ def run_multisource(args, torch, gbx, _lib, dg, W, dev, stream, peak):
     s_ms = timed(singles, max(1, min(args.steps, 2)))
     edges = sum(int(r.edges_traversed) for r in res)
     levels = int(res[0].top_down_steps + res[0].bottom_up_steps)
+    parity = None
+    if not args.no_parity:
+        from oracle import pyoracle as po
+
+        multi()
+        torch.cuda.synchronize()
+        host = po.HostCSR(V, g.out_degree, g.edges_idx, g.dest)
+        pull = po.HostCSR(V, g.inverse_out_degree, g.inverse_edges_idx, g.inverse_dest)
+        bad = []
+        cols = list(range(0, n_src, max(1, n_src // 8)))
+        for k in cols:
+            d, _, proc, it = po.bfs(host, int(src[k]), pull)
+            col = dist_d[:, k].cpu().numpy().view(np.uint32)
+            if not (np.array_equal(col, d) and res[k].processed_nodes == proc and res[k].iteration == it):
+                bad.append(k)
+        parity = {"sources_checked": len(cols), "exact": not bad, "mismatched": bad}
     del dist_d
-    return {"workload": f"rmat{args.scale}_bfs_{MS_SOURCES}_sources", "sources": MS_SOURCES,
+    dev_r = dev if dist else None
+    m_job, e_job = job_reduce(dist, m_ms, edges, dev_r)
+    return {"workload": f"rmat{args.scale}_bfs_{MS_SOURCES}_sources", "sources": n_src,
+            "rank_sources": [int(lo), int(hi)], "job_multisource_ms": round(m_job, 3),
+            "job_multisource_gteps": round(e_job / (m_job * 1e-3) / 1e9, 3),
             "multisource_ms": round(m_ms, 3), "per_source_ms": round(s_ms, 3),
             "speedup_vs_per_source": round(s_ms / m_ms, 2),
             "multisource_gteps": round(edges / (m_ms * 1e-3) / 1e9, 3),
             "per_source_gteps": round(edges / (s_ms * 1e-3) / 1e9, 3),
             "levels": levels, "push_levels": int(res[0].top_down_steps), "pull_levels": int(res[0].bottom_up_steps),
-            "edges_traversed": edges}
+            "edges_traversed": edges, "parity": parity}
 
 
 def run_c5(args, torch, gbx, _lib, dev, stream, peak):
@@ -878,122 +1038,245 @@ def run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp, tuning=No
 # ---------------------------------------------------------------------------
 # CPU oracle port (baseline and reference arm)
 
+# The reference arm runs the kernel set in a cycle of CPU_CYCLE steps; one
+# cycle holds exactly one full kernel-set step: step i runs BFS from roots
+# [16 i, 16 i + 16), SSSP from root i, the triangles of the i-th quarter of
+# the pivots (by work), 5 PageRank iterations, and CC (i = 0), SpMV (i = 1)
+# or the degree reordering (i = 2).
+CPU_CYCLE = 4
 
-def cpu_sample(W, roots, n_bfs=4, pr_iters=PR_ITERS, n_sssp=1, with_tc=True, threads=0):
+
+def cpu_info():
+    model = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        model = next((ln.split(":", 1)[1].strip() for ln in out.splitlines() if ln.startswith("Model name")), "")
+    except Exception:
+        pass
+    if not model:
+        try:
+            txt = Path("/proc/cpuinfo").read_text()
+            model = next((ln.split(":", 1)[1].strip() for ln in txt.splitlines()
+                          if ln.lower().startswith(("model name", "cpu part"))), "")
+        except Exception:
+            pass
+    return {"cpu_model": model or "unknown", "nproc": os.cpu_count(),
+            "omp_proc_bind": os.environ.get("OMP_PROC_BIND", "unset"),
+            "omp_places": os.environ.get("OMP_PLACES", "unset")}
+
+
+def cpu_plan(Wc):
+    """Host views of the oracle-built graphs and the cycle's TC pivot slices
+    (equal shares of sum over DAG edges (u,v) of d+(v), the pull count's work)."""
     from oracle import pyoracle as po
 
-    g, gs, gsr = W["g"], W["gs"], W["gsr"]
+    g, gs, gsr = Wc["g"], Wc["gs"], Wc["gsr"]
     V = g.num_vertices
     host = po.HostCSR(V, g.out_degree, g.edges_idx, g.dest, g.weight, g.src)
     pull = po.HostCSR(V, g.inverse_out_degree, g.inverse_edges_idx, g.inverse_dest, g.inverse_weight)
     hs = po.HostCSR(V, gs.out_degree, gs.edges_idx, gs.dest)
     hr = po.HostCSR(V, gsr.out_degree, gsr.edges_idx, gsr.dest)
+    src = np.repeat(np.arange(V, dtype=np.int64), gsr.out_degree.astype(np.int64))
+    dst = gsr.dest.astype(np.int64)
+    lower = dst <= src
+    dplus = np.bincount(src[lower], minlength=V)
+    cost = np.cumsum(np.bincount(src[lower], weights=dplus[dst[lower]], minlength=V))
+    cuts = [0] + [int(np.searchsorted(cost, cost[-1] * k / CPU_CYCLE)) for k in range(1, CPU_CYCLE)] + [V]
+    dag_per_pivot = np.cumsum(np.bincount(src[lower], minlength=V))
+    dag_edges = [int((dag_per_pivot[hi - 1] if hi else 0) - (dag_per_pivot[lo - 1] if lo else 0))
+                 for lo, hi in zip(cuts[:-1], cuts[1:])]
+    return dict(host=host, pull=pull, hs=hs, hr=hr, tc_cuts=cuts, tc_dag_edges=dag_edges)
+
+
+def cpu_step(Wc, plan, i, threads=0):
+    """Step i of the cycle on the host cores (oracle/gbx_oracle.c, OpenMP).
+    Returns ({kernel: (traversed edges, seconds)}, tc count of the slice);
+    only the oracle calls are timed."""
+    from oracle import pyoracle as po
+
+    g = Wc["g"]
+    V, E = g.num_vertices, g.num_edges
+    host, pull, hs, hr = plan["host"], plan["pull"], plan["hs"], plan["hr"]
+    i %= CPU_CYCLE
+    per = N_ROOTS // CPU_CYCLE
+    deg = g.out_degree.astype(np.int64)
     res = {}
-
-    def timed(name, fn, edges):
+    t = e = 0.0
+    for r in Wc["roots"][per * i:per * (i + 1)]:
         t0 = time.perf_counter()
-        fn()
-        dt = time.perf_counter() - t0
-        res[name] = (edges() if callable(edges) else edges, dt)
-
-    bfs_edges = []
-
-    def bfs():
-        for r in roots[:n_bfs]:
-            d, _, _, _ = po.bfs(host, r, pull, threads)
-            reached = (d > 0)
-            reached[r] = True
-            bfs_edges.append(int(g.out_degree[reached].astype(np.int64).sum()))
-
-    timed("bfs", bfs, lambda: sum(bfs_edges))
-    sssp_edges = []
-
-    def sssp():
-        for r in roots[:n_sssp]:
-            d = po.sssp(host, r, 64, threads)
-            sssp_edges.append(int(g.out_degree[d != 0x7FFFFFFF].astype(np.int64).sum()))
-
-    timed("sssp", sssp, lambda: sum(sssp_edges))
-    timed("cc", lambda: po.cc(hs, 1, None, threads), gs.num_edges)
-    if with_tc:
-        e_plus = int((gsr.dest <= gsr.src).sum())
-        timed("tc", lambda: po.triangle_count(hr, threads), e_plus)
-    timed("spmv", lambda: po.spmv(host, W["x"], W["vals"], pull=pull, threads=threads), g.num_edges)
-    timed("pr", lambda: po.pagerank(host, pr_iters, 0.0, pull, threads), g.num_edges * pr_iters)
-    timed("reorder", lambda: po.degree_reorder(V, g.src, g.dest, 1, threads=threads), g.num_edges)
-    return res
-
-
-def step_mix(W, res, n_bfs, n_sssp):
-    """Traversed edges of one full kernel-set step (64 BFS roots, 4 SSSP roots,
-    CC, TC, SpMV, 20 PR iterations, reorder), BFS/SSSP from the sampled roots'
-    mean reach."""
-    g, gs, gsr = W["g"], W["gs"], W["gsr"]
-    E = g.num_edges
-    return {"bfs": res["bfs"][0] / n_bfs * N_ROOTS, "sssp": res["sssp"][0] / n_sssp * N_SSSP_ROOTS,
-            "cc": gs.num_edges, "tc": int((gsr.dest <= gsr.src).sum()), "spmv": E, "pr": E * PR_ITERS,
-            "reorder": E}
+        d, _, _, _ = po.bfs(host, r, pull, threads)
+        t += time.perf_counter() - t0
+        reached = d > 0
+        reached[r] = True
+        e += int(deg[reached].sum())
+    res["bfs"] = (e, t)
+    r = Wc["roots"][i % N_SSSP_ROOTS]
+    t0 = time.perf_counter()
+    d = po.sssp(host, r, 64, threads)
+    res["sssp"] = (int(deg[d != 0x7FFFFFFF].sum()), time.perf_counter() - t0)
+    lo, hi = plan["tc_cuts"][i], plan["tc_cuts"][i + 1]
+    t0 = time.perf_counter()
+    tri = po.triangle_count(hr, threads, lo, hi)
+    res["tc"] = (plan["tc_dag_edges"][i], time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    po.pagerank(host, PR_ITERS // CPU_CYCLE, 0.0, pull, threads)
+    res["pr"] = (E * (PR_ITERS // CPU_CYCLE), time.perf_counter() - t0)
+    if i == 0:
+        t0 = time.perf_counter()
+        po.cc(hs, 1, None, threads)
+        res["cc"] = (Wc["gs"].num_edges, time.perf_counter() - t0)
+    elif i == 1:
+        t0 = time.perf_counter()
+        po.spmv(host, Wc["x"], Wc["vals"], pull=pull, threads=threads)
+        res["spmv"] = (E, time.perf_counter() - t0)
+    elif i == 2:
+        t0 = time.perf_counter()
+        po.degree_reorder(V, g.src, g.dest, 1, threads=threads)
+        res["reorder"] = (E, time.perf_counter() - t0)
+    return res, tri
 
 
-def mix_gteps(res, mix):
-    """Aggregate GTEPS of the full step at the sampled per-kernel rates: the
-    same kernel mix as the GPU `value`."""
-    secs = sum(mix[k] / (e / t) for k, (e, t) in res.items())
-    return sum(mix[k] for k in res) / secs / 1e9, secs
+def cpu_baseline(Wc):
+    """One full cycle (one kernel-set step) on the host cores, all threads."""
+    plan = cpu_plan(Wc)
+    per = {}
+    tri = 0
+    for i in range(CPU_CYCLE):
+        res, t = cpu_step(Wc, plan, i)
+        tri += t
+        for k, (e, s) in res.items():
+            pe, ps = per.get(k, (0, 0.0))
+            per[k] = (pe + e, ps + s)
+    edges = sum(e for e, _ in per.values())
+    secs = sum(s for _, s in per.values())
+    out = {"value": round(edges / secs / 1e9, 4), "unit": "GTEPS", "cores": os.cpu_count(), "kind": "port",
+           "sample": "one full kernel-set step on the RMAT-22 graph built on the host cores by the oracle, "
+                     "run as four quarter steps (oracle/gbx_oracle.c, OpenMP, all host threads): BFS from the "
+                     "64 roots, SSSP from 4 (delta 64), TC, 20 PR iterations, CC, SpMV, degree reorder",
+           "seconds": round(secs, 2), "per_kernel_gteps": {k: round(e / s / 1e9, 4) for k, (e, s) in per.items()},
+           **cpu_info()}
+    return out, tri
 
 
-def cpu_baseline(W, args, roots):
-    res = cpu_sample(W, roots)
-    value, secs = mix_gteps(res, step_mix(W, res, 4, 1))
-    return {"value": round(value, 4), "unit": "GTEPS", "cores": os.cpu_count(), "kind": "port",
-            "sample": "RMAT-22 kernel set on the host cores: BFS 4 roots, SSSP 1 root (delta 64), CC Afforest, "
-                      "TC, SpMV, PR 20 iterations, degree reorder (oracle/gbx_oracle.c, OpenMP); value = the "
-                      "full step's edges (64 BFS roots, 4 SSSP roots, ...) at the sampled per-kernel rates",
-            "seconds_sampled": round(sum(t for _, t in res.values()), 2), "seconds_full_step": round(secs, 2),
-            "per_kernel_gteps": {n: round(e / t / 1e9, 4) for n, (e, t) in res.items()}}
+def parity_kernel_set(torch, gbx, W, Wc, dg, dgs, dgr, tri_oracle, stream):
+    """The GPU results of the kernel set on the RMAT-22 graph against the
+    oracle on the same inputs (outside every timed region): the CSR builds
+    and the degree reordering array for array; BFS levels, processed_nodes
+    and iteration for all 64 roots; SSSP distances for the 4 roots; CC
+    labels; the triangle count -- all bit-exact; PageRank (20 iterations)
+    and SpMV as relative L1 against the FP64 restatement (tolerance 1e-6)."""
+    from oracle import pyoracle as po
+
+    sp = stream.cuda_stream
+    g, gc = W["g"], Wc["g"]
+    V = g.num_vertices
+    out = {}
+    fields = {"g": ("out_degree", "edges_idx", "dest", "weight", "inverse_out_degree", "inverse_edges_idx",
+                    "inverse_dest", "inverse_weight"),
+              "gs": ("out_degree", "edges_idx", "dest"), "gsr": ("out_degree", "edges_idx", "dest")}
+
+    def same(a, b):
+        if a is None or b is None:
+            return a is None and b is None
+        return a.shape == b.shape and np.array_equal(np.asarray(a).view(np.uint32), np.asarray(b).view(np.uint32))
+
+    out["csr_build"] = all(same(getattr(W[k], f), getattr(Wc[k], f)) for k, fs in fields.items() for f in fs)
+    out["degree_reorder_build"] = (same(W["reorder_labels"][0], Wc["reorder_labels"][0])
+                                   and same(W["reorder_labels"][1], Wc["reorder_labels"][1]))
+    host = po.HostCSR(V, gc.out_degree, gc.edges_idx, gc.dest, gc.weight, gc.src)
+    pull = po.HostCSR(V, gc.inverse_out_degree, gc.inverse_edges_idx, gc.inverse_dest, gc.inverse_weight)
+    dh = np.zeros(V, np.uint32)
+    ph = np.zeros(V, np.int32)
+    bad = []
+    for r in W["roots"]:
+        st = gbx.breadth_first_search(dg, r, 2, distances=dh, parents=ph, stream=sp)
+        d, _, proc, it = po.bfs(host, r, pull)
+        if not (np.array_equal(dh, d) and st.processed_nodes == proc and st.iteration == it):
+            bad.append(int(r))
+    out["bfs"] = {"roots": len(W["roots"]), "exact": not bad, "mismatched_roots": bad}
+    bad = []
+    for r in W["roots"][:N_SSSP_ROOTS]:
+        gbx.sssp(dg, r, 0, distances=dh, stream=sp)
+        if not np.array_equal(dh, po.sssp(host, r, 64)):
+            bad.append(int(r))
+    out["sssp"] = {"roots": N_SSSP_ROOTS, "exact": not bad, "mismatched_roots": bad}
+    comp, _ = gbx.connected_components(dgs, 1, components=np.zeros(V, np.uint32), stream=sp)
+    out["cc"] = bool(np.array_equal(np.asarray(comp), po.cc(po.HostCSR(V, Wc["gs"].out_degree, Wc["gs"].edges_idx,
+                                                                         Wc["gs"].dest), 1)))
+    tri = gbx.triangle_count(dgr, stream=sp)
+    out["tc"] = {"count": int(tri), "oracle": int(tri_oracle), "exact": int(tri) == int(tri_oracle)}
+    lab = np.arange(V, dtype=np.uint32)
+    inv = np.arange(V, dtype=np.uint32)
+    el = gbx.EdgeList(V, g.src.copy(), g.dest.copy(), None, lab, inv)
+    gbx.degree_reorder(el, 1, stream=sp)
+    rs, rd, olab, oinv = po.degree_reorder(V, gc.src, gc.dest, 1)
+    out["reorder"] = bool(same(el.label_array, olab) and same(el.inverse_label_array, oinv)
+                          and same(el.src, rs) and same(el.dst, rd))
+    pr = np.asarray(gbx.page_rank(dg, PR_ITERS, 0.0, ranks=np.zeros(V, np.float32), stream=sp).pageRanks)
+    r64, _, _ = po.pagerank(host, PR_ITERS, 0.0, pull, fp64=True)
+    ok, err, sub = po.fp32_close(pr, r64, 1e-6)
+    out["pr"] = {"iterations": PR_ITERS, "rel_l1_vs_fp64": float(f"{err:.3e}"), "within_1e-6": bool(ok)}
+    y = np.zeros(V, np.float32)
+    gbx.spmv(dg, Wc["x"], values=Wc["vals"], iterations=1, y=y, stream=sp)
+    y64 = po.spmv(host, Wc["x"], Wc["vals"], pull=pull, fp64=True)
+    ok, err, sub = po.fp32_close(y, y64, 1e-6)
+    out["spmv"] = {"rel_l1_vs_fp64": float(f"{err:.3e}"), "within_1e-6": bool(ok)}
+    out["all_exact"] = bool(out["csr_build"] and out["degree_reorder_build"] and out["bfs"]["exact"]
+                            and out["sssp"]["exact"] and out["cc"] and out["tc"]["exact"] and out["reorder"]
+                            and out["pr"]["within_1e-6"] and out["spmv"]["within_1e-6"])
+    return out
+
+
+def workload_config(args, V, E, Esym, e_plus, world):
+    """The `config` both arms print (identical keys and values)."""
+    return {"workload": f"rmat{args.scale}_full_kernel_set", "scale": args.scale, "num_vertices": V,
+            "edges_generated": V * EDGE_FACTOR, "num_edges": E, "num_edges_symmetric": Esym,
+            "dag_edges": e_plus, "bfs_roots": N_ROOTS, "sssp_roots": N_SSSP_ROOTS, "pr_iterations": PR_ITERS,
+            "l2": "inputs larger than L2 (0.5 GB CSR); the GPU arm also writes 256 MiB before every kernel",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
 def run_reference(args):
+    """The reference arm: the oracle port of the reference's OpenMP kernels on
+    the host cores (all threads) on the same RMAT-22 workload, built on the
+    host by the oracle (nothing from the GPU library). Each step is one
+    quarter of the kernel set (CPU_CYCLE); value = traversed edges / seconds
+    over the timed steps, ms_per_step = their mean wall time."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import graphblox_gb300 as gbx
-
-    W = build_workload(gbx, scale=args.scale)
-    roots = W["roots"]
-    values, secs = [], []
-    tc_res = None
-    for i in range(args.warmup + args.steps):
-        # the oracle's triangle count is most of a sample's CPU time (~15 s at
-        # RMAT-22): it is timed once, in the first measured step, and its rate
-        # is reused for the others, so the run stays within a few minutes for
-        # any --steps / --warmup
-        timed_tc = i >= args.warmup and tc_res is None
-        res = cpu_sample(W, roots[i % len(roots):] + roots, n_bfs=2, pr_iters=5, n_sssp=1, with_tc=timed_tc)
-        if timed_tc:
-            tc_res = res["tc"]
-        if i >= args.warmup:
-            res["tc"] = tc_res
-            v, s = mix_gteps(res, step_mix(W, res, 2, 1))
-            values.append(v)
-            secs.append(s)
-    value = float(np.mean(values))
+    Wc = build_workload_oracle(scale=args.scale)
+    plan = cpu_plan(Wc)
+    for i in range(args.warmup):
+        cpu_step(Wc, plan, i)
+    edges = secs = 0.0
+    walls = []
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        res, _ = cpu_step(Wc, plan, i)
+        walls.append(time.perf_counter() - t0)
+        edges += sum(e for e, _ in res.values())
+        secs += sum(s for _, s in res.values())
+    value = edges / secs / 1e9
+    g, gs, gsr = Wc["g"], Wc["gs"], Wc["gsr"]
+    e_plus = int(sum(plan["tc_dag_edges"]))
     line = {
         "metric": "GTEPS per kernel (aggregate over the kernel set) & %HBM-peak per kernel",
         "value": round(value, 4), "unit": "GTEPS", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(float(np.mean(secs)) * 1e3, 2),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(float(np.mean(walls)) * 1e3, 2),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32 (ids, levels, distances) + f32 (ranks, SpMV)", "data": "synthetic",
-        "config": {"workload": f"rmat{args.scale}_full_kernel_set", "scale": args.scale, "num_vertices": W["V"],
-                   "num_edges": W["g"].num_edges},
+        "config": workload_config(args, g.num_vertices, g.num_edges, gs.num_edges, e_plus,
+                                  int(os.environ.get("WORLD_SIZE", "1"))),
         "impl": "reference",
         "cpu_baseline": {"value": round(value, 4), "unit": "GTEPS", "cores": os.cpu_count(), "kind": "port",
-                         "sample": "per step: BFS 2 roots, SSSP 1 root (delta 64), CC, SpMV, PR 5 "
-                                   "iterations, degree reorder on the RMAT-22 graph, TC timed once in the first "
-                                   "measured step (oracle/gbx_oracle.c, OpenMP; "
-                                   "the reference tree is not on the GPU host, so its compiled form cannot run); "
-                                   "value and ms_per_step = the full step's edges (64 BFS roots, 4 SSSP roots, "
-                                   "20 PR iterations, ...) at the sampled per-kernel rates, the GPU value's mix"},
+                         "sample": f"each step a quarter of the kernel set ({CPU_CYCLE} steps = one full step: "
+                                   "16 BFS roots, 1 SSSP root (delta 64), a quarter of the TC pivots by work, "
+                                   "5 PR iterations, and CC, SpMV or the degree reordering) on the RMAT-22 "
+                                   "graph the oracle built on the host cores (oracle/gbx_oracle.c, OpenMP, "
+                                   "all threads; the reference tree is not on the GPU host, so its compiled "
+                                   "form cannot run there)",
+                         "seconds_timed": round(secs, 2), **cpu_info()},
         "e2e": {"value": round(value, 4), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -1009,6 +1292,8 @@ def main():
     ap.add_argument("--scale", type=int, default=SCALE, help="RMAT scale (22 is the benchmark workload)")
     ap.add_argument("--only", default="", help="comma-separated kernel subset (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the full-size checks of the GPU results against the oracle")
     ap.add_argument("--no-ppr", action="store_true", help="skip the personalised PageRank forward/adjoint section")
     ap.add_argument("--no-more", action="store_true",
                     help="skip the betweenness / Bellman-Ford / DFS section")
@@ -1022,6 +1307,16 @@ def main():
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the dominant kernel from an ncu capture")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: re-launch this command under torchrun
+        import socket
+
+        with socket.socket() as so:
+            so.bind(("127.0.0.1", 0))
+            port = so.getsockname()[1]
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+               "--master-addr=127.0.0.1", f"--master-port={port}", str(Path(__file__).resolve()), *sys.argv[1:]]
+        sys.exit(subprocess.call(cmd))
     if args.warmup < 3 and args.impl == "gbx":
         log("note: fewer than 3 warm-up steps requested")
     if args.impl == "reference":

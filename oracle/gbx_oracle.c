@@ -44,60 +44,99 @@ static void counting_pass(uint32_t n, const uint32_t *key, uint32_t nkeys,
     free(cnt);
 }
 
-/* A stable sort of perm_in by key[] into perm_out: one counting pass for
- * keys below 2^24, else two 16-bit digit passes (ids that carry the mask
- * bits of mask mode reach 2^32 - 1). */
-static void stable_key_sort(uint32_t n, const uint32_t *key, uint32_t maxkey,
-                            uint32_t *perm_in, uint32_t *perm_out) {
-    if (maxkey < (1u << 24)) {
-        counting_pass(n, key, maxkey + 1, perm_in, perm_out);
-        return;
+/* One stable LSD radix pass over (key, index) pairs: digit = key bits
+ * [shift, shift + 11). Each thread counts and scatters a contiguous chunk,
+ * and the chunks' offsets are laid out thread after thread within a digit,
+ * so equal digits keep their input order. */
+#define ORC_RADIX_BITS 11
+#define ORC_RADIX (1u << ORC_RADIX_BITS)
+static void radix_pass(uint32_t n, int shift, const uint64_t *kin, const uint32_t *iin, uint64_t *kout,
+                       uint32_t *iout) {
+    const int T = omp_get_max_threads();
+    uint32_t *hist = (uint32_t *)calloc((size_t)T * ORC_RADIX, 4);
+    if (!hist) abort();
+    const uint32_t chunk = (uint32_t)(((uint64_t)n + T - 1) / T);
+    #pragma omp parallel num_threads(T)
+    {
+        const int t = omp_get_thread_num();
+        const uint32_t lo = (uint32_t)((uint64_t)t * chunk < n ? (uint64_t)t * chunk : n);
+        const uint32_t hi = (uint32_t)((uint64_t)lo + chunk < n ? (uint64_t)lo + chunk : n);
+        uint32_t *h = hist + (size_t)t * ORC_RADIX;
+        for (uint32_t i = lo; i < hi; ++i) h[(kin[i] >> shift) & (ORC_RADIX - 1)]++;
+        #pragma omp barrier
+        #pragma omp single
+        {
+            uint32_t run = 0;
+            for (uint32_t d = 0; d < ORC_RADIX; ++d)
+                for (int u = 0; u < T; ++u) {
+                    const uint32_t c = hist[(size_t)u * ORC_RADIX + d];
+                    hist[(size_t)u * ORC_RADIX + d] = run;
+                    run += c;
+                }
+        }
+        for (uint32_t i = lo; i < hi; ++i) {
+            const uint32_t pos = h[(kin[i] >> shift) & (ORC_RADIX - 1)]++;
+            kout[pos] = kin[i];
+            iout[pos] = iin[i];
+        }
     }
-    uint32_t *digit = (uint32_t *)calloc((size_t)n + 1, 4);
-    if (!digit) abort();
-    for (uint32_t i = 0; i < n; ++i) digit[i] = key[i] & 0xFFFFu;
-    counting_pass(n, digit, 1u << 16, perm_in, perm_out);
-    for (uint32_t i = 0; i < n; ++i) digit[i] = key[i] >> 16;
-    counting_pass(n, digit, 1u << 16, perm_out, perm_in);
-    memcpy(perm_out, perm_in, (size_t)n * 4);
-    free(digit);
+    free(hist);
 }
 
 /* radixSortEdgesBySource / ...BySourceAndDestination (radixsort.c:231-339):
- * LSD order -- destination pass first, then a stable source pass, on the
- * full 32-bit ids. */
+ * a stable sort by source (sort_mode 0/2) or by (source, destination)
+ * (sort_mode 1/3) on the full 32-bit ids, as LSD radix passes over the
+ * composite key (source << 32 | destination); edges with equal keys keep
+ * their input order. */
 void orc_sort_edges(uint32_t num_edges, uint32_t *src, uint32_t *dst, float *w,
                     int sort_mode, int num_threads) {
-    (void)num_threads;
+    set_threads(num_threads);
     if (num_edges == 0) return;
-    uint32_t maxid = 0;
-    for (uint32_t i = 0; i < num_edges; ++i) {
-        if (src[i] > maxid) maxid = src[i];
-        if (dst[i] > maxid) maxid = dst[i];
+    const uint32_t n = num_edges;
+    const int by_dst = sort_mode == 1 || sort_mode == 3;
+    uint32_t maxs = 0, maxd = 0;
+    #pragma omp parallel for reduction(max : maxs, maxd)
+    for (uint32_t i = 0; i < n; ++i) {
+        if (src[i] > maxs) maxs = src[i];
+        if (dst[i] > maxd) maxd = dst[i];
     }
-    uint32_t *p0 = (uint32_t *)xmalloc((size_t)num_edges * 4);
-    uint32_t *p1 = (uint32_t *)xmalloc((size_t)num_edges * 4);
-    for (uint32_t i = 0; i < num_edges; ++i) p0[i] = i;
-    uint32_t *cur = p0, *nxt = p1;
-    if (sort_mode == 1 || sort_mode == 3) {
-        stable_key_sort(num_edges, dst, maxid, cur, nxt);
-        uint32_t *t = cur; cur = nxt; nxt = t;
+    uint64_t *k0 = (uint64_t *)xmalloc((size_t)n * 8), *k1 = (uint64_t *)xmalloc((size_t)n * 8);
+    uint32_t *i0 = (uint32_t *)xmalloc((size_t)n * 4), *i1 = (uint32_t *)xmalloc((size_t)n * 4);
+    #pragma omp parallel for
+    for (uint32_t i = 0; i < n; ++i) {
+        k0[i] = ((uint64_t)src[i] << 32) | (by_dst ? dst[i] : 0u);
+        i0[i] = i;
     }
-    stable_key_sort(num_edges, src, maxid, cur, nxt);
-    cur = nxt;
-    uint32_t *ts = (uint32_t *)xmalloc((size_t)num_edges * 4);
-    for (uint32_t i = 0; i < num_edges; ++i) ts[i] = src[cur[i]];
-    memcpy(src, ts, (size_t)num_edges * 4);
-    for (uint32_t i = 0; i < num_edges; ++i) ts[i] = dst[cur[i]];
-    memcpy(dst, ts, (size_t)num_edges * 4);
+    int bits_d = 0, bits_s = 0;
+    while (by_dst && bits_d < 32 && (maxd >> bits_d)) bits_d++;
+    while (bits_s < 32 && (maxs >> bits_s)) bits_s++;
+    for (int sh = 0; sh < bits_d; sh += ORC_RADIX_BITS) {
+        radix_pass(n, sh, k0, i0, k1, i1);
+        uint64_t *tk = k0; k0 = k1; k1 = tk;
+        uint32_t *ti = i0; i0 = i1; i1 = ti;
+    }
+    for (int sh = 0; sh < bits_s; sh += ORC_RADIX_BITS) {
+        radix_pass(n, 32 + sh, k0, i0, k1, i1);
+        uint64_t *tk = k0; k0 = k1; k1 = tk;
+        uint32_t *ti = i0; i0 = i1; i1 = ti;
+    }
+    /* apply the permutation i0 */
+    uint32_t *t = (uint32_t *)k1;
+    #pragma omp parallel for
+    for (uint32_t i = 0; i < n; ++i) t[i] = dst[i0[i]];
+    memcpy(dst, t, (size_t)n * 4);
+    #pragma omp parallel for
+    for (uint32_t i = 0; i < n; ++i) src[i] = (uint32_t)(k0[i] >> 32);
     if (w) {
-        float *tw = (float *)ts;
-        for (uint32_t i = 0; i < num_edges; ++i) tw[i] = w[cur[i]];
-        memcpy(w, tw, (size_t)num_edges * 4);
+        float *tw = (float *)k1;
+        #pragma omp parallel for
+        for (uint32_t i = 0; i < n; ++i) tw[i] = w[i0[i]];
+        memcpy(w, tw, (size_t)n * 4);
     }
-    free(ts);
-    free(p0);
-    free(p1);
+    free(k0);
+    free(k1);
+    free(i0);
+    free(i1);
 }
 
 /* removeDulpicatesSelfLoopEdges (edgeList.c:255-321). The reference keeps
@@ -803,12 +842,14 @@ void orc_cc(uint32_t num_vertices, const uint32_t *out_degree, const uint32_t *e
 /* triangleCountPullGraphCSR (triangleCount.c:254-334). The innermost scan
  * of N(u) for the first element >= w is a membership test on a sorted
  * list, done here with a binary search; the count is the same. */
-uint64_t orc_triangle_count(uint32_t num_vertices, const uint32_t *out_degree,
-                            const uint32_t *edges_idx, const uint32_t *dest, int num_threads) {
+uint64_t orc_triangle_count_range(uint32_t num_vertices, const uint32_t *out_degree,
+                                  const uint32_t *edges_idx, const uint32_t *dest, uint32_t lo,
+                                  uint32_t hi, int num_threads) {
     set_threads(num_threads);
     uint64_t count = 0;
+    if (hi > num_vertices) hi = num_vertices;
     #pragma omp parallel for schedule(dynamic, 128) reduction(+ : count)
-    for (uint32_t u = 0; u < num_vertices; ++u) {
+    for (uint32_t u = lo; u < hi; ++u) {
         const uint32_t *nu = dest + edges_idx[u];
         uint32_t du = out_degree[u];
         for (uint32_t a = 0; a < du; ++a) {
@@ -820,16 +861,21 @@ uint64_t orc_triangle_count(uint32_t num_vertices, const uint32_t *out_degree,
                 uint32_t w = nv[c] & 0x3FFFFFFFu;
                 if (w > v) break;
                 /* first element of N(u) that is >= w */
-                uint32_t lo = 0, hi = du;
-                while (lo < hi) {
-                    uint32_t mid = (lo + hi) >> 1;
-                    if ((nu[mid] & 0x3FFFFFFFu) < w) lo = mid + 1; else hi = mid;
+                uint32_t l = 0, h = du;
+                while (l < h) {
+                    uint32_t mid = (l + h) >> 1;
+                    if ((nu[mid] & 0x3FFFFFFFu) < w) l = mid + 1; else h = mid;
                 }
-                if (lo < du && (nu[lo] & 0x3FFFFFFFu) == w) count++;
+                if (l < du && (nu[l] & 0x3FFFFFFFu) == w) count++;
             }
         }
     }
     return count;
+}
+
+uint64_t orc_triangle_count(uint32_t num_vertices, const uint32_t *out_degree,
+                            const uint32_t *edges_idx, const uint32_t *dest, int num_threads) {
+    return orc_triangle_count_range(num_vertices, out_degree, edges_idx, dest, 0, num_vertices, num_threads);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1044,4 +1090,73 @@ void orc_dfs(uint32_t num_vertices, const uint32_t *out_degree, const uint32_t *
     }
     *processed_nodes = processed;
     free(stack);
+}
+
+/* ------------------------------------------------------------------------ */
+/* synthetic inputs (no reference counterpart)                              */
+/* ------------------------------------------------------------------------ */
+
+/* splitmix64's finaliser (Steele, Lea and Flood, 2014) */
+static inline uint64_t orc_mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+/* the start of the stream of draw `index` under `seed` */
+static inline uint64_t orc_stream(uint64_t seed, uint64_t index) {
+    return orc_mix64(seed * 0xD1B54A32D192ED03ull + 0x9E3779B97F4A7C15ull) ^ (index * 0x9E3779B97F4A7C15ull);
+}
+
+int orc_generate_rmat(uint32_t scale, uint64_t num_edges, double a, double b, double c, uint64_t seed,
+                      uint32_t *src, uint32_t *dst) {
+    if (!src || !dst || scale == 0 || scale > 30 || a < 0 || b < 0 || c < 0 || a + b + c > 1.0) return -1;
+    /* quadrant cut points on a 32-bit uniform */
+    const double two32 = 4294967296.0;
+    const uint64_t cut_a = (uint64_t)(a * two32), cut_ab = (uint64_t)((a + b) * two32);
+    const uint64_t cut_abc = (uint64_t)((a + b + c) * two32);
+    #pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < (int64_t)num_edges; ++e) {
+        uint64_t state = orc_stream(seed, (uint64_t)e), word = 0;
+        uint32_t s = 0, d = 0;
+        for (uint32_t level = 0; level < scale; ++level) {
+            /* one 64-bit draw serves two levels: low half, then high half */
+            if (!(level & 1u)) {
+                state += 0x9E3779B97F4A7C15ull;
+                word = orc_mix64(state);
+            }
+            const uint64_t r = (level & 1u) ? (word >> 32) : (word & 0xFFFFFFFFull);
+            const uint32_t right = r >= cut_abc || (r >= cut_a && r < cut_ab);  /* quadrants b, d */
+            const uint32_t down = r >= cut_ab;                                 /* quadrants c, d */
+            s = (s << 1) | down;
+            d = (d << 1) | right;
+        }
+        src[e] = s;
+        dst[e] = d;
+    }
+    return 0;
+}
+
+int orc_generate_values(uint64_t count, int kind, uint32_t lo, uint32_t hi, uint64_t seed, float *out) {
+    if (!out || kind < 0 || kind > 3 || (kind == 0 && hi < lo)) return -1;
+    const uint64_t span = (uint64_t)hi - lo + 1;
+    #pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)count; ++i) {
+        const uint64_t h = orc_mix64(orc_stream(seed, (uint64_t)i) + 0x632BE59BD9B4E019ull);
+        float v;
+        if (kind == 0) {
+            v = (float)(lo + (uint32_t)(h % span));
+        } else if (kind == 1) {
+            v = (float)((double)((h >> 40) + 1) / 16777216.0);
+        } else if (kind == 2) {
+            v = (float)((double)(h >> 40) / 8388608.0 - 1.0);
+        } else {
+            /* Box-Muller on two 26-bit uniforms in (0, 1) */
+            const double u1 = ((double)(h >> 38) + 0.5) / 67108864.0;
+            const double u2 = ((double)((h >> 12) & 0x3FFFFFFull) + 0.5) / 67108864.0;
+            v = (float)exp(sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2));
+        }
+        out[i] = v;
+    }
+    return 0;
 }

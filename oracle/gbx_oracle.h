@@ -125,6 +125,23 @@ void orc_dfs(uint32_t num_vertices, const uint32_t *out_degree, const uint32_t *
              const uint32_t *dest, uint32_t source, uint32_t *distances, int32_t *parents,
              uint32_t *processed_nodes);
 
+/* ---- synthetic inputs (no reference counterpart) ----------------------
+ * The same counter-based streams as the library's generators (every edge or
+ * value drawn from a stream keyed by (seed, index)), so the CPU side builds
+ * the benchmark's inputs without the GPU library: RMAT edges with quadrant
+ * probabilities a, b, c (d = 1-a-b-c), and values of `kind` 0 (integers in
+ * [lo, hi]), 1 (uniform (0, 1]), 2 (uniform [-1, 1)), 3 (lognormal(0, 1)). */
+int orc_generate_rmat(uint32_t scale, uint64_t num_edges, double a, double b, double c, uint64_t seed,
+                      uint32_t *src, uint32_t *dst);
+int orc_generate_values(uint64_t count, int kind, uint32_t lo, uint32_t hi, uint64_t seed, float *out);
+
+/* Triangles whose largest vertex u lies in [lo, hi) (the pull count of
+ * orc_triangle_count restricted to those pivots): the counts of a partition
+ * of [0, V) sum to the whole count. */
+uint64_t orc_triangle_count_range(uint32_t num_vertices, const uint32_t *out_degree,
+                                  const uint32_t *edges_idx, const uint32_t *dest, uint32_t lo,
+                                  uint32_t hi, int num_threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -48,6 +48,9 @@ def load():
             "orc_sssp": (None, [u32, vp, vp, vp, vp, u32, u32, vp, vp, C.c_int]),
             "orc_cc": (None, [u32, vp, vp, vp, vp, vp, vp, C.c_int, vp, vp, C.c_int]),
             "orc_triangle_count": (u64, [u32, vp, vp, vp, C.c_int]),
+            "orc_triangle_count_range": (u64, [u32, vp, vp, vp, u32, u32, C.c_int]),
+            "orc_generate_rmat": (C.c_int, [u32, u64, C.c_double, C.c_double, C.c_double, u64, vp, vp]),
+            "orc_generate_values": (C.c_int, [u64, C.c_int, u32, u32, u64, vp]),
             "orc_spmv_pull": (None, [u32, vp, vp, vp, vp, C.c_float, vp, vp, u32, C.c_int]),
             "orc_spmv_pull_f64": (None, [u32, vp, vp, vp, vp, C.c_float, vp, vp, u32, C.c_int]),
         }
@@ -208,8 +211,28 @@ def cc(g: HostCSR, variant=1, pull: Optional[HostCSR] = None, threads=0):
     return comp
 
 
-def triangle_count(g: HostCSR, threads=0):
-    return int(load().orc_triangle_count(g.num_vertices, _p(g.out_degree), _p(g.edges_idx), _p(g.dest), threads))
+def triangle_count(g: HostCSR, threads=0, lo=0, hi=None):
+    """Triangles whose largest vertex is in [lo, hi) (all of them by default)."""
+    hi = g.num_vertices if hi is None else hi
+    return int(load().orc_triangle_count_range(g.num_vertices, _p(g.out_degree), _p(g.edges_idx), _p(g.dest),
+                                               int(lo), int(hi), threads))
+
+
+def generate_rmat(scale, num_edges, a=0.57, b=0.19, c=0.19, seed=1):
+    """RMAT edges from the same stream as the library's generator."""
+    src = np.zeros(int(num_edges), np.uint32)
+    dst = np.zeros(int(num_edges), np.uint32)
+    if load().orc_generate_rmat(int(scale), int(num_edges), a, b, c, int(seed), _p(src), _p(dst)) != 0:
+        raise ValueError("bad RMAT parameters")
+    return src, dst
+
+
+def generate_values(count, kind, lo=0, hi=0, seed=1):
+    """Values from the same stream as the library's generator."""
+    out = np.zeros(int(count), np.float32)
+    if load().orc_generate_values(int(count), int(kind), int(lo), int(hi), int(seed), _p(out)) != 0:
+        raise ValueError("bad value-generator parameters")
+    return out
 
 
 def spmv(g: HostCSR, x, values=None, default_value=0.0001, iterations=1, y=None, pull: Optional[HostCSR] = None,

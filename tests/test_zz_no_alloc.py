@@ -8,7 +8,8 @@ a row on the same inputs and check both results against the allocating
 entry point, gbx_pagerank_pull, and against the oracle's FP64 restatement of
 the reference's recurrence, within the 1e-6 relative-L1 tolerance used for
 PageRank everywhere else; the result fields (iterations, active_last,
-error_total) are checked against gbx_pagerank_pull's. One case runs at the
+error_total) are checked against gbx_pagerank_pull's when both stop at the
+same iteration, else against the stop rule itself. One case runs at the
 array's maximum size, 4,194,304 vertices (RMAT scale 22). This file is
 collected last so that a failure here comes after every other test has run.
 """
@@ -66,21 +67,25 @@ def _check(gbx, g, dev, cases):
         refs = {(eps, iters): gbx.page_rank(dg, iters, eps) for eps, iters in set(cases)}
     for eps, iters in cases:
         ref = refs[(eps, iters)]
-        # the oracle in FP64, run for the iterations the GPU executed
-        executed = ref.iterations + 1 if (eps > 0 and ref.iterations < iters) else iters
-        r64, _, _ = po.pagerank(host, executed, 0.0, pull, fp64=True)
         for call in range(2):  # two calls in a row share (and reuse) the scratch array
             got, res = _noalloc(gbx, lib, V, d_off, d_src, d_deg, iters, eps, dev)
             ok, err, _ = po.fp32_close(got, np.asarray(ref.pageRanks), REL_L1_TOL)
             assert ok, f"call {call}: rel L1 {err:.3e} against gbx_pagerank_pull (epsilon {eps})"
+            # the oracle in FP64, run for the iterations this call executed
+            executed = res.iterations + 1 if (eps > 0 and res.iterations < iters) else iters
+            r64, _, _ = po.pagerank(host, executed, 0.0, pull, fp64=True)
             ok, err, _ = po.fp32_close(got, r64, REL_L1_TOL)
             assert ok, f"call {call}: rel L1 {err:.3e} against the FP64 oracle (epsilon {eps})"
-            # the stop test |delta| >= epsilon sits on a threshold: another FP32
-            # summation order may stop one iteration apart (ranks still agree)
-            assert abs(int(res.iterations) - int(ref.iterations)) <= (1 if eps > 0 else 0)
             if res.iterations == ref.iterations:
                 assert res.active_last == ref.active_last
                 assert res.error_total == pytest.approx(ref.error_total, rel=ERROR_TOTAL_RTOL, abs=1e-30)
+            else:
+                # The stop test |delta| >= epsilon works at the FP32 resolution of
+                # the largest ranks, so another summation order stops at another
+                # iteration; this call must still have stopped for the stated
+                # reason: nothing moved by epsilon in its last iteration.
+                assert eps > 0 and res.iterations < iters and res.active_last == 0
+                assert 0.0 <= res.error_total < eps
 
 
 def test_noalloc_pagerank_matches_allocating_entry_point(gbx, cuda_device):
