@@ -58,7 +58,10 @@ SIGNATURES = {
     "gbx_graph_get_tuning": (C.c_int, [vp, C.c_char_p, C.POINTER(C.c_double)]),
     "gbx_autotune": (C.c_int, [vp, u32, u32, vp]),
     "gbx_bfs": (C.c_int, [vp, u32, C.c_int, vp, vp, C.POINTER(BfsResult), vp]),
+    "gbx_bfs_top_down_step": (C.c_int, [vp, vp, u32, vp, vp, vp, u32, C.POINTER(u32), C.POINTER(u32), vp]),
+    "gbx_bfs_bottom_up_step": (C.c_int, [vp, vp, vp, vp, vp, C.POINTER(u32), vp]),
     "gbx_pagerank_pull": (C.c_int, [vp, u32, C.c_double, vp, C.POINTER(PrResult), vp]),
+    "gbx_pagerank_pull_fp64": (C.c_int, [vp, u32, vp, vp]),
     "gbx_pagerank_pull_noalloc": (C.c_int, [u32, vp, vp, vp, u32, C.c_double, vp, C.POINTER(PrResult), vp]),
     "gbx_bfs_multisource": (C.c_int, [vp, u32, vp, vp, vp, vp]),
     "gbx_batch_create": (C.c_int, [C.POINTER(vp), u32, vp, vp, vp, vp, vp, vp]),

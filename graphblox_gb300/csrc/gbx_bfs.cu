@@ -44,7 +44,8 @@ namespace gbx {
 constexpr uint32_t kHubDeg = 1024;    // out-degree above which a vertex is a hub
 constexpr uint32_t kHubChunk = 256;   // edges per hub work unit
 constexpr uint32_t kBuProbe = 64;     // bottom-up: in-edges a lane probes alone before the warp helps
-constexpr uint32_t kTdMaxSplit = 8;   // top-down: most warps sharing one 32-vertex group's edges
+constexpr uint32_t kTdMaxSplit = 64;  // top-down: most warps sharing one 32-vertex group's edges
+constexpr uint32_t kBuWords = 16;     // bottom-up: frontier-bitmap words (32 vertices each) per work unit
 constexpr int kBfsThreads = 256;
 constexpr int kBfsWarps = kBfsThreads / 32;
 
@@ -95,6 +96,7 @@ struct BfsArgs {
     uint32_t V, words, E, mode, source;
     uint32_t alpha, beta;  // direction switch: bottom-up when mf > mu/alpha, stay while nf > V/beta
     uint32_t pull_live;    // every pull neighbour has out-degree > 0
+    const uint32_t *live;  // bit v: v has pull in-edges (only such vertices can be found bottom-up)
     uint32_t *level;
     int32_t *parent;
     uint32_t *visited;
@@ -112,13 +114,14 @@ struct Claimer {
     const BfsArgs &a;
     uint32_t lnext;
     uint32_t *qout, *hvout, *hcout;
+    uint32_t *fbm;  // frontier bitmap of level lnext to fill, or null
     BfsStep *cnt;
     WarpQueue wq;
     unsigned nf = 0, mf = 0;
     unsigned long long edges = 0;
     __device__ __forceinline__ Claimer(const BfsArgs &a_, uint32_t l, uint32_t *q, uint32_t *hv, uint32_t *hc,
-                                       BfsStep *c, uint32_t *wbuf)
-        : a(a_), lnext(l), qout(q), hvout(hv), hcout(hc), cnt(c), wq(wbuf) {}
+                                       uint32_t *f, BfsStep *c, uint32_t *wbuf)
+        : a(a_), lnext(l), qout(q), hvout(hv), hcout(hc), fbm(f), cnt(c), wq(wbuf) {}
     // Four candidate edges per lane: the visited-word loads, then the
     // atomicOr claims, are issued back to back so their latencies overlap.
     __device__ __forceinline__ void claim4(const uint32_t (&v)[4], const uint32_t (&u)[4], const bool (&act)[4]) {
@@ -137,6 +140,7 @@ struct Claimer {
             if (won) {
                 a.level[u[q]] = lnext;
                 a.parent[u[q]] = (int32_t)v[q];
+                if (fbm) atomicOr(fbm + (u[q] >> 5), 1u << (u[q] & 31));
             }
         }
 #pragma unroll
@@ -171,22 +175,31 @@ struct Claimer {
     }
 };
 
-// last h in [0, n) with hc[h] <= c
-__device__ __forceinline__ uint32_t hub_of_chunk(const uint32_t *hc, uint32_t n, uint32_t c) {
-    uint32_t lo = 0, hi = n - 1;
-    while (lo < hi) {
-        uint32_t mid = (lo + hi + 1) >> 1;
-        if (__ldcg(hc + mid) <= c) lo = mid; else hi = mid - 1;
+// Position of the r-th set bit (from 0) of m; m has more than r set bits.
+__device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t r) {
+    uint32_t pos = 0;
+#pragma unroll
+    for (uint32_t w = 16; w >= 1; w >>= 1) {
+        const uint32_t low = __popc((m >> pos) & ((1u << w) - 1u));
+        if (r >= low) {
+            r -= low;
+            pos += w;
+        }
     }
-    return lo;
+    return pos;
 }
 
 __device__ void top_down_phase(const BfsArgs &a, const uint32_t *qin, uint32_t qn, const uint32_t *hvin,
                                const uint32_t *hcin, uint32_t nh, uint32_t nc, BfsStep *cur, uint32_t *qout,
-                               uint32_t *hvout, uint32_t *hcout, uint32_t lnext, uint32_t *s_pre,
-                               uint32_t *s_base, uint32_t *s_v, uint32_t *s_wq) {
+                               uint32_t *hvout, uint32_t *hcout, uint32_t lnext, uint32_t *fbm, uint32_t *clear_bm,
+                               uint32_t *s_pre, uint32_t *s_base, uint32_t *s_v, uint32_t *s_wq) {
     const uint32_t lane = threadIdx.x & 31;
-    Claimer claim(a, lnext, qout, hvout, hcout, cur, s_wq);
+    if (clear_bm) {
+        // the bitmap the next top-down step fills (not read during this one)
+        for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < a.words; w += gridDim.x * blockDim.x)
+            clear_bm[w] = 0u;
+    }
+    Claimer claim(a, lnext, qout, hvout, hcout, fbm, cur, s_wq);
     // a frontier with fewer 32-vertex groups than warps cuts each group's
     // edges into `split` interleaved parts of 128-edge batches
     const uint32_t groups = (qn + 31) / 32;
@@ -199,7 +212,7 @@ __device__ void top_down_phase(const BfsArgs &a, const uint32_t *qin, uint32_t q
         if (unit >= units) break;
         if (unit < nc) {
             // kHubChunk edges of one hub
-            const uint32_t h = hub_of_chunk(hcin, nh, unit);
+            const uint32_t h = warp_chunk_owner(hcin, nh, unit);
             const uint32_t v = __ldcg(hvin + h);
             const uint32_t rb = __ldg(a.off + v), re = __ldg(a.off + v + 1);
             const uint32_t cb = rb + (unit - __ldcg(hcin + h)) * kHubChunk;
@@ -279,115 +292,131 @@ __device__ __forceinline__ uint32_t bu_probe(const BfsArgs &a, const uint32_t *c
     return pick;
 }
 
+// One bottom-up step. A work unit is kBuWords frontier-bitmap words; its
+// candidates -- vertices not yet visited that have pull in-edges (the live
+// bitmap), the only ones a bottom-up step can find -- are numbered word by
+// word and dealt to the lanes 32 at a time, so a lane never idles on a
+// visited or edgeless vertex. Each lane probes its candidate's in-edges
+// until one is in the current frontier bitmap (4, then 16 in flight; the
+// warp finishes rows longer than kBuProbe together). The found bits of the
+// unit's words are gathered in shared memory and written once, with the
+// next-frontier word of every word of the unit (zero when nothing was
+// found). Found vertices are also appended to the next generation's queue /
+// hub list, so leaving bottom-up needs no bitmap-to-list pass.
 __device__ void bottom_up_phase(const BfsArgs &a, const uint32_t *cur_bm, uint32_t *next_bm, uint32_t lnext,
-                                BfsStep *cnt, uint32_t *qout, uint32_t *hvout, uint32_t *hcout, uint32_t *s_wq) {
+                                BfsStep *cnt, uint32_t *qout, uint32_t *hvout, uint32_t *hcout, uint32_t *s_wq,
+                                uint32_t *s_found) {
     const uint32_t lane = threadIdx.x & 31;
     unsigned nf = 0;
     unsigned long long edges = 0;
     WarpQueue wq(s_wq);
-    constexpr uint32_t kWordsPerUnit = 8;
-    const uint32_t units = (a.words + kWordsPerUnit - 1) / kWordsPerUnit;
+    const uint32_t units = (a.words + kBuWords - 1) / kBuWords;
     UnitDealer dealer(&cnt->cursor);
-    // The unit's visited words come in one load (lane k holds word k; only
-    // this warp writes them during the step), and each lane's row bounds and
-    // out-degree for the next word are fetched while the current word is
-    // probed, so a word's dependent chain starts at the in-edge loads.
     for (uint32_t unit = dealer.take(units); unit < units; unit = dealer.take(units)) {
-        const uint32_t w0 = unit * kWordsPerUnit;
-        const uint32_t nw = min(a.words - w0, kWordsPerUnit);
-        const uint32_t vis_unit = lane < nw ? __ldcg(a.visited + w0 + lane) : 0xFFFFFFFFu;
-        auto row_of = [&](uint32_t k, uint32_t &rb, uint32_t &re, uint32_t &rd) {
-            const uint32_t vk = __shfl_sync(0xffffffffu, vis_unit, k);
-            const uint32_t vv = (w0 + k) * 32 + lane;
-            rb = re = rd = 0;
-            if (vk != 0xFFFFFFFFu && vv < a.V && !((vk >> lane) & 1u)) {
-                rb = __ldg(a.poff + vv);
-                re = __ldg(a.poff + vv + 1);
-                rd = __ldg(a.outdeg + vv);
-            }
-        };
-        uint32_t nb, ne, nd;
-        row_of(0, nb, ne, nd);
-    for (uint32_t k = 0; k < nw; ++k) {
-        const uint32_t w = w0 + k;
-        const uint32_t vis = __shfl_sync(0xffffffffu, vis_unit, k);
-        const uint32_t b = nb, e = ne, dv_pre = nd;
-        if (k + 1 < nw) row_of(k + 1, nb, ne, nd);
-        if (vis == 0xFFFFFFFFu) {
-            if (lane == 0) next_bm[w] = 0;
-            continue;
-        }
-        const uint32_t v = w * 32 + lane;
-        bool found = false;
-        uint32_t tb = 0, te = 0;  // in-edges still to probe after the lane's own first kBuProbe
-        if (v < a.V && !((vis >> lane) & 1u)) {
-            const uint32_t el = min(e, b + kBuProbe);
-            // a short first round (most vertices that have a frontier
-            // in-neighbour meet it among their first few), then wide rounds
-            uint32_t pu = bu_probe<4>(a, cur_bm, b, el);
-            for (uint32_t j = b + 4; pu == 0xFFFFFFFFu && j < el; j += 16) pu = bu_probe<16>(a, cur_bm, j, el);
-            if (pu != 0xFFFFFFFFu) {
-                a.level[v] = lnext;
-                a.parent[v] = (int32_t)pu;
-                found = true;
-            } else if (el < e) {
-                tb = el;
-                te = e;
-            }
-        }
-        // rows longer than kBuProbe that found nothing in their first part: the
-        // whole warp scans the rest, 128 in-edges per step, one row at a time
-        for (unsigned tv = __ballot_sync(0xffffffffu, tb < te); tv; tv &= tv - 1) {
-            const uint32_t k = __ffs(tv) - 1;
-            const uint32_t hb = __shfl_sync(0xffffffffu, tb, k), he = __shfl_sync(0xffffffffu, te, k);
-            for (uint32_t j0 = hb; j0 < he; j0 += 128) {
-                uint32_t u[4], fw[4];
+        const uint32_t w0 = unit * kBuWords;
+        const uint32_t nw = min(a.words - w0, kBuWords);
+        // lane k < nw holds word w0 + k (only this warp writes these words in the step)
+        const uint32_t vis = lane < nw ? __ldcg(a.visited + w0 + lane) : 0xFFFFFFFFu;
+        const uint32_t cand = lane < nw ? (~vis & __ldg(a.live + w0 + lane)) : 0u;
+        const uint32_t c = __popc(cand);
+        uint32_t incl = c;
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const uint32_t j = j0 + q * 32 + lane;
-                    u[q] = j < he ? __ldg(a.psrc + j) : 0u;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += t;
+        }
+        const uint32_t excl = incl - c, total = __shfl_sync(0xffffffffu, incl, 31);
+        if (lane < kBuWords) s_found[lane] = 0u;
+        __syncwarp();
+        for (uint32_t base = 0; base < total; base += 32) {
+            const uint32_t i = base + lane;
+            // the word of candidate i: last k with excl_k <= i
+            uint32_t k = 0;
+#pragma unroll
+            for (uint32_t step = 16; step > 0; step >>= 1)
+                if (__shfl_sync(0xffffffffu, excl, k + step) <= i) k += step;
+            const uint32_t mk = __shfl_sync(0xffffffffu, cand, k);
+            const uint32_t ek = __shfl_sync(0xffffffffu, excl, k);
+            const bool act = i < total;
+            uint32_t v = 0, b = 0, e = 0, dv = 0;
+            if (act) {
+                v = (w0 + k) * 32 + nth_set_bit(mk, i - ek);
+                b = __ldg(a.poff + v);
+                e = __ldg(a.poff + v + 1);
+                dv = __ldg(a.outdeg + v);
+            }
+            bool found = false;
+            uint32_t tb = 0, te = 0;  // in-edges still to probe after the lane's own first kBuProbe
+            if (act) {
+                const uint32_t el = min(e, b + kBuProbe);
+                // a short first round (most vertices that have a frontier
+                // in-neighbour meet it among their first few), then wide rounds
+                uint32_t pu = bu_probe<4>(a, cur_bm, b, el);
+                for (uint32_t j = b + 4; pu == 0xFFFFFFFFu && j < el; j += 16) pu = bu_probe<16>(a, cur_bm, j, el);
+                if (pu != 0xFFFFFFFFu) {
+                    a.level[v] = lnext;
+                    a.parent[v] = (int32_t)pu;
+                    found = true;
+                } else if (el < e) {
+                    tb = el;
+                    te = e;
                 }
+            }
+            // rows longer than kBuProbe that found nothing in their first part:
+            // the whole warp scans the rest, 128 in-edges per step, one row at a time
+            for (unsigned tv = __ballot_sync(0xffffffffu, tb < te); tv; tv &= tv - 1) {
+                const uint32_t owner = __ffs(tv) - 1;
+                const uint32_t hb = __shfl_sync(0xffffffffu, tb, owner), he = __shfl_sync(0xffffffffu, te, owner);
+                for (uint32_t j0 = hb; j0 < he; j0 += 128) {
+                    uint32_t u[4], fw[4];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) fw[q] = j0 + q * 32 + lane < he ? cur_bm[u[q] >> 5] : 0u;
-                uint32_t pick = 0xFFFFFFFFu;
-#pragma unroll
-                for (int q = 3; q >= 0; --q)
-                    if ((fw[q] >> (u[q] & 31)) & 1u) pick = u[q];
-                const unsigned hm = __ballot_sync(0xffffffffu, pick != 0xFFFFFFFFu);
-                if (hm) {
-                    const uint32_t pu = __shfl_sync(0xffffffffu, pick, __ffs(hm) - 1);
-                    if (lane == k) {
-                        a.level[v] = lnext;
-                        a.parent[v] = (int32_t)pu;
-                        found = true;
+                    for (int q = 0; q < 4; ++q) {
+                        const uint32_t j = j0 + q * 32 + lane;
+                        u[q] = j < he ? __ldg(a.psrc + j) : 0u;
                     }
-                    break;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) fw[q] = j0 + q * 32 + lane < he ? cur_bm[u[q] >> 5] : 0u;
+                    uint32_t pick = 0xFFFFFFFFu;
+#pragma unroll
+                    for (int q = 3; q >= 0; --q)
+                        if ((fw[q] >> (u[q] & 31)) & 1u) pick = u[q];
+                    const unsigned hm = __ballot_sync(0xffffffffu, pick != 0xFFFFFFFFu);
+                    if (hm) {
+                        const uint32_t pu = __shfl_sync(0xffffffffu, pick, __ffs(hm) - 1);
+                        if (lane == owner) {
+                            a.level[v] = lnext;
+                            a.parent[v] = (int32_t)pu;
+                            found = true;
+                        }
+                        break;
+                    }
                 }
             }
-        }
-        const unsigned m = __ballot_sync(0xffffffffu, found);
-        // the vertices found also form the next step's lists, in case the
-        // traversal returns to top-down after this step (bitmapToArrayQueue)
-        uint32_t dv = 0;
-        if (found) {
-            dv = dv_pre;
-            edges += dv;
-            if (dv > kHubDeg) {
-                const unsigned long long h = atomicAdd(&cnt->hub, (1ull << 32) | hub_chunks(dv));
-                const uint32_t slot = (uint32_t)(h >> 32);
-                hvout[slot] = v;
-                hcout[slot] = (uint32_t)h;
+            if (found) {
+                atomicOr(s_found + k, 1u << (v & 31));
+                edges += dv;
+                if (dv > kHubDeg) {
+                    const unsigned long long h = atomicAdd(&cnt->hub, (1ull << 32) | hub_chunks(dv));
+                    const uint32_t slot = (uint32_t)(h >> 32);
+                    hvout[slot] = v;
+                    hcout[slot] = (uint32_t)h;
+                }
             }
+            // the vertices found also form the next step's lists, in case the
+            // traversal returns to top-down after this step (bitmapToArrayQueue)
+            wq.push(v, found && dv > 0 && dv <= kHubDeg, qout, &cnt->qlen);
         }
-        wq.push(v, found && dv > 0 && dv <= kHubDeg, qout, &cnt->qlen);
-        if (lane == 0) {
-            next_bm[w] = m;
-            if (m) a.visited[w] = vis | m;
+        __syncwarp();
+        if (lane < nw) {
+            const uint32_t m = s_found[lane];
+            next_bm[w0 + lane] = m;
+            if (m) a.visited[w0 + lane] = vis | m;
             nf += __popc(m);
         }
-    }
+        __syncwarp();
     }
     wq.flush(qout, &cnt->qlen);
+    nf = warp_sum(nf);
     edges = warp_sum(edges);
     if (lane == 0 && (nf || edges)) {
         atomicAdd(&cnt->nf, nf);
@@ -439,11 +468,12 @@ __device__ __forceinline__ void zero_step(BfsStep *s) {
     s->edges = 0;
 }
 
-__global__ void __launch_bounds__(kBfsThreads) bfs_persistent_kernel(BfsArgs a) {
+__global__ void __launch_bounds__(kBfsThreads, 3) bfs_persistent_kernel(BfsArgs a) {
     __shared__ uint32_t s_pre[kBfsWarps][33];
     __shared__ uint32_t s_base[kBfsWarps][32];
     __shared__ uint32_t s_v[kBfsWarps][32];
     __shared__ uint32_t s_wq[kBfsWarps][kWarpQueueCap];
+    __shared__ uint32_t s_found[kBfsWarps][kBuWords];
     const uint32_t wid = threadIdx.x >> 5;
     BfsState *st = a.st;
     grid_barrier_init();
@@ -454,6 +484,11 @@ __global__ void __launch_bounds__(kBfsThreads) bfs_persistent_kernel(BfsArgs a) 
     unsigned long long edges_total = __ldg(a.outdeg + a.source);
     bool in_bu = false, done = false, failed = false;
     bool bm_clean[2] = {true, true};  // frontier bitmaps still all zero (cleared by bfs_init_kernel)
+    // Until the first bottom-up step, top-down steps also set the bits of the
+    // vertices they claim in the next frontier bitmap (and clear the other
+    // bitmap for the step after), so the switch to bottom-up finds the
+    // frontier bitmap ready (bm_ready) and needs no conversion pass.
+    bool bm_track = a.mode == 2, bm_ready = false;
     const uint32_t max_steps = 2 * a.V + 16;
     // lists for step 0: prepared by the host in generation 0
     uint32_t qn = __ldcg(&st->conv.qlen);
@@ -480,20 +515,24 @@ __global__ void __launch_bounds__(kBfsThreads) bfs_persistent_kernel(BfsArgs a) 
         }
         if (use_bu) {
             if (!in_bu) {
-                // arrayQueueToBitmap: frontier bitmap of the current level,
-                // scattered from the lists when they hold the whole frontier
-                // and the bitmap is still clear, else from level[]
-                if (bm_clean[ib] && (a.pull_live || qsize == qn + nh))
-                    lists_to_bitmap_phase(a.q[ib], qn, a.hv[ib], nh, a.bm[ib]);
-                else
-                    level_to_bitmap_phase(a, L, a.bm[ib]);
+                if (!bm_ready) {
+                    // arrayQueueToBitmap: frontier bitmap of the current level,
+                    // scattered from the lists when they hold the whole frontier
+                    // and the bitmap is still clear, else from level[]
+                    if (bm_clean[ib] && (a.pull_live || qsize == qn + nh))
+                        lists_to_bitmap_phase(a.q[ib], qn, a.hv[ib], nh, a.bm[ib]);
+                    else
+                        level_to_bitmap_phase(a, L, a.bm[ib]);
+                    if (!grid_barrier(&st->gs)) { failed = true; break; }
+                    trace_step(st, kTrToBitmap, qsize);
+                }
                 bm_clean[ib] = false;
-                if (!grid_barrier(&st->gs)) { failed = true; break; }
-                trace_step(st, kTrToBitmap, qsize);
+                bm_track = bm_ready = false;
                 nf_prev = qsize;
                 in_bu = true;
             }
-            bottom_up_phase(a, a.bm[ib], a.bm[ob], L + 1, cur, a.q[ob], a.hv[ob], a.hc[ob], s_wq[wid]);
+            bottom_up_phase(a, a.bm[ib], a.bm[ob], L + 1, cur, a.q[ob], a.hv[ob], a.hc[ob], s_wq[wid],
+                            s_found[wid]);
             bm_clean[ob] = false;
             if (!grid_barrier(&st->gs)) { failed = true; break; }
             const uint32_t nf = __ldcg(&cur->nf);
@@ -522,8 +561,16 @@ __global__ void __launch_bounds__(kBfsThreads) bfs_persistent_kernel(BfsArgs a) 
             }
         } else {
             mu -= mf;
+            // bm[ob] is clear here while tracking: bfs_init_kernel cleared both
+            // bitmaps, and each tracking step clears bm[ib] for the next one
             top_down_phase(a, a.q[ib], qn, a.hv[ib], a.hc[ib], nh, nc, cur, a.q[ob], a.hv[ob], a.hc[ob], L + 1,
-                           s_pre[wid], s_base[wid], s_v[wid], s_wq[wid]);
+                           bm_track ? a.bm[ob] : nullptr, bm_track && s > 0 ? a.bm[ib] : nullptr, s_pre[wid],
+                           s_base[wid], s_v[wid], s_wq[wid]);
+            if (bm_track) {
+                bm_clean[ob] = false;
+                bm_clean[ib] = true;
+                bm_ready = true;
+            }
             if (!grid_barrier(&st->gs)) { failed = true; break; }
             const uint32_t nf = __ldcg(&cur->nf);
             trace_step(st, kTrTopDown, nf);
@@ -593,6 +640,18 @@ __global__ void bfs_init_kernel(uint32_t *level, int32_t *parent, uint32_t *visi
             c.qlen = 1;
         }
         st->conv = c;
+    }
+}
+
+// live[w] bit b: vertex 32w + b exists and has pull in-edges
+__global__ void live_bits_kernel(const uint32_t *poff, uint32_t V, uint32_t words, uint32_t *live) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += nw) {
+        const uint32_t v = w * 32 + lane;
+        const bool has = v < V && __ldg(poff + v + 1) > __ldg(poff + v);
+        const unsigned m = __ballot_sync(0xffffffffu, has);
+        if (lane == 0) live[w] = m;
     }
 }
 
@@ -675,6 +734,13 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
         GBX_CUDA(cudaStreamSynchronize(s));
         g->pull_sources_live = h ? 0 : 1;
     }
+    if (!g->bu_live) {
+        // kept with the graph: which vertices a bottom-up step can find
+        GBX_CUDA(cudaMalloc(&g->bu_live, (size_t)words * 4));
+        live_bits_kernel<<<std::min<unsigned>(ceil_div(words * 32, 256), (unsigned)num_sms() * 8), 256, 0, s>>>(
+            g->pull_offsets(), V, words, g->bu_live);
+        GBX_LAUNCH_CHECK();
+    }
     // levels and parents live in the output arrays (device memory, or their
     // device staging) when the caller asked for them
     uint32_t *lev = dist.d ? dist.d : w.level;
@@ -696,6 +762,7 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
     a.alpha = g->bfs_alpha;
     a.beta = g->bfs_beta;
     a.pull_live = g->pull_sources_live == 1 ? 1u : 0u;
+    a.live = g->bu_live;
     a.level = lev;
     a.parent = parp;
     a.visited = w.visited;

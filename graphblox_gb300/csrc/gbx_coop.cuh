@@ -129,6 +129,25 @@ struct UnitDealer {
     }
 };
 
+// Owner of work chunk c in a list whose entry h owns chunks [hc[h], hc[h+1])
+// (hc strictly increasing, hc[0] = 0): the last h in [0, n) with hc[h] <= c,
+// searched 32 ways at a time by the whole warp -- log32(n) rounds of one
+// load per lane instead of log2(n) dependent loads. All lanes call together
+// and get the same answer.
+__device__ __forceinline__ uint32_t warp_chunk_owner(const uint32_t *hc, uint32_t n, uint32_t c) {
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t lo = 0, hi = n;  // answer in [lo, hi); hc[lo] <= c
+    while (hi - lo > 1) {
+        const uint32_t step = (hi - lo + 31) / 32;
+        const uint32_t idx = lo + lane * step;
+        const bool ok = idx < hi && __ldcg(hc + idx) <= c;
+        const unsigned m = __ballot_sync(0xffffffffu, ok);  // lane 0 always holds
+        lo += (31u - __clz(m)) * step;
+        hi = min(lo + step, hi);
+    }
+    return lo;
+}
+
 // Largest co-resident grid for `kernel` with `threads` per CTA. `cache`
 // (one per call site, indexed by device) keeps the answer after the first
 // occupancy query.

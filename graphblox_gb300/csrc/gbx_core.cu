@@ -380,6 +380,7 @@ int gbx_graph_destroy(gbx_graph *g) {
     cudaFree(g->in_weight);
     cudaFree(g->in_degree);
     cudaFree(g->low_count);
+    cudaFree(g->bu_live);
     gbx_free_tc_plan(g->tc_plan);
     gbx_free_ppr_cache(g->ppr);
     gbx_free_ms_plan(g->ms_plan);

@@ -221,6 +221,8 @@ struct gbx_graph {
     // every pull-CSR neighbour has out-degree > 0 (true for an inverse CSR of
     // the same edges, and for symmetric graphs): -1 unknown, 0 no, 1 yes
     int pull_sources_live = -1;
+    // BFS: bit v set when v has pull in-edges (built on first use, gbx_bfs.cu)
+    uint32_t *bu_live = nullptr;
     // tuning (gbx_graph_set_tuning / gbx_autotune): BFS direction switch and
     // SSSP bucket width (0 = default for the graph's weights)
     uint32_t bfs_alpha = 15, bfs_beta = 18;

@@ -27,7 +27,7 @@ namespace gbx {
 
 constexpr uint32_t kSsspHubDeg = 1024;
 constexpr uint32_t kSsspHubChunk = 1024;
-constexpr uint32_t kSsspMaxSplit = 8;  // most warps sharing one 32-vertex group's edges
+constexpr uint32_t kSsspMaxSplit = 64;  // most warps sharing one 32-vertex group's edges
 constexpr int kSsspThreads = 256;
 constexpr int kSsspWarps = kSsspThreads / 32;
 
@@ -112,34 +112,41 @@ struct Relaxer {
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) old[q] = (act[q] && nd[q] < cur[q]) ? atomicMin(a.dist + u[q], nd[q]) : 0u;
-        bool to_near[4], to_far[4], below[4];
+        // the improvements' follow-ups -- the next-near claim, the far flag and
+        // the out-degree of a next-near candidate -- are independent of each
+        // other, so all of them are issued before any reply is used
+        bool imp[4], below[4], far_cl[4];
+        uint32_t du[4], stamp_old[4], far_old[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             relaxed += act[q] ? 1u : 0u;
-            const bool imp = act[q] && nd[q] < cur[q] && nd[q] < old[q];
-            below[q] = imp && nd[q] < threshold;
-            to_near[q] = below[q] && atomicExch(a.stamp + u[q], round) != round;
-            to_far[q] = imp && nd[q] >= threshold && atomicExch(a.in_far + u[q], 1u) == 0u;
-            if (imp && nd[q] >= threshold) far_min = min(far_min, nd[q]);
+            imp[q] = act[q] && nd[q] < cur[q] && nd[q] < old[q];
+            below[q] = imp[q] && nd[q] < threshold;
+            far_cl[q] = imp[q] && nd[q] >= threshold;
+            if (far_cl[q]) far_min = min(far_min, nd[q]);
+            du[q] = below[q] ? __ldg(a.outdeg + u[q]) : 1u;
+            stamp_old[q] = below[q] ? atomicExch(a.stamp + u[q], round) : round;
+            far_old[q] = far_cl[q] ? atomicExch(a.in_far + u[q], 1u) : 1u;
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
+            const bool to_near = below[q] && stamp_old[q] != round;
+            const bool to_far = far_cl[q] && far_old[q] == 0u;
             bool hub = false;
-            const uint32_t du = below[q] ? __ldg(a.outdeg + u[q]) : 1u;
-            if (du == 0) {
+            if (du[q] == 0) {
                 // nothing to expand: its snapshot is simply its distance, so
                 // a far entry it left behind is dropped, not re-bucketed
                 atomicMin(a.settled + u[q], nd[q]);
                 hub = true;
-            } else if (to_near[q] && du > kSsspHubDeg) {
+            } else if (to_near && du[q] > kSsspHubDeg) {
                 hub = true;
-                unsigned long long h = atomicAdd(&cnt->near_hub, (1ull << 32) | sssp_chunks(du));
+                unsigned long long h = atomicAdd(&cnt->near_hub, (1ull << 32) | sssp_chunks(du[q]));
                 uint32_t slot = (uint32_t)(h >> 32);
                 hvout[slot] = u[q];
                 hcout[slot] = (uint32_t)h;
             }
-            wnear.push(u[q], to_near[q] && !hub, qout, &cnt->near_len);
-            wfar.push(u[q], to_far[q], far, &cnt->far_len);
+            wnear.push(u[q], to_near && !hub, qout, &cnt->near_len);
+            wfar.push(u[q], to_far, far, &cnt->far_len);
         }
     }
     __device__ __forceinline__ void flush() {
@@ -151,15 +158,6 @@ struct Relaxer {
         if ((threadIdx.x & 31) == 0 && m != 0xFFFFFFFFu) atomicMin(&cnt->far_min, m);
     }
 };
-
-__device__ __forceinline__ uint32_t sssp_hub_of_chunk(const uint32_t *hc, uint32_t n, uint32_t c) {
-    uint32_t lo = 0, hi = n - 1;
-    while (lo < hi) {
-        uint32_t mid = (lo + hi + 1) >> 1;
-        if (__ldcg(hc + mid) <= c) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
 
 __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn, const uint32_t *hvin,
                             const uint32_t *hcin, uint32_t nh, uint32_t nc, Relaxer &rx, SsspRound *cur,
@@ -177,7 +175,7 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
         const uint32_t unit = dealer.take(units);
         if (unit >= units) break;
         if (unit < nc) {
-            const uint32_t h = sssp_hub_of_chunk(hcin, nh, unit);
+            const uint32_t h = warp_chunk_owner(hcin, nh, unit);
             const uint32_t v = __ldcg(hvin + h);
             const uint32_t d = __ldcg(a.settled + v);
             const uint32_t rb = __ldg(a.off + v), re = __ldg(a.off + v + 1);

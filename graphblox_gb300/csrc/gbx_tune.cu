@@ -113,17 +113,26 @@ extern "C" int gbx_autotune(gbx_graph *g, uint32_t flags, uint32_t num_samples, 
     DevBuf<uint32_t> out;
     GBX_TRY(out.alloc(g->V, s));
     if ((flags & 1u) && g->has_inverse()) {
+        // a traversal's cost depends strongly on its source, so every
+        // candidate runs the same (at least 16) sources, twice, and keeps its
+        // faster pass
+        std::vector<uint32_t> bsrc;
+        GBX_TRY(sample_sources(g, std::max<uint32_t>(num_samples, 16), s, &bsrc));
         const uint32_t cands[] = {4, 15, 64, 256, 1024, 4096};
         float best = 1e30f;
         uint32_t best_a = g->bfs_alpha;
         for (uint32_t c : cands) {
             g->bfs_alpha = c;
-            GBX_TRY(gbx_bfs(g, src[0], 2, out.p, nullptr, nullptr, stream));  // warm
-            float ms = 0.f;
-            GBX_TRY(time_ms([&]() {
-                for (uint32_t v : src) GBX_TRY(gbx_bfs(g, v, 2, out.p, nullptr, nullptr, stream));
-                return GBX_OK;
-            }, s, &ms));
+            GBX_TRY(gbx_bfs(g, bsrc[0], 2, out.p, nullptr, nullptr, stream));  // warm
+            float ms = 1e30f;
+            for (int pass = 0; pass < 2; ++pass) {
+                float t = 0.f;
+                GBX_TRY(time_ms([&]() {
+                    for (uint32_t v : bsrc) GBX_TRY(gbx_bfs(g, v, 2, out.p, nullptr, nullptr, stream));
+                    return GBX_OK;
+                }, s, &t));
+                ms = std::min(ms, t);
+            }
             if (trace_enabled()) fprintf(stderr, "| autotune bfs_alpha %-4u | %9.3f ms |\n", c, ms);
             if (ms < best) {
                 best = ms;

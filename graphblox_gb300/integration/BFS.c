@@ -82,3 +82,45 @@ struct BFSStats *breadthFirstSearchGraphCSR(struct Arguments *arguments, struct 
     default: return breadthFirstSearchDirectionOptimizedGraphCSR(arguments, graph);
     }
 }
+
+/* BFS.c:498-546: expand the shared queue's current frontier [head, tail);
+ * the vertices claimed are appended from tail_next on. The reference
+ * gathers them in the per-thread queues and flushes those into the shared
+ * one, which leaves them empty; here they are not used, so they stay as the
+ * caller passed them (empty between steps). Returns mf, the sum of -parent
+ * over the claimed vertices. A failure prints the library's message and
+ * returns 0 with nothing appended. */
+uint32_t topDownStepGraphCSR(struct GraphCSR *graph, struct ArrayQueue *sharedFrontierQueue,
+                             struct ArrayQueue **localFrontierQueues, struct BFSStats *stats) {
+    gbx_graph *g = gbx_shim_graph(graph);
+    if (!g) return 0;
+    struct ArrayQueue *q = sharedFrontierQueue;
+    const uint32_t n = q->tail - q->head;
+    uint32_t next_len = 0, mf = 0;
+    const uint32_t cap = q->size > q->tail_next ? q->size - q->tail_next : 0;
+    int st = gbx_bfs_top_down_step(g, q->queue + q->head, n, stats->parents, stats->distances,
+                                   q->queue + q->tail_next, cap, &next_len, &mf, NULL);
+    if (st != GBX_OK) {
+        gbx_shim_fail("gbx_bfs_top_down_step", st);
+        return 0;
+    }
+    q->tail_next += next_len;
+    return mf;
+}
+
+/* BFS.c:562-613: every vertex without a parent looks for an in-neighbour in
+ * bitmapCurr; the found ones are set in bitmapNext. Returns nf, the number
+ * found; a failure prints the library's message and returns 0. */
+uint32_t bottomUpStepGraphCSR(struct GraphCSR *graph, struct Bitmap *bitmapCurr, struct Bitmap *bitmapNext,
+                              struct BFSStats *stats) {
+    gbx_graph *g = gbx_shim_graph(graph);
+    if (!g) return 0;
+    uint32_t nf = 0;
+    int st = gbx_bfs_bottom_up_step(g, bitmapCurr->bitarray, bitmapNext->bitarray, stats->parents,
+                                    stats->distances, &nf, NULL);
+    if (st != GBX_OK) {
+        gbx_shim_fail("gbx_bfs_bottom_up_step", st);
+        return 0;
+    }
+    return nf;
+}

@@ -14,6 +14,7 @@ struct shim_entry {
     struct GraphCSR *graph;
     const void *key[4];
     uint32_t V, E;
+    uint64_t fingerprint;
     gbx_graph *dev;
     unsigned long long stamp;
 };
@@ -62,14 +63,70 @@ static void fill_key(struct GraphCSR *g, const void *key[4]) {
 #endif
 }
 
+/* FNV-1a over 32-bit words: every word of arrays up to GBX_FULL_HASH words,
+ * else about GBX_SAMPLE_WORDS words at an even stride plus the first and
+ * last 64. */
+#define GBX_FULL_HASH (1u << 20)
+#define GBX_SAMPLE_WORDS 65536u
+static uint64_t fnv_words(uint64_t h, const void *p, uint32_t n) {
+    const uint32_t *w = (const uint32_t *)p;
+    if (!w || !n) return h * 1099511628211ull;
+    uint32_t stride = n <= GBX_FULL_HASH ? 1u : n / GBX_SAMPLE_WORDS;
+    for (uint32_t i = 0; i < n; i += stride) {
+        h ^= w[i];
+        h *= 1099511628211ull;
+    }
+    if (stride > 1) {
+        for (uint32_t i = 0; i < 64 && i < n; ++i) {
+            h ^= w[i] ^ w[n - 1 - i];
+            h *= 1099511628211ull;
+        }
+    }
+    return h;
+}
+
+/* A fingerprint of the CSR's contents: sizes and the arrays the device copy
+ * is built from, so a graph rewritten in place (new weights, new edges) or
+ * a new graph at a reused address is uploaded again. */
+static uint64_t fingerprint(struct GraphCSR *g) {
+    uint64_t h = 1469598103934665603ull;
+    h = fnv_words(h, &g->num_vertices, 1);
+    h = fnv_words(h, &g->num_edges, 1);
+    const uint32_t V = g->num_vertices, E = g->num_edges;
+    if (g->vertices) {
+        h = fnv_words(h, g->vertices->edges_idx, V);
+        h = fnv_words(h, g->vertices->out_degree, V);
+    }
+    if (g->sorted_edges_array) {
+        h = fnv_words(h, g->sorted_edges_array->edges_array_dest, E);
+#if WEIGHTED
+        h = fnv_words(h, g->sorted_edges_array->edges_array_weight, E);
+#endif
+    }
+#if DIRECTED
+    if (g->inverse_vertices) {
+        h = fnv_words(h, g->inverse_vertices->edges_idx, V);
+        h = fnv_words(h, g->inverse_vertices->out_degree, V);
+    }
+    if (g->inverse_sorted_edges_array) {
+        h = fnv_words(h, g->inverse_sorted_edges_array->edges_array_dest, E);
+#if WEIGHTED
+        h = fnv_words(h, g->inverse_sorted_edges_array->edges_array_weight, E);
+#endif
+    }
+#endif
+    return h;
+}
+
 gbx_graph *gbx_shim_graph(struct GraphCSR *graph) {
     const void *key[4];
     fill_key(graph, key);
+    const uint64_t fp = fingerprint(graph);
     pthread_mutex_lock(&g_lock);
     for (int i = 0; i < GBX_SHIM_CACHE; ++i) {
         struct shim_entry *e = &g_cache[i];
         if (e->dev && e->graph == graph && e->V == graph->num_vertices && e->E == graph->num_edges &&
-            !memcmp(e->key, key, sizeof(key))) {
+            !memcmp(e->key, key, sizeof(key)) && e->fingerprint == fp) {
             e->stamp = ++g_stamp;
             pthread_mutex_unlock(&g_lock);
             return e->dev;
@@ -100,6 +157,9 @@ gbx_graph *gbx_shim_graph(struct GraphCSR *graph) {
         return (gbx_graph *)gbx_shim_fail("gbx_graph_create_csr", st);
     }
     int victim = -1;
+    /* a stale copy of this same GraphCSR goes first */
+    for (int i = 0; i < GBX_SHIM_CACHE && victim < 0; ++i)
+        if (g_cache[i].dev && g_cache[i].graph == graph) victim = i;
     for (int i = 0; i < GBX_SHIM_CACHE && victim < 0; ++i)
         if (!g_cache[i].dev) victim = i;
     if (victim < 0) {
@@ -112,6 +172,7 @@ gbx_graph *gbx_shim_graph(struct GraphCSR *graph) {
     memcpy(g_cache[victim].key, key, sizeof(key));
     g_cache[victim].V = graph->num_vertices;
     g_cache[victim].E = graph->num_edges;
+    g_cache[victim].fingerprint = fp;
     g_cache[victim].dev = dev;
     g_cache[victim].stamp = ++g_stamp;
     pthread_mutex_unlock(&g_lock);

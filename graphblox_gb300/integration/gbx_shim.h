@@ -9,7 +9,11 @@
 #include "graphCSR.h"
 
 /* Device copy of a GraphCSR, uploaded on first use and cached (a few most
- * recent graphs, keyed by the GraphCSR pointer and its array pointers).
+ * recent graphs, keyed by the GraphCSR pointer, its array pointers and a
+ * fingerprint of its contents: every word of arrays up to 2^20 entries,
+ * an even sample of 65,536 words plus both ends of larger ones). A graph
+ * rewritten in place is uploaded again; a caller that changes only a few
+ * entries of a large graph calls gbx_shim_release first.
  * Returns NULL and prints the library's message on failure. */
 gbx_graph *gbx_shim_graph(struct GraphCSR *graph);
 /* Drop the cached device copy of `graph` (call before freeing it). */

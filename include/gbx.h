@@ -159,6 +159,29 @@ typedef struct gbx_pr_result {
     double error_total;   /* mean |delta| of the last iteration (FP64 reduction) */
 } gbx_pr_result;
 
+/* One top-down BFS step over a caller-held frontier: the reference's
+ * topDownStepGraphCSR (BFS.c:498-546). For every frontier vertex v and edge
+ * v -> u with parents[u] < 0 (unvisited: -out_degree or -1), u is claimed
+ * by a compare-and-swap of that value to v (the winner among frontier
+ * vertices is a race, as in the reference), distances[u] = distances[v] + 1,
+ * u is appended to next (at most next_capacity entries; more is
+ * GBX_ERR_INVALID) and mf grows by -parents_old[u]. parents and distances
+ * (num_vertices each) are read and updated in place; *next_len gets the
+ * next frontier's size. */
+int gbx_bfs_top_down_step(gbx_graph *g, const uint32_t *frontier, uint32_t frontier_len, int32_t *parents,
+                          uint32_t *distances, uint32_t *next, uint32_t next_capacity, uint32_t *next_len,
+                          uint32_t *mf, void *stream);
+
+/* One bottom-up BFS step: the reference's bottomUpStepGraphCSR
+ * (BFS.c:562-613). Every vertex v with parents[v] < 0 takes as parent the
+ * first pull in-neighbour u (inverse CSR when the graph has one) that is set
+ * in bitmap_curr, with distances[v] = distances[u] + 1, and is OR-ed into
+ * bitmap_next. Bitmaps hold (num_vertices + 31) / 32 words, bit v in word
+ * v / 32 at position v % 32 (the reference's struct Bitmap bitarray).
+ * *nf gets the number of vertices found. */
+int gbx_bfs_bottom_up_step(gbx_graph *g, const uint32_t *bitmap_curr, uint32_t *bitmap_next, int32_t *parents,
+                           uint32_t *distances, uint32_t *nf, void *stream);
+
 /* Pull PageRank with the reference's recurrence (damping 0.85f, ranks start
  * at 1-d, dangling mass dropped, stop when no vertex moves by >= epsilon,
  * final ranks divided by N). epsilon = 0 runs exactly max_iterations. FP32
@@ -166,6 +189,13 @@ typedef struct gbx_pr_result {
  * the convergence residual is reduced in FP64. */
 int gbx_pagerank_pull(gbx_graph *g, uint32_t max_iterations, double epsilon, float *ranks,
                       gbx_pr_result *result, void *stream);
+
+/* The pull PageRank recurrence of gbx_pagerank_pull evaluated in FP64 for
+ * exactly `iterations` iterations (no early exit), final ranks divided by
+ * N: the double-precision yardstick FP32 ranks are reported against on
+ * graphs too large for a CPU restatement (pageRank.c:245-368). No
+ * counterpart in the reference. ranks: num_vertices doubles. */
+int gbx_pagerank_pull_fp64(gbx_graph *g, uint32_t iterations, double *ranks, void *stream);
 
 /* Pull PageRank that allocates no memory. No counterpart in the reference.
  * For callers that cannot call cudaMalloc: hosts whose own allocator took all

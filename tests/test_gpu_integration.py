@@ -313,3 +313,42 @@ def test_reference_bf_dfs_undirected(gbx, cuda_device, name):
         np.testing.assert_array_equal(_arr(s.contents.parents, b.V, np.int32), more[f"{key}_dfs_parents_r{r}"])
         assert s.contents.processed_nodes == int(more[f"{key}_dfs_processed_r{r}"])
         lib.freeDFSStats(s)
+
+
+def test_graph_rewritten_in_place_is_uploaded_again(gbx, cuda_device):
+    """The drop-in caches the device copy of a GraphCSR; rewriting its
+    weights in place (same pointers) between two SSSPGraphCSR calls must give
+    the new graph's distances, and so must a different graph built at the
+    same addresses (edges rewritten too)."""
+    fx = load_golden("v1000_e10000")
+    b = Built(fx, "dw", directed=True)
+    lib = _lib(gbx, "dw", GraphCSRdw)
+    g = C.byref(b.g)
+    V = b.V
+    src = int(np.argmax(fx["dw_out_degree"]))
+
+    def sssp():
+        a = _args(source=src)
+        s = lib.SSSPGraphCSR(C.byref(a), g)
+        assert s, "NULL SSSPStats"
+        d = _arr(s.contents.distances, V, np.uint32)
+        lib.freeSSSPStats(s)
+        return d
+
+    def oracle(weights):
+        host = po.HostCSR(V, fx["dw_out_degree"], fx["dw_edges_idx"], fx["dw_dest"], weights)
+        return po.sssp(host, src, 1)
+
+    w = np.ctypeslib.as_array(b.el.edges_array_weight, shape=(b.E,))
+    iw = np.ctypeslib.as_array(b.iel.edges_array_weight, shape=(b.E,))
+    first = sssp()
+    np.testing.assert_array_equal(first, oracle(w.copy()))
+    # new integer weights, written into the same arrays (forward and inverse)
+    rng = np.random.default_rng(3)
+    neww = rng.integers(1, 50, b.E).astype(np.float32)
+    w[:] = neww
+    inv = po.build_csr(V, fx["dw_dest"], fx["dw_src"], neww, sort_mode=1)
+    iw[:] = inv.weight
+    second = sssp()
+    np.testing.assert_array_equal(second, oracle(neww))
+    assert not np.array_equal(first, second)
