@@ -169,19 +169,24 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
     const uint32_t groups = (qn + 31) / 32;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t split = groups ? max(1u, min(kSsspMaxSplit, nwarps / groups)) : 1u;
-    const uint32_t units = nc + groups * split;
+    // likewise a round with fewer hub chunks than warps deals each chunk's
+    // 128-edge batches to `hsplit` warps (batch part, part + hsplit, ...)
+    const uint32_t hsplit = nc ? max(1u, min(kSsspHubChunk / 128, nwarps / nc)) : 1u;
+    const uint32_t hunits = nc * hsplit;
+    const uint32_t units = hunits + groups * split;
     UnitDealer dealer(&cur->cursor);
     for (;;) {
         const uint32_t unit = dealer.take(units);
         if (unit >= units) break;
-        if (unit < nc) {
-            const uint32_t h = warp_chunk_owner(hcin, nh, unit);
+        if (unit < hunits) {
+            const uint32_t chunk = unit / hsplit, hpart = unit % hsplit;
+            const uint32_t h = warp_chunk_owner(hcin, nh, chunk);
             const uint32_t v = __ldcg(hvin + h);
             const uint32_t d = __ldcg(a.settled + v);
             const uint32_t rb = __ldg(a.off + v), re = __ldg(a.off + v + 1);
-            const uint32_t cb = rb + (unit - __ldcg(hcin + h)) * kSsspHubChunk;
+            const uint32_t cb = rb + (chunk - __ldcg(hcin + h)) * kSsspHubChunk;
             const uint32_t ce = min(cb + kSsspHubChunk, re);
-            for (uint32_t j0 = cb; j0 < ce; j0 += 128) {
+            for (uint32_t j0 = cb + hpart * 128; j0 < ce; j0 += hsplit * 128) {
                 uint32_t u[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
@@ -194,7 +199,7 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
                 rx.relax4(dq, eq, u, act);
             }
         } else {
-            const uint32_t group = (unit - nc) / split, part = (unit - nc) % split;
+            const uint32_t group = (unit - hunits) / split, part = (unit - hunits) % split;
             const uint32_t qi = group * 32 + lane;
             uint32_t b = 0, deg = 0, d = 0;
             if (qi < qn) {

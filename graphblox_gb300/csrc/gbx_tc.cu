@@ -26,6 +26,14 @@
 // element is searched in global memory. The prefixes are read as aligned
 // 16-byte quads.
 //
+// Hub pivots (fast path, v below the hub range H, at most 4,096): every
+// vertex x keeps the bitmap of N(x) ∩ [0, H) (H/32 words, built once per
+// graph), and the pair term is popc(bits(u) & bits(v)) over the words that
+// cover [0, v) -- at most H/32 words per pair instead of |N(u) ∩ [0, v]|
+// streamed elements. These low ids are the highest-degree vertices of the
+// degree order, which hold most of the pairs' prefix work. Lanes take one
+// word each, several pairs per warp step when v needs fewer than 32 words.
+//
 // General path (repeated neighbours, or a CSR that is not symmetric): the
 // reference's multiplicities, centred on u, with a binary search of N+(u) in
 // global memory per element of N+(v).
@@ -441,6 +449,116 @@ struct TcBig {  // a v whose upper neighbours are dealt out in kUpperChunk units
     uint32_t v, ub, ue, first_unit;
 };
 
+constexpr uint32_t kHubWordsMax = 128;          // H = 32 * words <= 4,096
+constexpr uint64_t kHubBytesMax = 1ull << 31;   // bitmap rows of all vertices <= 2 GiB
+constexpr uint32_t kHubStepsPerUnit = 64;       // warp steps of pair work per unit
+
+// pairs per warp step for a pivot whose prefix needs nw words (<= 32: lane
+// groups of the next power of two; above: one pair, lanes striding words)
+__host__ __device__ __forceinline__ uint32_t hub_group(uint32_t nw) {
+    uint32_t gs = 1;
+    while (gs < nw && gs < 32) gs <<= 1;
+    return gs;
+}
+__host__ __device__ __forceinline__ uint32_t hub_uppers_per_unit(uint32_t v) {
+    const uint32_t nw = (v >> 5) + 1;
+    return nw <= 32 ? kHubStepsPerUnit * (32 / hub_group(nw)) : kHubStepsPerUnit / ((nw + 31) / 32);
+}
+
+// bits[x * hw + k] bit b: 32k + b is a neighbour of x below 32 hw (rows are
+// sorted, so those neighbours are a prefix of the row); bits zeroed before
+__global__ void tc_hub_bits_kernel(const uint32_t *__restrict__ off, const uint32_t *__restrict__ dest, uint32_t V,
+                                   uint32_t hw, uint32_t *bits) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t H = hw * 32;
+    for (uint32_t x = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; x < V; x += nwarps) {
+        const uint32_t b = __ldg(off + x), e = __ldg(off + x + 1);
+        uint32_t *row = bits + (size_t)x * hw;
+        for (uint32_t j0 = b; j0 < e; j0 += 32) {
+            const uint32_t j = j0 + lane;
+            const uint32_t w = j < e ? __ldg(dest + j) : 0xFFFFFFFFu;
+            if (w < H) atomicOr(row + (w >> 5), 1u << (w & 31));
+            if (!__any_sync(0xffffffffu, w < H) || __ldg(dest + min(j0 + 31, e - 1)) >= H) break;
+        }
+    }
+}
+
+// Units of hub pivots: for v and its upper neighbours [ub, ue), the sum over
+// u of popc(bits(u) & bits(v)) over the words covering [0, v).
+__global__ void __launch_bounds__(kTcThreads)
+    tc_hub_kernel(const uint32_t *__restrict__ off, const uint32_t *__restrict__ dest,
+                  const uint32_t *__restrict__ bits, uint32_t hw, const TcBig *__restrict__ hub, uint32_t n_hub,
+                  uint32_t n_units, unsigned *cursor, unsigned long long *total) {
+    __shared__ unsigned long long sred[32];
+    const uint32_t lane = threadIdx.x & 31;
+    unsigned long long count = 0;
+    for (;;) {
+        uint32_t unit = 0;
+        if (lane == 0) unit = atomicAdd(cursor, 1u);
+        unit = __shfl_sync(0xffffffffu, unit, 0);
+        if (unit >= n_units) break;
+        uint32_t lo = 0, hi = n_hub - 1;  // last entry with first_unit <= unit
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (hub[mid].first_unit <= unit) lo = mid; else hi = mid - 1;
+        }
+        const TcBig hv = hub[lo];
+        const uint32_t v = hv.v;
+        const uint32_t per = hub_uppers_per_unit(v);
+        const uint32_t ub = hv.ub + (unit - hv.first_unit) * per;
+        const uint32_t ue = min(ub + per, hv.ue);
+        const uint32_t *nv = dest + __ldg(off + v);
+        const uint32_t *vb = bits + (size_t)v * hw;
+        const uint32_t nw = (v >> 5) + 1;                  // words covering [0, v]
+        const uint32_t last = (1u << (v & 31)) - 1u;       // ids below v in the last word
+        if (nw <= 32) {
+            const uint32_t gs = hub_group(nw), ppw = 32 / gs;
+            const uint32_t j = lane & (gs - 1), grp = lane / gs;
+            uint32_t pw = 0;
+            if (j < nw) pw = __ldg(vb + j) & (j == nw - 1 ? last : 0xFFFFFFFFu);
+            // eight steps' neighbour ids, then their words, in flight per lane
+            for (uint32_t a0 = ub; a0 < ue; a0 += 8 * ppw) {
+                uint32_t u[8], w[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const uint32_t a = a0 + q * ppw + grp;
+                    u[q] = (a < ue && j < nw) ? __ldg(nv + a) : 0xFFFFFFFFu;
+                }
+#pragma unroll
+                for (int q = 0; q < 8; ++q) w[q] = u[q] != 0xFFFFFFFFu ? __ldg(bits + (size_t)u[q] * hw + j) : 0u;
+#pragma unroll
+                for (int q = 0; q < 8; ++q) count += __popc(w[q] & pw);
+            }
+        } else {
+            uint32_t pw[kHubWordsMax / 32];
+#pragma unroll
+            for (uint32_t q = 0; q < kHubWordsMax / 32; ++q) {
+                const uint32_t k = q * 32 + lane;
+                pw[q] = k < nw ? (__ldg(vb + k) & (k == nw - 1 ? last : 0xFFFFFFFFu)) : 0u;
+            }
+            // two pairs' neighbour ids, then all their words, in flight
+            for (uint32_t a = ub; a < ue; a += 2) {
+                const uint32_t u0 = __ldg(nv + a);
+                const uint32_t u1 = a + 1 < ue ? __ldg(nv + a + 1) : 0xFFFFFFFFu;
+                const uint32_t *r0 = bits + (size_t)u0 * hw;
+                const uint32_t *r1 = bits + (size_t)(u1 != 0xFFFFFFFFu ? u1 : u0) * hw;
+                uint32_t w0[kHubWordsMax / 32], w1[kHubWordsMax / 32];
+#pragma unroll
+                for (uint32_t q = 0; q < kHubWordsMax / 32; ++q) {
+                    const uint32_t k = q * 32 + lane;
+                    w0[q] = k < nw ? __ldg(r0 + k) : 0u;
+                    w1[q] = (k < nw && u1 != 0xFFFFFFFFu) ? __ldg(r1 + k) : 0u;
+                }
+#pragma unroll
+                for (uint32_t q = 0; q < kHubWordsMax / 32; ++q) count += __popc(w0[q] & pw[q]) + __popc(w1[q] & pw[q]);
+            }
+        }
+    }
+    count = block_sum(count, sred);
+    if (threadIdx.x == 0 && count) atomicAdd(total, count);
+}
+
 __global__ void __launch_bounds__(kTcThreads, 4)
     tc_vcentric_kernel(const uint32_t *__restrict__ off, const uint32_t *__restrict__ dest,
                        const uint32_t *__restrict__ low, const TcBig *__restrict__ big, uint32_t n_big,
@@ -586,39 +704,45 @@ __global__ void __launch_bounds__(kWideThreads, 1)
     if (threadIdx.x == 0 && count) atomicAdd(total, count);
 }
 
-// Work lists of the v-centric count. kind 0: v's with more than kUpperChunk
-// upper neighbours and |N+(v)| within the warp table (units of kUpperChunk);
-// kind 1: v's with |N+(v)| above the warp table and within the CTA table
-// (units of kWideChunk, for tc_wide_kernel); kind 2: every other v with
-// N+(v) and an upper neighbour (one warp each). v's without both have no
-// pairs and are in no list.
+// Work lists of the v-centric count. kind 3: v's below the hub range H with
+// pairs (units of hub_uppers_per_unit(v), tc_hub_kernel); for the others,
+// kind 0: v's with more than kUpperChunk upper neighbours and |N+(v)| within
+// the warp table (units of kUpperChunk); kind 1: v's with |N+(v)| above the
+// warp table and within the CTA table (units of kWideChunk, for
+// tc_wide_kernel); kind 2: every other v with N+(v) and an upper neighbour
+// (one warp each). v's without both have no pairs and are in no list.
 __global__ void tc_plan_flags_kernel(const uint32_t *off, const uint32_t *dest, const uint32_t *low, uint32_t V,
-                                     uint32_t *flag /* 3V: kinds 0, 1, 2 */, uint32_t *units /* 2V */,
-                                     uint32_t *ub_out) {
+                                     uint32_t H, uint32_t *flag /* 4V: kinds 0, 1, 2, 3 */,
+                                     uint32_t *units /* 3V: kinds 0, 1, 3 */, uint32_t *ub_out) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
         const uint32_t b = off[v], d = off[v + 1] - b;
         const uint32_t ub = count_lt(dest + b, d, v);
         const uint32_t up = d - ub, pv = low[v];
-        const bool wide = pv > kTcTableMax && pv <= kWideSlotsMax / 2;
-        const bool big = !wide && (up > kUpperChunk || pv > kTcTableMax);
         const bool pairs = pv > 0 && up > 0;
+        const bool hub = v < H;
+        const bool wide = !hub && pv > kTcTableMax && pv <= kWideSlotsMax / 2;
+        const bool big = !hub && !wide && (up > kUpperChunk || pv > kTcTableMax);
         flag[v] = pairs && big ? 1u : 0u;
         flag[(size_t)V + v] = pairs && wide ? 1u : 0u;
-        flag[2 * (size_t)V + v] = pairs && !big && !wide ? 1u : 0u;
+        flag[2 * (size_t)V + v] = pairs && !hub && !big && !wide ? 1u : 0u;
+        flag[3 * (size_t)V + v] = pairs && hub ? 1u : 0u;
         units[v] = pairs && big ? (up + kUpperChunk - 1) / kUpperChunk : 0u;
         units[(size_t)V + v] = pairs && wide ? (up + kWideChunk - 1) / kWideChunk : 0u;
+        const uint32_t per = hub_uppers_per_unit(v);
+        units[2 * (size_t)V + v] = pairs && hub ? (up + per - 1) / per : 0u;
         ub_out[v] = ub;
     }
 }
 
 __global__ void tc_plan_scatter_kernel(const uint32_t *off, const uint32_t *flag, const uint32_t *pos,
                                        const uint32_t *unit_pre, const uint32_t *ub, uint32_t V, TcBig *big,
-                                       TcBig *wide, TcBig *small) {
+                                       TcBig *wide, TcBig *small, TcBig *hub) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
         const uint32_t d = off[v + 1] - off[v];
         if (flag[v]) big[pos[v]] = TcBig{v, ub[v], d, unit_pre[v]};
         if (flag[(size_t)V + v]) wide[pos[(size_t)V + v]] = TcBig{v, ub[v], d, unit_pre[(size_t)V + v]};
         if (flag[2 * (size_t)V + v]) small[pos[2 * (size_t)V + v]] = TcBig{v, ub[v], d, 0u};
+        if (flag[3 * (size_t)V + v]) hub[pos[3 * (size_t)V + v]] = TcBig{v, ub[v], d, unit_pre[2 * (size_t)V + v]};
     }
 }
 
@@ -629,9 +753,13 @@ struct gbx_tc_plan {
     gbx::TcBig *big = nullptr;   // warp-table v's with many upper neighbours
     gbx::TcBig *wide = nullptr;  // CTA-table v's (|N+(v)| above the warp table)
     gbx::TcBig *small = nullptr; // the other v's with pairs, one warp each
+    gbx::TcBig *hub = nullptr;   // v's below the hub range (bitmap rows)
+    uint32_t *hub_bits = nullptr;  // V rows of hub_words words: N(x) ∩ [0, 32 hub_words)
+    uint32_t hub_words = 0;
     uint32_t n_big = 0, n_units = 0;
     uint32_t n_wide = 0, n_wunits = 0;
     uint32_t n_small = 0;
+    uint32_t n_hub = 0, n_hunits = 0;
 };
 
 using namespace gbx;
@@ -667,36 +795,54 @@ static int tc_prepare(gbx_graph *g, cudaStream_t s) {
     }
     if (g->simple_rows == 1 && g->symmetric == 1 && !g->tc_plan) {
         DevBuf<uint32_t> flag, pos, units, unit_pre, ub, tot;
-        GBX_TRY(flag.alloc(3 * (size_t)V, s));
-        GBX_TRY(pos.alloc(3 * (size_t)V, s));
-        GBX_TRY(units.alloc(2 * (size_t)V, s));
-        GBX_TRY(unit_pre.alloc(2 * (size_t)V, s));
+        GBX_TRY(flag.alloc(4 * (size_t)V, s));
+        GBX_TRY(pos.alloc(4 * (size_t)V, s));
+        GBX_TRY(units.alloc(3 * (size_t)V, s));
+        GBX_TRY(unit_pre.alloc(3 * (size_t)V, s));
         GBX_TRY(ub.alloc(V, s));
-        GBX_TRY(tot.alloc(5, s));
+        GBX_TRY(tot.alloc(7, s));
         gbx_tc_plan *p = new gbx_tc_plan();
+        // hub range: 32 hw ids, hw a power of two <= kHubWordsMax with the
+        // bitmap rows of all V vertices within kHubBytesMax
+        uint32_t hw = kHubWordsMax;
+        while (hw > 1 && (uint64_t)V * hw * 4 > kHubBytesMax) hw >>= 1;
+        if ((uint64_t)V * hw * 4 > kHubBytesMax) hw = 0;
+        const uint32_t H = hw * 32;
         auto build = [&]() -> int {
-            // the three work lists in one classification pass, five scans
+            // the four work lists in one classification pass, seven scans
             // and one host round trip for the list sizes
-            tc_plan_flags_kernel<<<grid, 256, 0, s>>>(g->offsets, g->dest, g->low_count, V, flag.p, units.p, ub.p);
+            tc_plan_flags_kernel<<<grid, 256, 0, s>>>(g->offsets, g->dest, g->low_count, V, H, flag.p, units.p,
+                                                      ub.p);
             GBX_LAUNCH_CHECK();
-            for (int k = 0; k < 3; ++k)
+            for (int k = 0; k < 4; ++k)
                 GBX_TRY(exclusive_scan_u32(flag.p + (size_t)k * V, pos.p + (size_t)k * V, V, s, tot.p + k));
-            for (int k = 0; k < 2; ++k)
-                GBX_TRY(exclusive_scan_u32(units.p + (size_t)k * V, unit_pre.p + (size_t)k * V, V, s, tot.p + 3 + k));
-            uint32_t h[5];
+            for (int k = 0; k < 3; ++k)
+                GBX_TRY(exclusive_scan_u32(units.p + (size_t)k * V, unit_pre.p + (size_t)k * V, V, s, tot.p + 4 + k));
+            uint32_t h[7];
             GBX_CUDA(cudaMemcpyAsync(h, tot.p, sizeof(h), cudaMemcpyDeviceToHost, s));
             GBX_CUDA(cudaStreamSynchronize(s));
             p->n_big = h[0];
             p->n_wide = h[1];
             p->n_small = h[2];
-            p->n_units = h[3];
-            p->n_wunits = h[4];
+            p->n_hub = h[3];
+            p->n_units = h[4];
+            p->n_wunits = h[5];
+            p->n_hunits = h[6];
             GBX_CUDA(cudaMalloc(&p->big, sizeof(TcBig) * (h[0] ? h[0] : 1)));
             GBX_CUDA(cudaMalloc(&p->wide, sizeof(TcBig) * (h[1] ? h[1] : 1)));
             GBX_CUDA(cudaMalloc(&p->small, sizeof(TcBig) * (h[2] ? h[2] : 1)));
+            GBX_CUDA(cudaMalloc(&p->hub, sizeof(TcBig) * (h[3] ? h[3] : 1)));
             tc_plan_scatter_kernel<<<grid, 256, 0, s>>>(g->offsets, flag.p, pos.p, unit_pre.p, ub.p, V, p->big,
-                                                        p->wide, p->small);
+                                                        p->wide, p->small, p->hub);
             GBX_LAUNCH_CHECK();
+            if (p->n_hub) {
+                const size_t bytes = (size_t)V * hw * 4;
+                GBX_CUDA(cudaMalloc(&p->hub_bits, bytes));
+                GBX_CUDA(cudaMemsetAsync(p->hub_bits, 0, bytes, s));
+                tc_hub_bits_kernel<<<wgrid, 256, 0, s>>>(g->offsets, g->dest, V, hw, p->hub_bits);
+                GBX_LAUNCH_CHECK();
+                p->hub_words = hw;
+            }
             return GBX_OK;
         };
         const int st = build();
@@ -715,6 +861,8 @@ void gbx_free_tc_plan(gbx_tc_plan *p) {
     cudaFree(p->big);
     cudaFree(p->wide);
     cudaFree(p->small);
+    cudaFree(p->hub);
+    cudaFree(p->hub_bits);
     delete p;
 }
 
@@ -728,9 +876,9 @@ extern "C" int gbx_tc(gbx_graph *g, uint64_t *total, void *stream) {
     DevBuf<unsigned long long> d;
     DevBuf<unsigned> cursor;
     GBX_TRY(d.alloc(1, s));
-    GBX_TRY(cursor.alloc(2, s));
+    GBX_TRY(cursor.alloc(3, s));
     GBX_CUDA(cudaMemsetAsync(d.p, 0, 8, s));
-    GBX_CUDA(cudaMemsetAsync(cursor.p, 0, 8, s));
+    GBX_CUDA(cudaMemsetAsync(cursor.p, 0, 12, s));
     if (g->tc_plan) {
         int per_sm = 0;
         GBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc_vcentric_kernel, kTcThreads, 0));
@@ -748,6 +896,15 @@ extern "C" int gbx_tc(gbx_graph *g, uint64_t *total, void *stream) {
             const unsigned wgrid = std::min<unsigned>((unsigned)std::max(1, wper) * (unsigned)num_sms(), p->n_wunits);
             tc_wide_kernel<<<wgrid, kWideThreads, smem, s>>>(g->offsets, g->dest, g->low_count, p->wide, p->n_wide,
                                                               p->n_wunits, kWideSlotsMax, cursor.p + 1, d.p);
+        }
+        if (p->n_hub) {
+            GBX_LAUNCH_CHECK();
+            int hper = 0;
+            GBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&hper, tc_hub_kernel, kTcThreads, 0));
+            const unsigned hgrid = std::min<unsigned>((unsigned)std::max(1, hper) * (unsigned)num_sms(),
+                                                      ceil_div(p->n_hunits, kTcWarps));
+            tc_hub_kernel<<<hgrid, kTcThreads, 0, s>>>(g->offsets, g->dest, p->hub_bits, p->hub_words, p->hub,
+                                                       p->n_hub, p->n_hunits, cursor.p + 2, d.p);
         }
     } else {
         const unsigned wgrid = std::min<unsigned>(ceil_div((uint64_t)V * 32, kTcThreads), (unsigned)num_sms() * 8);
