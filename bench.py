@@ -47,9 +47,9 @@ N_ROOTS = 64
 N_SSSP_ROOTS = 4
 PR_ITERS = 20
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each
-# kernel, from one `ncu --set full` capture of this workload on a GB300
-# (tc, spmv: one launch; pr: one iteration; bfs, sssp: one source).
-NCU_TRAFFIC_PER_LAUNCH = {"tc": 14.773e9, "pr": 0.4006e9, "bfs": 0.1761e9, "sssp": 1.427e9, "spmv": 0.6775e9}
+# kernel, from ncu captures of this workload on a GB300 (profiles/): bfs and
+# sssp one source (--set full), pr one iteration, spmv one launch.
+NCU_TRAFFIC_PER_LAUNCH = {"pr": 0.4006e9, "bfs": 0.1678e9, "sssp": 1.428e9, "spmv": 0.6775e9}
 W_LO, W_HI = 1, 255
 # differentiable personalised PageRank: RMAT-20, 2^24 edges as generated,
 # lognormal(0,1) weights, 64 teleport columns of 32 seeds, d 0.85 to 1e-7 L1
