@@ -60,8 +60,11 @@ MS_SOURCES = 256  # multi-source bitmask BFS on the RMAT-22 graph
 C5_V, C5_MEAN = 40_000_000, 30  # scale-up: Chung-Lu 4e7 vertices, 1.2e9 edges (opt-in, --c5)
 
 
+T0 = time.time()
+
+
 def log(*a):
-    print(*a, file=sys.stderr, flush=True)
+    print(f"[{time.time() - T0:6.1f}s]", *a, file=sys.stderr, flush=True)
 
 
 def peaks():
@@ -473,6 +476,7 @@ def run_gpu(args):
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
+        log("bench done")
     if dist:
         dist.destroy_process_group()
 

@@ -42,7 +42,7 @@
 namespace gbx {
 
 constexpr uint32_t kHubDeg = 1024;    // out-degree above which a vertex is a hub
-constexpr uint32_t kHubChunk = 256;   // edges per hub work unit
+constexpr uint32_t kHubChunk = 1024;  // edges per hub work unit
 constexpr uint32_t kBuProbe = 64;     // bottom-up: in-edges a lane probes alone before the warp helps
 constexpr uint32_t kTdMaxSplit = 64;  // top-down: most warps sharing one 32-vertex group's edges
 constexpr uint32_t kBuWords = 16;     // bottom-up: frontier-bitmap words (32 vertices each) per work unit
@@ -56,6 +56,7 @@ struct BfsStep {
     unsigned qlen;            // next queue length
     unsigned long long hub;   // next hub list: (count << 32) | chunks
     unsigned long long edges; // sum of out_degree over claimed
+    unsigned long long busy_sum, busy_max;  // warps' time in the step's phase (traced runs only)
 };
 
 // Step trace (printed when GBX_TRACE is set): kind, frontier size, time.
@@ -63,7 +64,7 @@ constexpr unsigned kTraceMax = 96;
 enum : unsigned { kTrStart = 0, kTrTopDown = 1, kTrBottomUp = 2, kTrToBitmap = 3, kTrToLists = 4 };
 struct TraceRec {
     unsigned kind, value;
-    unsigned long long ns;
+    unsigned long long ns, busy_sum, busy_max;
 };
 
 struct BfsState {
@@ -82,20 +83,39 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-__device__ __forceinline__ void trace_step(BfsState *st, unsigned kind, unsigned value) {
+__device__ __forceinline__ void trace_step(BfsState *st, unsigned kind, unsigned value,
+                                           const BfsStep *step = nullptr) {
     if (blockIdx.x == 0 && threadIdx.x == 0 && st->ntrace < kTraceMax) {
         TraceRec &r = st->trace[st->ntrace++];
         r.kind = kind;
         r.value = value;
         r.ns = global_ns();
+        r.busy_sum = step ? __ldcg(&step->busy_sum) : 0;
+        r.busy_max = step ? __ldcg(&step->busy_max) : 0;
     }
 }
+
+// Traced runs: each warp's time inside a step's phase, summed and maxed over
+// warps, tells a load-imbalanced step (max close to the step) from a
+// throughput-bound one (mean close to the step).
+struct BusyClock {
+    bool on;
+    unsigned long long t0;
+    __device__ __forceinline__ explicit BusyClock(bool trace) : on(trace), t0(trace ? global_ns() : 0) {}
+    __device__ __forceinline__ void stop(BfsStep *cnt) {
+        if (!on || (threadIdx.x & 31) != 0) return;
+        const unsigned long long d = global_ns() - t0;
+        atomicAdd(&cnt->busy_sum, d);
+        atomicMax(&cnt->busy_max, d);
+    }
+};
 
 struct BfsArgs {
     const uint32_t *off, *dest, *poff, *psrc, *outdeg;
     uint32_t V, words, E, mode, source;
     uint32_t alpha, beta;  // direction switch: bottom-up when mf > mu/alpha, stay while nf > V/beta
     uint32_t pull_live;    // every pull neighbour has out-degree > 0
+    uint32_t trace;        // record per-step warp busy times
     const uint32_t *live;  // bit v: v has pull in-edges (only such vertices can be found bottom-up)
     uint32_t *level;
     int32_t *parent;
@@ -122,12 +142,17 @@ struct Claimer {
     __device__ __forceinline__ Claimer(const BfsArgs &a_, uint32_t l, uint32_t *q, uint32_t *hv, uint32_t *hc,
                                        uint32_t *f, BfsStep *c, uint32_t *wbuf)
         : a(a_), lnext(l), qout(q), hvout(hv), hcout(hc), fbm(f), cnt(c), wq(wbuf) {}
-    // Four candidate edges per lane: the visited-word loads, then the
-    // atomicOr claims, are issued back to back so their latencies overlap.
+    // Four candidate edges per lane: the visited-word loads and the
+    // targets' out-degrees (needed only by the winners, but loading them
+    // here takes them off the claim's dependent chain), then the atomicOr
+    // claims, are issued back to back so their latencies overlap.
     __device__ __forceinline__ void claim4(const uint32_t (&v)[4], const uint32_t (&u)[4], const bool (&act)[4]) {
-        uint32_t pre[4], old[4], du[4];
+        uint32_t pre[4], old[4], du[4], dpre[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) pre[q] = act[q] ? __ldcg(a.visited + (u[q] >> 5)) : 0xFFFFFFFFu;
+        for (int q = 0; q < 4; ++q) {
+            pre[q] = act[q] ? __ldcg(a.visited + (u[q] >> 5)) : 0xFFFFFFFFu;
+            dpre[q] = act[q] ? __ldg(a.outdeg + u[q]) : 0u;
+        }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const uint32_t bit = 1u << (u[q] & 31);
@@ -136,7 +161,7 @@ struct Claimer {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const bool won = !(old[q] & (1u << (u[q] & 31)));
-            du[q] = won ? __ldg(a.outdeg + u[q]) : 0u;
+            du[q] = won ? dpre[q] : 0u;
             if (won) {
                 a.level[u[q]] = lnext;
                 a.parent[u[q]] = (int32_t)v[q];
@@ -194,6 +219,7 @@ __device__ void top_down_phase(const BfsArgs &a, const uint32_t *qin, uint32_t q
                                uint32_t *hvout, uint32_t *hcout, uint32_t lnext, uint32_t *fbm, uint32_t *clear_bm,
                                uint32_t *s_pre, uint32_t *s_base, uint32_t *s_v, uint32_t *s_wq) {
     const uint32_t lane = threadIdx.x & 31;
+    BusyClock clock(a.trace != 0);
     if (clear_bm) {
         // the bitmap the next top-down step fills (not read during this one)
         for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < a.words; w += gridDim.x * blockDim.x)
@@ -222,12 +248,21 @@ __device__ void top_down_phase(const BfsArgs &a, const uint32_t *qin, uint32_t q
             const uint32_t rb = __ldg(a.off + v), re = __ldg(a.off + v + 1);
             const uint32_t cb = rb + (chunk - __ldcg(hcin + h)) * kHubChunk;
             const uint32_t ce = min(cb + kHubChunk, re);
-            for (uint32_t j0 = cb + hpart * 128; j0 < ce; j0 += hsplit * 128) {
+            // the next batch's ids are loaded before this batch is claimed
+            const uint32_t stride = hsplit * 128;
+            uint32_t un[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint32_t j = cb + hpart * 128 + q * 32 + lane;
+                un[q] = j < ce ? __ldg(a.dest + j) : 0u;
+            }
+            for (uint32_t j0 = cb + hpart * 128; j0 < ce; j0 += stride) {
                 uint32_t u[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    uint32_t j = j0 + q * 32 + lane;
-                    u[q] = j < ce ? __ldg(a.dest + j) : 0u;
+                    u[q] = un[q];
+                    const uint32_t j = j0 + stride + q * 32 + lane;
+                    un[q] = j < ce ? __ldg(a.dest + j) : 0u;
                 }
                 const uint32_t vv[4] = {v, v, v, v};
                 const bool act[4] = {j0 + lane < ce, j0 + 32 + lane < ce, j0 + 64 + lane < ce, j0 + 96 + lane < ce};
@@ -255,20 +290,32 @@ __device__ void top_down_phase(const BfsArgs &a, const uint32_t *qin, uint32_t q
             if (lane == 31) s_pre[32] = incl;
             __syncwarp();
             const uint32_t tot = s_pre[32];
+            // each batch's ids are loaded one batch ahead (k: owner lane of
+            // the loading stream, advanced monotonically)
             uint32_t k = 0;
+            uint32_t un[4], sn[4];
+            auto load = [&](uint32_t i0, uint32_t (&uu)[4], uint32_t (&ss)[4]) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const uint32_t i = i0 + q * 32 + lane;
+                    uu[q] = 0;
+                    ss[q] = 0;
+                    if (i < tot) {
+                        while (s_pre[k + 1] <= i) ++k;
+                        ss[q] = s_v[k];
+                        uu[q] = __ldg(a.dest + s_base[k] + (i - s_pre[k]));
+                    }
+                }
+            };
+            load(part * 128, un, sn);
             for (uint32_t i0 = part * 128; i0 < tot; i0 += split * 128) {
                 uint32_t u[4], src[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    uint32_t i = i0 + q * 32 + lane;
-                    u[q] = 0;
-                    src[q] = 0;
-                    if (i < tot) {
-                        while (s_pre[k + 1] <= i) ++k;
-                        src[q] = s_v[k];
-                        u[q] = __ldg(a.dest + s_base[k] + (i - s_pre[k]));
-                    }
+                    u[q] = un[q];
+                    src[q] = sn[q];
                 }
+                load(i0 + split * 128, un, sn);
                 const bool act[4] = {i0 + lane < tot, i0 + 32 + lane < tot, i0 + 64 + lane < tot, i0 + 96 + lane < tot};
                 claim.claim4(src, u, act);
             }
@@ -276,6 +323,7 @@ __device__ void top_down_phase(const BfsArgs &a, const uint32_t *qin, uint32_t q
         }
     }
     claim.flush();
+    clock.stop(cur);
 }
 
 // Probe in-edges [j, el) of one vertex, N at a time: the ids, then their
@@ -312,6 +360,7 @@ __device__ void bottom_up_phase(const BfsArgs &a, const uint32_t *cur_bm, uint32
                                 BfsStep *cnt, uint32_t *qout, uint32_t *hvout, uint32_t *hcout, uint32_t *s_wq,
                                 uint32_t *s_found) {
     const uint32_t lane = threadIdx.x & 31;
+    BusyClock clock(a.trace != 0);
     unsigned nf = 0;
     unsigned long long edges = 0;
     WarpQueue wq(s_wq);
@@ -333,23 +382,30 @@ __device__ void bottom_up_phase(const BfsArgs &a, const uint32_t *cur_bm, uint32
         const uint32_t excl = incl - c, total = __shfl_sync(0xffffffffu, incl, 31);
         if (lane < kBuWords) s_found[lane] = 0u;
         __syncwarp();
-        for (uint32_t base = 0; base < total; base += 32) {
-            const uint32_t i = base + lane;
-            // the word of candidate i: last k with excl_k <= i
-            uint32_t k = 0;
+        // candidate i -> (its word k, its vertex, that vertex's row bounds and
+        // out-degree); the next round's rows are loaded while this round probes
+        auto candidate = [&](uint32_t i, uint32_t &k, uint32_t &v, uint32_t &b, uint32_t &e, uint32_t &dv) {
+            k = 0;
 #pragma unroll
             for (uint32_t step = 16; step > 0; step >>= 1)
                 if (__shfl_sync(0xffffffffu, excl, k + step) <= i) k += step;
             const uint32_t mk = __shfl_sync(0xffffffffu, cand, k);
             const uint32_t ek = __shfl_sync(0xffffffffu, excl, k);
-            const bool act = i < total;
-            uint32_t v = 0, b = 0, e = 0, dv = 0;
-            if (act) {
+            v = b = e = dv = 0;
+            if (i < total) {
                 v = (w0 + k) * 32 + nth_set_bit(mk, i - ek);
                 b = __ldg(a.poff + v);
                 e = __ldg(a.poff + v + 1);
                 dv = __ldg(a.outdeg + v);
             }
+        };
+        uint32_t nk, nv_, nb, ne, nd;
+        candidate(lane, nk, nv_, nb, ne, nd);
+        for (uint32_t base = 0; base < total; base += 32) {
+            const uint32_t i = base + lane;
+            const bool act = i < total;
+            const uint32_t k = nk, v = nv_, b = nb, e = ne, dv = nd;
+            if (base + 32 < total) candidate(base + 32 + lane, nk, nv_, nb, ne, nd);
             bool found = false;
             uint32_t tb = 0, te = 0;  // in-edges still to probe after the lane's own first kBuProbe
             if (act) {
@@ -427,6 +483,7 @@ __device__ void bottom_up_phase(const BfsArgs &a, const uint32_t *cur_bm, uint32
         atomicAdd(&cnt->nf, nf);
         atomicAdd(&cnt->edges, edges);
     }
+    clock.stop(cnt);
 }
 
 // arrayQueueToBitmap (arrayQueue.c:284-308) from the lists themselves, into a
@@ -471,6 +528,8 @@ __device__ __forceinline__ void zero_step(BfsStep *s) {
     s->qlen = 0;
     s->hub = 0;
     s->edges = 0;
+    s->busy_sum = 0;
+    s->busy_max = 0;
 }
 
 __global__ void __launch_bounds__(kBfsThreads, 3) bfs_persistent_kernel(BfsArgs a) {
@@ -541,7 +600,7 @@ __global__ void __launch_bounds__(kBfsThreads, 3) bfs_persistent_kernel(BfsArgs 
             bm_clean[ob] = false;
             if (!grid_barrier(&st->gs)) { failed = true; break; }
             const uint32_t nf = __ldcg(&cur->nf);
-            trace_step(st, kTrBottomUp, nf);
+            trace_step(st, kTrBottomUp, nf, cur);
             processed += nf;
             iteration++;
             bu++;
@@ -578,7 +637,7 @@ __global__ void __launch_bounds__(kBfsThreads, 3) bfs_persistent_kernel(BfsArgs 
             }
             if (!grid_barrier(&st->gs)) { failed = true; break; }
             const uint32_t nf = __ldcg(&cur->nf);
-            trace_step(st, kTrTopDown, nf);
+            trace_step(st, kTrTopDown, nf, cur);
             mf = __ldcg(&cur->mf);
             qsize = nf;
             processed += nf;
@@ -768,6 +827,7 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
     a.beta = g->bfs_beta;
     a.pull_live = g->pull_sources_live == 1 ? 1u : 0u;
     a.live = g->bu_live;
+    a.trace = trace_enabled() ? 1u : 0u;
     a.level = lev;
     a.parent = parp;
     a.visited = w.visited;
@@ -797,10 +857,13 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
     GBX_REQUIRE(hs.status == 0, GBX_ERR_ITER_CAP, "BFS step cap reached");
     if (trace_enabled()) {
         static const char *names[] = {"start", "TD", "BU", "->bitmap", "->lists"};
-        fprintf(stderr, "| gbx_bfs source %u: %-9s | %-10s | %-10s |\n", source, "step", "vertices", "us");
+        const unsigned nwarps = (unsigned)grid * (kBfsThreads / 32);
+        fprintf(stderr, "| gbx_bfs source %u: %-9s | %-10s | %-10s | %-12s | %-12s |\n", source, "step", "vertices",
+                "us", "warp max us", "warp mean us");
         for (unsigned i = 1; i < hs.ntrace && i < kTraceMax; ++i)
-            fprintf(stderr, "| %-23s | %-10u | %-10.2f |\n", names[hs.trace[i].kind % 5], hs.trace[i].value,
-                    (hs.trace[i].ns - hs.trace[i - 1].ns) * 1e-3);
+            fprintf(stderr, "| %-23s | %-10u | %-10.2f | %-12.2f | %-12.2f |\n", names[hs.trace[i].kind % 5],
+                    hs.trace[i].value, (hs.trace[i].ns - hs.trace[i - 1].ns) * 1e-3, hs.trace[i].busy_max * 1e-3,
+                    hs.trace[i].busy_sum * 1e-3 / nwarps);
     }
     if (result) {
         result->processed_nodes = hs.processed;

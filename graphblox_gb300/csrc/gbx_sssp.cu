@@ -186,12 +186,21 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
             const uint32_t rb = __ldg(a.off + v), re = __ldg(a.off + v + 1);
             const uint32_t cb = rb + (chunk - __ldcg(hcin + h)) * kSsspHubChunk;
             const uint32_t ce = min(cb + kSsspHubChunk, re);
-            for (uint32_t j0 = cb + hpart * 128; j0 < ce; j0 += hsplit * 128) {
+            // the next batch's ids are loaded before this batch is relaxed
+            const uint32_t stride = hsplit * 128;
+            uint32_t un[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint32_t j = cb + hpart * 128 + q * 32 + lane;
+                un[q] = j < ce ? __ldcs(a.dest + j) : 0u;
+            }
+            for (uint32_t j0 = cb + hpart * 128; j0 < ce; j0 += stride) {
                 uint32_t u[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    uint32_t j = j0 + q * 32 + lane;
-                    u[q] = j < ce ? __ldcs(a.dest + j) : 0u;
+                    u[q] = un[q];
+                    const uint32_t j = j0 + stride + q * 32 + lane;
+                    un[q] = j < ce ? __ldcs(a.dest + j) : 0u;
                 }
                 const uint32_t dq[4] = {d, d, d, d};
                 const uint32_t eq[4] = {j0 + lane, j0 + 32 + lane, j0 + 64 + lane, j0 + 96 + lane};
@@ -349,40 +358,54 @@ __global__ void __launch_bounds__(kSsspThreads, 5) sssp_persistent_kernel(SsspAr
             const uint32_t thr = threshold > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)threshold;
             uint32_t kmin = 0xFFFFFFFFu;
             WarpQueue wnear(s_wn[wid]), wfar(s_wf[wid]);
-            for (uint32_t base = blockIdx.x * blockDim.x; base < far_len; base += nthreads) {
-                const uint32_t i = base + threadIdx.x;
-                bool to_near = false, keep = false, hub = false;
-                uint32_t u = 0;
-                if (i < far_len) {
-                    u = __ldcg(a.far[fb] + i);
-                    const uint32_t d = __ldcg(a.dist + u);
-                    if (__ldcg(a.settled + u) == d) {
-                        a.in_far[u] = 0;
-                    } else if (d < thr) {
-                        a.in_far[u] = 0;
-                        to_near = atomicExch(a.stamp + u, round) != round;
-                    } else {
-                        keep = true;
-                        kmin = min(kmin, d);
-                    }
-                    if (to_near) {
-                        const uint32_t du = __ldg(a.outdeg + u);
-                        if (du > kSsspHubDeg) {
-                            hub = true;
+            // four pile entries per thread in flight: their ids, then their
+            // distances and snapshots, then the claims and degrees
+            constexpr uint32_t kSplitIlp = 4;
+            for (uint32_t base = blockIdx.x * blockDim.x; base < far_len; base += kSplitIlp * nthreads) {
+                uint32_t u[kSplitIlp], d[kSplitIlp], sv[kSplitIlp], stamp_old[kSplitIlp], du[kSplitIlp];
+                bool in[kSplitIlp], to_near[kSplitIlp], keep[kSplitIlp], hub[kSplitIlp];
+#pragma unroll
+                for (uint32_t q = 0; q < kSplitIlp; ++q) {
+                    const uint32_t i = base + q * nthreads + threadIdx.x;
+                    in[q] = i < far_len;
+                    u[q] = in[q] ? __ldcg(a.far[fb] + i) : 0u;
+                }
+#pragma unroll
+                for (uint32_t q = 0; q < kSplitIlp; ++q) {
+                    d[q] = in[q] ? __ldcg(a.dist + u[q]) : 0u;
+                    sv[q] = in[q] ? __ldcg(a.settled + u[q]) : 0u;
+                }
+#pragma unroll
+                for (uint32_t q = 0; q < kSplitIlp; ++q) {
+                    const bool expanded = in[q] && sv[q] == d[q];
+                    const bool below = in[q] && !expanded && d[q] < thr;
+                    keep[q] = in[q] && !expanded && !below;
+                    if (keep[q]) kmin = min(kmin, d[q]);
+                    if (expanded || below) a.in_far[u[q]] = 0;
+                    stamp_old[q] = below ? atomicExch(a.stamp + u[q], round) : round;
+                    du[q] = below ? __ldg(a.outdeg + u[q]) : 1u;
+                    to_near[q] = below && stamp_old[q] != round;
+                    hub[q] = false;
+                }
+#pragma unroll
+                for (uint32_t q = 0; q < kSplitIlp; ++q) {
+                    if (to_near[q]) {
+                        if (du[q] > kSsspHubDeg) {
+                            hub[q] = true;
                             const unsigned long long h =
-                                atomicAdd(&cur->near_hub, (1ull << 32) | sssp_chunks(du));
+                                atomicAdd(&cur->near_hub, (1ull << 32) | sssp_chunks(du[q]));
                             const uint32_t slot = (uint32_t)(h >> 32);
-                            a.hv[ib][slot] = u;
+                            a.hv[ib][slot] = u[q];
                             a.hc[ib][slot] = (uint32_t)h;
-                        } else if (du == 0) {
+                        } else if (du[q] == 0) {
                             // nothing to relax: settled right here
-                            hub = true;
-                            a.settled[u] = d;
+                            hub[q] = true;
+                            a.settled[u[q]] = d[q];
                         }
                     }
+                    wnear.push(u[q], to_near[q] && !hub[q], a.q[ib], &cur->near_len);
+                    wfar.push(u[q], keep[q], a.far[fb ^ 1], &cur->far_len);
                 }
-                wnear.push(u, to_near && !hub, a.q[ib], &cur->near_len);
-                wfar.push(u, keep, a.far[fb ^ 1], &cur->far_len);
             }
             wnear.flush(a.q[ib], &cur->near_len);
             wfar.flush(a.far[fb ^ 1], &cur->far_len);
