@@ -9,6 +9,7 @@ from .graph import (  # noqa: F401
     BellmanFordStats,
     BetweennessCentralityStats,
     BFSStats,
+    CSRSegments,
     DFSStats,
     DeviceGraph,
     EdgeList,
@@ -18,6 +19,7 @@ from .graph import (  # noqa: F401
     PageRankStats,
     PPRAdjointStats,
     PPRStats,
+    Segment,
     SSSPStats,
     bellman_ford,
     betweenness_centrality,
@@ -25,6 +27,7 @@ from .graph import (  # noqa: F401
     breadth_first_search,
     connected_components,
     csr_build,
+    csr_segments,
     degree_reorder,
     depth_first_search,
     read_label_file,

@@ -62,6 +62,8 @@ SIGNATURES = {
     "gbx_bfs_bottom_up_step": (C.c_int, [vp, vp, vp, vp, vp, C.POINTER(u32), vp]),
     "gbx_pagerank_pull": (C.c_int, [vp, u32, C.c_double, vp, C.POINTER(PrResult), vp]),
     "gbx_pagerank_pull_fp64": (C.c_int, [vp, u32, vp, vp]),
+    "gbx_csr_segments_count": (u32, [u32, u32]),
+    "gbx_csr_segments": (C.c_int, [u32, vp, vp, vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     "gbx_pagerank_pull_noalloc": (C.c_int, [u32, vp, vp, vp, u32, C.c_double, vp, C.POINTER(PrResult), vp]),
     "gbx_bfs_multisource": (C.c_int, [vp, u32, vp, vp, vp, vp]),
     "gbx_batch_create": (C.c_int, [C.POINTER(vp), u32, vp, vp, vp, vp, vp, vp]),

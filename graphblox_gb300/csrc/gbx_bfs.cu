@@ -228,21 +228,24 @@ __device__ void top_down_phase(const BfsArgs &a, const uint32_t *qin, uint32_t q
     Claimer claim(a, lnext, qout, hvout, hcout, fbm, cur, s_wq);
     // a frontier with fewer 32-vertex groups than warps cuts each group's
     // edges into `split` interleaved parts of 128-edge batches
+    // Work units: a frontier with few units per warp cuts each 32-vertex
+    // group's edges into `split` interleaved parts of 128-edge batches and
+    // each hub chunk's batches into `hsplit` parts (a small step's work is
+    // then not one warp's serial chain); the group parts are dealt first,
+    // the hub chunks after them.
     const uint32_t groups = (qn + 31) / 32;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t split = groups ? max(1u, min(kTdMaxSplit, nwarps / groups)) : 1u;
-    // and a frontier with fewer hub chunks than warps deals each chunk's
-    // 128-edge batches to `hsplit` warps
     const uint32_t hsplit = nc ? max(1u, min(kHubChunk / 128, nwarps / nc)) : 1u;
-    const uint32_t hunits = nc * hsplit;
-    const uint32_t units = hunits + groups * split;
+    const uint32_t gunits = groups * split;
+    const uint32_t units = gunits + nc * hsplit;
     UnitDealer dealer(&cur->cursor);
     for (;;) {
         const uint32_t unit = dealer.take(units);
         if (unit >= units) break;
-        if (unit < hunits) {
+        if (unit >= gunits) {
             // kHubChunk edges of one hub (every hsplit-th batch of them)
-            const uint32_t chunk = unit / hsplit, hpart = unit % hsplit;
+            const uint32_t chunk = (unit - gunits) / hsplit, hpart = (unit - gunits) % hsplit;
             const uint32_t h = warp_chunk_owner(hcin, nh, chunk);
             const uint32_t v = __ldcg(hvin + h);
             const uint32_t rb = __ldg(a.off + v), re = __ldg(a.off + v + 1);
@@ -270,7 +273,7 @@ __device__ void top_down_phase(const BfsArgs &a, const uint32_t *qin, uint32_t q
             }
         } else {
             // 32 queued vertices, edges flattened over the warp (one part)
-            const uint32_t group = (unit - hunits) / split, part = (unit - hunits) % split;
+            const uint32_t group = unit / split, part = unit % split;
             const uint32_t qi = group * 32 + lane;
             uint32_t v = 0, b = 0, d = 0;
             if (qi < qn) {
@@ -538,6 +541,7 @@ __global__ void __launch_bounds__(kBfsThreads, 3) bfs_persistent_kernel(BfsArgs 
     __shared__ uint32_t s_v[kBfsWarps][32];
     __shared__ uint32_t s_wq[kBfsWarps][kWarpQueueCap];
     __shared__ uint32_t s_found[kBfsWarps][kBuWords];
+    __shared__ BfsStep s_cnt;  // the finished step's counters (fetch_counters)
     const uint32_t wid = threadIdx.x >> 5;
     BfsState *st = a.st;
     grid_barrier_init();
@@ -599,12 +603,13 @@ __global__ void __launch_bounds__(kBfsThreads, 3) bfs_persistent_kernel(BfsArgs 
                             s_found[wid]);
             bm_clean[ob] = false;
             if (!grid_barrier(&st->gs)) { failed = true; break; }
-            const uint32_t nf = __ldcg(&cur->nf);
+            fetch_counters(cur, &s_cnt);
+            const uint32_t nf = s_cnt.nf;
             trace_step(st, kTrBottomUp, nf, cur);
             processed += nf;
             iteration++;
             bu++;
-            edges_total += __ldcg(&cur->edges);
+            edges_total += s_cnt.edges;
             if (nf) L++;
             bool again = a.mode == 0 ? nf > 0 : (nf > nf_prev || nf > a.V / beta);
             nf_prev = nf;
@@ -616,8 +621,8 @@ __global__ void __launch_bounds__(kBfsThreads, 3) bfs_persistent_kernel(BfsArgs 
                 } else {
                     // bitmapToArrayQueue: the step itself wrote the lists of
                     // generation s+1
-                    qn = __ldcg(&cur->qlen);
-                    unsigned long long hb = __ldcg(&cur->hub);
+                    qn = s_cnt.qlen;
+                    unsigned long long hb = s_cnt.hub;
                     nh = (uint32_t)(hb >> 32);
                     nc = (uint32_t)hb;
                     mf = 1;
@@ -636,16 +641,17 @@ __global__ void __launch_bounds__(kBfsThreads, 3) bfs_persistent_kernel(BfsArgs 
                 bm_ready = true;
             }
             if (!grid_barrier(&st->gs)) { failed = true; break; }
-            const uint32_t nf = __ldcg(&cur->nf);
+            fetch_counters(cur, &s_cnt);
+            const uint32_t nf = s_cnt.nf;
             trace_step(st, kTrTopDown, nf, cur);
-            mf = __ldcg(&cur->mf);
+            mf = s_cnt.mf;
             qsize = nf;
             processed += nf;
             iteration++;
             td++;
-            edges_total += __ldcg(&cur->edges);
-            qn = __ldcg(&cur->qlen);
-            unsigned long long hb = __ldcg(&cur->hub);
+            edges_total += s_cnt.edges;
+            qn = s_cnt.qlen;
+            unsigned long long hb = s_cnt.hub;
             nh = (uint32_t)(hb >> 32);
             nc = (uint32_t)hb;
             if (nf) L++;

@@ -71,6 +71,20 @@ __device__ __forceinline__ bool grid_barrier(GridSync *gs) {
     return s_ok != 0;
 }
 
+// After a grid barrier: the first warp copies the step counters *src (a
+// struct of 32-bit words) into the CTA's shared *dst, and the CTA waits for
+// it. The other warps then read shared memory instead of sending the same
+// few L2 lines thousands of requests per step. The barrier's acquire (by
+// thread 0) and its closing __syncthreads order the loads after the other
+// CTAs' counter updates.
+template <class T>
+__device__ __forceinline__ void fetch_counters(const T *src, T *dst) {
+    static_assert(sizeof(T) % 4 == 0 && sizeof(T) / 4 <= 32, "counters are at most 32 words");
+    if (threadIdx.x < sizeof(T) / 4)
+        reinterpret_cast<uint32_t *>(dst)[threadIdx.x] = __ldcg(reinterpret_cast<const uint32_t *>(src) + threadIdx.x);
+    __syncthreads();
+}
+
 // Per-warp staging of queue appends in shared memory: lanes append with
 // ballot ranks into the warp's buffer, and the warp reserves space in the
 // global queue with one atomic per kWarpQueueCap/2..kWarpQueueCap entries

@@ -168,18 +168,21 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
     // ...) so that its relaxations are not one warp's serial chain
     const uint32_t groups = (qn + 31) / 32;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t split = groups ? max(1u, min(kSsspMaxSplit, nwarps / groups)) : 1u;
-    // likewise a round with fewer hub chunks than warps deals each chunk's
-    // 128-edge batches to `hsplit` warps (batch part, part + hsplit, ...)
-    const uint32_t hsplit = nc ? max(1u, min(kSsspHubChunk / 128, nwarps / nc)) : 1u;
-    const uint32_t hunits = nc * hsplit;
-    const uint32_t units = hunits + groups * split;
+    // likewise each hub chunk's 128-edge batches are dealt to `hsplit`
+    // warps (batch part, part + hsplit, ...); both splits aim at
+    // kUnitsPerWarp units per warp so that the dealer can even the warps out,
+    // and the group parts (uneven) are dealt before the hub chunks (even)
+    constexpr uint32_t kUnitsPerWarp = 4;
+    const uint32_t split = groups ? max(1u, min(kSsspMaxSplit, kUnitsPerWarp * nwarps / groups)) : 1u;
+    const uint32_t hsplit = nc ? max(1u, min(kSsspHubChunk / 128, kUnitsPerWarp * nwarps / nc)) : 1u;
+    const uint32_t gunits = groups * split;
+    const uint32_t units = gunits + nc * hsplit;
     UnitDealer dealer(&cur->cursor);
     for (;;) {
         const uint32_t unit = dealer.take(units);
         if (unit >= units) break;
-        if (unit < hunits) {
-            const uint32_t chunk = unit / hsplit, hpart = unit % hsplit;
+        if (unit >= gunits) {
+            const uint32_t chunk = (unit - gunits) / hsplit, hpart = (unit - gunits) % hsplit;
             const uint32_t h = warp_chunk_owner(hcin, nh, chunk);
             const uint32_t v = __ldcg(hvin + h);
             const uint32_t d = __ldcg(a.settled + v);
@@ -208,7 +211,7 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
                 rx.relax4(dq, eq, u, act);
             }
         } else {
-            const uint32_t group = (unit - hunits) / split, part = (unit - hunits) % split;
+            const uint32_t group = unit / split, part = unit % split;
             const uint32_t qi = group * 32 + lane;
             uint32_t b = 0, deg = 0, d = 0;
             if (qi < qn) {
@@ -271,6 +274,7 @@ __global__ void __launch_bounds__(kSsspThreads, 5) sssp_persistent_kernel(SsspAr
     __shared__ uint32_t s_d[kSsspWarps][32];
     __shared__ uint32_t s_wn[kSsspWarps][kWarpQueueCap];
     __shared__ uint32_t s_wf[kSsspWarps][kWarpQueueCap];
+    __shared__ SsspRound s_cnt;  // the finished round's counters (fetch_counters)
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t nthreads = gridDim.x * blockDim.x;
@@ -317,14 +321,15 @@ __global__ void __launch_bounds__(kSsspThreads, 5) sssp_persistent_kernel(SsspAr
             Relaxer rx(a, thr, round, cur, a.q[ib ^ 1], a.hv[ib ^ 1], a.hc[ib ^ 1], a.far[fb], s_wn[wid], s_wf[wid]);
             relax_phase(a, a.q[ib], qn, a.hv[ib], a.hc[ib], nh, nc, rx, cur, s_pre[wid], s_base[wid], s_d[wid]);
             if (!grid_barrier(&st->gs)) { failed = true; break; }
-            relaxed += __ldcg(&cur->relaxed);
-            sssp_trace(st, 1, qn + nh, __ldcg(&cur->relaxed));
-            qn = __ldcg(&cur->near_len);
-            unsigned long long hb = __ldcg(&cur->near_hub);
+            fetch_counters(cur, &s_cnt);
+            relaxed += s_cnt.relaxed;
+            sssp_trace(st, 1, qn + nh, s_cnt.relaxed);
+            qn = s_cnt.near_len;
+            unsigned long long hb = s_cnt.near_hub;
             nh = (uint32_t)(hb >> 32);
             nc = (uint32_t)hb;
-            far_len = __ldcg(&cur->far_len);
-            far_lb = min(far_lb, __ldcg(&cur->far_min));
+            far_len = s_cnt.far_len;
+            far_lb = min(far_lb, s_cnt.far_min);
             gen++;
             rounds++;
             continue;
@@ -413,12 +418,13 @@ __global__ void __launch_bounds__(kSsspThreads, 5) sssp_persistent_kernel(SsspAr
             if (lane == 0 && kmin != 0xFFFFFFFFu) atomicMin(&cur->kept_min, kmin);
         }
         if (!grid_barrier(&st->gs)) { failed = true; break; }
-        qn = __ldcg(&cur->near_len);
-        unsigned long long hb = __ldcg(&cur->near_hub);
+        fetch_counters(cur, &s_cnt);
+        qn = s_cnt.near_len;
+        unsigned long long hb = s_cnt.near_hub;
         nh = (uint32_t)(hb >> 32);
         nc = (uint32_t)hb;
-        far_len = __ldcg(&cur->far_len);
-        far_lb = __ldcg(&cur->kept_min);
+        far_len = s_cnt.far_len;
+        far_lb = s_cnt.kept_min;
         sssp_trace(st, 2, threshold > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)threshold, far_len);
         fb ^= 1;
     }

@@ -258,6 +258,74 @@ def graph_csr_preprocessing(el: EdgeList, *, sort: int = 0, dedup: bool = False,
 
 
 # ---------------------------------------------------------------------------
+# CSR segments (the reference's csrSegments / graphCSRSegments)
+
+
+@dataclass
+class Segment:
+    """struct Segment (csrSegments.h:19-27): the segment's edges and the
+    GraphCSR the reference builds from them. num_vertices is the reference's
+    value, the largest id among the segment's edge ends; the segment's
+    GraphCSR has one vertex more, so that this id has a row."""
+    num_edges: int
+    num_vertices: int
+    edge_list: Optional[EdgeList]
+    graph: Optional[GraphCSR] = None
+
+
+@dataclass
+class CSRSegments:
+    """struct CSRSegments (csrSegments.h:30-43) with host arrays."""
+    num_vertices: int
+    num_edges: int
+    num_segments: int
+    out_degree: np.ndarray
+    in_degree: np.ndarray
+    vertex_segment_index: np.ndarray
+    segments: list
+
+
+def csr_segments(el: EdgeList, cache_size: int = 32768, num_segments: Optional[int] = None,
+                 build_graphs: bool = True, directed: bool = True, keep_weights: bool = True,
+                 stream=None) -> CSRSegments:
+    """csrSegmentsNew (csrSegments.c:157-240) on the GPU: the partition by
+    destination segment (gbx_csr_segments), then, per segment with edges,
+    the preprocessing csrSegmentsCreationPreprocessing applies to it
+    (:330-375: the argumentsNew defaults -- radix sort by source, no dedup --
+    with degree reordering, lmode 1), on the segment's edges with
+    largest id + 1 vertices."""
+    V = int(el.num_vertices)
+    S = int(num_segments) if num_segments else int(_lib.load().gbx_csr_segments_count(V, int(cache_size)))
+    src, dst = _u32(el.src), _u32(el.dst)
+    E = src.shape[0]
+    w = _f32(el.weight) if keep_weights else None
+    od, idg, vsi = (np.zeros(V, np.uint32) for _ in range(3))
+    cnt, mx = np.zeros(S, np.uint32), np.zeros(S, np.uint32)
+    ss, sd = np.zeros(max(E, 1), np.uint32), np.zeros(max(E, 1), np.uint32)
+    sw = np.zeros(max(E, 1), np.float32) if w is not None else None
+    call("gbx_csr_segments", E, _ptr(src), _ptr(dst), _ptr(w), V, S, _ptr(od), _ptr(idg), _ptr(vsi), _ptr(cnt),
+         _ptr(mx), _ptr(ss), _ptr(sd), _ptr(sw), stream)
+    segs = []
+    pos = 0
+    for j in range(S):
+        n = int(cnt[j])
+        if n == 0:
+            segs.append(Segment(0, 0, None))
+            continue
+        es = EdgeList(int(mx[j]) + 1, ss[pos:pos + n].copy(), sd[pos:pos + n].copy(),
+                      None if sw is None else sw[pos:pos + n].copy())
+        seg = Segment(n, int(mx[j]), es)
+        if build_graphs:
+            seg.graph = graph_csr_preprocessing(EdgeList(es.num_vertices, es.src.copy(), es.dst.copy(),
+                                                         None if es.weight is None else es.weight.copy()),
+                                                sort=0, lmode=1, directed=directed,
+                                                keep_weights=es.weight is not None, stream=stream)
+        segs.append(seg)
+        pos += n
+    return CSRSegments(V, E, S, od, idg, vsi, segs)
+
+
+# ---------------------------------------------------------------------------
 # the reference's binary CSR file (.csr)
 
 

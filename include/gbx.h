@@ -351,6 +351,28 @@ int gbx_betweenness(gbx_graph *g, uint32_t num_roots, const uint32_t *roots, flo
  * GBX_ERR_INVALID when no vertex qualifies. */
 int gbx_reference_roots(gbx_graph *g, uint32_t seed, uint32_t n, uint32_t *roots);
 
+/* ---- CSR segments ------------------------------------------------------
+ * The reference's cache-blocked graph form (csrSegmentsNew,
+ * csrSegments.c:157-578; graphCSRSegmentsNew, graphCSRSegments.c:100-131).
+ * gbx_csr_segments_count is csrSegmentsCalculateSegments (:538-553):
+ * ceil(8 num_vertices / cache_size), at least 4. gbx_csr_segments builds the
+ * partition on the GPU: the vertex range cut as getSegmentID (:555-570)
+ * cuts it, every edge in the segment of its destination. Outputs:
+ * out_degree / in_degree (num_vertices, over all edges),
+ * vertex_segment_index (num_vertices: the segment of every destination, 0
+ * for vertices that are no destination), segment_num_edges and
+ * segment_max_id (num_segments: edge count and largest id among the
+ * segment's edge ends, the reference's per-segment num_vertices), and
+ * seg_src / seg_dst / seg_weight (num_edges: the edges grouped by segment,
+ * input order inside a segment; seg_weight may be NULL). Any array may be
+ * host or device memory; edge ends outside [0, num_vertices) fail with
+ * GBX_ERR_INVALID. */
+uint32_t gbx_csr_segments_count(uint32_t num_vertices, uint32_t cache_size);
+int gbx_csr_segments(uint32_t num_edges, const uint32_t *src, const uint32_t *dst, const float *weight,
+                     uint32_t num_vertices, uint32_t num_segments, uint32_t *out_degree, uint32_t *in_degree,
+                     uint32_t *vertex_segment_index, uint32_t *segment_num_edges, uint32_t *segment_max_id,
+                     uint32_t *seg_src, uint32_t *seg_dst, float *seg_weight, void *stream);
+
 /* One draw of the Mersenne Twister MT19937 (Matsumoto and Nishimura, 1998)
  * from a state laid out like the reference's mt19937state (624 unsigned long
  * words and the index; mt19937.h:58-62), which it advances in place: the

@@ -1160,3 +1160,60 @@ int orc_generate_values(uint64_t count, int kind, uint32_t lo, uint32_t hi, uint
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* CSR segments                                                             */
+/* ------------------------------------------------------------------------ */
+
+uint32_t orc_csr_segments_count(uint32_t num_vertices, uint32_t cache_size) {
+    /* csrSegmentsCalculateSegments (csrSegments.c:538-553) */
+    uint32_t n = cache_size ? ((num_vertices * 8u) + cache_size - 1) / cache_size : 4u;
+    return n < 4 ? 4 : n;
+}
+
+/* getSegmentID (csrSegments.c:555-570) */
+static uint32_t orc_segment_id(uint32_t V, uint32_t S, uint32_t id) {
+    uint32_t size = V / S;
+    if (V % S == 0) return id / size;
+    size += 1;
+    uint32_t split = (V % S) * size;
+    return id < split ? id / size : (id - split) / (size - 1) + (V % S);
+}
+
+void orc_csr_segments(uint32_t num_edges, const uint32_t *src, const uint32_t *dst, const float *w,
+                      uint32_t num_vertices, uint32_t num_segments, uint32_t *out_degree, uint32_t *in_degree,
+                      uint32_t *vertex_segment_index, uint32_t *segment_num_edges, uint32_t *segment_max_id,
+                      uint32_t *seg_src, uint32_t *seg_dst, float *seg_w) {
+    const uint32_t V = num_vertices, S = num_segments;
+    memset(out_degree, 0, (size_t)V * 4);
+    memset(in_degree, 0, (size_t)V * 4);
+    memset(vertex_segment_index, 0, (size_t)V * 4);
+    memset(segment_num_edges, 0, (size_t)S * 4);
+    memset(segment_max_id, 0, (size_t)S * 4);
+    /* graphCSRSegmentsProcessInOutDegrees, csrSegmentsSegmentEdgeListSizePreprocessing */
+    for (uint32_t i = 0; i < num_edges; ++i) {
+        out_degree[src[i]]++;
+        in_degree[dst[i]]++;
+        uint32_t seg = orc_segment_id(V, S, dst[i]);
+        segment_num_edges[seg]++;
+        vertex_segment_index[dst[i]] = seg;
+    }
+    /* csrSegmentsSegmentEdgePopulation (one thread: input order), and the
+     * largest id of csrSegmentsSegmentVertexSizePreprocessing */
+    uint32_t *pos = (uint32_t *)xmalloc((size_t)S * 4 + 4);
+    uint32_t run = 0;
+    for (uint32_t j = 0; j < S; ++j) {
+        pos[j] = run;
+        run += segment_num_edges[j];
+    }
+    for (uint32_t i = 0; i < num_edges; ++i) {
+        uint32_t seg = orc_segment_id(V, S, dst[i]);
+        uint32_t k = pos[seg]++;
+        seg_src[k] = src[i];
+        seg_dst[k] = dst[i];
+        if (w && seg_w) seg_w[k] = w[i];
+        uint32_t m = src[i] > dst[i] ? src[i] : dst[i];
+        if (m > segment_max_id[seg]) segment_max_id[seg] = m;
+    }
+    free(pos);
+}

@@ -142,6 +142,18 @@ uint64_t orc_triangle_count_range(uint32_t num_vertices, const uint32_t *out_deg
                                   const uint32_t *edges_idx, const uint32_t *dest, uint32_t lo,
                                   uint32_t hi, int num_threads);
 
+/* ---- CSR segments (csrSegments.c:157-578) --------------------------------
+ * csrSegmentsCalculateSegments and the partition csrSegmentsNew computes
+ * before its per-segment preprocessing: degrees, the segment of every
+ * destination, per-segment edge counts and largest ids, and the edges
+ * grouped by the segment of their destination in input order (the order
+ * the reference's population loop gives with one thread). */
+uint32_t orc_csr_segments_count(uint32_t num_vertices, uint32_t cache_size);
+void orc_csr_segments(uint32_t num_edges, const uint32_t *src, const uint32_t *dst, const float *w,
+                      uint32_t num_vertices, uint32_t num_segments, uint32_t *out_degree, uint32_t *in_degree,
+                      uint32_t *vertex_segment_index, uint32_t *segment_num_edges, uint32_t *segment_max_id,
+                      uint32_t *seg_src, uint32_t *seg_dst, float *seg_w);
+
 #ifdef __cplusplus
 }
 #endif

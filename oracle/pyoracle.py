@@ -51,6 +51,8 @@ def load():
             "orc_triangle_count_range": (u64, [u32, vp, vp, vp, u32, u32, C.c_int]),
             "orc_generate_rmat": (C.c_int, [u32, u64, C.c_double, C.c_double, C.c_double, u64, vp, vp]),
             "orc_generate_values": (C.c_int, [u64, C.c_int, u32, u32, u64, vp]),
+            "orc_csr_segments_count": (u32, [u32, u32]),
+            "orc_csr_segments": (None, [u32, vp, vp, vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp]),
             "orc_spmv_pull": (None, [u32, vp, vp, vp, vp, C.c_float, vp, vp, u32, C.c_int]),
             "orc_spmv_pull_f64": (None, [u32, vp, vp, vp, vp, C.c_float, vp, vp, u32, C.c_int]),
         }
@@ -216,6 +218,29 @@ def triangle_count(g: HostCSR, threads=0, lo=0, hi=None):
     hi = g.num_vertices if hi is None else hi
     return int(load().orc_triangle_count_range(g.num_vertices, _p(g.out_degree), _p(g.edges_idx), _p(g.dest),
                                                int(lo), int(hi), threads))
+
+
+def csr_segments(num_vertices, src, dst, weight=None, cache_size=32768, num_segments=None):
+    """The partition of the reference's csrSegmentsNew: a dict with
+    num_segments, out_degree, in_degree, vertex_segment_index,
+    segment_num_edges, segment_max_id, seg_src, seg_dst[, seg_weight]."""
+    lib = load()
+    V = int(num_vertices)
+    S = int(num_segments) if num_segments else int(lib.orc_csr_segments_count(V, int(cache_size)))
+    s, d = _u32(src), _u32(dst)
+    E = s.shape[0]
+    w = None if weight is None else np.ascontiguousarray(weight, np.float32)
+    out = {k: np.zeros(V, np.uint32) for k in ("out_degree", "in_degree", "vertex_segment_index")}
+    out.update(segment_num_edges=np.zeros(S, np.uint32), segment_max_id=np.zeros(S, np.uint32),
+               seg_src=np.zeros(E, np.uint32), seg_dst=np.zeros(E, np.uint32))
+    sw = None if w is None else np.zeros(E, np.float32)
+    lib.orc_csr_segments(E, _p(s), _p(d), _p(w), V, S, _p(out["out_degree"]), _p(out["in_degree"]),
+                         _p(out["vertex_segment_index"]), _p(out["segment_num_edges"]), _p(out["segment_max_id"]),
+                         _p(out["seg_src"]), _p(out["seg_dst"]), _p(sw))
+    if sw is not None:
+        out["seg_weight"] = sw
+    out["num_segments"] = S
+    return out
 
 
 def generate_rmat(scale, num_edges, a=0.57, b=0.19, c=0.19, seed=1):

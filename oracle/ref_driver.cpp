@@ -17,7 +17,8 @@
 //   cc_components.u32, spmv_y.f32, spmv_x.f32
 //
 // Usage: gbx_ref_<variant> FILE OUTDIR [flags]
-//   -a ALG  (0 bfs, 1 pr, 2 sssp, 5 spmv, 6 cc, 8 tc, -1 csr only)
+//   -a ALG  (0 bfs, 1 pr, 2 sssp, 5 spmv, 6 cc, 8 tc, -1 csr only,
+//            100 CSR segments: see dump_segments)
 //   -p PP   pushpull variant        -s symmetric      -k dedup (+sort 1)
 //   -w      weighted .wbin input    -o SORT           -l LMODE
 //   -r ROOT -i ITERS -e EPS -b DELTA -n THREADS
@@ -27,6 +28,7 @@
 #include <cstring>
 #include <cstdint>
 #include <string>
+#include <vector>
 #include <omp.h>
 
 extern "C" {
@@ -42,6 +44,11 @@ extern "C" {
 #include "DFS.h"
 #include "betweennessCentrality.h"
 #include "SPMV.h"
+#include "csrSegments.h"
+#include "edgeList.h"
+#include "sortRun.h"
+#include "reorder.h"
+#include "myMalloc.h"
 }
 
 static void dump(const std::string &dir, const char *name, const void *p, size_t bytes) {
@@ -50,6 +57,96 @@ static void dump(const std::string &dir, const char *name, const void *p, size_t
     if (!f) { std::perror(path.c_str()); std::exit(2); }
     if (bytes && std::fwrite(p, 1, bytes, f) != bytes) { std::perror("fwrite"); std::exit(2); }
     std::fclose(f);
+}
+
+// CSR segments, the reference's own functions in the order csrSegmentsNew
+// (csrSegments.c:157-240) calls them, on the edge list that
+// graphCSRSegmentsPreProcessingStep (graphCSRSegments.c:134-194) prepares.
+// The last step of csrSegmentsNew, csrSegmentsCreationPreprocessing, builds a
+// GraphCSR per segment from an edge list whose num_vertices is the segment's
+// largest id (csrSegmentsSegmentVertexSizePreprocessing), one short of the
+// arrays that id needs; here each segment's edge list gets largest id + 1
+// vertices (identity labels) before the same per-segment preprocessing
+// (argumentsNew defaults with lmode 1, as csrSegmentsCreationPreprocessing
+// sets them), so the dump is well defined. Dumped (concatenated over
+// segments): seg_* partition arrays, segcsr_* per-segment CSR arrays.
+static int dump_segments(struct Arguments *a, const std::string &out) {
+    struct EdgeList *el = readEdgeListsbin(a->fnameb, 0, a->symmetric, a->weighted);
+    el = sortRunAlgorithms(el, a->sort);
+    if (a->dflag) el = removeDulpicatesSelfLoopEdges(el);
+    if (a->lmode) {
+        el = reorderGraphProcess(el, a);
+        el = sortRunAlgorithms(el, a->sort);
+    }
+    struct CSRSegments *cs = (struct CSRSegments *)std::calloc(1, sizeof(struct CSRSegments));
+    cs->num_edges = el->num_edges;
+    cs->num_vertices = el->num_vertices;
+    cs->num_segments = csrSegmentsCalculateSegments(el, a->cache_size);
+    const uint32_t S = cs->num_segments, V = cs->num_vertices, E = cs->num_edges;
+    cs->segments = (struct Segment *)std::calloc(S, sizeof(struct Segment));
+    cs->activeSegments = (uint32_t *)std::calloc(S, 4);
+    cs->out_degree = (uint32_t *)std::calloc(V + 1, 4);
+    cs->in_degree = (uint32_t *)std::calloc(V + 1, 4);
+    cs->vertex_segment_index = (uint32_t *)std::calloc(V + 1, 4);
+    graphCSRSegmentsProcessInOutDegrees(cs, el);
+    csrSegmentsSegmentEdgeListSizePreprocessing(cs, el);
+    csrSegmentsSegmentsMemoryAllocations(cs);
+    csrSegmentsSegmentEdgePopulation(cs, el);
+    csrSegmentsSegmentVertexSizePreprocessing(cs);
+    FILE *sc = std::fopen((out + "/scalars.txt").c_str(), "w");
+    if (!sc) { std::perror("scalars"); return 2; }
+    std::fprintf(sc, "num_vertices %u\nnum_edges %u\nnum_segments %u\n", V, E, S);
+    std::fclose(sc);
+    dump(out, "seg_out_degree.u32", cs->out_degree, V * 4ull);
+    dump(out, "seg_in_degree.u32", cs->in_degree, V * 4ull);
+    dump(out, "seg_vertex_index.u32", cs->vertex_segment_index, V * 4ull);
+    std::string ne, nv, ssrc, sdst, sw, cdeg, cidx, cdst, clab, cilab, cnv;
+    std::vector<uint32_t> seg_ne(S), seg_nv(S), csr_nv;
+    std::vector<uint32_t> all_src, all_dst, c_deg, c_idx, c_dst, c_lab, c_ilab;
+    std::vector<float> all_w;
+    for (uint32_t j = 0; j < S; ++j) {
+        struct Segment &sg = cs->segments[j];
+        seg_ne[j] = sg.num_edges;
+        seg_nv[j] = sg.num_vertices;
+        if (!sg.num_edges) continue;
+        struct EdgeList *se = sg.edgeList;
+        all_src.insert(all_src.end(), se->edges_array_src, se->edges_array_src + se->num_edges);
+        all_dst.insert(all_dst.end(), se->edges_array_dest, se->edges_array_dest + se->num_edges);
+        all_w.insert(all_w.end(), se->edges_array_weight, se->edges_array_weight + se->num_edges);
+        // one more vertex than the largest id, identity labels
+        const uint32_t nvs = se->num_vertices + 1;
+        se->num_vertices = nvs;
+        se->mask_array = (uint32_t *)std::calloc(nvs, 4);
+        se->label_array = (uint32_t *)std::malloc(nvs * 4ull);
+        se->inverse_label_array = (uint32_t *)std::malloc(nvs * 4ull);
+        for (uint32_t i = 0; i < nvs; ++i) se->label_array[i] = se->inverse_label_array[i] = i;
+        se->avg_degree = se->num_edges / nvs;
+        struct Arguments *al = argumentsNew();
+        al->lmode = 1;
+        al->pre_numThreads = a->pre_numThreads;
+        struct GraphCSR *gs = graphCSRPreProcessingStepFromEdgelist(al, se);
+        csr_nv.push_back(gs->num_vertices);
+        c_deg.insert(c_deg.end(), gs->vertices->out_degree, gs->vertices->out_degree + gs->num_vertices);
+        c_idx.insert(c_idx.end(), gs->vertices->edges_idx, gs->vertices->edges_idx + gs->num_vertices);
+        c_dst.insert(c_dst.end(), gs->sorted_edges_array->edges_array_dest,
+                     gs->sorted_edges_array->edges_array_dest + gs->num_edges);
+        c_lab.insert(c_lab.end(), gs->sorted_edges_array->label_array,
+                     gs->sorted_edges_array->label_array + gs->num_vertices);
+        c_ilab.insert(c_ilab.end(), gs->sorted_edges_array->inverse_label_array,
+                      gs->sorted_edges_array->inverse_label_array + gs->num_vertices);
+    }
+    dump(out, "seg_num_edges.u32", seg_ne.data(), S * 4ull);
+    dump(out, "seg_num_vertices.u32", seg_nv.data(), S * 4ull);
+    dump(out, "seg_src.u32", all_src.data(), all_src.size() * 4ull);
+    dump(out, "seg_dst.u32", all_dst.data(), all_dst.size() * 4ull);
+    if (a->weighted) dump(out, "seg_weight.f32", all_w.data(), all_w.size() * 4ull);
+    dump(out, "segcsr_num_vertices.u32", csr_nv.data(), csr_nv.size() * 4ull);
+    dump(out, "segcsr_out_degree.u32", c_deg.data(), c_deg.size() * 4ull);
+    dump(out, "segcsr_edges_idx.u32", c_idx.data(), c_idx.size() * 4ull);
+    dump(out, "segcsr_dest.u32", c_dst.data(), c_dst.size() * 4ull);
+    dump(out, "segcsr_label.u32", c_lab.data(), c_lab.size() * 4ull);
+    dump(out, "segcsr_inverse_label.u32", c_ilab.data(), c_ilab.size() * 4ull);
+    return 0;
 }
 
 int main(int argc, char **argv) {
@@ -91,6 +188,10 @@ int main(int argc, char **argv) {
     a->ker_numThreads = threads;
     a->algorithm = (uint32_t)(alg < 0 ? 0 : alg);
     if (a->dflag) a->sort = 1;  // GraphBlox.c:355-356
+    if (alg == 100) {
+        omp_set_num_threads(threads);
+        return dump_segments(a, out);
+    }
 
     struct GraphCSR *g = (struct GraphCSR *)generateGraphDataStructure(a);
     omp_set_num_threads(threads);

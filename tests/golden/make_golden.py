@@ -250,6 +250,42 @@ def more_algorithms(ref_root: str) -> None:
     print(f"wrote {out_path.name}")
 
 
+SMALL_FOR_SEGMENTS = ["v51_e1021", "v300_e2730", "v500_e500", "v529_e3500", "v1000_e10000", "v1024_e4096", "test"]
+
+
+def csr_segments(ref_root: str) -> None:
+    """csr_segments.npz: the reference's CSR segments (csrSegmentsNew's
+    partition and the per-segment preprocessing, -a 100 of
+    oracle/ref_driver.cpp, one thread) on every test graph: the directed
+    weighted build on the graph as read (sorted by source and destination)
+    with the fewest segments (4) and, on the graphs below 1,100 vertices, with
+    many (cache size 512), and the undirected build on the symmetrised,
+    deduplicated graph. The per-segment CSRs hold every vertex up to the
+    segment's largest id, so many segments on a large graph would make the
+    fixture large."""
+    test_dir = Path(ref_root) / "03_data" / "TEST"
+    fx: dict[str, np.ndarray] = {}
+    for name in GRAPHS:
+        gdir = test_dir / name
+        weighted = (gdir / "graph.wbin").exists() and not (gdir / "graph.bin").exists()
+        f = gdir / ("graph.wbin" if weighted else "graph.bin")
+        wflag = ["-w"] if weighted else []
+        runs = [(f"{name}_dw_c1048576", "dw", ["-o", "1", "-C", "1048576"]),
+                (f"{name}_u_c1048576", "u", ["-o", "1", "-s", "-k", "-C", "1048576"])]
+        if name in SMALL_FOR_SEGMENTS:
+            runs.append((f"{name}_dw_c512", "dw", ["-o", "1", "-C", "512"]))
+        for key, exe, flags in runs:
+            out = po.ref_run(f, exe, 100, [*wflag, *flags], threads=1)
+            for k, v in out.items():
+                if k in ("num_vertices", "num_edges", "num_segments"):
+                    fx[f"{key}_{k}"] = np.array(v)
+                else:
+                    fx[f"{key}_{k}"] = v
+    out_path = Path(__file__).resolve().parent / "csr_segments.npz"
+    np.savez_compressed(out_path, **fx)
+    print(f"wrote {out_path.name}")
+
+
 if __name__ == "__main__":
     # the reference tree: the first argument, else $GBX_REFERENCE_ROOT, else
     # the tree oracle/build_ref.sh compiled oracle/_ref from
@@ -266,6 +302,8 @@ if __name__ == "__main__":
         mask_modes(root)
     elif len(sys.argv) > 2 and sys.argv[2] == "more":
         more_algorithms(root)
+    elif len(sys.argv) > 2 and sys.argv[2] == "segments":
+        csr_segments(root)
     else:
         main(root)
         reorder_modes(root)
