@@ -142,10 +142,10 @@ extern "C" int gbx_autotune(gbx_graph *g, uint32_t flags, uint32_t num_samples, 
         g->bfs_alpha = best_a;
     }
     if (flags & 2u) {
-        const uint32_t cands_w[] = {64, 128, 256, 512, 1024, 4096};
+        const uint32_t cands_w[] = {64, 96, 128, 192, 256, 512, 1024, 4096};
         const uint32_t cands_u[] = {1, 2, 4};
         const uint32_t *cands = g->weight ? cands_w : cands_u;
-        const int nc = g->weight ? 6 : 3;
+        const int nc = g->weight ? 8 : 3;
         float best = 1e30f;
         uint32_t best_d = g->sssp_delta;
         const uint32_t n = std::min<uint32_t>(2, (uint32_t)src.size());
