@@ -8,10 +8,17 @@
 // "far" pile (each vertex at most once, flagged). When near drains, the
 // threshold jumps one delta past the smallest pending far distance (empty
 // buckets cost nothing, unlike the reference's full-V bucket sweeps), and far
-// entries below it move to near. Each round first snapshots the distance of
-// every near vertex (settled[v]); edges are relaxed from that snapshot, and a
-// far entry whose distance still equals its snapshot is dropped as already
-// expanded. The result is the unique fixed point
+// entries below it move to near. A near vertex is expanded from the
+// distance read when its work unit starts, which its first unit records
+// (settled[v]); a far entry whose distance still equals that record is
+// dropped as already expanded. A near vertex improved again during the
+// round (its stamp already holds the round: the improvement queued it for
+// the next round) is not expanded in this one, since the next round expands
+// it from the better distance; units that started before the improvement
+// relax from the older distance, which is harmless, and a vertex's last
+// expansion, in a round without an improvement of it, reads one distance in
+// all its units. One grid barrier per round. The result is the unique fixed
+// point
 //   dist[u] = min over (v->u) of (uint32)((float)dist[v] + w),
 // i.e. the reference's distances. Work units and hub splitting are those of
 // the persistent BFS (gbx_bfs.cu): 32 near vertices flattened per warp, or
@@ -28,6 +35,7 @@ namespace gbx {
 constexpr uint32_t kSsspHubDeg = 1024;
 constexpr uint32_t kSsspHubChunk = 1024;
 constexpr uint32_t kSsspMaxSplit = 64;  // most warps sharing one 32-vertex group's edges
+constexpr uint32_t kStaleRow = 0xFFFFFFFFu;  // snapshot marker of a near row skipped this round
 constexpr int kSsspThreads = 256;
 constexpr int kSsspWarps = kSsspThreads / 32;
 
@@ -184,11 +192,14 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
         if (unit >= gunits) {
             const uint32_t chunk = (unit - gunits) / hsplit, hpart = (unit - gunits) % hsplit;
             const uint32_t h = warp_chunk_owner(hcin, nh, chunk);
-            const uint32_t v = __ldcg(hvin + h);
-            const uint32_t d = __ldcg(a.settled + v);
+            const uint32_t v = __ldcg(hvin + h), first = __ldcg(hcin + h);
+            const uint32_t sv = __ldcg(a.stamp + v), d = __ldcg(a.dist + v);
             const uint32_t rb = __ldg(a.off + v), re = __ldg(a.off + v + 1);
-            const uint32_t cb = rb + (chunk - __ldcg(hcin + h)) * kSsspHubChunk;
-            const uint32_t ce = min(cb + kSsspHubChunk, re);
+            const uint32_t cb = rb + (chunk - first) * kSsspHubChunk;
+            // a hub improved in this round is in the next near list already
+            const bool stale = sv == rx.round;
+            if (!stale && chunk == first && hpart == 0 && lane == 0) a.settled[v] = d;
+            const uint32_t ce = stale ? cb : min(cb + kSsspHubChunk, re);
             // the next batch's ids are loaded before this batch is relaxed
             const uint32_t stride = hsplit * 128;
             uint32_t un[4];
@@ -218,7 +229,13 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
                 const uint32_t v = __ldcg(qin + qi);
                 b = __ldg(a.off + v);
                 deg = __ldg(a.off + v + 1) - b;
-                d = __ldcg(a.settled + v);
+                const uint32_t sv = __ldcg(a.stamp + v);
+                d = __ldcg(a.dist + v);
+                // improved in this round (so in the next near list): its edges
+                // are masked, but the row keeps its place, because every part
+                // of a split group must flatten the group identically
+                if (sv == rx.round) d = kStaleRow;
+                else if (part == 0) a.settled[v] = d;
             }
             uint32_t incl = deg;
 #pragma unroll
@@ -245,11 +262,12 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
                         while (s_pre[k + 1] <= i) ++k;
                         e[q] = s_base[k] + (i - s_pre[k]);
                         dd[q] = s_d[k];
-                        u[q] = __ldcs(a.dest + e[q]);
+                        if (dd[q] != kStaleRow) u[q] = __ldcs(a.dest + e[q]);
                     }
                 }
-                const bool act[4] = {i0 + lane < tot, i0 + 32 + lane < tot, i0 + 64 + lane < tot,
-                                     i0 + 96 + lane < tot};
+                const bool act[4] = {i0 + lane < tot && dd[0] != kStaleRow, i0 + 32 + lane < tot && dd[1] != kStaleRow,
+                                     i0 + 64 + lane < tot && dd[2] != kStaleRow,
+                                     i0 + 96 + lane < tot && dd[3] != kStaleRow};
                 rx.relax4(dd, e, u, act);
             }
             __syncwarp();
@@ -295,30 +313,20 @@ __global__ void __launch_bounds__(kSsspThreads, 5) sssp_persistent_kernel(SsspAr
     unsigned long long relaxed = 0;
     bool failed = false;
     const uint32_t max_rounds = 4 * a.V + 64;
-    // round 0's counters (the host zeroed the state; the minima start at
-    // "none"); nothing touches them before the first grid barrier
-    if (blockIdx.x == 0 && threadIdx.x == 0) zero_round(&st->r[0], 0);
+    // round 0's counters were set by sssp_init_kernel: the first round's
+    // relaxations start before any grid barrier
     sssp_trace(st, 0, 1, 0);
     for (uint32_t s = 0;; ++s) {
         SsspRound *cur = &st->r[s % 3];
         if (blockIdx.x == 0 && threadIdx.x == 0) zero_round(&st->r[(s + 1) % 3], 0);
         if (qn + nh > 0) {
             if (rounds >= max_rounds) { failed = true; break; }
-            // snapshot the distances this round relaxes from
             const uint32_t ib = gen & 1;
-            for (uint32_t i = gtid; i < qn; i += nthreads) {
-                uint32_t v = __ldcg(a.q[ib] + i);
-                a.settled[v] = __ldcg(a.dist + v);
-            }
-            for (uint32_t i = gtid; i < nh; i += nthreads) {
-                uint32_t v = __ldcg(a.hv[ib] + i);
-                a.settled[v] = __ldcg(a.dist + v);
-            }
-            if (blockIdx.x == 0 && threadIdx.x == 0) cur->far_len = far_len;
-            if (!grid_barrier(&st->gs)) { failed = true; break; }
             round++;
             const uint32_t thr = threshold > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)threshold;
-            Relaxer rx(a, thr, round, cur, a.q[ib ^ 1], a.hv[ib ^ 1], a.hc[ib ^ 1], a.far[fb], s_wn[wid], s_wf[wid]);
+            // far pushes of this round append after the pile's far_len entries
+            Relaxer rx(a, thr, round, cur, a.q[ib ^ 1], a.hv[ib ^ 1], a.hc[ib ^ 1], a.far[fb] + far_len, s_wn[wid],
+                       s_wf[wid]);
             relax_phase(a, a.q[ib], qn, a.hv[ib], a.hc[ib], nh, nc, rx, cur, s_pre[wid], s_base[wid], s_d[wid]);
             if (!grid_barrier(&st->gs)) { failed = true; break; }
             fetch_counters(cur, &s_cnt);
@@ -328,7 +336,7 @@ __global__ void __launch_bounds__(kSsspThreads, 5) sssp_persistent_kernel(SsspAr
             unsigned long long hb = s_cnt.near_hub;
             nh = (uint32_t)(hb >> 32);
             nc = (uint32_t)hb;
-            far_len = s_cnt.far_len;
+            far_len += s_cnt.far_len;
             far_lb = min(far_lb, s_cnt.far_min);
             gen++;
             rounds++;
@@ -437,7 +445,7 @@ __global__ void __launch_bounds__(kSsspThreads, 5) sssp_persistent_kernel(SsspAr
 
 __global__ void sssp_init_kernel(uint32_t *dist, uint32_t *settled, uint32_t *stamp, uint32_t *in_far,
                                  uint32_t V, uint32_t source, const uint32_t *outdeg, uint32_t *q0,
-                                 uint32_t *hv0, uint32_t *hc0) {
+                                 uint32_t *hv0, uint32_t *hc0, SsspRound *r0) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
         dist[v] = v == source ? 0u : kSsspInf;
         settled[v] = 0xFFFFFFFFu;
@@ -448,6 +456,7 @@ __global__ void sssp_init_kernel(uint32_t *dist, uint32_t *settled, uint32_t *st
         q0[0] = source;
         hv0[0] = source;
         hc0[0] = 0;
+        zero_round(r0, 0);
     }
 }
 
@@ -502,10 +511,10 @@ extern "C" int gbx_sssp(gbx_graph *g, uint32_t source, uint32_t delta, uint32_t 
     OutArray<uint32_t> out;
     GBX_TRY(out.bind(distances, V, s, out_stage, out_dev));
     const unsigned grid1 = std::min<unsigned>(ceil_div(V, 256), (unsigned)num_sms() * 8);
-    sssp_init_kernel<<<grid1, 256, 0, s>>>(dist, settled, stamp, in_far, V, source, g->out_degree,
-                                           q0, hv0, hc0);
-    GBX_LAUNCH_CHECK();
     GBX_CUDA(cudaMemsetAsync(st, 0, sizeof(SsspState), s));
+    sssp_init_kernel<<<grid1, 256, 0, s>>>(dist, settled, stamp, in_far, V, source, g->out_degree,
+                                           q0, hv0, hc0, &st->r[0]);
+    GBX_LAUNCH_CHECK();
     SsspArgs a;
     a.off = g->offsets;
     a.dest = g->dest;
