@@ -49,7 +49,7 @@ PR_ITERS = 20
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each
 # kernel, from ncu captures of this workload on a GB300 (profiles/): bfs and
 # sssp one source (--set full), pr one iteration, spmv one launch.
-NCU_TRAFFIC_PER_LAUNCH = {"pr": 0.4006e9, "bfs": 0.1678e9, "sssp": 1.428e9, "spmv": 0.6775e9}
+NCU_TRAFFIC_PER_LAUNCH = {"pr": 0.4006e9, "bfs": 0.1692e9, "sssp": 1.428e9, "spmv": 0.6775e9}
 W_LO, W_HI = 1, 255
 # differentiable personalised PageRank: RMAT-20, 2^24 edges as generated,
 # lognormal(0,1) weights, 64 teleport columns of 32 seeds, d 0.85 to 1e-7 L1
@@ -322,9 +322,10 @@ def run_gpu(args):
     def kernels():
         """(name, fn) -> fn returns (traversed edges, algorithmic bytes)"""
         def bfs():
+            # the reference's trial loop: one traversal per root, enqueued
+            # back to back (gbx_bfs_trials), one host synchronisation
             te = tb = 0
-            for r in roots:
-                st = gbx.breadth_first_search(dg, r, 2, distances=dist_d, parents=par_d, stream=sp)
+            for st in gbx.breadth_first_search_trials(dg, roots, 2, distances=dist_d, parents=par_d, stream=sp):
                 te += st.edges_traversed
                 tb += 4 * (V + 1) + 4 * st.edges_traversed + 8 * V
             return te, tb

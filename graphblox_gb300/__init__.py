@@ -25,6 +25,7 @@ from .graph import (  # noqa: F401
     betweenness_centrality,
     bfs_multisource,
     breadth_first_search,
+    breadth_first_search_trials,
     connected_components,
     csr_build,
     csr_segments,

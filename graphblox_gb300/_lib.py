@@ -58,6 +58,7 @@ SIGNATURES = {
     "gbx_graph_get_tuning": (C.c_int, [vp, C.c_char_p, C.POINTER(C.c_double)]),
     "gbx_autotune": (C.c_int, [vp, u32, u32, vp]),
     "gbx_bfs": (C.c_int, [vp, u32, C.c_int, vp, vp, C.POINTER(BfsResult), vp]),
+    "gbx_bfs_trials": (C.c_int, [vp, vp, u32, C.c_int, vp, vp, C.c_uint64, vp, vp]),
     "gbx_bfs_top_down_step": (C.c_int, [vp, vp, u32, vp, vp, vp, u32, C.POINTER(u32), C.POINTER(u32), vp]),
     "gbx_bfs_bottom_up_step": (C.c_int, [vp, vp, vp, vp, vp, C.POINTER(u32), vp]),
     "gbx_pagerank_pull": (C.c_int, [vp, u32, C.c_double, vp, C.POINTER(PrResult), vp]),

@@ -36,6 +36,7 @@
 // suffice. processed_nodes and iteration therefore match the reference.
 #include <algorithm>
 #include <cstddef>
+#include <vector>
 
 #include "gbx_coop.cuh"
 
@@ -65,6 +66,13 @@ enum : unsigned { kTrStart = 0, kTrTopDown = 1, kTrBottomUp = 2, kTrToBitmap = 3
 struct TraceRec {
     unsigned kind, value;
     unsigned long long ns, busy_sum, busy_max;
+};
+
+// One traversal's results where the host collects them after a run of
+// traversals (gbx_bfs_trials): the final counters and the error words.
+struct BfsSlot {
+    unsigned processed, iteration, td_steps, bu_steps, depth, status, timeout, pad;
+    unsigned long long edges_total;
 };
 
 struct BfsState {
@@ -125,6 +133,7 @@ struct BfsArgs {
     uint32_t *hv[2];
     uint32_t *hc[2];
     BfsState *st;
+    BfsSlot *slot;  // NULL, or where this traversal's results are copied at its end
 };
 
 __device__ __forceinline__ uint32_t hub_chunks(uint32_t d) { return (d + kHubChunk - 1) / kHubChunk; }
@@ -666,6 +675,17 @@ __global__ void __launch_bounds__(kBfsThreads, 3) bfs_persistent_kernel(BfsArgs 
         st->depth = L;
         st->edges_total = edges_total;
         st->status = failed ? 1u : 0u;
+        if (a.slot) {
+            BfsSlot &o = *a.slot;
+            o.processed = processed;
+            o.iteration = iteration;
+            o.td_steps = td;
+            o.bu_steps = bu;
+            o.depth = L;
+            o.edges_total = edges_total;
+            o.status = failed ? 1u : 0u;
+            o.timeout = ld_acquire_u32(&st->gs.error);
+        }
     }
 }
 
@@ -765,31 +785,10 @@ struct BfsWork {
     }
 };
 
-}  // namespace gbx
-
-using namespace gbx;
-
-extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distances,
-                       int32_t *parents, gbx_bfs_result *result, void *stream) {
-    clear_error();
-    GBX_REQUIRE(g, GBX_ERR_INVALID, "graph is NULL");
-    GBX_REQUIRE(source < g->V, GBX_ERR_INVALID, "source %u out of range [0, %u)", source, g->V);
-    GBX_REQUIRE(mode >= 0 && mode <= 2, GBX_ERR_INVALID, "mode must be 0, 1 or 2");
-    GBX_TRY(ensure_device());
-    cudaStream_t s = (cudaStream_t)stream;
+// Graph-level set-up shared by every traversal of the graph: whether every
+// pull source has out-edges, and the bitmap of vertices with pull in-edges.
+int bfs_graph_setup(gbx_graph *g, cudaStream_t s) {
     const uint32_t V = g->V, words = (V + 31) / 32;
-    const int dist_dev = distances ? (is_device_ptr(distances) ? 1 : 0) : 1;
-    const int par_dev = parents ? (is_device_ptr(parents) ? 1 : 0) : 1;
-    const bool stage = !dist_dev || !par_dev;
-    Scratch sc;
-    GBX_TRY(sc.take(g, BfsWork::bytes(V, stage), s));
-    BfsWork w;
-    GBX_TRY(w.carve(sc, V, stage));
-    OutArray<uint32_t> dist;
-    OutArray<int32_t> par;
-    GBX_TRY(dist.bind(distances, V, s, w.dist_stage, dist_dev));
-    GBX_TRY(par.bind(parents, V, s, w.par_stage, par_dev));
-    const unsigned grid1 = std::min<unsigned>(ceil_div(V, 256), (unsigned)num_sms() * 8);
     if (g->pull_sources_live < 0) {
         DevBuf<uint32_t> bad;
         GBX_TRY(bad.alloc(1, s));
@@ -811,10 +810,16 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
             g->pull_offsets(), V, words, g->bu_live);
         GBX_LAUNCH_CHECK();
     }
-    // levels and parents live in the output arrays (device memory, or their
-    // device staging) when the caller asked for them
-    uint32_t *lev = dist.d ? dist.d : w.level;
-    int32_t *parp = par.d ? par.d : w.parent;
+    return GBX_OK;
+}
+
+// One traversal from `source` on stream s: the init kernel, then the
+// persistent kernel, levels into lev and parents into parp (device arrays
+// of V entries).
+int bfs_enqueue(gbx_graph *g, const BfsWork &w, uint32_t source, int mode, uint32_t *lev, int32_t *parp,
+                BfsSlot *slot, cudaStream_t s) {
+    const uint32_t V = g->V, words = (V + 31) / 32;
+    const unsigned grid1 = std::min<unsigned>(ceil_div(V, 256), (unsigned)num_sms() * 8);
     bfs_init_kernel<<<grid1, 256, 0, s>>>(lev, parp, w.visited, w.bm0, w.bm1, V, words, source, g->out_degree,
                                           w.q0, w.hv0, w.hc0, w.st);
     GBX_LAUNCH_CHECK();
@@ -846,12 +851,55 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
     a.hc[0] = w.hc0;
     a.hc[1] = w.hc1;
     a.st = w.st;
+    a.slot = slot;
     int grid = 0;
     static int grid_cache[64] = {0};
     GBX_TRY(coop_grid(bfs_persistent_kernel, kBfsThreads, 0, &grid, &grid_cache));
     void *args[] = {&a};
     GBX_CUDA(cudaLaunchCooperativeKernel((const void *)bfs_persistent_kernel, grid, kBfsThreads, args, 0, s));
     GBX_LAUNCH_CHECK();
+    return GBX_OK;
+}
+
+void bfs_fill_result(gbx_bfs_result *r, unsigned processed, unsigned iteration, unsigned depth, unsigned td,
+                     unsigned bu, unsigned long long edges) {
+    r->processed_nodes = processed;
+    r->iteration = iteration;
+    r->depth = depth;
+    r->top_down_steps = td;
+    r->bottom_up_steps = bu;
+    r->reserved = 0;
+    r->edges_traversed = edges;
+}
+
+}  // namespace gbx
+
+using namespace gbx;
+
+extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distances,
+                       int32_t *parents, gbx_bfs_result *result, void *stream) {
+    clear_error();
+    GBX_REQUIRE(g, GBX_ERR_INVALID, "graph is NULL");
+    GBX_REQUIRE(source < g->V, GBX_ERR_INVALID, "source %u out of range [0, %u)", source, g->V);
+    GBX_REQUIRE(mode >= 0 && mode <= 2, GBX_ERR_INVALID, "mode must be 0, 1 or 2");
+    GBX_TRY(ensure_device());
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t V = g->V;
+    const int dist_dev = distances ? (is_device_ptr(distances) ? 1 : 0) : 1;
+    const int par_dev = parents ? (is_device_ptr(parents) ? 1 : 0) : 1;
+    const bool stage = !dist_dev || !par_dev;
+    Scratch sc;
+    GBX_TRY(sc.take(g, BfsWork::bytes(V, stage), s));
+    BfsWork w;
+    GBX_TRY(w.carve(sc, V, stage));
+    OutArray<uint32_t> dist;
+    OutArray<int32_t> par;
+    GBX_TRY(dist.bind(distances, V, s, w.dist_stage, dist_dev));
+    GBX_TRY(par.bind(parents, V, s, w.par_stage, par_dev));
+    GBX_TRY(bfs_graph_setup(g, s));
+    // levels and parents live in the output arrays (device memory, or their
+    // device staging) when the caller asked for them
+    GBX_TRY(bfs_enqueue(g, w, source, mode, dist.d ? dist.d : w.level, par.d ? par.d : w.parent, nullptr, s));
     GBX_TRY(dist.finish(s));
     GBX_TRY(par.finish(s));
     // the counters (and the step trace only when it is printed)
@@ -863,6 +911,9 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
     GBX_REQUIRE(hs.status == 0, GBX_ERR_ITER_CAP, "BFS step cap reached");
     if (trace_enabled()) {
         static const char *names[] = {"start", "TD", "BU", "->bitmap", "->lists"};
+        int grid = 0;
+        static int grid_cache[64] = {0};
+        GBX_TRY(coop_grid(bfs_persistent_kernel, kBfsThreads, 0, &grid, &grid_cache));
         const unsigned nwarps = (unsigned)grid * (kBfsThreads / 32);
         fprintf(stderr, "| gbx_bfs source %u: %-9s | %-10s | %-10s | %-12s | %-12s |\n", source, "step", "vertices",
                 "us", "warp max us", "warp mean us");
@@ -871,14 +922,50 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
                     hs.trace[i].value, (hs.trace[i].ns - hs.trace[i - 1].ns) * 1e-3, hs.trace[i].busy_max * 1e-3,
                     hs.trace[i].busy_sum * 1e-3 / nwarps);
     }
-    if (result) {
-        result->processed_nodes = hs.processed;
-        result->iteration = hs.iteration;
-        result->depth = hs.depth;
-        result->top_down_steps = hs.td_steps;
-        result->bottom_up_steps = hs.bu_steps;
-        result->reserved = 0;
-        result->edges_traversed = hs.edges_total;
+    if (result)
+        bfs_fill_result(result, hs.processed, hs.iteration, hs.depth, hs.td_steps, hs.bu_steps, hs.edges_total);
+    return GBX_OK;
+}
+
+extern "C" int gbx_bfs_trials(gbx_graph *g, const uint32_t *sources, uint32_t num_sources, int mode,
+                              uint32_t *distances, int32_t *parents, uint64_t out_stride,
+                              gbx_bfs_result *results, void *stream) {
+    clear_error();
+    GBX_REQUIRE(g, GBX_ERR_INVALID, "graph is NULL");
+    GBX_REQUIRE(num_sources == 0 || (sources && results), GBX_ERR_INVALID, "sources or results is NULL");
+    GBX_REQUIRE(mode >= 0 && mode <= 2, GBX_ERR_INVALID, "mode must be 0, 1 or 2");
+    for (uint32_t i = 0; i < num_sources; ++i)
+        GBX_REQUIRE(sources[i] < g->V, GBX_ERR_INVALID, "source %u (trial %u) out of range [0, %u)", sources[i], i,
+                    g->V);
+    GBX_REQUIRE(out_stride == 0 || out_stride >= g->V, GBX_ERR_INVALID, "out_stride must be 0 or >= %u", g->V);
+    if (num_sources == 0) return GBX_OK;
+    GBX_TRY(ensure_device());
+    GBX_REQUIRE(!distances || is_device_ptr(distances), GBX_ERR_INVALID, "distances must be device memory");
+    GBX_REQUIRE(!parents || is_device_ptr(parents), GBX_ERR_INVALID, "parents must be device memory");
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t V = g->V;
+    Scratch sc;
+    GBX_TRY(sc.take(g, BfsWork::bytes(V, false), s));
+    BfsWork w;
+    GBX_TRY(w.carve(sc, V, false));
+    GBX_TRY(bfs_graph_setup(g, s));
+    DevBuf<BfsSlot> slots;
+    GBX_TRY(slots.alloc(num_sources, s));
+    // every traversal re-initialises the shared work arrays on the stream, so
+    // the traversals run back to back without the host in between
+    for (uint32_t i = 0; i < num_sources; ++i) {
+        uint32_t *lev = distances ? distances + (size_t)i * out_stride : w.level;
+        int32_t *parp = parents ? parents + (size_t)i * out_stride : w.parent;
+        GBX_TRY(bfs_enqueue(g, w, sources[i], mode, lev, parp, slots.p + i, s));
+    }
+    std::vector<BfsSlot> hs(num_sources);
+    GBX_CUDA(cudaMemcpyAsync(hs.data(), slots.p, num_sources * sizeof(BfsSlot), cudaMemcpyDeviceToHost, s));
+    GBX_CUDA(cudaStreamSynchronize(s));
+    for (uint32_t i = 0; i < num_sources; ++i) {
+        GBX_REQUIRE(hs[i].timeout == 0, GBX_ERR_DEVICE_TIMEOUT, "BFS grid barrier wait expired (trial %u)", i);
+        GBX_REQUIRE(hs[i].status == 0, GBX_ERR_ITER_CAP, "BFS step cap reached (trial %u)", i);
+        bfs_fill_result(results + i, hs[i].processed, hs[i].iteration, hs[i].depth, hs[i].td_steps,
+                        hs[i].bu_steps, hs[i].edges_total);
     }
     return GBX_OK;
 }

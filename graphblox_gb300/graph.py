@@ -539,6 +539,25 @@ def breadth_first_search(dg: DeviceGraph, source: int, pushpull: int = 2, distan
     return BFSStats(distances, parents, r.processed_nodes, r.iteration, r.depth, r.edges_traversed, src)
 
 
+def breadth_first_search_trials(dg: DeviceGraph, sources, pushpull: int = 2, distances=None, parents=None,
+                                out_stride: int = 0, stream=None, map_source: bool = True) -> list:
+    """The reference's BFS trial loop (graphRun.c:463-595) through
+    gbx_bfs_trials: one traversal per source, back to back on the stream,
+    one host synchronisation. distances / parents are device tensors (or
+    None); with out_stride 0 the last trial's output remains in them, with
+    out_stride >= V trial i writes [i*out_stride, i*out_stride + V).
+    Returns one BFSStats per trial (its distances / parents fields hold the
+    arrays passed in)."""
+    srcs = np.asarray([_map_source(dg, s) if map_source else int(s) for s in sources], np.uint32)
+    n = len(srcs)
+    res = (BfsResult * max(n, 1))()
+    mode = {0: 0, 1: 1}.get(int(pushpull), 2)
+    call("gbx_bfs_trials", dg.handle, srcs.ctypes.data, n, mode, _ptr(distances), _ptr(parents), int(out_stride),
+         res, stream)
+    return [BFSStats(distances, parents, res[i].processed_nodes, res[i].iteration, res[i].depth,
+                     res[i].edges_traversed, int(srcs[i])) for i in range(n)]
+
+
 @dataclass
 class PageRankStats:
     pageRanks: object
