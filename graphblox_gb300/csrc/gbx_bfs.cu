@@ -47,7 +47,7 @@ constexpr uint32_t kHubChunk = 1024;  // edges per hub work unit
 constexpr uint32_t kBuProbe = 64;     // bottom-up: in-edges a lane probes alone before the warp helps
 constexpr uint32_t kTdMaxSplit = 64;  // top-down: most warps sharing one 32-vertex group's edges
 constexpr uint32_t kBuWords = 16;     // bottom-up: frontier-bitmap words (32 vertices each) per work unit
-constexpr int kBfsThreads = 256;
+constexpr int kBfsThreads = 768;
 constexpr int kBfsWarps = kBfsThreads / 32;
 
 struct BfsStep {
@@ -544,7 +544,7 @@ __device__ __forceinline__ void zero_step(BfsStep *s) {
     s->busy_max = 0;
 }
 
-__global__ void __launch_bounds__(kBfsThreads, 3) bfs_persistent_kernel(BfsArgs a) {
+__global__ void __launch_bounds__(kBfsThreads, 1) bfs_persistent_kernel(BfsArgs a) {
     __shared__ uint32_t s_pre[kBfsWarps][33];
     __shared__ uint32_t s_base[kBfsWarps][32];
     __shared__ uint32_t s_v[kBfsWarps][32];
@@ -927,6 +927,31 @@ extern "C" int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distan
     return GBX_OK;
 }
 
+// A second stream and two pairs of events for copies that overlap the next
+// trial: done[b] marks a trial's output in staging buffer b as complete,
+// copied[b] marks its copy to the host as finished. The destructor waits for
+// the copy stream, so staging buffers are never released under a copy.
+struct CopyLane {
+    cudaStream_t cs = nullptr;
+    cudaEvent_t done[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
+    int create() {
+        GBX_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        for (int b = 0; b < 2; ++b) {
+            GBX_CUDA(cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming));
+            GBX_CUDA(cudaEventCreateWithFlags(&copied[b], cudaEventDisableTiming));
+        }
+        return GBX_OK;
+    }
+    ~CopyLane() {
+        if (cs) cudaStreamSynchronize(cs);
+        for (int b = 0; b < 2; ++b) {
+            if (done[b]) cudaEventDestroy(done[b]);
+            if (copied[b]) cudaEventDestroy(copied[b]);
+        }
+        if (cs) cudaStreamDestroy(cs);
+    }
+};
+
 extern "C" int gbx_bfs_trials(gbx_graph *g, const uint32_t *sources, uint32_t num_sources, int mode,
                               uint32_t *distances, int32_t *parents, uint64_t out_stride,
                               gbx_bfs_result *results, void *stream) {
@@ -940,10 +965,10 @@ extern "C" int gbx_bfs_trials(gbx_graph *g, const uint32_t *sources, uint32_t nu
     GBX_REQUIRE(out_stride == 0 || out_stride >= g->V, GBX_ERR_INVALID, "out_stride must be 0 or >= %u", g->V);
     if (num_sources == 0) return GBX_OK;
     GBX_TRY(ensure_device());
-    GBX_REQUIRE(!distances || is_device_ptr(distances), GBX_ERR_INVALID, "distances must be device memory");
-    GBX_REQUIRE(!parents || is_device_ptr(parents), GBX_ERR_INVALID, "parents must be device memory");
     cudaStream_t s = (cudaStream_t)stream;
     const uint32_t V = g->V;
+    const bool dist_host = distances && !is_device_ptr(distances);
+    const bool par_host = parents && !is_device_ptr(parents);
     Scratch sc;
     GBX_TRY(sc.take(g, BfsWork::bytes(V, false), s));
     BfsWork w;
@@ -951,15 +976,38 @@ extern "C" int gbx_bfs_trials(gbx_graph *g, const uint32_t *sources, uint32_t nu
     GBX_TRY(bfs_graph_setup(g, s));
     DevBuf<BfsSlot> slots;
     GBX_TRY(slots.alloc(num_sources, s));
+    // host outputs: each array gets two device staging buffers, used by
+    // alternate trials; trial i's copy to the host runs on a second stream
+    // while trial i+1 traverses, and trial i+2 waits for it before writing
+    // into the same buffer
+    DevBuf<uint32_t> dstage;
+    DevBuf<int32_t> pstage;
+    if (dist_host) GBX_TRY(dstage.alloc(2 * (size_t)V, s));
+    if (par_host) GBX_TRY(pstage.alloc(2 * (size_t)V, s));
+    CopyLane copies;
+    if (dist_host || par_host) GBX_TRY(copies.create());
     // every traversal re-initialises the shared work arrays on the stream, so
     // the traversals run back to back without the host in between
     for (uint32_t i = 0; i < num_sources; ++i) {
-        uint32_t *lev = distances ? distances + (size_t)i * out_stride : w.level;
-        int32_t *parp = parents ? parents + (size_t)i * out_stride : w.parent;
+        const uint32_t b = i & 1;
+        const size_t off = (size_t)i * out_stride;
+        uint32_t *lev = dist_host ? dstage.p + (size_t)b * V : distances ? distances + off : w.level;
+        int32_t *parp = par_host ? pstage.p + (size_t)b * V : parents ? parents + off : w.parent;
+        if (copies.cs && i >= 2) GBX_CUDA(cudaStreamWaitEvent(s, copies.copied[b], 0));
         GBX_TRY(bfs_enqueue(g, w, sources[i], mode, lev, parp, slots.p + i, s));
+        if (copies.cs) {
+            GBX_CUDA(cudaEventRecord(copies.done[b], s));
+            GBX_CUDA(cudaStreamWaitEvent(copies.cs, copies.done[b], 0));
+            if (dist_host)
+                GBX_CUDA(cudaMemcpyAsync(distances + off, lev, (size_t)V * 4, cudaMemcpyDeviceToHost, copies.cs));
+            if (par_host)
+                GBX_CUDA(cudaMemcpyAsync(parents + off, parp, (size_t)V * 4, cudaMemcpyDeviceToHost, copies.cs));
+            GBX_CUDA(cudaEventRecord(copies.copied[b], copies.cs));
+        }
     }
     std::vector<BfsSlot> hs(num_sources);
     GBX_CUDA(cudaMemcpyAsync(hs.data(), slots.p, num_sources * sizeof(BfsSlot), cudaMemcpyDeviceToHost, s));
+    if (copies.cs) GBX_CUDA(cudaStreamSynchronize(copies.cs));
     GBX_CUDA(cudaStreamSynchronize(s));
     for (uint32_t i = 0; i < num_sources; ++i) {
         GBX_REQUIRE(hs[i].timeout == 0, GBX_ERR_DEVICE_TIMEOUT, "BFS grid barrier wait expired (trial %u)", i);

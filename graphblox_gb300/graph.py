@@ -543,9 +543,10 @@ def breadth_first_search_trials(dg: DeviceGraph, sources, pushpull: int = 2, dis
                                 out_stride: int = 0, stream=None, map_source: bool = True) -> list:
     """The reference's BFS trial loop (graphRun.c:463-595) through
     gbx_bfs_trials: one traversal per source, back to back on the stream,
-    one host synchronisation. distances / parents are device tensors (or
-    None); with out_stride 0 the last trial's output remains in them, with
-    out_stride >= V trial i writes [i*out_stride, i*out_stride + V).
+    one host synchronisation. distances / parents are device tensors, host
+    arrays (copied back while the next trial runs) or None; with out_stride
+    0 the last trial's output remains in them, with out_stride >= V trial i
+    writes [i*out_stride, i*out_stride + V).
     Returns one BFSStats per trial (its distances / parents fields hold the
     arrays passed in)."""
     srcs = np.asarray([_map_source(dg, s) if map_source else int(s) for s in sources], np.uint32)

@@ -157,10 +157,12 @@ int gbx_bfs(gbx_graph *g, uint32_t source, int mode, uint32_t *distances, int32_
  * new root): one gbx_bfs traversal per source, enqueued back to back on
  * `stream` with a single host synchronisation after the last. sources and
  * results are host arrays of num_sources entries; results[i] is what gbx_bfs
- * returns for sources[i]. distances / parents: NULL, or DEVICE arrays; with
- * out_stride 0 every trial writes the same V entries (the last trial's
- * levels and parents remain), with out_stride >= V trial i writes entries
- * [i * out_stride, i * out_stride + V). */
+ * returns for sources[i]. distances / parents: NULL, or device or host
+ * arrays; with out_stride 0 every trial writes the same V entries (the last
+ * trial's levels and parents remain), with out_stride >= V trial i writes
+ * entries [i * out_stride, i * out_stride + V). A host array is filled
+ * through two device staging buffers: trial i's copy to the host overlaps
+ * trial i+1's traversal (pinned host memory makes the copies asynchronous). */
 int gbx_bfs_trials(gbx_graph *g, const uint32_t *sources, uint32_t num_sources, int mode,
                    uint32_t *distances, int32_t *parents, uint64_t out_stride, gbx_bfs_result *results,
                    void *stream);

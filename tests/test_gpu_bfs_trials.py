@@ -5,8 +5,8 @@ Every trial must give what gbx_bfs gives for its root alone and what the
 oracle's restatement of breadthFirstSearchGraphCSR gives: levels,
 processed_nodes and iteration bit-exact, parents a BFS tree. Both output
 layouts are checked (one slice per trial, and one shared array that keeps
-the last trial's output), with repeated roots, every direction mode, and
-the argument errors the entry point reports.
+the last trial's output), in device and host memory, with repeated roots,
+every direction mode, and the argument errors the entry point reports.
 """
 import numpy as np
 import pytest
@@ -97,6 +97,29 @@ def test_trials_shared_output_keeps_the_last(gbx, cuda_device, rmat14):
         assert (t.processed_nodes, t.iteration) == (proc, it)
 
 
+@pytest.mark.parametrize("stride", [0, 1])
+def test_trials_host_outputs(gbx, cuda_device, rmat14, stride):
+    """Host arrays: filled through the alternating staging buffers and the
+    copy stream; with out_stride 0 the last trial's output remains."""
+    import torch
+
+    g, host, pull, roots = rmat14
+    V = g.num_vertices
+    n = len(roots)
+    rows = n if stride else 1
+    dist = torch.full((rows * V,), 7, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    par = np.full(rows * V, 7, np.int32)  # pageable: the copies are synchronous there
+    with gbx.DeviceGraph.from_graph_csr(g) as dg:
+        trials = gbx.breadth_first_search_trials(dg, roots, 2, distances=dist, parents=par, out_stride=stride * V)
+    for i, (r, t) in enumerate(zip(roots, trials)):
+        d, _, proc, it = po.bfs(host, r, pull)
+        assert (t.processed_nodes, t.iteration) == (proc, it)
+        if stride or i == n - 1:
+            row = i if stride else 0
+            np.testing.assert_array_equal(dist[row * V:(row + 1) * V], d, err_msg=f"trial {i} root {r}")
+            _check_parents(g, r, d, par[row * V:(row + 1) * V])
+
+
 def test_trials_argument_errors(gbx, cuda_device, rmat14):
     import torch
 
@@ -105,8 +128,6 @@ def test_trials_argument_errors(gbx, cuda_device, rmat14):
     with gbx.DeviceGraph.from_graph_csr(g) as dg:
         with pytest.raises(gbx.GbxError, match="out of range"):
             gbx.breadth_first_search_trials(dg, [0, V], 2, map_source=False)
-        with pytest.raises(gbx.GbxError, match="device memory"):
-            gbx.breadth_first_search_trials(dg, roots[:2], 2, distances=np.zeros(V, np.uint32))
         d = torch.empty(2 * V, dtype=torch.int32, device=cuda_device)
         with pytest.raises(gbx.GbxError, match="out_stride"):
             gbx.breadth_first_search_trials(dg, roots[:2], 2, distances=d, out_stride=V - 1)
