@@ -46,7 +46,7 @@ constexpr uint32_t kHubDeg = 1024;    // out-degree above which a vertex is a hu
 constexpr uint32_t kHubChunk = 1024;  // edges per hub work unit
 constexpr uint32_t kBuProbe = 64;     // bottom-up: in-edges a lane probes alone before the warp helps
 constexpr uint32_t kTdMaxSplit = 64;  // top-down: most warps sharing one 32-vertex group's edges
-constexpr uint32_t kBuWords = 16;     // bottom-up: frontier-bitmap words (32 vertices each) per work unit
+constexpr uint32_t kBuWords = 8;      // bottom-up: frontier-bitmap words (32 vertices each) per work unit
 constexpr int kBfsThreads = 768;
 constexpr int kBfsWarps = kBfsThreads / 32;
 

@@ -36,7 +36,7 @@ constexpr uint32_t kSsspHubDeg = 1024;
 constexpr uint32_t kSsspHubChunk = 1024;
 constexpr uint32_t kSsspMaxSplit = 64;  // most warps sharing one 32-vertex group's edges
 constexpr uint32_t kStaleRow = 0xFFFFFFFFu;  // snapshot marker of a near row skipped this round
-constexpr int kSsspThreads = 256;
+constexpr int kSsspThreads = 1024;
 constexpr int kSsspWarps = kSsspThreads / 32;
 
 struct SsspRound {
@@ -286,7 +286,7 @@ __device__ __forceinline__ void zero_round(SsspRound *r, uint32_t far_len) {
     r->kept_min = 0xFFFFFFFFu;
 }
 
-__global__ void __launch_bounds__(kSsspThreads, 5) sssp_persistent_kernel(SsspArgs a) {
+__global__ void __launch_bounds__(kSsspThreads, 1) sssp_persistent_kernel(SsspArgs a) {
     __shared__ uint32_t s_pre[kSsspWarps][33];
     __shared__ uint32_t s_base[kSsspWarps][32];
     __shared__ uint32_t s_d[kSsspWarps][32];
