@@ -15,13 +15,17 @@
 // mask is one 4*NW-byte access. Pull rows above kMsLight in-edges are cut into
 // kMsChunk-edge chunks worked by whole warps and OR-ed into Fn with atomics
 // (OR is order-free, so the result is deterministic). An update pass then
-// sets new = Fn & ~seen, seen |= new, writes the level into distances for
-// every new bit, and compacts the next frontier list.
+// sets new = Fn & ~seen, seen |= new, and compacts the next frontier list;
+// the new masks of each level are kept (up to kMsMaxStoredLevels of them).
 //
 // distances is vertex-major: distances[v * S + i] is the level of v from
 // sources[i] (0 for sources[i] itself and for unreached vertices, as the
-// reference reports). Per-source results come from one final reduction.
+// reference reports). One final pass writes every row of distances from the
+// kept level masks (a warp per vertex, whole 16-byte stores) and reduces the
+// per-source results; only levels past the kept ones write their distances
+// bit by bit during the traversal.
 #include <algorithm>
+#include <cstdint>
 #include <vector>
 
 #include "gbx_internal.cuh"
@@ -159,9 +163,11 @@ __global__ void __launch_bounds__(kMsThreads)
 }
 
 // ---- update ----------------------------------------------------------------------
-// new = Fn & ~seen; seen |= new; F_next = new (written into Fn); distances for
-// every new bit; v appended to the next frontier list when any bit is new.
-template <int NW>
+// new = Fn & ~seen; seen |= new; F_next = new (written into Fn, which is kept
+// as this level's mask while levels are stored); v appended to the next
+// frontier list when any bit is new. Past the stored levels (kWriteDist) the
+// distances of the new bits are written here, one by one.
+template <int NW, bool kWriteDist>
 __global__ void __launch_bounds__(kMsThreads)
     ms_update_kernel(uint32_t V, uint32_t S, uint32_t level, const uint32_t *__restrict__ off,
                      uint32_t *__restrict__ seen, uint32_t *__restrict__ Fn, uint32_t *__restrict__ dist,
@@ -180,8 +186,10 @@ __global__ void __launch_bounds__(kMsThreads)
             Fn[i] = nw;
             if (nw) {
                 seen[i] = s0 | nw;
-                uint32_t *row = dist + (size_t)v * S + 32 * k;
-                for (uint32_t m = nw; m; m &= m - 1) row[__ffs(m) - 1] = level;
+                if (kWriteDist) {
+                    uint32_t *row = dist + (size_t)v * S + 32 * k;
+                    for (uint32_t m = nw; m; m &= m - 1) row[__ffs(m) - 1] = level;
+                }
             }
         }
         // one append per vertex with any new bit: the group's lowest lane
@@ -213,29 +221,110 @@ __global__ void ms_seed_kernel(const uint32_t *sources, uint32_t S, uint32_t NW,
     if (threadIdx.x == 0) cnt->qn = S;
 }
 
-// Per source: reached count, out-degree sum of reached vertices, deepest level.
-__global__ void ms_results_kernel(const uint32_t *__restrict__ dist, uint32_t V, uint32_t S,
-                                  const uint32_t *__restrict__ off, const uint32_t *__restrict__ sources,
-                                  uint32_t *cnt, unsigned long long *edges, uint32_t *depth) {
-    // grid * blockDim is a multiple of S: thread t owns column t % S
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t c = tid % S, r0 = tid / S, rs = (gridDim.x * blockDim.x) / S;
-    if (r0 >= rs) return;
-    uint32_t n = 0, mx = 0;
-    unsigned long long ed = 0;
-    for (uint32_t v = r0; v < V; v += rs) {
-        const uint32_t l = dist[(size_t)v * S + c];
-        if (l) {
-            ++n;
-            ed += off[v + 1] - off[v];
-            mx = max(mx, l);
+// Level masks kept for the final pass: masks[L][v * NW + k] holds the
+// sources (bits of word k) that reached v at level L (level 0: the seeds).
+constexpr uint32_t kMsMaxStoredLevels = 32;
+struct MsLevels {
+    const uint32_t *m[kMsMaxStoredLevels];
+    uint32_t n;
+};
+
+// The distances and the per-source results in one pass: a warp per vertex,
+// lane l owning sources l*NW .. l*NW + NW-1 (NW consecutive bits of mask
+// word l*NW/32). A source's level at v is the first stored level whose mask
+// holds its bit; a bit that is seen but in no stored mask was reached past
+// the stored levels, and its distance was written by the update kernel; the
+// rest are unreached (0, as is the source's own entry at level 0). Per
+// source: reached vertices (level >= 1), the out-degree sum over them, the
+// deepest level.
+template <int NW>
+__global__ void __launch_bounds__(kMsThreads)
+    ms_final_kernel(MsLevels lv, const uint32_t *__restrict__ seen, uint32_t V, uint32_t S,
+                    const uint32_t *__restrict__ off, const uint32_t *__restrict__ sources, bool vec_rows,
+                    uint32_t *__restrict__ dist, uint32_t *__restrict__ cnt, unsigned long long *__restrict__ edges,
+                    uint32_t *__restrict__ depth) {
+    __shared__ uint32_t s_cnt[32 * NW], s_depth[32 * NW];
+    __shared__ unsigned long long s_edges[32 * NW];
+    for (uint32_t i = threadIdx.x; i < 32 * NW; i += blockDim.x) {
+        s_cnt[i] = 0;
+        s_depth[i] = 0;
+        s_edges[i] = 0;
+    }
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t k = lane * NW / 32, sh = (lane * NW) % 32;
+    const uint32_t bmask = NW == 32 ? 0xFFFFFFFFu : ((1u << NW) - 1u);
+    const uint32_t s0 = lane * NW;  // this lane's first source
+    uint32_t c[NW], dm[NW];
+    unsigned long long ed[NW];
+#pragma unroll
+    for (int j = 0; j < NW; ++j) c[j] = dm[j] = 0, ed[j] = 0;
+    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarp = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t v = warp0; v < V; v += nwarp) {
+        const size_t w = (size_t)v * NW + k;
+        const uint32_t sw = (__ldg(seen + w) >> sh) & bmask;
+        const uint32_t deg = __ldg(off + v + 1) - __ldg(off + v);
+        uint32_t lvl[NW];
+#pragma unroll
+        for (int j = 0; j < NW; ++j) lvl[j] = 0;
+        uint32_t found = 0;
+        for (uint32_t L0 = 0; L0 < lv.n && found != sw; L0 += 8) {
+            uint32_t m[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) m[q] = L0 + q < lv.n ? (__ldg(lv.m[L0 + q] + w) >> sh) & bmask : 0u;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const uint32_t nb = m[q] & ~found;
+#pragma unroll
+                for (int j = 0; j < NW; ++j)
+                    if ((nb >> j) & 1u) lvl[j] = L0 + q;
+                found |= m[q];
+            }
+        }
+        uint32_t *row = dist + (size_t)v * S + s0;
+        const uint32_t deep = sw & ~found;  // written by the update kernel past the stored levels
+        if (deep) {
+#pragma unroll
+            for (int j = 0; j < NW; ++j)
+                if ((deep >> j) & 1u) lvl[j] = row[j];
+        }
+        const bool full = s0 + NW <= S;
+        if (NW % 4 == 0 && vec_rows && full) {
+#pragma unroll
+            for (int q = 0; q < NW / 4; ++q)
+                reinterpret_cast<uint4 *>(row)[q] = make_uint4(lvl[4 * q], lvl[4 * q + 1], lvl[4 * q + 2], lvl[4 * q + 3]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < NW; ++j)
+                if (s0 + j < S) row[j] = lvl[j];
+        }
+#pragma unroll
+        for (int j = 0; j < NW; ++j) {
+            if (lvl[j]) {  // only sources below S can hold a level
+                c[j] += 1;
+                ed[j] += deg;
+                dm[j] = max(dm[j], lvl[j]);
+            }
         }
     }
-    if (tid < S) ed += off[sources[tid] + 1] - off[sources[tid]];  // the source's own out-edges
-    if (n || ed) {
-        atomicAdd(cnt + c, n);
-        atomicAdd(edges + c, ed);
-        atomicMax(depth + c, mx);
+#pragma unroll
+    for (int j = 0; j < NW; ++j) {
+        if (s0 + j < S && c[j]) {
+            atomicAdd(s_cnt + s0 + j, c[j]);
+            atomicAdd(s_edges + s0 + j, ed[j]);
+            atomicMax(s_depth + s0 + j, dm[j]);
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < S; i += blockDim.x) {
+        // block 0 adds each source's own out-edges
+        const unsigned long long own = blockIdx.x == 0 ? __ldg(off + sources[i] + 1) - __ldg(off + sources[i]) : 0u;
+        if (s_cnt[i] || own) {
+            atomicAdd(cnt + i, s_cnt[i]);
+            atomicAdd(edges + i, s_edges[i] + own);
+            atomicMax(depth + i, s_depth[i]);
+        }
     }
 }
 
@@ -298,29 +387,44 @@ int msbfs_impl(gbx_graph *g, uint32_t S, const uint32_t *src_d, uint32_t *dist, 
     gbx_ms_plan *plan = nullptr;
     GBX_TRY(ms_plan(g, s, &plan));
     const size_t words = (size_t)V * NW;
-    DevBuf<uint32_t> seen, F0, F1, q0, q1, rc, rd;
+    // the level masks kept for the final pass: as many levels as fit 8 GiB
+    // (at least two), at most kMsMaxStoredLevels; deeper levels use the two
+    // `deep` buffers in turn and write their distances bit by bit
+    const uint32_t max_stored = (uint32_t)std::max<size_t>(
+        2, std::min<size_t>(kMsMaxStoredLevels, (8ull << 30) / std::max<size_t>(1, words * 4)));
+    std::vector<DevBuf<uint32_t>> lvbuf(max_stored);
+    DevBuf<uint32_t> seen, deep[2], q0, q1, rc, rd;
     DevBuf<unsigned long long> re;
     DevBuf<MsCounters> cnt;
     GBX_TRY(seen.alloc(words, s));
-    GBX_TRY(F0.alloc(words, s));
-    GBX_TRY(F1.alloc(words, s));
+    GBX_TRY(lvbuf[0].alloc(words, s));
     GBX_TRY(q0.alloc(std::max(V, S), s));
     GBX_TRY(q1.alloc(std::max(V, S), s));
     GBX_TRY(cnt.alloc(1, s));
     GBX_CUDA(cudaMemsetAsync(seen.p, 0, words * 4, s));
-    GBX_CUDA(cudaMemsetAsync(F0.p, 0, words * 4, s));
+    GBX_CUDA(cudaMemsetAsync(lvbuf[0].p, 0, words * 4, s));
     GBX_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(MsCounters), s));
-    GBX_CUDA(cudaMemsetAsync(dist, 0, (size_t)V * S * 4, s));
-    ms_seed_kernel<<<1, 256, 0, s>>>(src_d, S, NW, g->offsets, seen.p, F0.p, q0.p, cnt.p);
+    ms_seed_kernel<<<1, 256, 0, s>>>(src_d, S, NW, g->offsets, seen.p, lvbuf[0].p, q0.p, cnt.p);
     GBX_LAUNCH_CHECK();
     MsCounters h{};
     GBX_CUDA(cudaMemcpyAsync(&h, cnt.p, sizeof(h), cudaMemcpyDeviceToHost, s));
     GBX_CUDA(cudaStreamSynchronize(s));
-    uint32_t *F = F0.p, *Fn = F1.p, *q = q0.p, *qn = q1.p;
+    uint32_t *F = lvbuf[0].p, *q = q0.p, *qn = q1.p;
     const unsigned grid = (unsigned)num_sms() * 8;
     const unsigned long long E = g->E;
-    uint32_t level = 0, pushes = 0, pulls = 0;
+    uint32_t level = 0, pushes = 0, pulls = 0, stored = 1;
     while (h.qn > 0 && level <= V) {
+        const uint32_t next = level + 1;
+        const bool keep = next < max_stored;
+        uint32_t *Fn;
+        if (keep) {
+            GBX_TRY(lvbuf[next].alloc(words, s));
+            Fn = lvbuf[next].p;
+        } else {
+            DevBuf<uint32_t> &d = deep[next & 1];
+            if (!d.p) GBX_TRY(d.alloc(words, s));
+            Fn = d.p;
+        }
         GBX_CUDA(cudaMemsetAsync(Fn, 0, words * 4, s));
         if (h.mf * 16 < E) {
             ms_push_kernel<NW><<<grid, kMsThreads, 0, s>>>(g->offsets, g->dest, q, h.qn, F, seen.p, Fn);
@@ -337,26 +441,39 @@ int msbfs_impl(gbx_graph *g, uint32_t S, const uint32_t *src_d, uint32_t *dist, 
             }
             ++pulls;
         }
-        ++level;
+        level = next;
         GBX_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(MsCounters), s));
-        ms_update_kernel<NW><<<grid, kMsThreads, 0, s>>>(V, S, level, g->offsets, seen.p, Fn, dist, qn, cnt.p);
+        if (keep) {
+            ms_update_kernel<NW, false><<<grid, kMsThreads, 0, s>>>(V, S, level, g->offsets, seen.p, Fn, dist, qn,
+                                                                    cnt.p);
+            stored = next + 1;
+        } else {
+            ms_update_kernel<NW, true><<<grid, kMsThreads, 0, s>>>(V, S, level, g->offsets, seen.p, Fn, dist, qn,
+                                                                   cnt.p);
+        }
         GBX_LAUNCH_CHECK();
         GBX_CUDA(cudaMemcpyAsync(&h, cnt.p, sizeof(h), cudaMemcpyDeviceToHost, s));
         GBX_CUDA(cudaStreamSynchronize(s));
-        std::swap(F, Fn);
+        F = Fn;
         std::swap(q, qn);
     }
     GBX_REQUIRE(h.qn == 0, GBX_ERR_ITER_CAP, "multi-source BFS level cap reached");
+    // distances of the stored levels, zeros for unreached pairs, and the
+    // per-source results, in one pass
+    MsLevels lv{};
+    lv.n = stored;
+    for (uint32_t L = 0; L < stored; ++L) lv.m[L] = lvbuf[L].p;
+    GBX_TRY(rc.alloc(S, s));
+    GBX_TRY(rd.alloc(S, s));
+    GBX_TRY(re.alloc(S, s));
+    GBX_CUDA(cudaMemsetAsync(rc.p, 0, 4 * (size_t)S, s));
+    GBX_CUDA(cudaMemsetAsync(rd.p, 0, 4 * (size_t)S, s));
+    GBX_CUDA(cudaMemsetAsync(re.p, 0, 8 * (size_t)S, s));
+    const bool vec_rows = S % 4 == 0 && (reinterpret_cast<uintptr_t>(dist) & 15u) == 0;
+    ms_final_kernel<NW><<<(unsigned)num_sms() * 4, kMsThreads, 0, s>>>(lv, seen.p, V, S, g->offsets, src_d,
+                                                                       vec_rows, dist, rc.p, re.p, rd.p);
+    GBX_LAUNCH_CHECK();
     if (res_host) {
-        GBX_TRY(rc.alloc(S, s));
-        GBX_TRY(rd.alloc(S, s));
-        GBX_TRY(re.alloc(S, s));
-        GBX_CUDA(cudaMemsetAsync(rc.p, 0, 4 * (size_t)S, s));
-        GBX_CUDA(cudaMemsetAsync(rd.p, 0, 4 * (size_t)S, s));
-        GBX_CUDA(cudaMemsetAsync(re.p, 0, 8 * (size_t)S, s));
-        // S * 64 blocks of 256 threads: 256 * 64 row strides per column
-        ms_results_kernel<<<S * 4, 256, 0, s>>>(dist, V, S, g->offsets, src_d, rc.p, re.p, rd.p);
-        GBX_LAUNCH_CHECK();
         std::vector<uint32_t> hc(S), hd(S);
         std::vector<unsigned long long> he(S);
         GBX_CUDA(cudaMemcpyAsync(hc.data(), rc.p, 4 * (size_t)S, cudaMemcpyDeviceToHost, s));
@@ -373,6 +490,8 @@ int msbfs_impl(gbx_graph *g, uint32_t S, const uint32_t *src_d, uint32_t *dist, 
             r.edges_traversed = he[i];
             res_host[i] = r;
         }
+    } else {
+        GBX_CUDA(cudaStreamSynchronize(s));
     }
     return GBX_OK;
 }

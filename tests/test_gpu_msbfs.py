@@ -2,7 +2,8 @@
 from every source alone: distances, processed_nodes and iteration bit-exact,
 edges_traversed equal to the single-source GPU BFS. Covers 1, 33, 100 and
 256 sources, repeated sources, sources without out-edges, undirected graphs
-(pull over the forward CSR), hub rows cut into chunks, and bad sources."""
+(pull over the forward CSR), hub rows cut into chunks, traversals deeper than
+the 32 level masks kept for the final pass (a long chain), and bad sources."""
 import numpy as np
 import pytest
 
@@ -76,3 +77,29 @@ def test_multisource_device_output_and_checks(gbx, cuda_device):
         with pytest.raises(_lib.GbxError) as ei:
             gbx.bfs_multisource(dg, np.zeros(257, np.uint32))
         assert ei.value.status == -1
+
+
+@pytest.mark.parametrize("n", [5, 64, 256])
+def test_multisource_deeper_than_the_stored_levels(gbx, cuda_device, n):
+    """An RMAT-10 graph with a 90-vertex chain hanging off vertex 0 (and a
+    shortcut into its middle): sources near the chain's start run past the
+    32 stored level masks, so their late levels take the bit-by-bit path."""
+    V0, chain = 1 << 10, 90
+    src, dst = gbx.generate_rmat(10, V0 * 8, seed=12)
+    c = np.arange(V0, V0 + chain, dtype=np.uint32)
+    src = np.concatenate([src, [0], c[:-1], [c[10]]]).astype(np.uint32)
+    dst = np.concatenate([dst, [c[0]], c[1:], [c[60]]]).astype(np.uint32)
+    el = gbx.EdgeList(V0 + chain, src, dst)
+    g = gbx.graph_csr_preprocessing(el, sort=1, dedup=True, directed=True, keep_weights=False)
+    host, pull = host_views(g)
+    rng = np.random.default_rng(n)
+    srcs = np.concatenate([[0, V0, V0 + 5, V0 + 40], rng.choice(np.nonzero(g.out_degree)[0], n - 4)])
+    srcs = srcs[:n].astype(np.uint32)
+    with gbx.DeviceGraph.from_graph_csr(g) as dg:
+        dg.label_array = None
+        dist, res = gbx.bfs_multisource(dg, srcs)
+    assert int(dist.max()) > 40
+    for i, s0 in enumerate(srcs):
+        d_ref, _, proc, it = po.bfs(host, int(s0), pull)
+        np.testing.assert_array_equal(dist[:, i], d_ref, err_msg=f"source {i} ({s0})")
+        assert (res["processed_nodes"][i], res["iteration"][i]) == (proc, it), i
