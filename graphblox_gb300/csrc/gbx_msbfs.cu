@@ -172,10 +172,27 @@ __global__ void __launch_bounds__(kMsThreads)
     ms_update_kernel(uint32_t V, uint32_t S, uint32_t level, const uint32_t *__restrict__ off,
                      uint32_t *__restrict__ seen, uint32_t *__restrict__ Fn, uint32_t *__restrict__ dist,
                      uint32_t *__restrict__ qnext, MsCounters *cnt) {
+    // next-frontier appends are staged per warp in shared memory and reserved
+    // with one atomic per batch (one per warp step would put V/GPW atomics
+    // on the one length counter), the out-degree sum with one per warp
+    constexpr uint32_t kCap = 128;
+    __shared__ uint32_t s_q[kMsThreads / 32][kCap];
     constexpr int GPW = 32 / NW;
     const uint32_t lane = threadIdx.x & 31, k = lane % NW, gi = lane / NW;
     const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarp = (gridDim.x * blockDim.x) >> 5;
+    uint32_t *wq = s_q[threadIdx.x >> 5];
+    uint32_t wn = 0;
+    unsigned long long mf = 0;
+    auto flush = [&]() {
+        __syncwarp();
+        uint32_t pos = 0;
+        if (lane == 0) pos = atomicAdd(&cnt->qn, wn);
+        pos = __shfl_sync(0xFFFFFFFFu, pos, 0);
+        for (uint32_t i = lane; i < wn; i += 32) qnext[pos + i] = wq[i];
+        __syncwarp();
+        wn = 0;
+    };
     for (uint32_t base = warp0 * GPW; base < V; base += nwarp * GPW) {
         const uint32_t v = base + gi;
         uint32_t nw = 0;
@@ -196,17 +213,15 @@ __global__ void __launch_bounds__(kMsThreads)
         const uint32_t any = __ballot_sync(0xFFFFFFFFu, nw != 0);
         const uint32_t gm = (NW == 32 ? 0xFFFFFFFFu : ((1u << NW) - 1u)) << (gi * NW);
         const bool leader = k == 0 && (any & gm);
+        if (leader) mf += off[v + 1] - off[v];
         const uint32_t lm = __ballot_sync(0xFFFFFFFFu, leader);
-        unsigned long long deg = leader ? (unsigned long long)(off[v + 1] - off[v]) : 0ull;
-        deg = warp_sum(deg);
-        uint32_t pos = 0;
-        if (lane == 0 && lm) {
-            pos = atomicAdd(&cnt->qn, (uint32_t)__popc(lm));
-            atomicAdd(&cnt->mf, deg);
-        }
-        pos = __shfl_sync(0xFFFFFFFFu, pos, 0);
-        if (leader) qnext[pos + __popc(lm & ((1u << lane) - 1u))] = v;
+        if (leader) wq[wn + __popc(lm & ((1u << lane) - 1u))] = v;
+        wn += __popc(lm);
+        if (wn > kCap - 32) flush();
     }
+    if (wn) flush();
+    mf = warp_sum(mf);
+    if (lane == 0 && mf) atomicAdd(&cnt->mf, mf);
 }
 
 __global__ void ms_seed_kernel(const uint32_t *sources, uint32_t S, uint32_t NW, const uint32_t *off, uint32_t *seen,

@@ -18,7 +18,8 @@
 // neighbour u the prefix N(u) ∩ [0, v] is streamed with consecutive lanes on
 // consecutive elements (coalesced), one or two shared-memory probes each.
 // Summed over pairs that streams |N(u) ∩ [0, v]| elements instead of |N+(v)|
-// (3.5x fewer on RMAT-20). A v with many upper neighbours is cut into units
+// (3.5x fewer on RMAT-20). The prefix length |N(u) ∩ [0, v]| of every pair
+// is computed once per graph into the plan (pre_len, one word per edge). A v with many upper neighbours is cut into units
 // of kUpperChunk of them, dealt to warps by an atomic cursor, so hubs are
 // spread over the GPU; the rest are one warp per v. A v whose N+(v) is
 // longer than the per-warp table (up to 16384 ids) goes to tc_wide_kernel:
@@ -183,6 +184,40 @@ __global__ void tc_shape_check_kernel(const uint32_t *off, const uint32_t *dest,
     }
 }
 
+// Prefix lengths of the fast path, kept in the plan: for every edge v->u
+// with u >= v, pre_len = |N(u) ∩ [0, v]| (v's position in the sorted row of
+// u, plus one, on a symmetric deduplicated CSR). The count kernels read it
+// next to u instead of searching u's row for v on every count. Edges in
+// fixed chunks per warp, each lane walking the rows of its edges.
+__global__ void tc_prefix_len_kernel(const uint32_t *__restrict__ off, const uint32_t *__restrict__ dest, uint32_t V,
+                                     uint32_t E, uint32_t *__restrict__ pre_len) {
+    constexpr uint32_t kChunk = 2048;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint64_t c0 = (uint64_t)gw * kChunk; c0 < E; c0 += (uint64_t)nw * kChunk) {
+        const uint32_t c1 = c0 + kChunk < (uint64_t)E ? (uint32_t)(c0 + kChunk) : E;
+        uint32_t j = (uint32_t)c0 + lane;
+        if (j >= c1) continue;
+        uint32_t lo = 0, hi = V - 1;  // last row r with off[r] <= j
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (__ldg(off + mid) <= j) lo = mid; else hi = mid - 1;
+        }
+        uint32_t r = lo;
+        for (; j < c1; j += 32) {
+            while (__ldg(off + r + 1) <= j) ++r;
+            const uint32_t u = __ldg(dest + j);
+            uint32_t n = 0;
+            if (u >= r) {
+                const uint32_t b = __ldg(off + u);
+                n = count_le_front(dest + b, __ldg(off + u + 1) - b, r);
+            }
+            pre_len[j] = n;
+        }
+    }
+}
+
 // Count the elements of the lanes' lists (base_k, len_k), flattened over the
 // warp, that `member` accepts. Every lane calls with its own list (len 0 when
 // it has none).
@@ -324,22 +359,22 @@ struct BitmapMember {
 };
 
 // For the upper neighbours u in [ub, ue) of v's row nv, 32 at a time: the
-// prefix N(u) ∩ [0, v] of each (one binary search per u), counted against m.
+// prefix N(u) ∩ [0, v] of each (its length pl[] from the plan, read next to
+// u), counted against m.
 template <class Member>
 __device__ __forceinline__ unsigned long long stream_pairs(const uint32_t *__restrict__ off,
                                                           const uint32_t *__restrict__ dest, const uint32_t *nv,
-                                                          uint32_t v, uint32_t ub, uint32_t ue, uint32_t *s_pre,
-                                                          uint32_t *s_base, uint32_t *s_end, const Member &m,
-                                                          uint32_t step = 32, bool front = false) {
+                                                          const uint32_t *pl, uint32_t ub, uint32_t ue,
+                                                          uint32_t *s_pre, uint32_t *s_base, uint32_t *s_end,
+                                                          const Member &m) {
     const uint32_t lane = threadIdx.x & 31;
     unsigned long long count = 0;
-    for (uint32_t a0 = ub; a0 < ue; a0 += step) {
+    for (uint32_t a0 = ub; a0 < ue; a0 += 32) {
         uint32_t base = 0, len = 0;
         if (a0 + lane < ue) {
             const uint32_t u = __ldg(nv + a0 + lane);
+            len = __ldg(pl + a0 + lane);
             base = __ldg(off + u);
-            const uint32_t du = __ldg(off + u + 1) - base;
-            len = front ? count_le_front(dest + base, du, v) : count_le(dest + base, du, v);
         }
         count += count_flat4(dest, base, len, s_pre, s_base, s_end, m);
     }
@@ -353,7 +388,7 @@ __device__ __forceinline__ unsigned long long stream_pairs(const uint32_t *__res
 template <class Member>
 __device__ __forceinline__ unsigned long long stream_pairs_dealt(const uint32_t *__restrict__ off,
                                                                 const uint32_t *__restrict__ dest,
-                                                                const uint32_t *nv, uint32_t v, uint32_t ub,
+                                                                const uint32_t *nv, const uint32_t *pl, uint32_t ub,
                                                                 uint32_t ue, uint32_t *s_pre, uint32_t *s_base,
                                                                 uint32_t *s_end, const Member &m,
                                                                 unsigned *s_next) {
@@ -367,8 +402,8 @@ __device__ __forceinline__ unsigned long long stream_pairs_dealt(const uint32_t 
         uint32_t base = 0, len = 0;
         if (a0 + lane < ue) {
             const uint32_t u = __ldg(nv + a0 + lane);
+            len = __ldg(pl + a0 + lane);
             base = __ldg(off + u);
-            len = count_le_front(dest + base, __ldg(off + u + 1) - base, v);
         }
         count += count_flat4(dest, base, len, s_pre, s_base, s_end, m);
     }
@@ -386,11 +421,13 @@ struct SortedMember {
 // One v, upper neighbours [ub, ue) of its row: build the membership test of
 // N+(v) (warp table, or the sorted list when it is too long) and count.
 __device__ __forceinline__ unsigned long long v_unit(const uint32_t *__restrict__ off,
-                                                    const uint32_t *__restrict__ dest, uint32_t v, uint32_t pv,
+                                                    const uint32_t *__restrict__ dest,
+                                                    const uint32_t *__restrict__ pre_len, uint32_t v, uint32_t pv,
                                                     uint32_t ub, uint32_t ue, uint32_t *table, uint32_t *htable,
                                                     uint32_t *s_pre, uint32_t *s_base, uint32_t *s_end) {
     const uint32_t lane = threadIdx.x & 31;
-    const uint32_t *nv = dest + __ldg(off + v);
+    const uint32_t row = __ldg(off + v);
+    const uint32_t *nv = dest + row, *pl = pre_len + row;
     unsigned long long count = 0;
     if (v < kTcWarpSlots * 32) {
         // exact bitmap of N+(v) over [0, v]: the warp's words are all zero
@@ -400,7 +437,7 @@ __device__ __forceinline__ unsigned long long v_unit(const uint32_t *__restrict_
             atomicOr(table + (w >> 5), 1u << (w & 31));
         }
         __syncwarp();
-        count = stream_pairs(off, dest, nv, v, ub, ue, s_pre, s_base, s_end,
+        count = stream_pairs(off, dest, nv, pl, ub, ue, s_pre, s_base, s_end,
                              BitmapMember{table, kTcWarpSlots * 32 - 1});
         __syncwarp();
         for (uint32_t i = lane; i < pv; i += 32) table[__ldg(nv + i) >> 5] = 0u;
@@ -420,7 +457,7 @@ __device__ __forceinline__ unsigned long long v_unit(const uint32_t *__restrict_
                 else hash_insert(htable, hmask, w);
             }
             __syncwarp();
-            count = stream_pairs(off, dest, nv, v, ub, ue, s_pre, s_base, s_end,
+            count = stream_pairs(off, dest, nv, pl, ub, ue, s_pre, s_base, s_end,
                                  HybridMember{table, htable, hmask});
             __syncwarp();
             for (uint32_t i = lane; i < pv; i += 32) {
@@ -435,12 +472,12 @@ __device__ __forceinline__ unsigned long long v_unit(const uint32_t *__restrict_
         __syncwarp();
         for (uint32_t i = lane; i < pv; i += 32) hash_insert(table, mask, __ldg(nv + i));
         __syncwarp();
-        count = stream_pairs(off, dest, nv, v, ub, ue, s_pre, s_base, s_end, HashMember{table, mask});
+        count = stream_pairs(off, dest, nv, pl, ub, ue, s_pre, s_base, s_end, HashMember{table, mask});
         __syncwarp();
         for (uint32_t i = lane; i <= mask; i += 32) table[i] = 0u;
         __syncwarp();
     } else {
-        count = stream_pairs(off, dest, nv, v, ub, ue, s_pre, s_base, s_end, SortedMember{nv, pv});
+        count = stream_pairs(off, dest, nv, pl, ub, ue, s_pre, s_base, s_end, SortedMember{nv, pv});
     }
     return count;
 }
@@ -561,7 +598,8 @@ __global__ void __launch_bounds__(kTcThreads)
 
 __global__ void __launch_bounds__(kTcThreads, 4)
     tc_vcentric_kernel(const uint32_t *__restrict__ off, const uint32_t *__restrict__ dest,
-                       const uint32_t *__restrict__ low, const TcBig *__restrict__ big, uint32_t n_big,
+                       const uint32_t *__restrict__ low, const uint32_t *__restrict__ pre_len,
+                       const TcBig *__restrict__ big, uint32_t n_big,
                        uint32_t n_units, const TcBig *__restrict__ small, uint32_t n_small, unsigned *cursor,
                        unsigned long long *total) {
     __shared__ uint32_t tables[kTcWarps][kTcWarpSlots];
@@ -588,7 +626,7 @@ __global__ void __launch_bounds__(kTcThreads, 4)
         const TcBig bg = big[lo];
         const uint32_t ub = bg.ub + (unit - bg.first_unit) * kUpperChunk;
         const uint32_t ue = min(ub + kUpperChunk, bg.ue);
-        count += v_unit(off, dest, bg.v, __ldg(low + bg.v), ub, ue, tables[wid], htables[wid], s_pre[wid],
+        count += v_unit(off, dest, pre_len, bg.v, __ldg(low + bg.v), ub, ue, tables[wid], htables[wid], s_pre[wid],
                         s_base[wid], s_end[wid]);
     }
     // the other pivots with work (the plan's compact list, with the first
@@ -597,7 +635,7 @@ __global__ void __launch_bounds__(kTcThreads, 4)
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t i = gw; i < n_small; i += nw) {
         const TcBig sm = small[i];
-        count += v_unit(off, dest, sm.v, __ldg(low + sm.v), sm.ub, sm.ue, tables[wid], htables[wid], s_pre[wid],
+        count += v_unit(off, dest, pre_len, sm.v, __ldg(low + sm.v), sm.ub, sm.ue, tables[wid], htables[wid], s_pre[wid],
                         s_base[wid], s_end[wid]);
     }
     count = block_sum(count, sred);
@@ -647,7 +685,8 @@ static_assert((kWideSlotsMax & (kWideSlotsMax - 1)) == 0 && (kTcWarpSlots & (kTc
 
 __global__ void __launch_bounds__(kWideThreads, 1)
     tc_wide_kernel(const uint32_t *__restrict__ off, const uint32_t *__restrict__ dest,
-                   const uint32_t *__restrict__ low, const TcBig *__restrict__ wide, uint32_t n_wide,
+                   const uint32_t *__restrict__ low, const uint32_t *__restrict__ pre_len,
+                   const TcBig *__restrict__ wide, uint32_t n_wide,
                    uint32_t n_units, uint32_t slots, unsigned *cursor, unsigned long long *total) {
     extern __shared__ uint32_t s_table[];
     __shared__ uint32_t s_pre[kWideThreads / 32][33];
@@ -674,7 +713,8 @@ __global__ void __launch_bounds__(kWideThreads, 1)
         const uint32_t v = bg.v, pv = __ldg(low + v);
         const uint32_t ub = bg.ub + (unit - bg.first_unit) * kWideChunk;
         const uint32_t ue = min(ub + kWideChunk, bg.ue);
-        const uint32_t *nv = dest + __ldg(off + v);
+        const uint32_t row = __ldg(off + v);
+        const uint32_t *nv = dest + row, *pl = pre_len + row;
         if (threadIdx.x == 0) s_next = 0;
         if (v < slots * 32) {
             // exact bitmap of N+(v) over [0, v]
@@ -683,7 +723,7 @@ __global__ void __launch_bounds__(kWideThreads, 1)
                 atomicOr(s_table + (w >> 5), 1u << (w & 31));
             }
             __syncthreads();
-            count += stream_pairs_dealt(off, dest, nv, v, ub, ue, s_pre[wid], s_base[wid], s_end[wid],
+            count += stream_pairs_dealt(off, dest, nv, pl, ub, ue, s_pre[wid], s_base[wid], s_end[wid],
                                         BitmapMember{s_table, slots * 32 - 1}, &s_next);
             __syncthreads();
             for (uint32_t i = threadIdx.x; i < pv; i += blockDim.x) s_table[__ldg(nv + i) >> 5] = 0u;
@@ -694,7 +734,7 @@ __global__ void __launch_bounds__(kWideThreads, 1)
             __syncthreads();
             for (uint32_t i = threadIdx.x; i < pv; i += blockDim.x) hash_insert(s_table, mask, __ldg(nv + i));
             __syncthreads();
-            count += stream_pairs_dealt(off, dest, nv, v, ub, ue, s_pre[wid], s_base[wid], s_end[wid],
+            count += stream_pairs_dealt(off, dest, nv, pl, ub, ue, s_pre[wid], s_base[wid], s_end[wid],
                                         HashMember{s_table, mask}, &s_next);
             __syncthreads();
             for (uint32_t i = threadIdx.x; i <= mask; i += blockDim.x) s_table[i] = 0u;
@@ -755,6 +795,7 @@ struct gbx_tc_plan {
     gbx::TcBig *small = nullptr; // the other v's with pairs, one warp each
     gbx::TcBig *hub = nullptr;   // v's below the hub range (bitmap rows)
     uint32_t *hub_bits = nullptr;  // V rows of hub_words words: N(x) ∩ [0, 32 hub_words)
+    uint32_t *pre_len = nullptr;   // per edge v->u with u >= v: |N(u) ∩ [0, v]|
     uint32_t hub_words = 0;
     uint32_t n_big = 0, n_units = 0;
     uint32_t n_wide = 0, n_wunits = 0;
@@ -835,6 +876,13 @@ static int tc_prepare(gbx_graph *g, cudaStream_t s) {
             tc_plan_scatter_kernel<<<grid, 256, 0, s>>>(g->offsets, flag.p, pos.p, unit_pre.p, ub.p, V, p->big,
                                                         p->wide, p->small, p->hub);
             GBX_LAUNCH_CHECK();
+            GBX_CUDA(cudaMalloc(&p->pre_len, (size_t)(g->E ? g->E : 1) * 4));
+            if (g->E) {
+                const unsigned egrid =
+                    std::min<unsigned>(ceil_div(ceil_div((uint64_t)g->E, 2048) * 32, 256), (unsigned)num_sms() * 8);
+                tc_prefix_len_kernel<<<egrid, 256, 0, s>>>(g->offsets, g->dest, V, g->E, p->pre_len);
+                GBX_LAUNCH_CHECK();
+            }
             if (p->n_hub) {
                 const size_t bytes = (size_t)V * hw * 4;
                 GBX_CUDA(cudaMalloc(&p->hub_bits, bytes));
@@ -863,6 +911,7 @@ void gbx_free_tc_plan(gbx_tc_plan *p) {
     cudaFree(p->small);
     cudaFree(p->hub);
     cudaFree(p->hub_bits);
+    cudaFree(p->pre_len);
     delete p;
 }
 
@@ -884,9 +933,9 @@ extern "C" int gbx_tc(gbx_graph *g, uint64_t *total, void *stream) {
         GBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc_vcentric_kernel, kTcThreads, 0));
         const unsigned grid = (unsigned)std::max(1, per_sm) * (unsigned)num_sms();
         const gbx_tc_plan *p = g->tc_plan;
-        tc_vcentric_kernel<<<grid, kTcThreads, 0, s>>>(g->offsets, g->dest, g->low_count, p->big, p->n_big,
-                                                       p->n_big ? p->n_units : 0u, p->small, p->n_small, cursor.p,
-                                                       d.p);
+        tc_vcentric_kernel<<<grid, kTcThreads, 0, s>>>(g->offsets, g->dest, g->low_count, p->pre_len, p->big,
+                                                       p->n_big, p->n_big ? p->n_units : 0u, p->small, p->n_small,
+                                                       cursor.p, d.p);
         GBX_LAUNCH_CHECK();
         if (p->n_wide) {
             const size_t smem = (size_t)kWideSlotsMax * 4;
@@ -894,8 +943,9 @@ extern "C" int gbx_tc(gbx_graph *g, uint64_t *total, void *stream) {
             int wper = 0;
             GBX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&wper, tc_wide_kernel, kWideThreads, smem));
             const unsigned wgrid = std::min<unsigned>((unsigned)std::max(1, wper) * (unsigned)num_sms(), p->n_wunits);
-            tc_wide_kernel<<<wgrid, kWideThreads, smem, s>>>(g->offsets, g->dest, g->low_count, p->wide, p->n_wide,
-                                                              p->n_wunits, kWideSlotsMax, cursor.p + 1, d.p);
+            tc_wide_kernel<<<wgrid, kWideThreads, smem, s>>>(g->offsets, g->dest, g->low_count, p->pre_len,
+                                                              p->wide, p->n_wide, p->n_wunits, kWideSlotsMax,
+                                                              cursor.p + 1, d.p);
         }
         if (p->n_hub) {
             GBX_LAUNCH_CHECK();
