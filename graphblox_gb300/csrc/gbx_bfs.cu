@@ -805,7 +805,9 @@ int bfs_graph_setup(gbx_graph *g, cudaStream_t s) {
     }
     if (!g->bu_live) {
         // kept with the graph: which vertices a bottom-up step can find
-        GBX_CUDA(cudaMalloc(&g->bu_live, (size_t)words * 4));
+        void *live = nullptr;
+        GBX_TRY(dev_alloc(&live, (size_t)words * 4, s));
+        g->bu_live = static_cast<uint32_t *>(live);
         live_bits_kernel<<<std::min<unsigned>(ceil_div(words * 32, 256), (unsigned)num_sms() * 8), 256, 0, s>>>(
             g->pull_offsets(), V, words, g->bu_live);
         GBX_LAUNCH_CHECK();

@@ -191,15 +191,32 @@ static int copy_in(void *dst, const void *src, size_t bytes, cudaStream_t s) {
     return GBX_OK;
 }
 
-static int dmalloc(void **p, size_t bytes) {
+int dev_alloc(void **p, size_t bytes, cudaStream_t s) {
     *p = nullptr;
-    cudaError_t e = cudaMalloc(p, bytes ? bytes : 4);
+    cudaError_t e = cudaMallocAsync(p, bytes ? bytes : 4, s);
+    if (e == cudaErrorMemoryAllocation) {
+        // memory the pool keeps from freed graphs goes back to the driver
+        // first, then the allocation is tried once more
+        (void)cudaGetLastError();
+        int dev = 0;
+        cudaMemPool_t pool;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            cudaDeviceSynchronize();
+            cudaMemPoolTrimTo(pool, 0);
+        }
+        e = cudaMallocAsync(p, bytes ? bytes : 4, s);
+    }
     if (e != cudaSuccess) {
         (void)cudaGetLastError();
+        *p = nullptr;
         set_error("device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
         return GBX_ERR_NOMEM;
     }
     return GBX_OK;
+}
+
+void dev_free(void *p) {
+    if (p) cudaFreeAsync(p, 0);
 }
 
 // Fill one direction of the graph (forward or inverse) from either layout.
@@ -207,12 +224,12 @@ static int fill_direction(uint32_t V, uint32_t E, const uint32_t *edges_idx, con
                           const uint32_t *offsets, const uint32_t *ids, const float *w,
                           uint32_t **d_off, uint32_t **d_ids, float **d_w, uint32_t **d_deg,
                           uint32_t *max_deg, cudaStream_t s) {
-    GBX_TRY(dmalloc((void **)d_off, (size_t)(V + 1) * 4));
-    GBX_TRY(dmalloc((void **)d_deg, (size_t)V * 4));
+    GBX_TRY(dev_alloc((void **)d_off, (size_t)(V + 1) * 4, s));
+    GBX_TRY(dev_alloc((void **)d_deg, (size_t)V * 4, s));
     // four ids of zeroed padding: kernels read rows as aligned 16-byte quads
-    GBX_TRY(dmalloc((void **)d_ids, ((size_t)E + 4) * 4));
+    GBX_TRY(dev_alloc((void **)d_ids, ((size_t)E + 4) * 4, s));
     GBX_CUDA(cudaMemsetAsync(*d_ids + E, 0, 16, s));
-    if (w) GBX_TRY(dmalloc((void **)d_w, (size_t)E * 4));
+    if (w) GBX_TRY(dev_alloc((void **)d_w, (size_t)E * 4, s));
     DevBuf<unsigned> bad;
     GBX_TRY(bad.alloc(3, s));
     GBX_CUDA(cudaMemsetAsync(bad.p, 0, 12, s));
@@ -371,22 +388,22 @@ int gbx_graph_destroy(gbx_graph *g) {
     cudaGetDevice(&prev);
     cudaSetDevice(g->device);
     cudaDeviceSynchronize();
-    cudaFree(g->offsets);
-    cudaFree(g->dest);
-    cudaFree(g->weight);
-    cudaFree(g->out_degree);
-    cudaFree(g->in_offsets);
-    cudaFree(g->in_src);
-    cudaFree(g->in_weight);
-    cudaFree(g->in_degree);
-    cudaFree(g->low_count);
-    cudaFree(g->bu_live);
+    dev_free(g->offsets);
+    dev_free(g->dest);
+    dev_free(g->weight);
+    dev_free(g->out_degree);
+    dev_free(g->in_offsets);
+    dev_free(g->in_src);
+    dev_free(g->in_weight);
+    dev_free(g->in_degree);
+    dev_free(g->low_count);
+    dev_free(g->bu_live);
     gbx_free_tc_plan(g->tc_plan);
     gbx_free_ppr_cache(g->ppr);
     gbx_free_ms_plan(g->ms_plan);
     gbx_free_pr_cache(g->pr_cache);
     gbx_free_bc_cache(g->bc_cache);
-    cudaFree(g->arena);
+    dev_free(g->arena);
     free_plan(g->plan_fwd);
     free_plan(g->plan_inv);
     cudaSetDevice(prev);

@@ -260,6 +260,15 @@ void gbx_free_pr_cache(struct gbx_pr_cache *c);
 void gbx_free_bc_cache(struct gbx_bc_cache *c);
 
 namespace gbx {
+// Long-lived device arrays (a graph's arrays, scratch arena and plans) come
+// from the device's stream-ordered pool, which keeps the memory of a freed
+// graph for the next one instead of handing it back to the driver (a
+// cudaMalloc/cudaFree of gigabytes costs milliseconds). dev_alloc orders the
+// allocation on stream s; dev_free is for memory no stream uses any more
+// (its callers synchronized first) and accepts nullptr.
+int dev_alloc(void **p, size_t bytes, cudaStream_t s);
+void dev_free(void *p);
+
 // Device scratch for one synchronous call: carved from the graph's arena
 // (grown on demand, kept between calls), or from a single stream-ordered
 // allocation when another call holds the arena. The holder's stream is
@@ -280,15 +289,16 @@ struct Scratch {
         if (__atomic_exchange_n(&g->arena_busy, 1, __ATOMIC_ACQ_REL) == 0) {
             held = g;
             if (g->arena_bytes < bytes) {
-                cudaFree(g->arena);  // idle: every holder synchronized before release
+                dev_free(g->arena);  // idle: every holder synchronized before release
                 g->arena = nullptr;
                 g->arena_bytes = 0;
-                if (cudaMalloc(&g->arena, bytes) != cudaSuccess) {
-                    (void)cudaGetLastError();
-                    g->arena = nullptr;
-                    set_error("device allocation of %zu bytes of scratch failed", bytes);
+                void *p = nullptr;
+                if (dev_alloc(&p, bytes, s) != GBX_OK) {
+                    __atomic_store_n(&g->arena_busy, 0, __ATOMIC_RELEASE);
+                    held = nullptr;
                     return GBX_ERR_NOMEM;
                 }
+                g->arena = static_cast<char *>(p);
                 g->arena_bytes = bytes;
             }
             base = g->arena;

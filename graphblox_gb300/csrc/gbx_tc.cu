@@ -19,9 +19,11 @@
 // consecutive elements (coalesced), one or two shared-memory probes each.
 // Summed over pairs that streams |N(u) ∩ [0, v]| elements instead of |N+(v)|
 // (3.5x fewer on RMAT-20). The prefix length |N(u) ∩ [0, v]| of every pair
-// is computed once per graph into the plan (pre_len, one word per edge). A v with many upper neighbours is cut into units
-// of kUpperChunk of them, dealt to warps by an atomic cursor, so hubs are
-// spread over the GPU; the rest are one warp per v. A v whose N+(v) is
+// is found by a search of u's row in the first count of a graph, and from
+// the second count on read from the plan (pre_len, one word per edge). A v
+// with many upper neighbours is cut into units of kUpperChunk of them, dealt
+// to warps by an atomic cursor, so hubs are spread over the GPU; the rest
+// are one warp per v. A v whose N+(v) is
 // longer than the per-warp table (up to 16384 ids) goes to tc_wide_kernel:
 // one CTA per unit of its upper neighbours, N+(v) in a CTA-wide table, so no
 // element is searched in global memory. The prefixes are read as aligned
@@ -360,11 +362,12 @@ struct BitmapMember {
 
 // For the upper neighbours u in [ub, ue) of v's row nv, 32 at a time: the
 // prefix N(u) ∩ [0, v] of each (its length pl[] from the plan, read next to
-// u), counted against m.
+// u, or a binary search of u's row before the plan has them), counted
+// against m.
 template <class Member>
 __device__ __forceinline__ unsigned long long stream_pairs(const uint32_t *__restrict__ off,
                                                           const uint32_t *__restrict__ dest, const uint32_t *nv,
-                                                          const uint32_t *pl, uint32_t ub, uint32_t ue,
+                                                          const uint32_t *pl, uint32_t v, uint32_t ub, uint32_t ue,
                                                           uint32_t *s_pre, uint32_t *s_base, uint32_t *s_end,
                                                           const Member &m) {
     const uint32_t lane = threadIdx.x & 31;
@@ -373,8 +376,8 @@ __device__ __forceinline__ unsigned long long stream_pairs(const uint32_t *__res
         uint32_t base = 0, len = 0;
         if (a0 + lane < ue) {
             const uint32_t u = __ldg(nv + a0 + lane);
-            len = __ldg(pl + a0 + lane);
             base = __ldg(off + u);
+            len = pl ? __ldg(pl + a0 + lane) : count_le(dest + base, __ldg(off + u + 1) - base, v);
         }
         count += count_flat4(dest, base, len, s_pre, s_base, s_end, m);
     }
@@ -388,8 +391,9 @@ __device__ __forceinline__ unsigned long long stream_pairs(const uint32_t *__res
 template <class Member>
 __device__ __forceinline__ unsigned long long stream_pairs_dealt(const uint32_t *__restrict__ off,
                                                                 const uint32_t *__restrict__ dest,
-                                                                const uint32_t *nv, const uint32_t *pl, uint32_t ub,
-                                                                uint32_t ue, uint32_t *s_pre, uint32_t *s_base,
+                                                                const uint32_t *nv, const uint32_t *pl, uint32_t v,
+                                                                uint32_t ub, uint32_t ue, uint32_t *s_pre,
+                                                                uint32_t *s_base,
                                                                 uint32_t *s_end, const Member &m,
                                                                 unsigned *s_next) {
     const uint32_t lane = threadIdx.x & 31;
@@ -402,8 +406,8 @@ __device__ __forceinline__ unsigned long long stream_pairs_dealt(const uint32_t 
         uint32_t base = 0, len = 0;
         if (a0 + lane < ue) {
             const uint32_t u = __ldg(nv + a0 + lane);
-            len = __ldg(pl + a0 + lane);
             base = __ldg(off + u);
+            len = pl ? __ldg(pl + a0 + lane) : count_le_front(dest + base, __ldg(off + u + 1) - base, v);
         }
         count += count_flat4(dest, base, len, s_pre, s_base, s_end, m);
     }
@@ -427,7 +431,7 @@ __device__ __forceinline__ unsigned long long v_unit(const uint32_t *__restrict_
                                                     uint32_t *s_pre, uint32_t *s_base, uint32_t *s_end) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t row = __ldg(off + v);
-    const uint32_t *nv = dest + row, *pl = pre_len + row;
+    const uint32_t *nv = dest + row, *pl = pre_len ? pre_len + row : nullptr;
     unsigned long long count = 0;
     if (v < kTcWarpSlots * 32) {
         // exact bitmap of N+(v) over [0, v]: the warp's words are all zero
@@ -437,7 +441,7 @@ __device__ __forceinline__ unsigned long long v_unit(const uint32_t *__restrict_
             atomicOr(table + (w >> 5), 1u << (w & 31));
         }
         __syncwarp();
-        count = stream_pairs(off, dest, nv, pl, ub, ue, s_pre, s_base, s_end,
+        count = stream_pairs(off, dest, nv, pl, v, ub, ue, s_pre, s_base, s_end,
                              BitmapMember{table, kTcWarpSlots * 32 - 1});
         __syncwarp();
         for (uint32_t i = lane; i < pv; i += 32) table[__ldg(nv + i) >> 5] = 0u;
@@ -457,7 +461,7 @@ __device__ __forceinline__ unsigned long long v_unit(const uint32_t *__restrict_
                 else hash_insert(htable, hmask, w);
             }
             __syncwarp();
-            count = stream_pairs(off, dest, nv, pl, ub, ue, s_pre, s_base, s_end,
+            count = stream_pairs(off, dest, nv, pl, v, ub, ue, s_pre, s_base, s_end,
                                  HybridMember{table, htable, hmask});
             __syncwarp();
             for (uint32_t i = lane; i < pv; i += 32) {
@@ -472,12 +476,12 @@ __device__ __forceinline__ unsigned long long v_unit(const uint32_t *__restrict_
         __syncwarp();
         for (uint32_t i = lane; i < pv; i += 32) hash_insert(table, mask, __ldg(nv + i));
         __syncwarp();
-        count = stream_pairs(off, dest, nv, pl, ub, ue, s_pre, s_base, s_end, HashMember{table, mask});
+        count = stream_pairs(off, dest, nv, pl, v, ub, ue, s_pre, s_base, s_end, HashMember{table, mask});
         __syncwarp();
         for (uint32_t i = lane; i <= mask; i += 32) table[i] = 0u;
         __syncwarp();
     } else {
-        count = stream_pairs(off, dest, nv, pl, ub, ue, s_pre, s_base, s_end, SortedMember{nv, pv});
+        count = stream_pairs(off, dest, nv, pl, v, ub, ue, s_pre, s_base, s_end, SortedMember{nv, pv});
     }
     return count;
 }
@@ -626,8 +630,8 @@ __global__ void __launch_bounds__(kTcThreads, 4)
         const TcBig bg = big[lo];
         const uint32_t ub = bg.ub + (unit - bg.first_unit) * kUpperChunk;
         const uint32_t ue = min(ub + kUpperChunk, bg.ue);
-        count += v_unit(off, dest, pre_len, bg.v, __ldg(low + bg.v), ub, ue, tables[wid], htables[wid], s_pre[wid],
-                        s_base[wid], s_end[wid]);
+        count += v_unit(off, dest, pre_len, bg.v, __ldg(low + bg.v), ub, ue, tables[wid], htables[wid],
+                        s_pre[wid], s_base[wid], s_end[wid]);
     }
     // the other pivots with work (the plan's compact list, with the first
     // upper neighbour precomputed): one warp each
@@ -635,8 +639,8 @@ __global__ void __launch_bounds__(kTcThreads, 4)
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t i = gw; i < n_small; i += nw) {
         const TcBig sm = small[i];
-        count += v_unit(off, dest, pre_len, sm.v, __ldg(low + sm.v), sm.ub, sm.ue, tables[wid], htables[wid], s_pre[wid],
-                        s_base[wid], s_end[wid]);
+        count += v_unit(off, dest, pre_len, sm.v, __ldg(low + sm.v), sm.ub, sm.ue, tables[wid], htables[wid],
+                        s_pre[wid], s_base[wid], s_end[wid]);
     }
     count = block_sum(count, sred);
     if (threadIdx.x == 0 && count) atomicAdd(total, count);
@@ -714,7 +718,7 @@ __global__ void __launch_bounds__(kWideThreads, 1)
         const uint32_t ub = bg.ub + (unit - bg.first_unit) * kWideChunk;
         const uint32_t ue = min(ub + kWideChunk, bg.ue);
         const uint32_t row = __ldg(off + v);
-        const uint32_t *nv = dest + row, *pl = pre_len + row;
+        const uint32_t *nv = dest + row, *pl = pre_len ? pre_len + row : nullptr;
         if (threadIdx.x == 0) s_next = 0;
         if (v < slots * 32) {
             // exact bitmap of N+(v) over [0, v]
@@ -723,7 +727,7 @@ __global__ void __launch_bounds__(kWideThreads, 1)
                 atomicOr(s_table + (w >> 5), 1u << (w & 31));
             }
             __syncthreads();
-            count += stream_pairs_dealt(off, dest, nv, pl, ub, ue, s_pre[wid], s_base[wid], s_end[wid],
+            count += stream_pairs_dealt(off, dest, nv, pl, v, ub, ue, s_pre[wid], s_base[wid], s_end[wid],
                                         BitmapMember{s_table, slots * 32 - 1}, &s_next);
             __syncthreads();
             for (uint32_t i = threadIdx.x; i < pv; i += blockDim.x) s_table[__ldg(nv + i) >> 5] = 0u;
@@ -734,7 +738,7 @@ __global__ void __launch_bounds__(kWideThreads, 1)
             __syncthreads();
             for (uint32_t i = threadIdx.x; i < pv; i += blockDim.x) hash_insert(s_table, mask, __ldg(nv + i));
             __syncthreads();
-            count += stream_pairs_dealt(off, dest, nv, pl, ub, ue, s_pre[wid], s_base[wid], s_end[wid],
+            count += stream_pairs_dealt(off, dest, nv, pl, v, ub, ue, s_pre[wid], s_base[wid], s_end[wid],
                                         HashMember{s_table, mask}, &s_next);
             __syncthreads();
             for (uint32_t i = threadIdx.x; i <= mask; i += blockDim.x) s_table[i] = 0u;
@@ -810,12 +814,14 @@ static int tc_prepare(gbx_graph *g, cudaStream_t s) {
     const unsigned grid = std::min<unsigned>(ceil_div(V, 256), (unsigned)num_sms() * 8);
     const unsigned wgrid = std::min<unsigned>(ceil_div((uint64_t)V * 32, kTcThreads), (unsigned)num_sms() * 8);
     if (!g->low_count) {
-        uint32_t *low = nullptr;
-        GBX_CUDA(cudaMalloc(&low, (size_t)V * 4));
+        void *lp = nullptr;
+        GBX_TRY(dev_alloc(&lp, (size_t)V * 4, s));
+        uint32_t *low = static_cast<uint32_t *>(lp);
         tc_low_count_kernel<<<grid, 256, 0, s>>>(g->offsets, g->dest, V, low);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) {
-            cudaFree(low);
+            cudaStreamSynchronize(s);
+            dev_free(low);
             return cuda_fail(e, "tc_low_count_kernel", __FILE__, __LINE__);
         }
         note_launch();
@@ -869,23 +875,16 @@ static int tc_prepare(gbx_graph *g, cudaStream_t s) {
             p->n_units = h[4];
             p->n_wunits = h[5];
             p->n_hunits = h[6];
-            GBX_CUDA(cudaMalloc(&p->big, sizeof(TcBig) * (h[0] ? h[0] : 1)));
-            GBX_CUDA(cudaMalloc(&p->wide, sizeof(TcBig) * (h[1] ? h[1] : 1)));
-            GBX_CUDA(cudaMalloc(&p->small, sizeof(TcBig) * (h[2] ? h[2] : 1)));
-            GBX_CUDA(cudaMalloc(&p->hub, sizeof(TcBig) * (h[3] ? h[3] : 1)));
+            GBX_TRY(dev_alloc((void **)&p->big, sizeof(TcBig) * (h[0] ? h[0] : 1), s));
+            GBX_TRY(dev_alloc((void **)&p->wide, sizeof(TcBig) * (h[1] ? h[1] : 1), s));
+            GBX_TRY(dev_alloc((void **)&p->small, sizeof(TcBig) * (h[2] ? h[2] : 1), s));
+            GBX_TRY(dev_alloc((void **)&p->hub, sizeof(TcBig) * (h[3] ? h[3] : 1), s));
             tc_plan_scatter_kernel<<<grid, 256, 0, s>>>(g->offsets, flag.p, pos.p, unit_pre.p, ub.p, V, p->big,
                                                         p->wide, p->small, p->hub);
             GBX_LAUNCH_CHECK();
-            GBX_CUDA(cudaMalloc(&p->pre_len, (size_t)(g->E ? g->E : 1) * 4));
-            if (g->E) {
-                const unsigned egrid =
-                    std::min<unsigned>(ceil_div(ceil_div((uint64_t)g->E, 2048) * 32, 256), (unsigned)num_sms() * 8);
-                tc_prefix_len_kernel<<<egrid, 256, 0, s>>>(g->offsets, g->dest, V, g->E, p->pre_len);
-                GBX_LAUNCH_CHECK();
-            }
             if (p->n_hub) {
                 const size_t bytes = (size_t)V * hw * 4;
-                GBX_CUDA(cudaMalloc(&p->hub_bits, bytes));
+                GBX_TRY(dev_alloc((void **)&p->hub_bits, bytes, s));
                 GBX_CUDA(cudaMemsetAsync(p->hub_bits, 0, bytes, s));
                 tc_hub_bits_kernel<<<wgrid, 256, 0, s>>>(g->offsets, g->dest, V, hw, p->hub_bits);
                 GBX_LAUNCH_CHECK();
@@ -900,18 +899,28 @@ static int tc_prepare(gbx_graph *g, cudaStream_t s) {
             return st;
         }
         g->tc_plan = p;
+    } else if (g->tc_plan && !g->tc_plan->pre_len && g->E) {
+        // the graph is counted again: from now on its counts read the
+        // prefix lengths (building them costs about as much as the row
+        // searches of one count, so a graph counted once never pays for them)
+        gbx_tc_plan *p = g->tc_plan;
+        GBX_TRY(dev_alloc((void **)&p->pre_len, (size_t)g->E * 4, s));
+        const unsigned egrid =
+            std::min<unsigned>(ceil_div(ceil_div((uint64_t)g->E, 2048) * 32, 256), (unsigned)num_sms() * 8);
+        tc_prefix_len_kernel<<<egrid, 256, 0, s>>>(g->offsets, g->dest, V, g->E, p->pre_len);
+        GBX_LAUNCH_CHECK();
     }
     return GBX_OK;
 }
 
 void gbx_free_tc_plan(gbx_tc_plan *p) {
     if (!p) return;
-    cudaFree(p->big);
-    cudaFree(p->wide);
-    cudaFree(p->small);
-    cudaFree(p->hub);
-    cudaFree(p->hub_bits);
-    cudaFree(p->pre_len);
+    dev_free(p->big);
+    dev_free(p->wide);
+    dev_free(p->small);
+    dev_free(p->hub);
+    dev_free(p->hub_bits);
+    dev_free(p->pre_len);
     delete p;
 }
 

@@ -172,12 +172,15 @@ def test_rmat_symmetric(gbx, cuda_device, scale, ef, seed):
             comp, _ = gbx.connected_components(dg, cv)
             np.testing.assert_array_equal(comp, ref)
         assert gbx.triangle_count(dg) == po.triangle_count(host)
-    # degree-ordered DAG: TC after degree reordering gives the same count
+    # degree-ordered DAG: TC after degree reordering gives the same count;
+    # the first count searches the rows for the prefix lengths, the second
+    # builds the plan's per-edge prefix lengths and the third reads them
     el = gbx.EdgeList(g.num_vertices, g.src.copy(), g.dest.copy())
     gbx.degree_reorder(el, 1)
     g2 = gbx.graph_csr_preprocessing(el, sort=1, directed=False, keep_weights=False)
+    tri = po.triangle_count(host)
     with gbx.DeviceGraph.from_graph_csr(g2) as dg2:
-        assert gbx.triangle_count(dg2) == po.triangle_count(host)
+        assert [gbx.triangle_count(dg2) for _ in range(3)] == [tri, tri, tri]
 
 
 def test_tc_asymmetric_simple_graphs(gbx, cuda_device):
