@@ -17,8 +17,11 @@
 // it from the better distance; units that started before the improvement
 // relax from the older distance, which is harmless, and a vertex's last
 // expansion, in a round without an improvement of it, reads one distance in
-// all its units. One grid barrier per round. The result is the unique fixed
-// point
+// all its units. One grid barrier per round, two for a large round: its
+// relaxations are reductions that nobody waits for (the lowered distance and
+// a touched bit), and a scan of the touched bitmap after the barrier queues
+// the lowered vertices (in such a round "improved again" is a touched bit).
+// The result is the unique fixed point
 //   dist[u] = min over (v->u) of (uint32)((float)dist[v] + w),
 // i.e. the reference's distances. Work units and hub splitting are those of
 // the persistent BFS (gbx_bfs.cu): 32 near vertices flattened per warp, or
@@ -84,6 +87,9 @@ struct SsspArgs {
     const float *w;
     uint32_t V, delta, source;
     uint32_t *dist, *settled, *stamp, *in_far;
+    uint32_t *touched;  // bit v: dist[v] lowered in this (scan-mode) round; all zero between rounds
+    uint32_t words;     // (V + 31) / 32
+    uint32_t scan_min;  // near vertices (+32 per hub chunk) from which a round runs in scan mode
     uint32_t *q[2], *hv[2], *hc[2];
     uint32_t *far[2];
     SsspState *st;
@@ -157,6 +163,28 @@ struct Relaxer {
             wfar.push(u[q], to_far, far, &cnt->far_len);
         }
     }
+    // Scan-mode relaxations: the lowered distance and its touched bit are
+    // reductions nobody waits for; the round's scan pass then queues the
+    // touched vertices. A warp's next batch is not held up by the replies,
+    // so a large round keeps many more relaxations in flight.
+    __device__ __forceinline__ void relax4_red(const uint32_t (&d)[4], const uint32_t (&e)[4],
+                                               const uint32_t (&u)[4], const bool (&act)[4]) {
+        uint32_t nd[4], cur[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float wt = (act[q] && a.w) ? __ldcs(a.w + e[q]) : 1.0f;
+            nd[q] = sssp_add(d[q], wt);
+            cur[q] = act[q] ? __ldcg(a.dist + u[q]) : 0u;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            relaxed += act[q] ? 1u : 0u;
+            if (act[q] && nd[q] < cur[q]) {
+                atomicMin(a.dist + u[q], nd[q]);
+                atomicOr(a.touched + (u[q] >> 5), 1u << (u[q] & 31));
+            }
+        }
+    }
     __device__ __forceinline__ void flush() {
         wnear.flush(qout, &cnt->near_len);
         wfar.flush(far, &cnt->far_len);
@@ -167,6 +195,11 @@ struct Relaxer {
     }
 };
 
+__device__ __forceinline__ bool touched_bit(const SsspArgs &a, uint32_t v) {
+    return (__ldcg(a.touched + (v >> 5)) >> (v & 31)) & 1u;
+}
+
+template <bool kScan>
 __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn, const uint32_t *hvin,
                             const uint32_t *hcin, uint32_t nh, uint32_t nc, Relaxer &rx, SsspRound *cur,
                             uint32_t *s_pre, uint32_t *s_base, uint32_t *s_d) {
@@ -197,7 +230,7 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
             const uint32_t rb = __ldg(a.off + v), re = __ldg(a.off + v + 1);
             const uint32_t cb = rb + (chunk - first) * kSsspHubChunk;
             // a hub improved in this round is in the next near list already
-            const bool stale = sv == rx.round;
+            const bool stale = kScan ? touched_bit(a, v) : sv == rx.round;
             if (!stale && chunk == first && hpart == 0 && lane == 0) a.settled[v] = d;
             const uint32_t ce = stale ? cb : min(cb + kSsspHubChunk, re);
             // the next batch's ids are loaded before this batch is relaxed
@@ -219,7 +252,7 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
                 const uint32_t dq[4] = {d, d, d, d};
                 const uint32_t eq[4] = {j0 + lane, j0 + 32 + lane, j0 + 64 + lane, j0 + 96 + lane};
                 const bool act[4] = {eq[0] < ce, eq[1] < ce, eq[2] < ce, eq[3] < ce};
-                rx.relax4(dq, eq, u, act);
+                if (kScan) rx.relax4_red(dq, eq, u, act); else rx.relax4(dq, eq, u, act);
             }
         } else {
             const uint32_t group = unit / split, part = unit % split;
@@ -234,7 +267,7 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
                 // improved in this round (so in the next near list): its edges
                 // are masked, but the row keeps its place, because every part
                 // of a split group must flatten the group identically
-                if (sv == rx.round) d = kStaleRow;
+                if (kScan ? touched_bit(a, v) : sv == rx.round) d = kStaleRow;
                 else if (part == 0) a.settled[v] = d;
             }
             uint32_t incl = deg;
@@ -268,12 +301,65 @@ __device__ void relax_phase(const SsspArgs &a, const uint32_t *qin, uint32_t qn,
                 const bool act[4] = {i0 + lane < tot && dd[0] != kStaleRow, i0 + 32 + lane < tot && dd[1] != kStaleRow,
                                      i0 + 64 + lane < tot && dd[2] != kStaleRow,
                                      i0 + 96 + lane < tot && dd[3] != kStaleRow};
-                rx.relax4(dd, e, u, act);
+                if (kScan) rx.relax4_red(dd, e, u, act); else rx.relax4(dd, e, u, act);
             }
             __syncwarp();
         }
     }
-    rx.flush();
+}
+
+// Scan-mode round, second pass: every vertex whose touched bit is set was
+// lowered in this round (some relaxation saw a larger distance and reduced
+// it), so it is queued exactly as the per-relaxation follow-ups would have:
+// below the threshold into the next near list (hubs into the hub list,
+// vertices without out-edges settled on the spot), else into the far pile
+// once. A warp takes 32 consecutive vertices (one bitmap word) at a time.
+__device__ void scan_phase(const SsspArgs &a, uint32_t thr, SsspRound *cnt, uint32_t *qout, uint32_t *hvout,
+                           uint32_t *hcout, uint32_t *far, uint32_t *bn, uint32_t *bf) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    WarpQueue wnear(bn), wfar(bf);
+    uint32_t far_min = 0xFFFFFFFFu;
+    for (uint32_t w = gw; w < a.words; w += nw) {
+        const uint32_t m = __ldcg(a.touched + w);
+        if (!m) continue;
+        if (lane == 0) a.touched[w] = 0u;
+        const uint32_t u = w * 32 + lane;
+        const bool t = (m >> lane) & 1u;
+        uint32_t d = 0, du = 0, inf = 1;
+        if (t) {
+            d = __ldcg(a.dist + u);
+            du = __ldg(a.outdeg + u);
+            inf = __ldcg(a.in_far + u);
+        }
+        const bool below = t && d < thr;
+        bool to_near = false, to_far = false;
+        if (below) {
+            if (du == 0) {
+                a.settled[u] = d;  // nothing to expand
+            } else if (du > kSsspHubDeg) {
+                const unsigned long long h = atomicAdd(&cnt->near_hub, (1ull << 32) | sssp_chunks(du));
+                const uint32_t slot = (uint32_t)(h >> 32);
+                hvout[slot] = u;
+                hcout[slot] = (uint32_t)h;
+            } else {
+                to_near = true;
+            }
+        } else if (t) {
+            far_min = min(far_min, d);
+            if (!inf) {
+                a.in_far[u] = 1u;
+                to_far = true;
+            }
+        }
+        wnear.push(u, to_near, qout, &cnt->near_len);
+        wfar.push(u, to_far, far, &cnt->far_len);
+    }
+    wnear.flush(qout, &cnt->near_len);
+    wfar.flush(far, &cnt->far_len);
+    const uint32_t fm = warp_min(far_min);
+    if (lane == 0 && fm != 0xFFFFFFFFu) atomicMin(&cnt->far_min, fm);
 }
 
 __device__ __forceinline__ void zero_round(SsspRound *r, uint32_t far_len) {
@@ -327,7 +413,22 @@ __global__ void __launch_bounds__(kSsspThreads, 1) sssp_persistent_kernel(SsspAr
             // far pushes of this round append after the pile's far_len entries
             Relaxer rx(a, thr, round, cur, a.q[ib ^ 1], a.hv[ib ^ 1], a.hc[ib ^ 1], a.far[fb] + far_len, s_wn[wid],
                        s_wf[wid]);
-            relax_phase(a, a.q[ib], qn, a.hv[ib], a.hc[ib], nh, nc, rx, cur, s_pre[wid], s_base[wid], s_d[wid]);
+            // a large round relaxes with reductions and queues what it
+            // lowered in a scan pass after one more barrier; a small one
+            // queues each improvement as it happens
+            const bool scan = (uint64_t)qn + 32ull * nc >= a.scan_min;
+            if (scan) {
+                relax_phase<true>(a, a.q[ib], qn, a.hv[ib], a.hc[ib], nh, nc, rx, cur, s_pre[wid], s_base[wid],
+                                  s_d[wid]);
+                rx.flush();
+                if (!grid_barrier(&st->gs)) { failed = true; break; }
+                scan_phase(a, thr, cur, a.q[ib ^ 1], a.hv[ib ^ 1], a.hc[ib ^ 1], a.far[fb] + far_len, s_wn[wid],
+                           s_wf[wid]);
+            } else {
+                relax_phase<false>(a, a.q[ib], qn, a.hv[ib], a.hc[ib], nh, nc, rx, cur, s_pre[wid], s_base[wid],
+                                   s_d[wid]);
+                rx.flush();
+            }
             if (!grid_barrier(&st->gs)) { failed = true; break; }
             fetch_counters(cur, &s_cnt);
             relaxed += s_cnt.relaxed;
@@ -444,14 +545,16 @@ __global__ void __launch_bounds__(kSsspThreads, 1) sssp_persistent_kernel(SsspAr
 }
 
 __global__ void sssp_init_kernel(uint32_t *dist, uint32_t *settled, uint32_t *stamp, uint32_t *in_far,
-                                 uint32_t V, uint32_t source, const uint32_t *outdeg, uint32_t *q0,
-                                 uint32_t *hv0, uint32_t *hc0, SsspRound *r0) {
+                                 uint32_t *touched, uint32_t V, uint32_t source, const uint32_t *outdeg,
+                                 uint32_t *q0, uint32_t *hv0, uint32_t *hc0, SsspRound *r0) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
         dist[v] = v == source ? 0u : kSsspInf;
         settled[v] = 0xFFFFFFFFu;
         stamp[v] = v == source ? 1u : 0u;
         in_far[v] = 0;
     }
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < (V + 31) / 32; w += gridDim.x * blockDim.x)
+        touched[w] = 0u;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         q0[0] = source;
         hv0[0] = source;
@@ -499,12 +602,16 @@ extern "C" int gbx_sssp(gbx_graph *g, uint32_t source, uint32_t delta, uint32_t 
     const bool stage = !out_dev;
     const size_t r = Scratch::round_up((size_t)V * 4);
     Scratch sc;
-    GBX_TRY(sc.take(g, (stage ? 13 : 12) * r + Scratch::round_up(sizeof(SsspState)) + Scratch::round_up(16), s));
+    const uint32_t words = (V + 31) / 32;
+    GBX_TRY(sc.take(g, (stage ? 13 : 12) * r + Scratch::round_up((size_t)words * 4) +
+                           Scratch::round_up(sizeof(SsspState)) + Scratch::round_up(16),
+                    s));
     uint32_t *dist = sc.carve<uint32_t>(V), *settled = sc.carve<uint32_t>(V), *stamp = sc.carve<uint32_t>(V);
     uint32_t *in_far = sc.carve<uint32_t>(V), *q0 = sc.carve<uint32_t>(V), *q1 = sc.carve<uint32_t>(V);
     uint32_t *hv0 = sc.carve<uint32_t>(V), *hv1 = sc.carve<uint32_t>(V), *hc0 = sc.carve<uint32_t>(V);
     uint32_t *hc1 = sc.carve<uint32_t>(V), *f0 = sc.carve<uint32_t>(V), *f1 = sc.carve<uint32_t>(V);
     uint32_t *out_stage = stage ? sc.carve<uint32_t>(V) : nullptr;
+    uint32_t *touched = sc.carve<uint32_t>(words);
     SsspState *st = sc.carve<SsspState>(1);
     unsigned long long *fin = sc.carve<unsigned long long>(2);
     GBX_REQUIRE(fin != nullptr, GBX_ERR_CUDA, "SSSP scratch carve overflow");
@@ -512,7 +619,7 @@ extern "C" int gbx_sssp(gbx_graph *g, uint32_t source, uint32_t delta, uint32_t 
     GBX_TRY(out.bind(distances, V, s, out_stage, out_dev));
     const unsigned grid1 = std::min<unsigned>(ceil_div(V, 256), (unsigned)num_sms() * 8);
     GBX_CUDA(cudaMemsetAsync(st, 0, sizeof(SsspState), s));
-    sssp_init_kernel<<<grid1, 256, 0, s>>>(dist, settled, stamp, in_far, V, source, g->out_degree,
+    sssp_init_kernel<<<grid1, 256, 0, s>>>(dist, settled, stamp, in_far, touched, V, source, g->out_degree,
                                            q0, hv0, hc0, &st->r[0]);
     GBX_LAUNCH_CHECK();
     SsspArgs a;
@@ -527,6 +634,9 @@ extern "C" int gbx_sssp(gbx_graph *g, uint32_t source, uint32_t delta, uint32_t 
     a.settled = settled;
     a.stamp = stamp;
     a.in_far = in_far;
+    a.touched = touched;
+    a.words = words;
+    a.scan_min = std::max<uint32_t>(4096u, V / 256);
     a.q[0] = q0;
     a.q[1] = q1;
     a.hv[0] = hv0;
