@@ -27,6 +27,7 @@ all host cores) on a bounded sample of the same workload.
 from __future__ import annotations
 
 import argparse
+import gc as pygc
 import json
 import os
 import subprocess
@@ -167,6 +168,23 @@ def tc_stats(gsr):
 
 # ---------------------------------------------------------------------------
 # clocks
+
+
+class collector_held:
+    """Python's cyclic garbage collector is held off while steps are timed
+    (it runs once just before): a collection inside a step stalls the host
+    thread that issues the library calls, by tens of milliseconds with the
+    workload's objects alive."""
+
+    def __enter__(self):
+        pygc.collect()
+        self.was = pygc.isenabled()
+        pygc.disable()
+
+    def __exit__(self, *exc):
+        if self.was:
+            pygc.enable()
+        return False
 
 
 class ClockSampler:
@@ -395,8 +413,9 @@ def run_gpu(args):
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
     t_start.record(stream)
-    for _ in range(args.steps):
-        one_step(True)
+    with collector_held():
+        for _ in range(args.steps):
+            one_step(True)
     t_end.record(stream)
     torch.cuda.synchronize()
     if dist:
@@ -1101,11 +1120,12 @@ def run_e2e(gbx, _lib, W, args, roots, sssp_roots, e_plus, stream, sp, tuning=No
     torch.cuda.synchronize()
     times = []
     edges = 0
-    for _ in range(max(1, min(args.steps, 5))):
-        t0 = time.perf_counter()
-        edges = step()
-        torch.cuda.synchronize()
-        times.append(time.perf_counter() - t0)
+    with collector_held():
+        for _ in range(max(1, min(args.steps, 5))):
+            t0 = time.perf_counter()
+            edges = step()
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
     t = float(np.mean(times))
     return {"value": round(edges / t / 1e9, 3), "unit": "GTEPS", "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h), "ms_per_step": round(t * 1e3, 2),
