@@ -166,7 +166,12 @@ struct Relaxer {
     // Scan-mode relaxations: the lowered distance and its touched bit are
     // reductions nobody waits for; the round's scan pass then queues the
     // touched vertices. A warp's next batch is not held up by the replies,
-    // so a large round keeps many more relaxations in flight.
+    // so a large round keeps many more relaxations in flight. The filtering
+    // read of the target's distance goes through L1 (the hubs that most
+    // edges point at stay there): a stale copy can only be larger than the
+    // current distance, so no improvement is missed; at worst a vertex that
+    // was not lowered is touched and expanded once more. The grid barrier's
+    // acquire starts every round with fresh copies.
     __device__ __forceinline__ void relax4_red(const uint32_t (&d)[4], const uint32_t (&e)[4],
                                                const uint32_t (&u)[4], const bool (&act)[4]) {
         uint32_t nd[4], cur[4];
@@ -174,7 +179,7 @@ struct Relaxer {
         for (int q = 0; q < 4; ++q) {
             const float wt = (act[q] && a.w) ? __ldcs(a.w + e[q]) : 1.0f;
             nd[q] = sssp_add(d[q], wt);
-            cur[q] = act[q] ? __ldcg(a.dist + u[q]) : 0u;
+            cur[q] = act[q] ? __ldca(a.dist + u[q]) : 0u;
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
