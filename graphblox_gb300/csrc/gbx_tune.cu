@@ -146,10 +146,10 @@ extern "C" int gbx_autotune(gbx_graph *g, uint32_t flags, uint32_t num_samples, 
         const int nc = g->weight ? 8 : 3;
         float best = 1e30f;
         uint32_t best_d = g->sssp_delta;
-        // as for alpha: the same (at least 8) sources for every candidate,
+        // as for alpha: the same (at least 16) sources for every candidate,
         // twice, keeping the faster pass
         std::vector<uint32_t> ssrc;
-        GBX_TRY(sample_sources(g, std::max<uint32_t>(num_samples, 8), s, &ssrc));
+        GBX_TRY(sample_sources(g, std::max<uint32_t>(num_samples, 16), s, &ssrc));
         for (int i = 0; i < nc; ++i) {
             GBX_TRY(gbx_sssp(g, ssrc[0], cands[i], out.p, nullptr, stream));  // warm
             float ms = 1e30f;
