@@ -51,7 +51,7 @@ PR_ITERS = 20
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each
 # kernel, from ncu captures of this workload on a GB300 (profiles/): bfs and
 # sssp one source (--set full), pr one iteration, spmv one launch.
-NCU_TRAFFIC_PER_LAUNCH = {"pr": 0.4006e9, "bfs": 0.1688e9, "sssp": 1.896e9, "spmv": 0.6775e9}
+NCU_TRAFFIC_PER_LAUNCH = {"pr": 0.4006e9, "bfs": 0.1688e9, "sssp": 1.946e9, "spmv": 0.6775e9}
 W_LO, W_HI = 1, 255
 # differentiable personalised PageRank: RMAT-20, 2^24 edges as generated,
 # lognormal(0,1) weights, 64 teleport columns of 32 seeds, d 0.85 to 1e-7 L1
