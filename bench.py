@@ -434,8 +434,8 @@ def run_gpu(args):
                   "frac": round(tb / (ms * 1e-3) / 1e9 / peak, 3), "edges": int(te), "alg_bytes": int(tb)}
         if n in NCU_TRAFFIC_PER_LAUNCH:
             # DRAM bytes one launch moved under ncu, over this run's time per launch
-            launches = {"bfs": len(roots), "sssp": len(sssp_roots), "pr": PR_ITERS}.get(n, 1)
-            per[n]["dram_frac"] = round(NCU_TRAFFIC_PER_LAUNCH[n] * launches / (ms * 1e-3) / 1e9 / peak, 3)
+            per_step = {"bfs": len(roots), "sssp": len(sssp_roots), "pr": PR_ITERS}.get(n, 1)
+            per[n]["dram_frac"] = round(NCU_TRAFFIC_PER_LAUNCH[n] * per_step / (ms * 1e-3) / 1e9 / peak, 3)
         if n == "tc":
             per[n]["merge_bytes"] = int(tc_merge_bytes)
             per[n]["note"] = ("alg_bytes = the DAG read once, 4(V+1) + 4|E+|; merge_bytes = what a merge "
