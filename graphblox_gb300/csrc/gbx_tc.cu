@@ -682,7 +682,7 @@ __global__ void __launch_bounds__(kTcThreads)
 // entries (load factor <= 1/2), every warp streaming 32 upper neighbours'
 // prefixes at a time against it.
 constexpr int kWideThreads = 1024;
-constexpr uint32_t kWideChunk = 2048;
+constexpr uint32_t kWideChunk = 4096;
 constexpr uint32_t kWideSlotsMax = 32768;  // 128 KiB: |N+(v)| <= 16384
 static_assert((kWideSlotsMax & (kWideSlotsMax - 1)) == 0 && (kTcWarpSlots & (kTcWarpSlots - 1)) == 0,
               "bitmap tables must cover a power-of-two id range (BitmapMember masks ids)");
