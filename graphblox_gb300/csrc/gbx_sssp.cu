@@ -327,9 +327,15 @@ __device__ void scan_phase(const SsspArgs &a, uint32_t thr, SsspRound *cnt, uint
     WarpQueue wnear(bn), wfar(bf);
     uint32_t far_min = 0xFFFFFFFFu;
     for (uint32_t w = gw; w < a.words; w += nw) {
-        const uint32_t m = __ldcg(a.touched + w);
+        // lane 0 reads and clears the word (one thread: the read is ordered
+        // before the clear), the warp gets it by a shuffle
+        uint32_t m = 0;
+        if (lane == 0) {
+            m = __ldcg(a.touched + w);
+            if (m) a.touched[w] = 0u;
+        }
+        m = __shfl_sync(0xffffffffu, m, 0);
         if (!m) continue;
-        if (lane == 0) a.touched[w] = 0u;
         const uint32_t u = w * 32 + lane;
         const bool t = (m >> lane) & 1u;
         uint32_t d = 0, du = 0, inf = 1;
