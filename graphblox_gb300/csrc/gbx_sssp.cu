@@ -36,7 +36,7 @@
 namespace gbx {
 
 constexpr uint32_t kSsspHubDeg = 1024;
-constexpr uint32_t kSsspHubChunk = 1024;
+constexpr uint32_t kSsspHubChunk = 2048;
 constexpr uint32_t kSsspMaxSplit = 64;  // most warps sharing one 32-vertex group's edges
 constexpr uint32_t kStaleRow = 0xFFFFFFFFu;  // snapshot marker of a near row skipped this round
 constexpr int kSsspThreads = 1024;
