@@ -78,7 +78,7 @@ int ensure_device() {
             g_props[dev].l2 = (size_t)p.l2CacheSize;
             // Working buffers come from the device's default stream-ordered
             // pool. With its default release threshold (0) every stream
-            // synchronize hands freed blocks back to the driver, and the next
+            // synchronize hands freed blocks back to the CUDA driver, and the next
             // call maps them again (hundreds of MB per BFS on large graphs);
             // keep up to a quarter of device memory (at most 64 GB) cached in
             // this process instead.
@@ -195,7 +195,7 @@ int dev_alloc(void **p, size_t bytes, cudaStream_t s) {
     *p = nullptr;
     cudaError_t e = cudaMallocAsync(p, bytes ? bytes : 4, s);
     if (e == cudaErrorMemoryAllocation) {
-        // memory the pool keeps from freed graphs goes back to the driver
+        // memory the pool keeps from freed graphs goes back to the CUDA driver
         // first, then the allocation is tried once more
         (void)cudaGetLastError();
         int dev = 0;

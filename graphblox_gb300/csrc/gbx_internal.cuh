@@ -262,7 +262,7 @@ void gbx_free_bc_cache(struct gbx_bc_cache *c);
 namespace gbx {
 // Long-lived device arrays (a graph's arrays, scratch arena and plans) come
 // from the device's stream-ordered pool, which keeps the memory of a freed
-// graph for the next one instead of handing it back to the driver (a
+// graph for the next one instead of handing it back to the CUDA driver (a
 // cudaMalloc/cudaFree of gigabytes costs milliseconds). dev_alloc orders the
 // allocation on stream s; dev_free is for memory no stream uses any more
 // (its callers synchronized first) and accepts nullptr.
