@@ -219,76 +219,115 @@ void dev_free(void *p) {
     if (p) cudaFreeAsync(p, 0);
 }
 
-// Fill one direction of the graph (forward or inverse) from either layout.
-static int fill_direction(uint32_t V, uint32_t E, const uint32_t *edges_idx, const uint32_t *degree,
-                          const uint32_t *offsets, const uint32_t *ids, const float *w,
-                          uint32_t **d_off, uint32_t **d_ids, float **d_w, uint32_t **d_deg,
-                          uint32_t *max_deg, cudaStream_t s) {
-    GBX_TRY(dev_alloc((void **)d_off, (size_t)(V + 1) * 4, s));
-    GBX_TRY(dev_alloc((void **)d_deg, (size_t)V * 4, s));
-    // four ids of zeroed padding: kernels read rows as aligned 16-byte quads
-    GBX_TRY(dev_alloc((void **)d_ids, ((size_t)E + 4) * 4, s));
-    GBX_CUDA(cudaMemsetAsync(*d_ids + E, 0, 16, s));
-    if (w) GBX_TRY(dev_alloc((void **)d_w, (size_t)E * 4, s));
-    DevBuf<unsigned> bad;
-    GBX_TRY(bad.alloc(3, s));
-    GBX_CUDA(cudaMemsetAsync(bad.p, 0, 12, s));
-    bool repack = false;
+// One direction of a graph (forward or inverse), filled from either layout
+// in two passes. fill_stage allocates the arrays and enqueues every copy of
+// the caller's arrays; fill_check then runs the validation kernels and their
+// host round trips and gathers runs that are out of vertex order. A graph
+// stages both directions before it checks either, so its copies follow one
+// another over the host link instead of each waiting for a check kernel,
+// which may itself wait for SMs that another stream's kernels hold.
+struct DirFill {
+    uint32_t V = 0, E = 0;
+    const uint32_t *edges_idx = nullptr, *degree = nullptr, *offsets = nullptr, *ids = nullptr;
+    const float *w = nullptr;
+    uint32_t **d_off = nullptr, **d_ids = nullptr, **d_deg = nullptr;
+    float **d_w = nullptr;
+    uint32_t *max_deg = nullptr;
     InArray<uint32_t> eidx;
-    if (offsets) {
-        GBX_TRY(copy_in(*d_off, offsets, (size_t)(V + 1) * 4, s));
-        check_offsets_kernel<<<grid_for(V), 256, 0, s>>>(*d_off, V, E, bad.p);
+    DevBuf<unsigned> bad;  // [0] layout / offset faults, [1] maximum degree, [2] runs past E
+    DevBuf<uint32_t> tot;
+};
+
+static int fill_stage(DirFill &f, cudaStream_t s) {
+    const uint32_t V = f.V, E = f.E;
+    GBX_TRY(dev_alloc((void **)f.d_off, (size_t)(V + 1) * 4, s));
+    GBX_TRY(dev_alloc((void **)f.d_deg, (size_t)V * 4, s));
+    // four ids of zeroed padding: kernels read rows as aligned 16-byte quads
+    GBX_TRY(dev_alloc((void **)f.d_ids, ((size_t)E + 4) * 4, s));
+    GBX_CUDA(cudaMemsetAsync(*f.d_ids + E, 0, 16, s));
+    if (f.w) GBX_TRY(dev_alloc((void **)f.d_w, (size_t)E * 4, s));
+    GBX_TRY(f.bad.alloc(3, s));
+    GBX_CUDA(cudaMemsetAsync(f.bad.p, 0, 12, s));
+    if (f.offsets) {
+        GBX_TRY(copy_in(*f.d_off, f.offsets, (size_t)(V + 1) * 4, s));
+    } else {
+        GBX_TRY(copy_in(*f.d_deg, f.degree, (size_t)V * 4, s));
+        GBX_TRY(f.eidx.bind(f.edges_idx, V, s));
+    }
+    // the edge arrays as given; fill_check gathers them into offset order
+    // when the runs turn out not to be in vertex order
+    GBX_TRY(copy_in(*f.d_ids, f.ids, (size_t)E * 4, s));
+    if (f.w) GBX_TRY(copy_in(*f.d_w, f.w, (size_t)E * 4, s));
+    return GBX_OK;
+}
+
+static int fill_check(DirFill &f, cudaStream_t s) {
+    const uint32_t V = f.V, E = f.E;
+    bool repack = false;
+    if (f.offsets) {
+        check_offsets_kernel<<<grid_for(V), 256, 0, s>>>(*f.d_off, V, E, f.bad.p);
         GBX_LAUNCH_CHECK();
-        degree_from_offsets_kernel<<<grid_for(V), 256, 0, s>>>(*d_off, *d_deg, V);
+        degree_from_offsets_kernel<<<grid_for(V), 256, 0, s>>>(*f.d_off, *f.d_deg, V);
         GBX_LAUNCH_CHECK();
     } else {
-        GBX_TRY(copy_in(*d_deg, degree, (size_t)V * 4, s));
-        uint32_t *total = nullptr;
-        DevBuf<uint32_t> tot;
-        GBX_TRY(tot.alloc(1, s));
-        total = tot.p;
-        GBX_TRY(exclusive_scan_u32(*d_deg, *d_off, V, s, total));
-        GBX_CUDA(cudaMemcpyAsync(*d_off + V, total, 4, cudaMemcpyDeviceToDevice, s));
-        GBX_TRY(eidx.bind(edges_idx, V, s));
-        check_layout_kernel<<<grid_for(V), 256, 0, s>>>(eidx.d, *d_deg, *d_off, V, E, bad.p);
+        GBX_TRY(f.tot.alloc(1, s));
+        GBX_TRY(exclusive_scan_u32(*f.d_deg, *f.d_off, V, s, f.tot.p));
+        GBX_CUDA(cudaMemcpyAsync(*f.d_off + V, f.tot.p, 4, cudaMemcpyDeviceToDevice, s));
+        check_layout_kernel<<<grid_for(V), 256, 0, s>>>(f.eidx.d, *f.d_deg, *f.d_off, V, E, f.bad.p);
         GBX_LAUNCH_CHECK();
         uint32_t hv = 0;
         unsigned hl[3] = {0, 0, 0};
-        GBX_CUDA(cudaMemcpyAsync(&hv, total, 4, cudaMemcpyDeviceToHost, s));
-        GBX_CUDA(cudaMemcpyAsync(hl, bad.p, 12, cudaMemcpyDeviceToHost, s));
+        GBX_CUDA(cudaMemcpyAsync(&hv, f.tot.p, 4, cudaMemcpyDeviceToHost, s));
+        GBX_CUDA(cudaMemcpyAsync(hl, f.bad.p, 12, cudaMemcpyDeviceToHost, s));
         GBX_CUDA(cudaStreamSynchronize(s));
         GBX_REQUIRE(hv == E, GBX_ERR_INVALID, "sum of degrees (%u) != num_edges (%u)", hv, E);
         GBX_REQUIRE(hl[2] == 0, GBX_ERR_INVALID,
                     "%u vertices whose edges_idx + out_degree exceeds num_edges (%u)", hl[2], E);
         repack = hl[0] != 0;
-        GBX_CUDA(cudaMemsetAsync(bad.p, 0, 4, s));
+        GBX_CUDA(cudaMemsetAsync(f.bad.p, 0, 4, s));
     }
     if (repack) {
-        // runs out of vertex order: gather them into offset order
-        InArray<uint32_t> raw_ids;
-        InArray<float> raw_w;
-        GBX_TRY(raw_ids.bind(ids, E, s));
-        GBX_TRY(raw_w.bind(w, E, s));
-        repack_runs_kernel<<<grid_for((uint64_t)V * 32), 256, 0, s>>>(eidx.d, *d_deg, *d_off, V, raw_ids.d,
-                                                                     w ? raw_w.d : nullptr, *d_ids,
-                                                                     w ? *d_w : nullptr);
-        GBX_LAUNCH_CHECK();
-        GBX_CUDA(cudaStreamSynchronize(s));
-    } else {
-        GBX_TRY(copy_in(*d_ids, ids, (size_t)E * 4, s));
-        if (w) GBX_TRY(copy_in(*d_w, w, (size_t)E * 4, s));
+        // runs out of vertex order: gather the copies just made into offset
+        // order in new arrays, which then replace them
+        uint32_t *ids2 = nullptr;
+        float *w2 = nullptr;
+        GBX_TRY(dev_alloc((void **)&ids2, ((size_t)E + 4) * 4, s));
+        if (f.w && dev_alloc((void **)&w2, (size_t)E * 4, s) != GBX_OK) {
+            cudaStreamSynchronize(s);
+            dev_free(ids2);
+            return GBX_ERR_NOMEM;
+        }
+        cudaError_t le = cudaMemsetAsync(ids2 + E, 0, 16, s);
+        if (le == cudaSuccess) {
+            repack_runs_kernel<<<grid_for((uint64_t)V * 32), 256, 0, s>>>(
+                f.eidx.d, *f.d_deg, *f.d_off, V, *f.d_ids, f.w ? *f.d_w : nullptr, ids2, w2);
+            le = cudaGetLastError();
+        }
+        cudaStreamSynchronize(s);
+        if (le != cudaSuccess) {
+            dev_free(ids2);
+            dev_free(w2);
+            return cuda_fail(le, "repack_runs_kernel", __FILE__, __LINE__);
+        }
+        note_launch();
+        dev_free(*f.d_ids);
+        *f.d_ids = ids2;
+        if (f.w) {
+            dev_free(*f.d_w);
+            *f.d_w = w2;
+        }
     }
     if (E) {
-        mask_ids_kernel<<<grid_for(E), 256, 0, s>>>(*d_ids, E);
+        mask_ids_kernel<<<grid_for(E), 256, 0, s>>>(*f.d_ids, E);
         GBX_LAUNCH_CHECK();
     }
-    max_u32_kernel<<<grid_for(V), 256, 0, s>>>(*d_deg, V, bad.p + 1);
+    max_u32_kernel<<<grid_for(V), 256, 0, s>>>(*f.d_deg, V, f.bad.p + 1);
     GBX_LAUNCH_CHECK();
     unsigned hb[2] = {0, 0};
-    GBX_CUDA(cudaMemcpyAsync(hb, bad.p, 8, cudaMemcpyDeviceToHost, s));
+    GBX_CUDA(cudaMemcpyAsync(hb, f.bad.p, 8, cudaMemcpyDeviceToHost, s));
     GBX_CUDA(cudaStreamSynchronize(s));
     GBX_REQUIRE(hb[0] == 0, GBX_ERR_INVALID, "offsets are not non-decreasing from 0 to num_edges");
-    *max_deg = hb[1];
+    *f.max_deg = hb[1];
     return GBX_OK;
 }
 
@@ -311,19 +350,27 @@ static int create_common(gbx_graph **out, uint32_t V, uint32_t E, const uint32_t
     cudaGetDevice(&g->device);
     g->V = V;
     g->E = E;
-    int st = fill_direction(V, E, edges_idx, deg, off, dest, w, &g->offsets, &g->dest, &g->weight,
-                            &g->out_degree, &g->max_out_degree, s);
-    bool want_inv = (in_off != nullptr) || (in_idx != nullptr && in_deg != nullptr);
-    if (st == GBX_OK && want_inv) {
-        if (E && !in_src) {
-            set_error("in_src is NULL");
-            st = GBX_ERR_INVALID;
-        } else {
-            st = fill_direction(V, E, in_idx, in_deg, in_off, in_src, in_w, &g->in_offsets,
-                                &g->in_src, &g->in_weight, &g->in_degree, &g->max_in_degree, s);
-        }
+    const bool want_inv = (in_off != nullptr) || (in_idx != nullptr && in_deg != nullptr);
+    if (want_inv && E && !in_src) {
+        delete g;
+        set_error("in_src is NULL");
+        return GBX_ERR_INVALID;
     }
+    DirFill fwd, inv;
+    fwd.V = inv.V = V;
+    fwd.E = inv.E = E;
+    fwd.edges_idx = edges_idx, fwd.degree = deg, fwd.offsets = off, fwd.ids = dest, fwd.w = w;
+    fwd.d_off = &g->offsets, fwd.d_ids = &g->dest, fwd.d_w = &g->weight, fwd.d_deg = &g->out_degree;
+    fwd.max_deg = &g->max_out_degree;
+    inv.edges_idx = in_idx, inv.degree = in_deg, inv.offsets = in_off, inv.ids = in_src, inv.w = in_w;
+    inv.d_off = &g->in_offsets, inv.d_ids = &g->in_src, inv.d_w = &g->in_weight, inv.d_deg = &g->in_degree;
+    inv.max_deg = &g->max_in_degree;
+    int st = fill_stage(fwd, s);
+    if (st == GBX_OK && want_inv) st = fill_stage(inv, s);
+    if (st == GBX_OK) st = fill_check(fwd, s);
+    if (st == GBX_OK && want_inv) st = fill_check(inv, s);
     if (st != GBX_OK) {
+        cudaStreamSynchronize(s);  // the stages' copies may still be in flight
         gbx_graph_destroy(g);
         return st;
     }
