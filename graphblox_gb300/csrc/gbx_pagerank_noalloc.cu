@@ -15,10 +15,9 @@
 // In host code the name g_pr_scratch is only a host-side stand-in for the
 // device array; its device address is looked up with cudaGetSymbolAddress
 // once per device, on the first call made with that device current (a lookup
-// that failed is retried by the next call). That first call therefore does
-// the set-up and should come before any stream capture. Every call reuses
-// the same array and keeps the previous call's contents; the iteration
-// counters are cleared at the start of each call. Calls that overlap on the
+// that failed is retried by the next call), so that first call does the
+// set-up. Every call reuses the same array and keeps the previous call's
+// contents; the iteration counters are cleared at the start of each call. Calls that overlap on the
 // GPU (two streams, or two host threads) race on the array: serialise them.
 // With a non-NULL result the call copies the result to the host and
 // synchronises the stream before it returns.

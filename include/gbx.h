@@ -220,7 +220,7 @@ int gbx_pagerank_pull_fp64(gbx_graph *g, uint32_t iterations, double *ranks, voi
  * num_vertices <= 4,194,304 and max_iterations <= 1024; larger sizes fail
  * with GBX_ERR_INVALID. pull_offsets (num_vertices+1), pull_src, out_degree
  * and ranks must be device memory. The first call on a device looks up the
- * array's address (make it before any stream capture). All calls share the
+ * array's address. All calls share the
  * array: calls that overlap on the GPU race, so serialise them. A non-NULL
  * result is copied to the host and the stream synchronised before return.
  * Same recurrence and result as gbx_pagerank_pull. */
